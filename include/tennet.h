@@ -1,0 +1,159 @@
+/*
+ * tennet.h -- C ABI of libtennet_cuda.so, the GB300 (sm_103a) sweep engine for the
+ * DMRG hot path of TenNetLib.jl.
+ *
+ * Every call returns 0 on success or a negative TN_E_* code; tn_last_error() returns the
+ * message of the last failure on the calling thread.  No call aborts or throws across
+ * the ABI.  Host arrays are copied on entry and never retained; all device memory is
+ * owned by the library and released by the matching *_destroy call.
+ *
+ * Conventions shared by all calls:
+ *  - sites are 0-based (site i of the ABI is site i+1 of the Julia API);
+ *  - a link (virtual bond) is a list of charge sectors (q, dim) sorted by q ascending;
+ *    link i sits left of site i (links 0..N);
+ *  - a physical site has d basis states with charges phys_q[0..d-1];
+ *  - dense tensors cross the ABI column-major (first index fastest, Julia order): a site
+ *    tensor is (Dl, d, Dr), a two-site tensor (Dl, d, d, Dr), a one-site tensor
+ *    (Dl, d, Dr); basis states of a link are ordered sector by sector;
+ *  - an MPO is given per site as a dense (w_left, w_right, d, d) array [a, b, s', s]
+ *    column-major with one charge per MPO link state; W[a,b,s',s] may be nonzero only when
+ *    q_{s'} - q_s = delta_b - delta_a.
+ */
+#ifndef TENNET_H
+#define TENNET_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TN_OK 0
+#define TN_E_INVALID (-1)      /* bad argument, layout or charge mismatch */
+#define TN_E_CUDA (-2)         /* CUDA runtime error */
+#define TN_E_NOMEM (-3)        /* device allocation failed */
+#define TN_E_NOTCONV (-4)      /* solver did not converge and check_convergence was set */
+#define TN_E_NOGPU (-5)        /* no usable sm_103 device */
+#define TN_E_TIMEOUT (-6)      /* a bounded device wait gave up */
+
+/* arithmetic of the contraction GEMMs */
+#define TN_PREC_FP64 0         /* FP64 on CUDA cores: the FP64 GPU oracle */
+#define TN_PREC_SPLIT 1        /* bf16 slices on tcgen05 tensor cores, FP64-recovered */
+
+#define TN_ORTHO_LEFT 0        /* ortho = "left": sweep moves right, U stays left */
+#define TN_ORTHO_RIGHT 1       /* ortho = "right": sweep moves left, V stays right */
+
+typedef struct tn_ctx tn_ctx;
+typedef struct tn_mpo tn_mpo;
+typedef struct tn_mps tn_mps;
+typedef struct tn_env tn_env;
+
+/* keyword arguments of update_position! / fullsweep! / eig_solver
+ * (TenNetLib src/mps/update_site.jl:235-245, src/base/solver.jl:26-35) */
+typedef struct tn_update_params {
+    int32_t maxdim;            /* typemax(Int) in Julia: pass INT32_MAX */
+    int32_t mindim;            /* default 1 */
+    double cutoff;             /* default Float64_threshold() = 1e-15 */
+    int32_t normalize;         /* default 1 */
+    int32_t krylovdim;         /* default 5 */
+    int32_t maxiter;           /* default 2 */
+    double tol;                /* default 1e-14 */
+    int32_t eager;             /* default 0 */
+    int32_t check_convergence; /* default 0 */
+    double noise;              /* must be 0: the density-matrix noise term is not built */
+} tn_update_params;
+
+typedef struct tn_update_result {
+    double energy;             /* Ritz value of the last solve */
+    double truncerr;           /* relative discarded weight of replacebond! */
+    int32_t newdim;            /* bond dimension after truncation */
+    int32_t matvecs;           /* H_eff applications of the solve */
+    int32_t converged;         /* converged Ritz pairs */
+    int32_t neigs;             /* number of kept S^2 values written to eigs (if given) */
+} tn_update_result;
+
+typedef struct tn_sweep_result {
+    double energy;             /* energy of the last update (bond 1 of the right pass) */
+    double maxtruncerr;
+    int32_t maxlinkdim;
+    int32_t matvecs;           /* total H_eff applications in the sweep */
+    double heff_flops;         /* algorithmic flops of all H_eff applications */
+    double heff_ms;            /* device time of the H_eff applications (CUDA events) */
+    double env_ms;             /* device time of environment updates */
+    double svd_ms;             /* device time of the block SVDs */
+    double lanczos_ms;         /* device time of the Krylov vector kernels */
+    double sweep_ms;           /* device time of the whole sweep */
+} tn_sweep_result;
+
+/* ---- context ------------------------------------------------------------------- */
+/* Replaces nothing in the reference (ITensors runs on the host); owns stream + pool. */
+int tn_ctx_create(int device, tn_ctx** out);
+int tn_ctx_destroy(tn_ctx* ctx);
+/* TN_PREC_FP64 or TN_PREC_SPLIT; slices = bf16 slices per FP64 operand (2..7). */
+int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices);
+const char* tn_last_error(void);
+const char* tn_version(void);
+
+/* ---- MPO --------------------------------------------------------------------------
+ * Replaces the ITensorMPS MPO handed to StateEnvs(psi, H::MPO)
+ * (TenNetLib src/mps/state_envs.jl:54-60).
+ * wdims[N+1]: MPO link dimensions (wdims[0] = wdims[N] = 1); wq: concatenated MPO link
+ * charges (sum wdims); W: concatenated dense site tensors. */
+int tn_mpo_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                  const int32_t* wdims, const int32_t* wq, const double* W, tn_mpo** out);
+int tn_mpo_destroy(tn_mpo* mpo);
+
+/* ---- MPS --------------------------------------------------------------------------
+ * Replaces the ITensorMPS MPS (psi) of StateEnvs.  nsec[N+1], sec_q/sec_dim concatenated
+ * sectors of links 0..N; site_data concatenated dense site tensors.  center = site of the
+ * orthogonality center: sites < center must be left isometries, sites > center right
+ * isometries (fullsweep! needs center = 0, TenNetLib src/mps/sweep.jl:100-104). */
+int tn_mps_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                  const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
+                  const double* site_data, int center, tn_mps** out);
+int tn_mps_destroy(tn_mps* mps);
+/* number of sectors of link i, and (when q/dim are non-null) their charges and dims */
+int tn_mps_link(const tn_mps* mps, int link, int32_t* nsec, int32_t* q, int32_t* dim, int cap);
+/* dense site tensor (Dl, d, Dr) column-major */
+int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap);
+int tn_mps_center(const tn_mps* mps);
+
+/* ---- StateEnvs --------------------------------------------------------------------
+ * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO
+ * environments lazily. */
+int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out);
+int tn_env_destroy(tn_env* env);
+/* getpsi(sysenv) (state_envs.jl:36): a copy of the current state */
+int tn_env_getpsi(tn_env* env, tn_mps** out);
+/* position!(sysenv, pos) + set_nsite!(sysenv, nsite) (state_envs.jl:352-367) */
+int tn_env_position(tn_env* env, int pos, int nsite);
+/* product(sysenv, v) = H_eff * v at the current position (state_envs.jl:376-378).
+ * v/out dense (Dl, d, Dr) for nsite = 1 or (Dl, d, d, Dr) for nsite = 2. */
+int tn_env_product(tn_env* env, const double* v, double* out, int64_t n);
+/* algorithmic flops of one product at the current position */
+int tn_env_product_flops(tn_env* env, double* flops);
+/* update_position!(sysenv, eig_solver, pos, 2, ortho; kwargs...)
+ * (TenNetLib src/mps/update_site.jl:231-277, two-site path :27-90).
+ * eigs (optional, capacity eigs_cap) receives the kept S^2 sorted descending. */
+int tn_env_update_position(tn_env* env, int pos, int ortho, const tn_update_params* p,
+                           tn_update_result* res, double* eigs, int eigs_cap);
+/* fullsweep!(sysenv, eig_solver, 2, swdata; kwargs...) (TenNetLib src/mps/sweep.jl:94-196).
+ * mid_eigs (optional) receives lasteigs[N/2] (1-based bond N/2), n_mid_eigs its length. */
+int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res,
+                     double* mid_eigs, int mid_cap, int32_t* n_mid_eigs);
+
+/* ---- block SVD + truncation -------------------------------------------------------
+ * The SVD/truncation of replacebond! (called at TenNetLib src/mps/update_site.jl:64-76)
+ * on explicit dense blocks (column-major, concatenated).  kept[nblocks] receives the
+ * kept dimension per block; svals (capacity sum min(rows,cols)) the singular values per
+ * block sorted descending (all of them, before truncation); truncerr the relative
+ * discarded weight. */
+int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t* cols,
+                    const double* data, int32_t maxdim, int32_t mindim, double cutoff,
+                    int32_t* kept, double* svals, double* truncerr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TENNET_H */

@@ -1,0 +1,669 @@
+"""CPU oracle for the two-site DMRG / TDVP sweep hot path (TEST INFRASTRUCTURE ONLY).
+
+This module is the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()``
+and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.  The
+product path (``libtennet_cuda.so``) never calls into it.
+
+It restates, in plain numpy FP64 with dense arrays carrying U(1) charge labels, what the
+reference computes on the sweep path:
+
+* the step order of ``_update_two_site!``     -- TenNetLib ``src/mps/update_site.jl:27-90``
+* the bond order and recorded data of ``fullsweep!`` -- ``src/mps/sweep.jl:94-196``
+* the stage/noise schedule of ``dmrg!``       -- ``src/mps/dmrg.jl:148-227``
+* the solver defaults of ``eig_solver``       -- ``src/base/solver.jl:23-43``
+* the entropy of the mid-bond spectrum        -- ``src/mps/measure.jl:4-20``
+
+The arithmetic of those steps lives in packages that are not part of the reference tree
+(ITensorMPS.jl 0.3 ``ProjMPO``/``replacebond!``, ITensors.jl 0.9 block-sparse ``svd`` and
+``truncate!``, KrylovKit.jl 0.9/0.10 ``eigsolve``; versions are compat ranges only, no
+Manifest).  They are restated here from their published behaviour:
+
+* ProjMPO product: contract v with L, W_b, W_{b+1}, R (the order does not change the result).
+* ITensors truncation: global sort of all blocks' S^2, maxdim first, then discard the
+  smallest while the accumulated discarded weight stays <= cutoff * sum(S^2) and more than
+  mindim remain; a cut value halfway between the last kept and the first discarded weight,
+  raised by 1e-3 of the last kept weight when those two are within 1e-3 relative of each
+  other (degenerate multiplets are cut as a whole); every block keeps its values whose
+  S^2 exceeds the cut value.
+* KrylovKit Lanczos eigsolve: thick-restart Lanczos (Wu & Simon 2000) with full
+  re-orthogonalisation, ``keep = (3*krylovdim + 2*converged) // 5`` Ritz vectors on restart,
+  convergence when |beta * U[K-1, j]| <= tol.
+
+Parity status: the reference ships no golden vectors (its tests assert nothing), so this
+oracle is pinned against exact diagonalisation of the Heisenberg chain (tests/golden) and
+against invariants; agreement with the reference itself is "parity unpinned".
+
+Conventions (shared with the engine):
+* physical charges q_s: S=1/2 with q = 2*Sz, state 0 = Up (+1), state 1 = Dn (-1);
+* a link is an int array of per-basis-state charges sorted ascending, so each charge
+  sector is a contiguous range;
+* MPS tensor A[l, s, r] is nonzero only when q_r = q_l + q_s;
+* MPO tensor W[a, b, s', s] is nonzero only when q_s' - q_s = delta_b - delta_a;
+* environments L[l', a, l] / R[r', c, r] are nonzero only when q_l' = q_l + delta_a.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+FLOAT64_THRESHOLD = 1e-15  # src/base/global_variables.jl:10
+
+
+# --------------------------------------------------------------------------------------
+# models
+# --------------------------------------------------------------------------------------
+
+SPIN_HALF_Q = np.array([1, -1], dtype=np.int64)  # Up, Dn in units of 2*Sz
+
+
+def spin_half_ops():
+    sz = np.array([[0.5, 0.0], [0.0, -0.5]])
+    sp = np.array([[0.0, 1.0], [0.0, 0.0]])  # |Up><Dn|
+    sm = sp.T.copy()
+    eye = np.eye(2)
+    return eye, sz, sp, sm
+
+
+@dataclass
+class MPO:
+    """Dense MPO with U(1) labels.  W[i] has shape (w_{i-1}, w_i, d, d) as [a, b, s', s]."""
+
+    W: list
+    delta: list  # delta[i] = charges of MPO link i (i = 0..N), int arrays
+    phys_q: np.ndarray
+
+    @property
+    def N(self):
+        return len(self.W)
+
+
+def heisenberg_mpo(N: int, J: float = 1.0, Jz: float | None = None, qn: bool = True) -> MPO:
+    """H = sum_i J (S^x S^x + S^y S^y) + Jz S^z S^z on an open chain (five-state MPO).
+
+    MPO states: 0 = nothing placed yet, 1 = S+ placed, 2 = S- placed, 3 = Sz placed,
+    4 = term complete.  Same operator content as the OpSum built in the reference test
+    ``test/test_MPS_DMRG.jl:29-33``.
+    """
+    if Jz is None:
+        Jz = J
+    eye, sz, sp, sm = spin_half_ops()
+    w = 5
+    bulk = np.zeros((w, w, 2, 2))
+    bulk[0, 0] = eye
+    bulk[0, 1] = 0.5 * J * sp
+    bulk[1, 4] = sm
+    bulk[0, 2] = 0.5 * J * sm
+    bulk[2, 4] = sp
+    bulk[0, 3] = Jz * sz
+    bulk[3, 4] = sz
+    bulk[4, 4] = eye
+    dq = np.array([0, 2, -2, 0, 0]) if qn else np.zeros(5, dtype=np.int64)
+    Ws = []
+    deltas = [np.array([0])]
+    for i in range(N):
+        lo = [0] if i == 0 else list(range(w))
+        hi = [4] if i == N - 1 else list(range(w))
+        Ws.append(bulk[np.ix_(lo, hi)].copy())
+        deltas.append(np.array([0]) if i == N - 1 else dq.copy())
+    return MPO(Ws, deltas, SPIN_HALF_Q.copy() if qn else np.zeros(2, dtype=np.int64))
+
+
+def mpo_from_terms(N: int, terms, qn: bool = True) -> MPO:
+    """Finite-state-automaton MPO for a sum of two-body terms c * O_i O_j (i < j).
+
+    ``terms``: list of (coef, opname_i, i, opname_j, j), opnames in {"Sz", "S+", "S-"}.
+    Automaton states on link k (between site k-1 and site k): "start" (nothing placed,
+    k < N), one pending state per (first operator, its site i) for i < k <= max j of its
+    terms, and "done" (k > 0).  A pending state is carried by identities and closed into
+    "done" by c * O_j at every site j of its terms.  The bond dimension is exact for this
+    construction (no compression); the J1-J2 cylinder gets a few dozen states.
+    """
+    eye, sz, sp, sm = spin_half_ops()
+    ops = {"Sz": (sz, 0), "S+": (sp, 2), "S-": (sm, -2)}
+    by_first = {}
+    for c, o1, i, o2, j in terms:
+        if not i < j:
+            raise ValueError("terms must have i < j")
+        by_first.setdefault((o1, i), []).append((c, o2, j))
+    jmax = {key: max(j for _, _, j in lst) for key, lst in by_first.items()}
+    order = sorted(by_first, key=lambda t: (t[1], t[0]))
+    links = []
+    for k in range(N + 1):
+        keys = []
+        if k < N:
+            keys.append("start")
+        keys += [key for key in order if key[1] < k <= jmax[key]]
+        if k > 0:
+            keys.append("done")
+        links.append(keys)
+    Ws = []
+    for s in range(N):
+        li = {key: n for n, key in enumerate(links[s])}
+        ri = {key: n for n, key in enumerate(links[s + 1])}
+        W = np.zeros((len(li), len(ri), 2, 2))
+        if "start" in li and "start" in ri:
+            W[li["start"], ri["start"]] += eye
+        if "done" in li and "done" in ri:
+            W[li["done"], ri["done"]] += eye
+        for key, lst in by_first.items():
+            o1, i = key
+            if i == s:
+                W[li["start"], ri[key]] += ops[o1][0]
+            if key in li and key in ri:
+                W[li[key], ri[key]] += eye
+            if key in li:
+                for c, o2, j in lst:
+                    if j == s:
+                        W[li[key], ri["done"]] += c * ops[o2][0]
+        Ws.append(W)
+    deltas = []
+    for keys in links:
+        deltas.append(np.array([0 if (key in ("start", "done") or not qn) else ops[key[0]][1]
+                                for key in keys], dtype=np.int64))
+    return MPO(Ws, deltas, SPIN_HALF_Q.copy() if qn else np.zeros(2, dtype=np.int64))
+
+
+def j1j2_cylinder_terms(Lx: int, Ly: int, J1: float = 1.0, J2: float = 0.5):
+    """Bonds of the J1-J2 model on an Lx x Ly cylinder (periodic in y, open in x),
+    snaked column-major: site = Ly * x + y.  Returns OpSum-like two-body terms."""
+    def site(x, y):
+        return Ly * x + (y % Ly)
+
+    bonds = set()
+    for x in range(Lx):
+        for y in range(Ly):
+            a = site(x, y)
+            nn = [(x, y + 1)] + ([(x + 1, y)] if x + 1 < Lx else [])
+            nnn = ([(x + 1, y + 1), (x + 1, y - 1)] if x + 1 < Lx else [])
+            for (xx, yy) in nn:
+                b = site(xx, yy)
+                if a != b:
+                    bonds.add((min(a, b), max(a, b), J1))
+            for (xx, yy) in nnn:
+                b = site(xx, yy)
+                if a != b:
+                    bonds.add((min(a, b), max(a, b), J2))
+    terms = []
+    for i, j, J in sorted(bonds):
+        terms.append((J, "Sz", i, "Sz", j))
+        terms.append((0.5 * J, "S+", i, "S-", j))
+        terms.append((0.5 * J, "S-", i, "S+", j))
+    return terms
+
+
+# --------------------------------------------------------------------------------------
+# MPS construction
+# --------------------------------------------------------------------------------------
+
+@dataclass
+class MPS:
+    A: list  # A[i] of shape (D_{i}, d, D_{i+1}) for i = 0..N-1
+    links: list  # links[i] = charges of link i (i = 0..N)
+    phys_q: np.ndarray
+    center: int = 0  # orthogonality center (0-based site); -1 unknown
+
+    @property
+    def N(self):
+        return len(self.A)
+
+    def maxlinkdim(self):
+        return max(len(q) for q in self.links)
+
+
+def product_mps(states, phys_q, vectors=None) -> MPS:
+    """Product-state MPS.  ``states`` are basis indices (QN case) or None when
+    ``vectors`` (N x d, normalised per site) give a dense product state."""
+    N = len(states) if states is not None else len(vectors)
+    A = []
+    links = [np.array([0])]
+    q = 0
+    for i in range(N):
+        d = len(phys_q)
+        t = np.zeros((1, d, 1))
+        if vectors is not None:
+            t[0, :, 0] = vectors[i]
+            qn = q  # all charges equal in the no-QN case
+        else:
+            t[0, states[i], 0] = 1.0
+            qn = q + int(phys_q[states[i]])
+        A.append(t)
+        q = qn
+        links.append(np.array([q]))
+    return MPS(A, links, np.asarray(phys_q), center=0)
+
+
+def random_product_vectors(N: int, d: int, seed: int):
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((N, d))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v
+
+
+# --------------------------------------------------------------------------------------
+# environments and the effective Hamiltonian (ProjMPO restated)
+# --------------------------------------------------------------------------------------
+
+def left_env_update(L, A, W):
+    """L_new[r', b, r] = sum conj(A[l', s', r']) L[l', a, l] W[a, b, s', s] A[l, s, r]."""
+    t = np.tensordot(L, A, axes=([2], [0]))          # [l', a, s, r]
+    t = np.tensordot(t, W, axes=([1, 2], [0, 3]))    # [l', r, b, s']
+    out = np.tensordot(A.conj(), t, axes=([0, 1], [0, 3]))  # [r', r, b]
+    return out.transpose(0, 2, 1).copy()
+
+
+def right_env_update(R, B, W):
+    """R_new[l', a, l] = sum conj(B[l', s', r']) R[r', c, r] W[a, c, s', s] B[l, s, r]."""
+    t = np.tensordot(R, B, axes=([2], [2]))          # [r', c, l, s]
+    t = np.tensordot(t, W, axes=([1, 3], [1, 3]))    # [r', l, a, s']
+    out = np.tensordot(B.conj(), t, axes=([1, 2], [3, 0]))  # [l', l, a]
+    return out.transpose(0, 2, 1).copy()
+
+
+def heff2_apply(L, W1, W2, R, phi):
+    """Two-site H_eff * phi, phi[l, s1, s2, r] (ProjMPO product restated)."""
+    t = np.tensordot(L, phi, axes=([2], [0]))            # [l', a, s1, s2, r]
+    t = np.tensordot(t, W1, axes=([1, 2], [0, 3]))       # [l', s2, r, b, s1']
+    t = np.tensordot(t, W2, axes=([3, 1], [0, 3]))       # [l', r, s1', c, s2']
+    t = np.tensordot(t, R, axes=([1, 3], [2, 1]))        # [l', s1', s2', r']
+    return t
+
+
+def heff1_apply(L, W, R, phi):
+    t = np.tensordot(L, phi, axes=([2], [0]))            # [l', a, s, r]
+    t = np.tensordot(t, W, axes=([1, 2], [0, 3]))        # [l', r, b, s']
+    t = np.tensordot(t, R, axes=([1, 2], [2, 1]))        # [l', s', r']
+    return t
+
+
+def heff2_flops(L_shape, W1, W2, R_shape, phi_shape):
+    """Dense multiply-add count of the four-step contraction above (x2 = flops)."""
+    Dl, w0, _ = L_shape
+    _, d1, d2, Dr = phi_shape
+    w1 = W1.shape[1]
+    w2 = W2.shape[1]
+    f = Dl * w0 * Dl * d1 * d2 * Dr
+    f += Dl * d2 * Dr * w1 * d1 * w0 * d1
+    f += Dl * Dr * d1 * w2 * d2 * w1 * d2
+    f += Dl * d1 * d2 * Dr * Dr * w2
+    return 2 * f
+
+
+# --------------------------------------------------------------------------------------
+# Lanczos eigensolver (KrylovKit eigsolve semantics restated)
+# --------------------------------------------------------------------------------------
+
+@dataclass
+class EigInfo:
+    matvecs: int = 0
+    converged: int = 0
+    numiter: int = 0
+    residual: float = float("nan")
+
+
+def _gs2(V, w):
+    """Classical Gram-Schmidt, applied twice; returns coefficients and the residual."""
+    if not V:
+        return np.zeros(0, dtype=w.dtype), w
+    M = np.stack(V, axis=0)
+    h = M.conj() @ w
+    w = w - h @ M
+    h2 = M.conj() @ w
+    w = w - h2 @ M
+    return h + h2, w
+
+
+def eigsolve_lowest(apply, x0, krylovdim=5, maxiter=2, tol=1e-14, eager=False):
+    """Lowest eigenpair of a Hermitian operator by thick-restart Lanczos.
+
+    Follows ``eig_solver`` (``src/base/solver.jl:23-43``): howmany = 1, :SR, Hermitian.
+    Returns (energy, vector, EigInfo).
+    """
+    info = EigInfo()
+    x = x0 / np.linalg.norm(x0)
+    V = [x]
+    w = apply(x)
+    info.matvecs += 1
+    h, r = _gs2(V, w)
+    H = np.zeros((krylovdim + 1, krylovdim + 1), dtype=np.result_type(x0, np.float64))
+    H[0, 0] = h[0].real
+    beta = np.linalg.norm(r)
+    numiter = 1
+    D = U = None
+    converged = 0
+    while True:
+        K = len(V)
+        # K >= n: the Krylov space spans the whole vector space, the Ritz pair is exact
+        exhausted = K >= x.size
+        if K == krylovdim or beta <= tol or (eager and K >= 1) or exhausted:
+            Hk = H[:K, :K]
+            Hk = 0.5 * (Hk + Hk.conj().T)
+            D, U = np.linalg.eigh(Hk)
+            f = beta * U[K - 1, :]
+            converged = 0
+            while converged < K and abs(f[converged]) <= tol:
+                converged += 1
+            info.residual = abs(f[0])
+            if converged >= 1 or exhausted:
+                break
+        if K < krylovdim:
+            v = r / beta
+            V.append(v)
+            w = apply(v)
+            info.matvecs += 1
+            h, r = _gs2(V, w)
+            H[: K + 1, K] = h
+            H[K, : K + 1] = h.conj()
+            H[K, K] = h[K].real
+            beta = np.linalg.norm(r)
+        else:
+            if numiter == maxiter:
+                break
+            keep = (3 * krylovdim + 2 * converged) // 5
+            M = np.stack(V, axis=0)
+            V = [U[:, j] @ M for j in range(keep)]
+            f = beta * U[K - 1, :]
+            H = np.zeros_like(H)
+            for j in range(keep):
+                H[j, j] = D[j]
+            # the residual r is unchanged; its coupling to Ritz vector j is f[j], which the
+            # explicit Gram-Schmidt of the next expansion recomputes.
+            numiter += 1
+    info.converged = converged
+    info.numiter = numiter
+    M = np.stack(V, axis=0)
+    vec = U[:, 0] @ M
+    vec = vec / np.linalg.norm(vec)
+    return float(D[0]), vec, info
+
+
+# --------------------------------------------------------------------------------------
+# SVD with ITensors-style global truncation
+# --------------------------------------------------------------------------------------
+
+@dataclass
+class Spectrum:
+    eigs: np.ndarray
+    truncerr: float
+
+
+def truncation_rule(P, maxdim, mindim, cutoff):
+    """ITensors ``truncate!`` restated.  P: all S^2, sorted descending.
+
+    Returns (n_kept_by_rank, truncerr, docut).  Per block, values with S^2 > docut are kept.
+    """
+    P = np.array(P, dtype=np.float64)
+    origm = len(P)
+    for n in range(origm - 1, -1, -1):
+        if P[n] >= 0:
+            break
+        P[n] = 0.0
+    n = origm
+    truncerr = 0.0
+    while n > maxdim:
+        truncerr += P[n - 1]
+        n -= 1
+    scale = float(np.sum(P))
+    if scale == 0.0:
+        scale = 1.0
+    while n > mindim and truncerr + P[n - 1] <= cutoff * scale:
+        truncerr += P[n - 1]
+        n -= 1
+    truncerr /= scale
+    if n < 1:
+        n = 1
+    docut = 0.0
+    if n < origm:
+        docut = 0.5 * (P[n - 1] + P[n])
+        if abs(P[n - 1] - P[n]) < 1e-3 * P[n - 1]:
+            docut += 1e-3 * P[n - 1]
+    return n, truncerr, docut
+
+
+def svd_blocks_truncate(blocks, maxdim, mindim, cutoff):
+    """SVD of a list of dense blocks, global truncation.
+
+    Returns per block (U_k, S_k, Vh_k) truncated, the Spectrum, and kept dims.
+    """
+    svds = []
+    allP = []
+    for M in blocks:
+        if M.size == 0:
+            svds.append((np.zeros((M.shape[0], 0)), np.zeros(0), np.zeros((0, M.shape[1]))))
+            continue
+        U, S, Vh = np.linalg.svd(M, full_matrices=False)
+        svds.append((U, S, Vh))
+        allP.append(S * S)
+    P = np.sort(np.concatenate(allP))[::-1] if allP else np.zeros(0)
+    n, truncerr, docut = truncation_rule(P, maxdim, mindim, cutoff)
+    out = []
+    kept = []
+    for (U, S, Vh) in svds:
+        k = int(np.sum(S * S > docut))
+        kept.append(k)
+        out.append((U[:, :k], S[:k], Vh[:k, :]))
+    if sum(kept) == 0:
+        # every value fell under the cut (fully degenerate spectrum at maxdim): keep the
+        # largest value so that the link never becomes empty.
+        best = int(np.argmax([s[1][0] if len(s[1]) else -1 for s in svds]))
+        U, S, Vh = svds[best]
+        out[best] = (U[:, :1], S[:1], Vh[:1, :])
+        kept[best] = 1
+    eigs = np.sort(np.concatenate([o[1] ** 2 for o in out]))[::-1]
+    return out, Spectrum(eigs=eigs, truncerr=truncerr), kept
+
+
+def split_two_site(phi, ql, qs, qr, maxdim, mindim, cutoff, ortho, normalize=True):
+    """``replacebond!`` restated: SVD phi[l, s1, s2, r] per middle charge, truncate.
+
+    Returns (A_left, A_right, qmid, spec).  ortho == "left": left tensor is U (left
+    isometry), right tensor is S V^H.  ortho == "right": left is U S, right is V^H.
+    The new link basis is sorted by charge ascending, then by singular value descending.
+    """
+    Dl, d1, d2, Dr = phi.shape
+    M = phi.reshape(Dl * d1, d2 * Dr)
+    qrow = (ql[:, None] + qs[None, :]).reshape(-1)
+    qcol = (qr[None, :] - qs[:, None]).reshape(-1)
+    charges = sorted(set(qrow.tolist()) & set(qcol.tolist()))
+    blocks, rows, cols = [], [], []
+    for m in charges:
+        ri = np.nonzero(qrow == m)[0]
+        ci = np.nonzero(qcol == m)[0]
+        rows.append(ri)
+        cols.append(ci)
+        blocks.append(M[np.ix_(ri, ci)])
+    res, spec, kept = svd_blocks_truncate(blocks, maxdim, mindim, cutoff)
+    chi = sum(kept)
+    Lm = np.zeros((Dl * d1, chi), dtype=phi.dtype)
+    Rm = np.zeros((chi, d2 * Dr), dtype=phi.dtype)
+    qmid = []
+    norm = math.sqrt(sum(float(np.sum(s ** 2)) for _, s, _ in res)) if normalize else 1.0
+    off = 0
+    for m, ri, ci, (U, S, Vh), k in zip(charges, rows, cols, res, kept):
+        if k == 0:
+            continue
+        Sn = S / norm
+        if ortho == "left":
+            Lm[np.ix_(ri, range(off, off + k))] = U
+            Rm[np.ix_(range(off, off + k), ci)] = Sn[:, None] * Vh
+        else:
+            Lm[np.ix_(ri, range(off, off + k))] = U * Sn[None, :]
+            Rm[np.ix_(range(off, off + k), ci)] = Vh
+        qmid.extend([m] * k)
+        off += k
+    A = Lm.reshape(Dl, d1, chi)
+    B = Rm.reshape(chi, d2, Dr)
+    return A, B, np.array(qmid, dtype=np.int64), spec
+
+
+def entropy(p):
+    """von Neumann entropy of a probability vector (``src/mps/measure.jl:4-20``)."""
+    p = np.asarray(p, dtype=np.float64)
+    s = float(np.sum(p))
+    if abs(s - 1.0) > 100 * FLOAT64_THRESHOLD:
+        p = p / s
+    return float(-sum(a * math.log(a) for a in p if a > 0.0))
+
+
+# --------------------------------------------------------------------------------------
+# sweeps (StateEnvs + fullsweep! + dmrg! restated)
+# --------------------------------------------------------------------------------------
+
+@dataclass
+class SweepData:
+    """Per-sweep history (``src/mps/sweep.jl:26-35``)."""
+
+    sweepcount: int = 0
+    maxchi: list = field(default_factory=list)
+    energy: list = field(default_factory=list)
+    entropy: list = field(default_factory=list)
+    maxtruncerr: list = field(default_factory=list)
+    lasteigs: list = field(default_factory=list)
+
+
+class StateEnvs:
+    """MPS + MPO environments.  ``L[i]`` contracts sites < i, ``R[i]`` sites > i."""
+
+    def __init__(self, psi: MPS, H: MPO):
+        assert psi.N == H.N
+        self.psi = MPS([a.copy() for a in psi.A], [q.copy() for q in psi.links],
+                       psi.phys_q.copy(), psi.center)
+        self.H = H
+        N = psi.N
+        self.L = [None] * (N + 1)
+        self.R = [None] * (N + 1)
+        self.L[0] = np.ones((1, 1, 1))
+        self.R[N - 1] = np.ones((1, 1, 1))
+        self.lpos = 0       # L[0..lpos] valid
+        self.rpos = N - 1   # R[rpos..N-1] valid
+        self.matvec_flops = 0
+
+    @property
+    def N(self):
+        return self.psi.N
+
+    def position(self, pos, nsite):
+        """Make L[pos] and R[pos+nsite-1] valid (ProjMPO ``position!`` restated)."""
+        while self.lpos < pos:
+            i = self.lpos
+            self.L[i + 1] = left_env_update(self.L[i], self.psi.A[i], self.H.W[i])
+            self.lpos += 1
+        self.lpos = pos
+        last = pos + nsite - 1
+        while self.rpos > last:
+            i = self.rpos
+            self.R[i - 1] = right_env_update(self.R[i], self.psi.A[i], self.H.W[i])
+            self.rpos -= 1
+        self.rpos = last
+
+    def product2(self, pos, phi):
+        return heff2_apply(self.L[pos], self.H.W[pos], self.H.W[pos + 1], self.R[pos + 1], phi)
+
+
+def update_two_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdim, maxiter,
+                    tol, normalize=True):
+    """``_update_two_site!`` (``src/mps/update_site.jl:27-90``) for the eigensolver."""
+    psi = env.psi
+    phi = np.tensordot(psi.A[pos], psi.A[pos + 1], axes=([2], [0]))
+    env.position(pos, 2)
+    shape = phi.shape
+
+    def apply(v):
+        return env.product2(pos, v.reshape(shape)).reshape(-1)
+
+    energy, vec, info = eigsolve_lowest(apply, phi.reshape(-1), krylovdim, maxiter, tol)
+    phi = vec.reshape(shape)
+    if normalize:
+        phi = phi / np.linalg.norm(phi)
+    A, B, qmid, spec = split_two_site(phi, psi.links[pos], psi.phys_q, psi.links[pos + 2],
+                                      maxdim, mindim, cutoff, ortho, normalize)
+    psi.A[pos] = A
+    psi.A[pos + 1] = B
+    psi.links[pos + 1] = qmid
+    psi.center = pos + 1 if ortho == "left" else pos
+    # environments that contain the changed sites become invalid
+    env.lpos = min(env.lpos, pos)
+    env.rpos = max(env.rpos, pos + 1)
+    return energy, spec, info
+
+
+def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,
+              maxiter=2, tol=1e-14, normalize=True):
+    """``fullsweep!`` with nsite = 2 (``src/mps/sweep.jl:94-196``)."""
+    N = env.N
+    assert env.psi.center == 0, "sweep starts with the orthogonality center on site 1"
+    swdata.sweepcount += 1
+    energy = float("nan")
+    maxtruncerr = 0.0
+    lasteigs = [None] * (N - 1)
+    for b in range(N - 1):
+        energy, spec, _ = update_two_site(env, b, "left", maxdim, mindim, cutoff, krylovdim,
+                                          maxiter, tol, normalize)
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+    for b in range(N - 2, -1, -1):
+        energy, spec, _ = update_two_site(env, b, "right", maxdim, mindim, cutoff, krylovdim,
+                                          maxiter, tol, normalize)
+        lasteigs[b] = spec.eigs
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+    swdata.maxchi.append(env.psi.maxlinkdim())
+    swdata.energy.append(energy)
+    mid = lasteigs[N // 2 - 1]
+    swdata.entropy.append(entropy(mid / np.sum(mid)))
+    swdata.maxtruncerr.append(maxtruncerr)
+    swdata.lasteigs = lasteigs
+    if swdata.sweepcount > 1:
+        return swdata.energy[-1] - swdata.energy[-2], swdata.entropy[-1] - swdata.entropy[-2]
+    return float("nan"), float("nan")
+
+
+def dmrg(psi0: MPS, H: MPO, maxdim, nsweeps, cutoff, krylovdim=5, maxiter=2, tol=1e-14,
+         mindim=1):
+    """``dmrg!`` stage loop without noise (``src/mps/dmrg.jl:148-227``)."""
+    env = StateEnvs(psi0, H)
+    sw = SweepData()
+    if np.isscalar(cutoff):
+        cutoff = [cutoff] * len(nsweeps)
+    for ii in range(len(nsweeps)):
+        for _ in range(nsweeps[ii]):
+            fullsweep(env, sw, maxdim[ii], cutoff[ii], mindim, krylovdim, maxiter, tol)
+    return sw, env
+
+
+# --------------------------------------------------------------------------------------
+# dense <-> charge-sector helpers used by the tests
+# --------------------------------------------------------------------------------------
+
+def sectors(q):
+    """(charges, dims, offsets) of a sorted link charge array."""
+    q = np.asarray(q)
+    ch, idx, cnt = np.unique(q, return_index=True, return_counts=True)
+    return ch, cnt, idx
+
+
+def random_qn_link(charges, dims):
+    return np.repeat(np.asarray(charges, dtype=np.int64), np.asarray(dims, dtype=np.int64))
+
+
+def qn_mask3(ql, qs, qr):
+    return (ql[:, None, None] + qs[None, :, None]) == qr[None, None, :]
+
+
+def qn_mask_env(qb, delta, qk):
+    return qb[:, None, None] == (qk[None, None, :] + delta[None, :, None])
+
+
+def random_qn_tensor(rng, ql, qs, qr, dtype=np.float64):
+    t = rng.standard_normal((len(ql), len(qs), len(qr)))
+    if dtype == np.complex128:
+        t = t + 1j * rng.standard_normal(t.shape)
+    return t * qn_mask3(ql, qs, qr)
+
+
+def random_env(rng, qlink, delta, hermitian=True):
+    """Random environment tensor E[x', a, x] respecting charges; each a-slice symmetric
+    when the MPO state is its own conjugate partner is not required for tests."""
+    D = len(qlink)
+    w = len(delta)
+    t = rng.standard_normal((D, w, D))
+    return t * qn_mask_env(qlink, delta, qlink)

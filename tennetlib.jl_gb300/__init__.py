@@ -1,0 +1,475 @@
+"""tennet_gb300: the DMRG sweep hot path of TenNetLib.jl on one GB300 (sm_103a).
+
+The Python API mirrors TenNetLib's Julia API for this path (Julia's trailing ``!`` becomes
+a trailing ``_``):
+
+=============================  ==============================================================
+Python                          TenNetLib (file:line)
+=============================  ==============================================================
+``StateEnvs(psi, H)``           ``StateEnvs(psi, H::MPO)``          src/mps/state_envs.jl:54-60
+``StateEnvs.position_``         ``position!``                       src/mps/state_envs.jl:364-367
+``StateEnvs.product``           ``product`` / ``sysenv(v)``         src/mps/state_envs.jl:376-380
+``update_position_``            ``update_position!``                src/mps/update_site.jl:231-277
+``fullsweep_``                  ``fullsweep!``                      src/mps/sweep.jl:94-196
+``SweepData``                   ``SweepData``                       src/mps/sweep.jl:26-35
+``DMRGParams``                  ``DMRGParams``                      src/mps/dmrg.jl:26-102
+``dmrg_`` / ``dmrg`` / ``dmrg2`` ``dmrg!`` / ``dmrg`` / ``dmrg2``    src/mps/dmrg.jl:148-301
+``eig_solver``                  ``eig_solver``                      src/base/solver.jl:23-43
+``entropy``                     ``_entropy``                        src/mps/measure.jl:4-20
+=============================  ==============================================================
+
+All arithmetic runs in libtennet_cuda.so; this module only moves host arrays across the C
+ABI.  It refuses to run without the library or without a GB300.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from . import models  # noqa: F401
+from ._lib import TenNetError
+
+FLOAT64_THRESHOLD = 1e-15
+INT32_MAX = 2**31 - 1
+
+__all__ = [
+    "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
+    "update_position_", "fullsweep_", "dmrg_", "dmrg", "dmrg2", "entropy", "svd_truncate",
+    "Float64_threshold", "TenNetError", "models",
+]
+
+_threshold = [FLOAT64_THRESHOLD]
+
+
+def Float64_threshold(value: float | None = None) -> float:
+    """``Float64_threshold()`` (src/base/global_variables.jl:19-26)."""
+    if value is not None:
+        _threshold[0] = float(value)
+    return _threshold[0]
+
+
+class Context:
+    """One GB300, one stream and its memory pool."""
+
+    _default = None
+
+    def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 4):
+        self.lib = L.load()
+        h = L.vp()
+        L.check(self.lib.tn_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.set_precision(precision, slices)
+
+    def set_precision(self, precision: str, slices: int = 4):
+        mode = {"fp64": L.TN_PREC_FP64, "split": L.TN_PREC_SPLIT}[precision]
+        L.check(self.lib.tn_ctx_set_precision(self.h, mode, slices))
+        self.precision = precision
+        self.slices = slices
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context()
+        return cls._default
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tn_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _links_to_sectors(links):
+    nsec, q, dim = [], [], []
+    for lk in links:
+        lk = np.asarray(lk)
+        if lk.size and np.any(np.diff(lk) < 0):
+            raise ValueError("link charges must be sorted ascending")
+        ch, cnt = np.unique(lk, return_counts=True)
+        nsec.append(len(ch))
+        q += ch.tolist()
+        dim += cnt.tolist()
+    return nsec, q, dim
+
+
+class MPO:
+    """Device copy of an MPO given as dense site tensors W[i] (w_i, w_{i+1}, d, d)."""
+
+    def __init__(self, W, delta, phys_q, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.N = len(W)
+        self.d = len(phys_q)
+        self.phys_q = np.asarray(phys_q, dtype=np.int32)
+        wd = [W[0].shape[0]] + [w.shape[1] for w in W]
+        flat = np.concatenate([np.asarray(w, dtype=np.float64).ravel(order="F") for w in W])
+        q = np.concatenate([np.asarray(x, dtype=np.int32) for x in delta])
+        a1, p1 = L.as_i32(self.phys_q)
+        a2, p2 = L.as_i32(wd)
+        a3, p3 = L.as_i32(q)
+        a4, p4 = L.as_f64(flat)
+        h = L.vp()
+        L.check(self.ctx.lib.tn_mpo_create(self.ctx.h, self.N, self.d, p1, p2, p3, p4, C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_terms(cls, N, terms, conserve_qns=True, ctx=None):
+        W, delta, pq = models.mpo_from_terms(N, terms, conserve_qns)
+        return cls(W, delta, pq, ctx)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.tn_mpo_destroy(self.h)
+        except Exception:
+            pass
+
+
+class MPS:
+    """Device MPS.  Created from dense site tensors (Dl, d, Dr) and link charge arrays."""
+
+    def __init__(self, tensors=None, links=None, phys_q=None, center: int = 0,
+                 ctx: Context | None = None, _handle=None, _N=None, _d=None):
+        self.ctx = ctx or Context.default()
+        if _handle is not None:
+            self.h = _handle
+            self.N = _N
+            self.d = _d
+            self.phys_q = np.asarray(phys_q, dtype=np.int32)
+            return
+        self.N = len(tensors)
+        self.d = len(phys_q)
+        self.phys_q = np.asarray(phys_q, dtype=np.int32)
+        nsec, q, dim = _links_to_sectors(links)
+        flat = np.concatenate([np.asarray(t, dtype=np.float64).ravel(order="F") for t in tensors])
+        bufs = [L.as_i32(self.phys_q), L.as_i32(nsec), L.as_i32(q), L.as_i32(dim), L.as_f64(flat)]
+        h = L.vp()
+        L.check(self.ctx.lib.tn_mps_create(self.ctx.h, self.N, self.d, bufs[0][1], bufs[1][1],
+                                           bufs[2][1], bufs[3][1], bufs[4][1], center,
+                                           C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def product(cls, states, phys_q, ctx=None):
+        t, lk = models.product_state(states, phys_q)
+        return cls(t, lk, phys_q, 0, ctx)
+
+    @classmethod
+    def random_product(cls, N, d, seed, ctx=None):
+        t, lk = models.random_product_state(N, d, seed)
+        return cls(t, lk, np.zeros(d, dtype=np.int32), 0, ctx)
+
+    def link(self, i):
+        """(charges, dims) of link i (0..N)."""
+        n = C.c_int32()
+        L.check(self.ctx.lib.tn_mps_link(self.h, i, C.byref(n), None, None, 0))
+        q = np.zeros(n.value, dtype=np.int32)
+        dm = np.zeros(n.value, dtype=np.int32)
+        L.check(self.ctx.lib.tn_mps_link(self.h, i, C.byref(n), q.ctypes.data_as(L.i32p),
+                                         dm.ctypes.data_as(L.i32p), n.value))
+        return q, dm
+
+    def link_charges(self, i):
+        q, dm = self.link(i)
+        return np.repeat(q, dm)
+
+    def linkdims(self):
+        return [int(self.link(i)[1].sum()) for i in range(1, self.N)]
+
+    def maxlinkdim(self):
+        return max(self.linkdims())
+
+    def site(self, i):
+        Dl = int(self.link(i)[1].sum())
+        Dr = int(self.link(i + 1)[1].sum())
+        out = np.zeros(Dl * self.d * Dr)
+        L.check(self.ctx.lib.tn_mps_site(self.h, i, out.ctypes.data_as(L.f64p), out.size))
+        return out.reshape((Dl, self.d, Dr), order="F")
+
+    @property
+    def center(self):
+        return self.ctx.lib.tn_mps_center(self.h)
+
+    def __len__(self):
+        return self.N
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.tn_mps_destroy(self.h)
+        except Exception:
+            pass
+
+
+class StateEnvs:
+    """``StateEnvs(psi, H::MPO)``: a copy of psi plus lazily built ProjMPO environments."""
+
+    def __init__(self, psi: MPS, H: MPO):
+        self.ctx = psi.ctx
+        self.H = H
+        self.phys_q = psi.phys_q
+        self.N = psi.N
+        self.d = psi.d
+        h = L.vp()
+        L.check(self.ctx.lib.tn_env_create(psi.h, H.h, C.byref(h)))
+        self.h = h
+
+    def __len__(self):
+        return self.N
+
+    @property
+    def psi(self) -> MPS:
+        return self.getpsi()
+
+    def getpsi(self) -> MPS:
+        h = L.vp()
+        L.check(self.ctx.lib.tn_env_getpsi(self.h, C.byref(h)))
+        return MPS(ctx=self.ctx, _handle=h, _N=self.N, _d=self.d, phys_q=self.phys_q)
+
+    def position_(self, pos: int, nsite: int = 2):
+        """``position!`` + ``set_nsite!`` (0-based pos)."""
+        L.check(self.ctx.lib.tn_env_position(self.h, pos, nsite))
+        self._pos = pos
+        return self
+
+    def product(self, v):
+        """H_eff * v at the current position, v dense (Dl, d, d, Dr)."""
+        v = np.asarray(v, dtype=np.float64)
+        flat = np.ascontiguousarray(v.ravel(order="F"))
+        out = np.zeros_like(flat)
+        L.check(self.ctx.lib.tn_env_product(self.h, flat.ctypes.data_as(L.f64p),
+                                            out.ctypes.data_as(L.f64p), flat.size))
+        return out.reshape(v.shape, order="F")
+
+    __call__ = product
+
+    def product_flops(self) -> float:
+        f = C.c_double()
+        L.check(self.ctx.lib.tn_env_product_flops(self.h, C.byref(f)))
+        return f.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.tn_env_destroy(self.h)
+        except Exception:
+            pass
+
+
+def eig_solver(*_args, **_kwargs):
+    """Token for the Lanczos ground-state solver (``src/base/solver.jl:23-43``).  The solve
+    itself runs inside libtennet_cuda.so as part of each update step."""
+    raise TypeError("eig_solver is passed to update_position_/fullsweep_, not called")
+
+
+def _params(kwargs) -> L.UpdateParams:
+    p = L.UpdateParams()
+    maxdim = kwargs.get("maxdim", INT32_MAX)
+    p.maxdim = int(min(maxdim, INT32_MAX))
+    p.mindim = int(kwargs.get("mindim", 1))
+    p.cutoff = float(kwargs.get("cutoff", Float64_threshold()))
+    p.normalize = int(bool(kwargs.get("normalize", True)))
+    p.krylovdim = int(kwargs.get("solver_krylovdim", 5))
+    p.maxiter = int(kwargs.get("solver_maxiter", 2))
+    p.tol = float(kwargs.get("solver_tol", 1e-14))
+    p.eager = int(bool(kwargs.get("solver_eager", False)))
+    p.check_convergence = int(bool(kwargs.get("solver_check_convergence", False)))
+    p.noise = float(kwargs.get("noise", 0.0))
+    if not kwargs.get("ishermitian", True):
+        raise ValueError("only Hermitian effective Hamiltonians are built")
+    if kwargs.get("time_step") is not None:
+        raise ValueError("time evolution (exp_solver) is not built in this engine")
+    return p
+
+
+def update_position_(sysenv: StateEnvs, solver, pos: int, nsite: int, ortho: str, **kwargs):
+    """``update_position!`` for two-site DMRG.  Returns (energy, truncerr, eigs)."""
+    if solver is not eig_solver:
+        raise ValueError("only eig_solver is built")
+    if nsite != 2:
+        raise ValueError("only nsite = 2 is built")
+    p = _params(kwargs)
+    res = L.UpdateResult()
+    cap = max(int(p.maxdim if p.maxdim < 1 << 20 else 1 << 16), 1)
+    eigs = np.zeros(cap)
+    o = {"left": L.TN_ORTHO_LEFT, "right": L.TN_ORTHO_RIGHT}[ortho]
+    L.check(sysenv.ctx.lib.tn_env_update_position(sysenv.h, pos, o, C.byref(p), C.byref(res),
+                                                  eigs.ctypes.data_as(L.f64p), cap))
+    return res.energy, res.truncerr, eigs[: res.neigs].copy()
+
+
+@dataclass
+class SweepData:
+    """History of full sweeps (``src/mps/sweep.jl:26-35``)."""
+
+    sweepcount: int = 0
+    maxchi: list = field(default_factory=list)
+    energy: list = field(default_factory=list)
+    entropy: list = field(default_factory=list)
+    maxtruncerr: list = field(default_factory=list)
+    lasteigs: list = field(default_factory=list)
+    # per-sweep device timings and work (not in the reference; from CUDA events)
+    stats: list = field(default_factory=list)
+
+
+def entropy(p) -> float:
+    """von Neumann entropy -sum p log p (``src/mps/measure.jl:4-20``)."""
+    p = np.asarray(p, dtype=np.float64)
+    s = float(p.sum())
+    if abs(s - 1.0) > 100 * Float64_threshold():
+        p = p / s
+    return float(-sum(a * math.log(a) for a in p if a > 0.0))
+
+
+def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwargs):
+    """``fullsweep!``: left-to-right then right-to-left two-site updates.
+
+    Returns (Delta E, Delta S) and appends to ``swdata``.
+    """
+    if solver is not eig_solver or nsite != 2:
+        raise ValueError("only two-site eig_solver sweeps are built")
+    p = _params(kwargs)
+    outputlevel = kwargs.get("outputlevel", 1)
+    res = L.SweepResult()
+    cap = max(int(p.maxdim if p.maxdim < 1 << 20 else 1 << 16), 1)
+    mid = np.zeros(cap)
+    nmid = C.c_int32()
+    swdata.sweepcount += 1
+    t0 = time.perf_counter()
+    L.check(sysenv.ctx.lib.tn_env_fullsweep(sysenv.h, C.byref(p), C.byref(res),
+                                            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    wall = time.perf_counter() - t0
+    mid = mid[: nmid.value].copy()
+    swdata.maxchi.append(int(res.maxlinkdim))
+    swdata.energy.append(float(res.energy))
+    swdata.entropy.append(entropy(mid / mid.sum()) if mid.size else 0.0)
+    swdata.maxtruncerr.append(float(res.maxtruncerr))
+    swdata.lasteigs = [mid]
+    swdata.stats.append({
+        "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
+        "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
+        "sweep_ms": res.sweep_ms, "wall_s": wall})
+    if swdata.sweepcount > 1:
+        enerr = swdata.energy[-1] - swdata.energy[-2]
+        enterr = swdata.entropy[-1] - swdata.entropy[-2]
+    else:
+        enerr = enterr = float("nan")
+    if outputlevel > 0:
+        print("-" * 83)
+        print(f"At sweep {swdata.sweepcount} => E={swdata.energy[-1]}, S={swdata.entropy[-1]}, "
+              f"MaxLinkDim={swdata.maxchi[-1]}, Noise={p.noise:.2g}")
+        print(f"At sweep {swdata.sweepcount} => ΔE={enerr}, ΔS={enterr}, "
+              f"MaxErr={swdata.maxtruncerr[-1]:.2g}, Time={round(wall, 3)}")
+        print("-" * 83)
+    return enerr, enterr
+
+
+@dataclass
+class DMRGParams:
+    """Stage schedule of DMRG (``src/mps/dmrg.jl:26-102``)."""
+
+    maxdim: list
+    nsweeps: list
+    cutoff: object = None
+    noise: object = 0.0
+    noisedecay: object = 1.0
+    disable_noise_after: object = -1
+
+    def __post_init__(self):
+        n = len(self.nsweeps)
+        if self.cutoff is None:
+            self.cutoff = Float64_threshold()
+
+        def vec(x, typ):
+            return [typ(v) for v in x] if isinstance(x, (list, tuple, np.ndarray)) else [typ(x)] * n
+
+        self.cutoff = vec(self.cutoff, float)
+        self.noise = vec(self.noise, float)
+        self.noisedecay = vec(self.noisedecay, float)
+        self.disable_noise_after = vec(self.disable_noise_after, int)
+        self.maxdim = [int(v) for v in self.maxdim]
+        self.nsweeps = [int(v) for v in self.nsweeps]
+        if not (len(self.maxdim) == n == len(self.cutoff) == len(self.noise) ==
+                len(self.noisedecay) == len(self.disable_noise_after)):
+            raise ValueError("`DMRGParams()` :: Size mismatch in input vectors !!")
+
+
+def dmrg_(sysenv: StateEnvs, params: DMRGParams, nsite: int, **kwargs) -> SweepData:
+    """``dmrg!`` stage loop (``src/mps/dmrg.jl:148-227``)."""
+    outputlevel = kwargs.get("outputlevel", 1)
+    enerrgoal = kwargs.get("energyErrGoal")
+    enterrgoal = kwargs.get("entropyErrGoal")
+    sw = SweepData()
+    for ii in range(len(params.nsweeps)):
+        noise = params.noise[ii]
+        if outputlevel > 0:
+            print("-" * 83)
+            print(f"DMRG level={ii + 1} => maxdim={params.maxdim[ii]}, "
+                  f"nsweeps={params.nsweeps[ii]}, cutoff={params.cutoff[ii]:.2E}")
+            print("-" * 83)
+        for jj in range(1, params.nsweeps[ii] + 1):
+            kw = dict(kwargs)
+            kw.update(maxdim=params.maxdim[ii], cutoff=params.cutoff[ii], noise=noise)
+            enerr, enterr = fullsweep_(sysenv, eig_solver, nsite, sw, **kw)
+            met = False
+            if enerrgoal is not None and enterrgoal is not None:
+                met = abs(enerr) < abs(enerrgoal) and abs(enterr) < abs(enterrgoal)
+            elif enerrgoal is not None:
+                met = abs(enerr) < abs(enerrgoal)
+            # the reference's entropy-only branch discards its comparison
+            # (src/mps/dmrg.jl:190-191), so it never stops early: kept as is.
+            if met and abs(noise) < Float64_threshold():
+                break
+            if jj == params.disable_noise_after[ii]:
+                noise = 0.0
+            noise /= params.noisedecay[ii]
+            if noise < 100 * Float64_threshold():
+                noise = 0.0
+    return sw
+
+
+def dmrg(psi0: MPS, H: MPO, params: DMRGParams, nsite: int, **kwargs):
+    """``dmrg(psi0, H, params, nsite)`` -> (energy, psi) (``src/mps/dmrg.jl:231-236``)."""
+    env = StateEnvs(psi0, H)
+    sw = dmrg_(env, params, nsite, **kwargs)
+    return sw.energy[-1], env.getpsi()
+
+
+def dmrg2(psi0: MPS, H: MPO, params: DMRGParams, **kwargs):
+    """``dmrg2`` (``src/mps/dmrg.jl:295-297``)."""
+    return dmrg(psi0, H, params, 2, **kwargs)
+
+
+def svd_truncate(blocks, maxdim=INT32_MAX, mindim=1, cutoff=None, ctx: Context | None = None):
+    """Block SVD + ITensors-style global truncation on explicit dense blocks.
+
+    Returns (kept per block, singular values per block sorted descending, truncerr).
+    """
+    ctx = ctx or Context.default()
+    cutoff = Float64_threshold() if cutoff is None else cutoff
+    rows = np.array([b.shape[0] for b in blocks], dtype=np.int32)
+    cols = np.array([b.shape[1] for b in blocks], dtype=np.int32)
+    data = np.concatenate([np.asarray(b, dtype=np.float64).ravel(order="F") for b in blocks])
+    ns = np.minimum(rows, cols)
+    sv = np.zeros(int(ns.sum()))
+    kept = np.zeros(len(blocks), dtype=np.int32)
+    te = C.c_double()
+    L.check(ctx.lib.tn_svd_truncate(ctx.h, len(blocks), rows.ctypes.data_as(L.i32p),
+                                    cols.ctypes.data_as(L.i32p), data.ctypes.data_as(L.f64p),
+                                    int(min(maxdim, INT32_MAX)), int(mindim), float(cutoff),
+                                    kept.ctypes.data_as(L.i32p), sv.ctypes.data_as(L.f64p),
+                                    C.byref(te)))
+    out, o = [], 0
+    for n in ns:
+        out.append(sv[o:o + n].copy())
+        o += n
+    return kept, out, te.value

@@ -1,0 +1,1400 @@
+// Sweep engine: environments (ProjMPO restated), two-site effective Hamiltonian plans,
+// thick-restart Lanczos driver, block SVD truncation and the full sweep, behind the C ABI
+// of include/tennet.h.
+#include "engine.h"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+using namespace tn;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(const std::exception& e) {
+    g_err = e.what();
+    if (auto* te = dynamic_cast<const Error*>(&e)) return te->code;
+    return TN_E_INVALID;
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return TN_OK;
+    } catch (const std::bad_alloc&) {
+        g_err = "host allocation failed";
+        return TN_E_NOMEM;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// -------------------------------------------------------------------------------------
+// small dense helpers (host, FP64)
+// -------------------------------------------------------------------------------------
+
+// Eigen-decomposition of a small symmetric matrix (cyclic Jacobi), ascending order.
+// A is n x n row-major; on return D[n], U (row-major, columns = eigenvectors).
+void sym_eig(int n, std::vector<double> A, std::vector<double>& D, std::vector<double>& U) {
+    U.assign(size_t(n) * n, 0.0);
+    for (int i = 0; i < n; ++i) U[size_t(i) * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A[size_t(i) * n + j] * A[size_t(i) * n + j];
+                if (i != j) off += A[size_t(i) * n + j] * A[size_t(i) * n + j];
+            }
+        if (off <= 1e-34 * tot || off == 0.0) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[size_t(p) * n + q];
+                if (apq == 0.0) continue;
+                const double app = A[size_t(p) * n + p], aqq = A[size_t(q) * n + q];
+                const double theta = (aqq - app) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {  // A = J^T A J
+                    const double akp = A[size_t(k) * n + p], akq = A[size_t(k) * n + q];
+                    A[size_t(k) * n + p] = c * akp - s * akq;
+                    A[size_t(k) * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = A[size_t(p) * n + k], aqk = A[size_t(q) * n + k];
+                    A[size_t(p) * n + k] = c * apk - s * aqk;
+                    A[size_t(q) * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double ukp = U[size_t(k) * n + p], ukq = U[size_t(k) * n + q];
+                    U[size_t(k) * n + p] = c * ukp - s * ukq;
+                    U[size_t(k) * n + q] = s * ukp + c * ukq;
+                }
+            }
+    }
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int a, int b) { return A[size_t(a) * n + a] < A[size_t(b) * n + b]; });
+    D.resize(n);
+    std::vector<double> U2(size_t(n) * n);
+    for (int j = 0; j < n; ++j) {
+        D[j] = A[size_t(idx[j]) * n + idx[j]];
+        for (int i = 0; i < n; ++i) U2[size_t(i) * n + j] = U[size_t(i) * n + idx[j]];
+    }
+    U.swap(U2);
+}
+
+// ITensors truncate! restated: P sorted descending.  Returns kept count by rank, the
+// relative discarded weight and the cut value (per block, S^2 > docut is kept).
+struct TruncOut {
+    int n;
+    double truncerr, docut;
+};
+TruncOut truncation_rule(std::vector<double> P, int maxdim, int mindim, double cutoff) {
+    const int origm = (int)P.size();
+    for (int n = origm - 1; n >= 0; --n) {
+        if (P[n] >= 0) break;
+        P[n] = 0.0;
+    }
+    int n = origm;
+    double truncerr = 0.0;
+    while (n > maxdim) {
+        truncerr += P[n - 1];
+        --n;
+    }
+    double scale = 0.0;
+    for (double x : P) scale += x;
+    if (scale == 0.0) scale = 1.0;
+    while (n > mindim && truncerr + P[n - 1] <= cutoff * scale) {
+        truncerr += P[n - 1];
+        --n;
+    }
+    truncerr /= scale;
+    if (n < 1) n = 1;
+    double docut = 0.0;
+    if (n < origm) {
+        docut = 0.5 * (P[n - 1] + P[n]);
+        if (std::fabs(P[n - 1] - P[n]) < 1e-3 * P[n - 1]) docut += 1e-3 * P[n - 1];
+    }
+    return TruncOut{n, truncerr, docut};
+}
+
+void check_params(const tn_update_params* p) {
+    TN_REQUIRE(p != nullptr, "null update parameters");
+    TN_REQUIRE(p->maxdim >= 1 && p->mindim >= 1, "maxdim and mindim must be >= 1");
+    TN_REQUIRE(p->krylovdim >= 1 && p->krylovdim <= 31, "krylovdim must be in [1, 31]");
+    TN_REQUIRE(p->maxiter >= 1, "maxiter must be >= 1");
+    TN_REQUIRE(p->noise == 0.0,
+               "noise > 0 needs the density-matrix perturbation term, which this engine "
+               "does not build");
+}
+
+// -------------------------------------------------------------------------------------
+// environments
+// -------------------------------------------------------------------------------------
+void sync(tn_ctx* c) { TN_CUDA(cudaStreamSynchronize(c->stream)); }
+
+void make_trivial_env(tn_ctx* ctx, tn_envt& E, const Link& link, const std::vector<int>& delta) {
+    E.lay = make_env_layout(link, delta);
+    TN_REQUIRE(E.lay.size == 1, "boundary link and boundary MPO link must have dimension 1");
+    E.buf.alloc(sizeof(double), ctx->stream);
+    const double one = 1.0;
+    TN_CUDA(cudaMemcpyAsync(E.buf.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    TN_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+bool need_left(const tn_mpo* H, int site, int a, int s) {
+    for (int b = 0; b < H->wd[site + 1]; ++b)
+        for (int sp = 0; sp < H->d; ++sp)
+            if (H->at(site, a, b, sp, s) != 0.0) return true;
+    return false;
+}
+bool need_right(const tn_mpo* H, int site, int c, int s) {
+    for (int a = 0; a < H->wd[site]; ++a)
+        for (int sp = 0; sp < H->d; ++sp)
+            if (H->at(site, a, c, sp, s) != 0.0) return true;
+    return false;
+}
+
+// L[i+1] from L[i] and the left isometry at site i.
+void env_left_step(tn_env* env, int i) {
+    tn_ctx* ctx = env->ctx;
+    const tn_mpo* H = env->H;
+    const tn_site& A = env->psi->sites[i];
+    TN_REQUIRE(A.lay.layout == LG, "left environment needs a left-grouped site tensor");
+    const Link& lk = env->psi->links[i];
+    const Link& rk = env->psi->links[i + 1];
+    const int d = env->psi->d;
+    const EnvLayout& Lin = env->L[i].lay;
+    tn_envt& Lout = env->L[i + 1];
+    Lout.lay = make_env_layout(rk, H->delta[i + 1]);
+    const int wl = H->wd[i], wr = H->wd[i + 1];
+    // T1(a, il, s) = L(a, il) * A[s](l, r)
+    GemmPlan g1, g3;
+    CombPlan cb;
+    std::vector<int64_t> t1off(size_t(wl) * lk.nsec() * d, -1);
+    int64_t t1 = 0;
+    for (int ir = 0; ir < rk.nsec(); ++ir)
+        for (int s = 0; s < d; ++s) {
+            const int sub = A.lay.sub[size_t(ir) * d + s];
+            if (sub < 0) continue;
+            const int il = A.lay.subsec[size_t(ir) * d + s];
+            for (int a = 0; a < wl; ++a) {
+                const int64_t lo = Lin.off[size_t(a) * Lin.nsec + il];
+                if (lo < 0 || !need_left(H, i, a, s)) continue;
+                const int Db = lk.dim[Lin.bra[size_t(a) * Lin.nsec + il]];
+                const size_t key = (size_t(a) * lk.nsec() + il) * d + s;
+                t1off[key] = t1;
+                g1.add_task(S_T1, t1, Db, rk.dim[ir], Db);
+                g1.add_seg(S_L, lo, Db, 0, S_X, A.lay.off[ir] + sub, A.lay.rows[ir], 0, lk.dim[il]);
+                t1 += int64_t(Db) * rk.dim[ir];
+            }
+        }
+    // T2(b, ir): rows = rows of A block r' (r' = r + delta_b), cols D_r
+    std::vector<int64_t> t2off(size_t(wr) * rk.nsec(), -1);
+    int64_t t2 = 0;
+    for (int b = 0; b < wr; ++b)
+        for (int ir = 0; ir < rk.nsec(); ++ir) {
+            const int64_t oo = Lout.lay.off[size_t(b) * rk.nsec() + ir];
+            if (oo < 0) continue;
+            const int irp = Lout.lay.bra[size_t(b) * rk.nsec() + ir];
+            const int rowsA = A.lay.rows[irp];
+            t2off[size_t(b) * rk.nsec() + ir] = t2;
+            for (int sp = 0; sp < d; ++sp) {
+                const int sub = A.lay.sub[size_t(irp) * d + sp];
+                if (sub < 0) continue;
+                const int ilpp = A.lay.subsec[size_t(irp) * d + sp];
+                CombOut o;
+                o.doff = t2 + sub;
+                o.dbuf = S_T2;
+                o.ldd = rowsA;
+                o.rows = lk.dim[ilpp];
+                o.cols = rk.dim[ir];
+                o.t0 = (int)cb.terms.size();
+                o.nt = 0;
+                for (int a = 0; a < wl; ++a)
+                    for (int s = 0; s < d; ++s) {
+                        const double w = H->at(i, a, b, sp, s);
+                        if (w == 0.0) continue;
+                        if (A.lay.sub[size_t(ir) * d + s] < 0) continue;
+                        const int il = A.lay.subsec[size_t(ir) * d + s];
+                        const size_t key = (size_t(a) * lk.nsec() + il) * d + s;
+                        if (t1off[key] < 0) continue;
+                        if (Lin.bra[size_t(a) * Lin.nsec + il] != ilpp) continue;
+                        cb.terms.push_back(CombTerm{t1off[key], S_T1, lk.dim[ilpp], w});
+                        o.nt++;
+                    }
+                cb.flops += 2.0 * o.nt * double(o.rows) * o.cols;
+                cb.outs.push_back(o);
+            }
+            const int Drp = rk.dim[irp];
+            g3.add_task(S_Y, oo, Drp, rk.dim[ir], Drp);
+            g3.add_seg(S_X, A.lay.off[irp], rowsA, 1, S_T2, t2, rowsA, 0, rowsA);
+            t2 += int64_t(rowsA) * rk.dim[ir];
+        }
+    cudaStream_t st = ctx->stream;
+    g1.finalize(st);
+    g3.finalize(st);
+    cb.finalize(st);
+    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8, st);
+    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8, st);
+    Lout.buf.alloc(size_t(std::max<int64_t>(Lout.lay.size, 1)) * 8, st);
+    Bases bs{};
+    bs.p[S_L] = env->L[i].buf.d();
+    bs.p[S_X] = A.buf.d();
+    bs.p[S_T1] = env->t1.d();
+    bs.p[S_T2] = env->t2.d();
+    bs.p[S_Y] = Lout.buf.d();
+    const int e0 = ctx->timer.mark();
+    launch_gemm_f64(g1, bs, st);
+    launch_combine(cb, bs, st);
+    launch_gemm_f64(g3, bs, st);
+    ctx->timer.add(T_ENV, e0, ctx->timer.mark());
+}
+
+// R[i-1] from R[i] and the right isometry at site i.
+void env_right_step(tn_env* env, int i) {
+    tn_ctx* ctx = env->ctx;
+    const tn_mpo* H = env->H;
+    const tn_site& B = env->psi->sites[i];
+    TN_REQUIRE(B.lay.layout == RG, "right environment needs a right-grouped site tensor");
+    const Link& lk = env->psi->links[i];
+    const Link& rk = env->psi->links[i + 1];
+    const int d = env->psi->d;
+    const EnvLayout& Rin = env->R[i].lay;
+    tn_envt& Rout = env->R[i - 1];
+    Rout.lay = make_env_layout(lk, H->delta[i]);
+    const int wl = H->wd[i], wr = H->wd[i + 1];
+    GemmPlan g1, g3;
+    CombPlan cb;
+    // T1(c, ir, s) = R(c, ir) * B[s](l, r)^T : D_r' x D_l
+    std::vector<int64_t> t1off(size_t(wr) * rk.nsec() * d, -1);
+    int64_t t1 = 0;
+    for (int il = 0; il < lk.nsec(); ++il)
+        for (int s = 0; s < d; ++s) {
+            const int sub = B.lay.sub[size_t(il) * d + s];
+            if (sub < 0) continue;
+            const int ir = B.lay.subsec[size_t(il) * d + s];
+            for (int c = 0; c < wr; ++c) {
+                const int64_t ro = Rin.off[size_t(c) * Rin.nsec + ir];
+                if (ro < 0 || !need_right(H, i, c, s)) continue;
+                const int Db = rk.dim[Rin.bra[size_t(c) * Rin.nsec + ir]];
+                const size_t key = (size_t(c) * rk.nsec() + ir) * d + s;
+                t1off[key] = t1;
+                g1.add_task(S_T1, t1, Db, lk.dim[il], Db);
+                g1.add_seg(S_R, ro, Db, 0, S_X, B.lay.off[il] + int64_t(sub) * lk.dim[il],
+                           lk.dim[il], 1, rk.dim[ir]);
+                t1 += int64_t(Db) * lk.dim[il];
+            }
+        }
+    int64_t t2 = 0;
+    for (int a = 0; a < wl; ++a)
+        for (int il = 0; il < lk.nsec(); ++il) {
+            const int64_t oo = Rout.lay.off[size_t(a) * lk.nsec() + il];
+            if (oo < 0) continue;
+            const int ilp = Rout.lay.bra[size_t(a) * lk.nsec() + il];
+            const int colsB = B.lay.cols[ilp];
+            for (int sp = 0; sp < d; ++sp) {
+                const int sub = B.lay.sub[size_t(ilp) * d + sp];
+                if (sub < 0) continue;
+                const int irpp = B.lay.subsec[size_t(ilp) * d + sp];
+                CombOut o;
+                o.doff = t2 + sub;
+                o.dbuf = S_T2;
+                o.ldd = colsB;
+                o.rows = rk.dim[irpp];
+                o.cols = lk.dim[il];
+                o.t0 = (int)cb.terms.size();
+                o.nt = 0;
+                for (int c = 0; c < wr; ++c)
+                    for (int s = 0; s < d; ++s) {
+                        const double w = H->at(i, a, c, sp, s);
+                        if (w == 0.0) continue;
+                        if (B.lay.sub[size_t(il) * d + s] < 0) continue;
+                        const int ir = B.lay.subsec[size_t(il) * d + s];
+                        const size_t key = (size_t(c) * rk.nsec() + ir) * d + s;
+                        if (t1off[key] < 0) continue;
+                        if (Rin.bra[size_t(c) * Rin.nsec + ir] != irpp) continue;
+                        cb.terms.push_back(CombTerm{t1off[key], S_T1, rk.dim[irpp], w});
+                        o.nt++;
+                    }
+                cb.flops += 2.0 * o.nt * double(o.rows) * o.cols;
+                cb.outs.push_back(o);
+            }
+            const int Dlp = lk.dim[ilp];
+            g3.add_task(S_Y, oo, Dlp, lk.dim[il], Dlp);
+            g3.add_seg(S_X, B.lay.off[ilp], Dlp, 0, S_T2, t2, colsB, 0, colsB);
+            t2 += int64_t(colsB) * lk.dim[il];
+        }
+    cudaStream_t st = ctx->stream;
+    g1.finalize(st);
+    g3.finalize(st);
+    cb.finalize(st);
+    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8, st);
+    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8, st);
+    Rout.buf.alloc(size_t(std::max<int64_t>(Rout.lay.size, 1)) * 8, st);
+    Bases bs{};
+    bs.p[S_R] = env->R[i].buf.d();
+    bs.p[S_X] = B.buf.d();
+    bs.p[S_T1] = env->t1.d();
+    bs.p[S_T2] = env->t2.d();
+    bs.p[S_Y] = Rout.buf.d();
+    const int e0 = ctx->timer.mark();
+    launch_gemm_f64(g1, bs, st);
+    launch_combine(cb, bs, st);
+    launch_gemm_f64(g3, bs, st);
+    ctx->timer.add(T_ENV, e0, ctx->timer.mark());
+}
+
+void position(tn_env* env, int pos, int nsite) {
+    const int N = env->psi->N;
+    TN_REQUIRE(nsite == 2, "this engine builds the two-site effective Hamiltonian only");
+    TN_REQUIRE(pos >= 0 && pos + nsite - 1 < N, "position out of range");
+    while (env->lpos < pos) {
+        env_left_step(env, env->lpos);
+        env->lpos++;
+    }
+    env->lpos = pos;
+    const int last = pos + nsite - 1;
+    while (env->rpos > last) {
+        env_right_step(env, env->rpos);
+        env->rpos--;
+    }
+    env->rpos = last;
+    if (env->pos != pos || env->nsite != nsite) env->hp_pos = -1;
+    env->pos = pos;
+    env->nsite = nsite;
+}
+
+// -------------------------------------------------------------------------------------
+// two-site effective Hamiltonian
+// -------------------------------------------------------------------------------------
+std::unique_ptr<Heff2Plan> build_heff2(tn_env* env, int p) {
+    auto P = std::make_unique<Heff2Plan>();
+    const tn_mpo* H = env->H;
+    const tn_mps* psi = env->psi.get();
+    const int d = psi->d;
+    const Link& lk = psi->links[p];
+    const Link& rk = psi->links[p + 2];
+    const EnvLayout& Lin = env->L[p].lay;
+    const EnvLayout& Rin = env->R[p + 1].lay;
+    P->ph = make_phi_layout(lk, rk, psi->pq);
+    const PhiLayout& ph = P->ph;
+    const int w0 = H->wd[p], w1 = H->wd[p + 1], w2 = H->wd[p + 2];
+    // step 1: Y(a, il, s1) = L(a, il) * phi[rows (s1, l) of block m]
+    std::vector<int64_t> yoff(size_t(w0) * lk.nsec() * d, -1);
+    int64_t y = 0;
+    for (int mi = 0; mi < ph.nblk(); ++mi)
+        for (int s1 = 0; s1 < d; ++s1) {
+            const int rs = ph.rsub[size_t(mi) * d + s1];
+            if (rs < 0) continue;
+            const int il = ph.rsec[size_t(mi) * d + s1];
+            for (int a = 0; a < w0; ++a) {
+                const int64_t lo = Lin.off[size_t(a) * Lin.nsec + il];
+                if (lo < 0 || !need_left(H, p, a, s1)) continue;
+                const int Db = lk.dim[Lin.bra[size_t(a) * Lin.nsec + il]];
+                yoff[(size_t(a) * lk.nsec() + il) * d + s1] = y;
+                P->g1.add_task(S_T1, y, Db, ph.cols[mi], Db);
+                P->g1.add_seg(S_L, lo, Db, 0, S_X, ph.off[mi] + rs, ph.rows[mi], 0, lk.dim[il]);
+                y += int64_t(Db) * ph.cols[mi];
+            }
+        }
+    // two-site MPO G[a, c](s1' s2', s1 s2) = sum_b W1[a,b,s1',s1] W2[b,c,s2',s2]
+    auto G = [&](int a, int c, int s1p, int s2p, int s1, int s2) {
+        double g = 0.0;
+        for (int b = 0; b < w1; ++b) {
+            const double x = H->at(p, a, b, s1p, s1);
+            if (x == 0.0) continue;
+            g += x * H->at(p + 1, b, c, s2p, s2);
+        }
+        return g;
+    };
+    // step 2/3: Z(c, mo, s2') then out[mo][:, cols (s2', r')] = sum_c Z * R(c)^T
+    int64_t z = 0;
+    for (int mo = 0; mo < ph.nblk(); ++mo)
+        for (int s2p = 0; s2p < d; ++s2p) {
+            const int cs = ph.csub[size_t(mo) * d + s2p];
+            if (cs < 0) continue;
+            const int irp = ph.csec[size_t(mo) * d + s2p];
+            P->g3.add_task(S_Y, ph.off[mo] + int64_t(cs) * ph.rows[mo], ph.rows[mo], rk.dim[irp],
+                           ph.rows[mo]);
+            struct PendingSeg { int64_t zo; int64_t ro; int Drp, Dr; };
+            std::vector<PendingSeg> segs;
+            for (int c = 0; c < w2; ++c) {
+                const int ir = rk.find(rk.q[irp] - H->delta[p + 2][c]);
+                if (ir < 0) continue;
+                const int64_t ro = Rin.off[size_t(c) * Rin.nsec + ir];
+                if (ro < 0 || Rin.bra[size_t(c) * Rin.nsec + ir] != irp) continue;
+                const int Dr = rk.dim[ir];
+                // Z block: rows(mo) x Dr; one combine output per row slab s1'
+                bool nonzero = false;
+                const size_t out0 = P->cb.outs.size();
+                for (int s1p = 0; s1p < d; ++s1p) {
+                    const int rs = ph.rsub[size_t(mo) * d + s1p];
+                    if (rs < 0) continue;
+                    const int ilp = ph.rsec[size_t(mo) * d + s1p];
+                    CombOut o;
+                    o.doff = z + rs;
+                    o.dbuf = S_T2;
+                    o.ldd = ph.rows[mo];
+                    o.rows = lk.dim[ilp];
+                    o.cols = Dr;
+                    o.t0 = (int)P->cb.terms.size();
+                    o.nt = 0;
+                    for (int a = 0; a < w0; ++a) {
+                        const int il = lk.find(lk.q[ilp] - H->delta[p][a]);
+                        if (il < 0) continue;
+                        for (int s1 = 0; s1 < d; ++s1) {
+                            const int64_t yo = yoff[(size_t(a) * lk.nsec() + il) * d + s1];
+                            if (yo < 0) continue;
+                            if (Lin.bra[size_t(a) * Lin.nsec + il] != ilp) continue;
+                            const int mi = ph.find(lk.q[il] + psi->pq[s1]);
+                            if (mi < 0) continue;
+                            for (int s2 = 0; s2 < d; ++s2) {
+                                const int csub = ph.csub[size_t(mi) * d + s2];
+                                if (csub < 0 || ph.csec[size_t(mi) * d + s2] != ir) continue;
+                                const double g = G(a, c, s1p, s2p, s1, s2);
+                                if (g == 0.0) continue;
+                                P->cb.terms.push_back(
+                                    CombTerm{yo + int64_t(csub) * lk.dim[ilp], S_T1, lk.dim[ilp], g});
+                                o.nt++;
+                            }
+                        }
+                    }
+                    if (o.nt > 0) nonzero = true;
+                    P->cb.flops += 2.0 * o.nt * double(o.rows) * o.cols;
+                    P->cb.outs.push_back(o);
+                }
+                if (!nonzero) {  // this c contributes nothing: drop its Z block
+                    P->cb.terms.resize(P->cb.outs[out0].t0);
+                    P->cb.outs.resize(out0);
+                    continue;
+                }
+                segs.push_back(PendingSeg{z, ro, rk.dim[irp], Dr});
+                z += int64_t(ph.rows[mo]) * Dr;
+            }
+            for (const auto& sg : segs)
+                P->g3.add_seg(S_T2, sg.zo, ph.rows[mo], 0, S_R, sg.ro, sg.Drp, 1, sg.Dr);
+        }
+    cudaStream_t st = env->ctx->stream;
+    P->g1.finalize(st);
+    P->g3.finalize(st);
+    P->cb.finalize(st);
+    P->ysize = y;
+    P->zsize = z;
+    P->flops = P->g1.flops + P->g3.flops + P->cb.flops;
+    return P;
+}
+
+Heff2Plan& heff_plan(tn_env* env) {
+    if (env->hp_pos != env->pos || !env->hp) {
+        env->hp = build_heff2(env, env->pos);
+        env->hp_pos = env->pos;
+        cudaStream_t st = env->ctx->stream;
+        env->t1.alloc(size_t(std::max<int64_t>(env->hp->ysize, 1)) * 8, st);
+        env->t2.alloc(size_t(std::max<int64_t>(env->hp->zsize, 1)) * 8, st);
+    }
+    return *env->hp;
+}
+
+void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
+    tn_ctx* ctx = env->ctx;
+    Bases bs{};
+    bs.p[S_L] = env->L[env->pos].buf.d();
+    bs.p[S_R] = env->R[env->pos + 1].buf.d();
+    bs.p[S_X] = const_cast<double*>(x);
+    bs.p[S_Y] = y;
+    bs.p[S_T1] = env->t1.d();
+    bs.p[S_T2] = env->t2.d();
+    const int e0 = ctx->timer.mark();
+    launch_gemm_f64(P.g1, bs, ctx->stream);
+    launch_combine(P.cb, bs, ctx->stream);
+    launch_gemm_f64(P.g3, bs, ctx->stream);
+    ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+    env->matvecs++;
+    env->heff_flops += P.flops;
+}
+
+// phi = site p * site p+1 in the phi layout
+void form_phi(tn_env* env, int p, const PhiLayout& ph, double* out) {
+    tn_mps* psi = env->psi.get();
+    const tn_site& X = psi->sites[p];
+    const tn_site& Y = psi->sites[p + 1];
+    const Link& mk = psi->links[p + 1];
+    const Link& lk = psi->links[p];
+    const int d = psi->d;
+    GemmPlan g;
+    for (int mi = 0; mi < ph.nblk(); ++mi) {
+        const int im = mk.find(ph.m[mi]);
+        if (X.lay.layout == RG && Y.lay.layout == RG) {
+            for (int s1 = 0; s1 < d; ++s1) {
+                const int rs = ph.rsub[size_t(mi) * d + s1];
+                if (rs < 0) continue;
+                const int il = ph.rsec[size_t(mi) * d + s1];
+                g.add_task(S_Y, ph.off[mi] + rs, lk.dim[il], ph.cols[mi], ph.rows[mi]);
+                if (im < 0) continue;
+                const int sub = X.lay.sub[size_t(il) * d + s1];
+                if (sub < 0) continue;
+                TN_REQUIRE(Y.lay.cols[im] == ph.cols[mi], "phi column layout mismatch");
+                g.add_seg(S_A, X.lay.off[il] + int64_t(sub) * lk.dim[il], lk.dim[il], 0, S_B,
+                          Y.lay.off[im], mk.dim[im], 0, mk.dim[im]);
+            }
+        } else if (X.lay.layout == LG && Y.lay.layout == LG) {
+            const Link& rk = psi->links[p + 2];
+            for (int s2 = 0; s2 < d; ++s2) {
+                const int cs = ph.csub[size_t(mi) * d + s2];
+                if (cs < 0) continue;
+                const int ir = ph.csec[size_t(mi) * d + s2];
+                g.add_task(S_Y, ph.off[mi] + int64_t(cs) * ph.rows[mi], ph.rows[mi], rk.dim[ir],
+                           ph.rows[mi]);
+                if (im < 0) continue;
+                const int sub = Y.lay.sub[size_t(ir) * d + s2];
+                if (sub < 0) continue;
+                TN_REQUIRE(X.lay.rows[im] == ph.rows[mi], "phi row layout mismatch");
+                g.add_seg(S_A, X.lay.off[im], ph.rows[mi], 0, S_B, Y.lay.off[ir] + sub,
+                          Y.lay.rows[ir], 0, mk.dim[im]);
+            }
+        } else if (X.lay.layout == LG && Y.lay.layout == RG) {
+            g.add_task(S_Y, ph.off[mi], ph.rows[mi], ph.cols[mi], ph.rows[mi]);
+            if (im < 0) continue;
+            g.add_seg(S_A, X.lay.off[im], ph.rows[mi], 0, S_B, Y.lay.off[im], mk.dim[im], 0,
+                      mk.dim[im]);
+        } else {
+            throw Error(TN_E_INVALID, "two-site tensor needs the orthogonality center on the bond");
+        }
+    }
+    g.finalize(env->ctx->stream);
+    Bases bs{};
+    bs.p[S_A] = X.buf.d();
+    bs.p[S_B] = Y.buf.d();
+    bs.p[S_Y] = out;
+    launch_gemm_f64(g, bs, env->ctx->stream);
+}
+
+// -------------------------------------------------------------------------------------
+// Lanczos (thick restart, full re-orthogonalisation), KrylovKit eigsolve semantics
+// -------------------------------------------------------------------------------------
+struct EigOut {
+    double energy;
+    int matvecs, converged;
+};
+
+EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
+                      const tn_update_params* prm) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    const int64_t n = P.ph.size;
+    const int kd = prm->krylovdim;
+    // vector pool: kd basis + kd restart + 1 residual
+    const int nvec = 2 * kd + 1;
+    env->kry.alloc(size_t(nvec) * size_t(std::max<int64_t>(n, 1)) * 8, st);
+    env->part.alloc(size_t(32) * blas_nparts() * 8, st);
+    env->dots.alloc(128 * 8, st);
+    std::vector<double*> pool;
+    for (int i = 0; i < nvec; ++i) pool.push_back(env->kry.d() + int64_t(i) * n);
+    double* dv = env->dots.d();
+    std::vector<double*> V;
+    double* w = pool.back();
+    pool.pop_back();
+    auto take = [&]() {
+        TN_REQUIRE(!pool.empty(), "internal: Krylov vector pool exhausted");
+        double* q = pool.back();
+        pool.pop_back();
+        return q;
+    };
+    EigOut out{0.0, 0, 0};
+    std::vector<double> hostd(65);
+
+    auto gs2 = [&](int K, std::vector<double>& h, double& beta) {
+        // h = V^T w ; w -= V h ; twice ; beta = |w|
+        const int e0 = ctx->timer.mark();
+        launch_multi_dot(V.data(), K, w, n, env->part.d(), dv, st);
+        launch_multi_axpy(w, V.data(), K, dv, -1.0, n, st);
+        launch_multi_dot(V.data(), K, w, n, env->part.d(), dv + 32, st);
+        launch_multi_axpy(w, V.data(), K, dv + 32, -1.0, n, st);
+        const double* wp = w;
+        launch_multi_dot(&wp, 1, w, n, env->part.d(), dv + 64, st);
+        ctx->timer.add(T_LANCZOS, e0, ctx->timer.mark());
+        TN_CUDA(cudaMemcpyAsync(hostd.data(), dv, 65 * 8, cudaMemcpyDeviceToHost, st));
+        sync(ctx);
+        h.resize(K);
+        for (int i = 0; i < K; ++i) h[i] = hostd[i] + hostd[32 + i];
+        beta = std::sqrt(std::max(hostd[64], 0.0));
+    };
+
+    // normalise x0 into V[0]
+    {
+        const double* xp = x0;
+        launch_multi_dot(&xp, 1, x0, n, env->part.d(), dv + 64, st);
+        double nrm2 = 0;
+        TN_CUDA(cudaMemcpyAsync(&nrm2, dv + 64, 8, cudaMemcpyDeviceToHost, st));
+        sync(ctx);
+        TN_REQUIRE(nrm2 > 0.0, "eigensolver start vector is zero");
+        double* v0 = take();
+        launch_scale_into(v0, x0, nullptr, 1.0 / std::sqrt(nrm2), n, st);
+        V.push_back(v0);
+    }
+    std::vector<double> Hm(size_t(kd + 1) * (kd + 1), 0.0);
+    auto Hat = [&](int i, int j) -> double& { return Hm[size_t(i) * (kd + 1) + j]; };
+    std::vector<double> h;
+    double beta = 0.0;
+    heff_apply(env, P, V[0], w);
+    out.matvecs++;
+    gs2(1, h, beta);
+    Hat(0, 0) = h[0];
+    int numiter = 1;
+    std::vector<double> D, U;
+    int converged = 0;
+    while (true) {
+        const int K = (int)V.size();
+        // K >= n: the Krylov space spans the whole vector space, the Ritz pair is exact
+        const bool exhausted = int64_t(K) >= n;
+        if (K == kd || beta <= prm->tol || (prm->eager && K >= 1) || exhausted) {
+            std::vector<double> A(size_t(K) * K);
+            for (int i = 0; i < K; ++i)
+                for (int j = 0; j < K; ++j) A[size_t(i) * K + j] = 0.5 * (Hat(i, j) + Hat(j, i));
+            sym_eig(K, A, D, U);
+            converged = 0;
+            while (converged < K && std::fabs(beta * U[size_t(K - 1) * K + converged]) <= prm->tol)
+                converged++;
+            if (converged >= 1 || exhausted) break;
+        }
+        if (K < kd) {
+            double* v = take();
+            launch_scale_into(v, w, nullptr, 1.0 / beta, n, st);
+            V.push_back(v);
+            heff_apply(env, P, v, w);
+            out.matvecs++;
+            gs2(K + 1, h, beta);
+            for (int i = 0; i <= K; ++i) {
+                Hat(i, K) = h[i];
+                Hat(K, i) = h[i];
+            }
+        } else {
+            if (numiter == prm->maxiter) break;
+            const int keep = (3 * kd + 2 * converged) / 5;
+            std::vector<double*> NV;
+            for (int j = 0; j < keep; ++j) {
+                double* q = take();
+                std::vector<double> coef(K);
+                for (int i = 0; i < K; ++i) coef[i] = U[size_t(i) * K + j];
+                TN_CUDA(cudaMemcpyAsync(dv + 96, coef.data(), K * 8, cudaMemcpyHostToDevice, st));
+                launch_lincomb(q, V.data(), K, dv + 96, n, st);
+                sync(ctx);  // coef staging slot is reused
+                NV.push_back(q);
+            }
+            for (double* q : V) pool.push_back(q);
+            V = NV;
+            std::fill(Hm.begin(), Hm.end(), 0.0);
+            for (int j = 0; j < keep; ++j) Hat(j, j) = D[j];
+            numiter++;
+        }
+    }
+    // Ritz vector of the lowest value, normalised
+    const int K = (int)V.size();
+    std::vector<double> coef(K);
+    for (int i = 0; i < K; ++i) coef[i] = U[size_t(i) * K + 0];
+    TN_CUDA(cudaMemcpyAsync(dv + 96, coef.data(), K * 8, cudaMemcpyHostToDevice, st));
+    launch_lincomb(result, V.data(), K, dv + 96, n, st);
+    const double* rp = result;
+    launch_multi_dot(&rp, 1, result, n, env->part.d(), dv + 64, st);
+    launch_scale_into(result, result, dv + 64, 1.0, n, st);
+    sync(ctx);
+    out.energy = D[0];
+    out.converged = converged;
+    return out;
+}
+
+// -------------------------------------------------------------------------------------
+// block SVD + truncation
+// -------------------------------------------------------------------------------------
+struct SvdResult {
+    std::vector<SvdBlockDesc> desc;
+    std::vector<double> S;  // sorted per block at desc.s_off
+    int64_t total_n = 0;
+};
+
+// SVD of the listed blocks of src (device); results stay in the env work buffers.
+void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dV, DevBuf& dS, DevBuf& dP, DevBuf& ddesc,
+               const std::vector<int>& rows, const std::vector<int>& cols,
+               const std::vector<int64_t>& offs, const double* src, SvdResult& R) {
+    cudaStream_t st = ctx->stream;
+    R.desc.clear();
+    int64_t xo = 0, vo = 0, so = 0;
+    int maxn = 1;
+    for (size_t b = 0; b < rows.size(); ++b) {
+        SvdBlockDesc d{};
+        d.src_off = offs[b];
+        d.rows = rows[b];
+        d.cols = cols[b];
+        d.trans = rows[b] < cols[b] ? 1 : 0;
+        d.m = std::max(rows[b], cols[b]);
+        d.n = std::min(rows[b], cols[b]);
+        d.x_off = xo;
+        d.v_off = vo;
+        d.s_off = so;
+        xo += int64_t(d.m) * d.n;
+        vo += int64_t(d.n) * d.n;
+        so += d.n;
+        maxn = std::max(maxn, d.n);
+        R.desc.push_back(d);
+    }
+    R.total_n = so;
+    const int nb = (int)R.desc.size();
+    dX.alloc(size_t(std::max<int64_t>(xo, 1)) * 8, st);
+    dV.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
+    dS.alloc(size_t(std::max<int64_t>(so, 1)) * 8, st);
+    dP.alloc(size_t(std::max<int64_t>(so, 1)) * 4, st);
+    ddesc.alloc(std::max<size_t>(size_t(nb) * sizeof(SvdBlockDesc), 16), st);
+    if (nb)
+        TN_CUDA(cudaMemcpyAsync(ddesc.p, R.desc.data(), nb * sizeof(SvdBlockDesc),
+                                cudaMemcpyHostToDevice, st));
+    const int e0 = ctx->timer.mark();
+    launch_svd_prepare(ddesc.as<SvdBlockDesc>(), nb, src, dX.d(), dV.d(), st);
+    launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nb, maxn, dX.d(), dV.d(), dS.d(), dP.as<int>(),
+                      nullptr, st);
+    ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    R.S.resize(size_t(so));
+    if (so)
+        TN_CUDA(cudaMemcpyAsync(R.S.data(), dS.p, size_t(so) * 8, cudaMemcpyDeviceToHost, st));
+    sync(ctx);
+}
+
+struct TruncDecision {
+    std::vector<int> kept;
+    double truncerr = 0, norm = 1;
+    std::vector<double> eigs;
+};
+
+TruncDecision decide(const SvdResult& R, int maxdim, int mindim, double cutoff) {
+    std::vector<double> P;
+    P.reserve(R.S.size());
+    for (double s : R.S) P.push_back(s * s);
+    std::sort(P.begin(), P.end(), std::greater<double>());
+    TruncOut t = truncation_rule(P, maxdim, mindim, cutoff);
+    TruncDecision D;
+    D.truncerr = t.truncerr;
+    D.kept.assign(R.desc.size(), 0);
+    int total = 0;
+    for (size_t b = 0; b < R.desc.size(); ++b) {
+        const auto& d = R.desc[b];
+        int k = 0;
+        while (k < d.n && R.S[d.s_off + k] * R.S[d.s_off + k] > t.docut) ++k;
+        D.kept[b] = k;
+        total += k;
+    }
+    if (total == 0 && !R.desc.empty()) {
+        // every value fell under the cut (fully degenerate spectrum at maxdim): keep the
+        // largest so that the link never becomes empty.
+        size_t best = 0;
+        double bv = -1;
+        for (size_t b = 0; b < R.desc.size(); ++b)
+            if (R.desc[b].n > 0 && R.S[R.desc[b].s_off] > bv) {
+                bv = R.S[R.desc[b].s_off];
+                best = b;
+            }
+        D.kept[best] = 1;
+    }
+    double nrm2 = 0;
+    for (size_t b = 0; b < R.desc.size(); ++b)
+        for (int k = 0; k < D.kept[b]; ++k) {
+            const double s = R.S[R.desc[b].s_off + k];
+            nrm2 += s * s;
+            D.eigs.push_back(s * s);
+        }
+    std::sort(D.eigs.begin(), D.eigs.end(), std::greater<double>());
+    D.norm = std::sqrt(nrm2);
+    return D;
+}
+
+// replacebond!: SVD of phi (phi layout ph, device), truncation, new site tensors p, p+1.
+void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
+                  const tn_update_params* prm, int ortho, tn_update_result* res,
+                  std::vector<double>& eigs) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    tn_mps* psi = env->psi.get();
+    SvdResult R;
+    block_svd(ctx, env->svdX, env->svdV, env->svdS, env->svdP, env->desc, ph.rows, ph.cols,
+              ph.off, phi, R);
+    TruncDecision D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
+    Link nl;
+    for (int b = 0; b < ph.nblk(); ++b)
+        if (D.kept[b] > 0) {
+            nl.q.push_back(ph.m[b]);
+            nl.dim.push_back(D.kept[b]);
+        }
+    const Link& lk = psi->links[p];
+    const Link& rk = psi->links[p + 2];
+    tn_site left, right;
+    left.lay = make_site_layout(LG, lk, nl, psi->pq);
+    right.lay = make_site_layout(RG, nl, rk, psi->pq);
+    left.buf.alloc(size_t(std::max<int64_t>(left.lay.size, 1)) * 8, st);
+    right.buf.alloc(size_t(std::max<int64_t>(right.lay.size, 1)) * 8, st);
+    std::vector<ExtractDesc> ed;
+    for (int b = 0, j = 0; b < ph.nblk(); ++b) {
+        if (D.kept[b] == 0) continue;
+        TN_REQUIRE(left.lay.rows[j] == ph.rows[b] && right.lay.cols[j] == ph.cols[b],
+                   "internal: SVD block layout mismatch");
+        ExtractDesc e{};
+        e.x_off = R.desc[b].x_off;
+        e.v_off = R.desc[b].v_off;
+        e.s_off = R.desc[b].s_off;
+        e.left_off = left.lay.off[j];
+        e.right_off = right.lay.off[j];
+        e.rows = ph.rows[b];
+        e.cols = ph.cols[b];
+        e.n = R.desc[b].n;
+        e.trans = R.desc[b].trans;
+        e.k = D.kept[b];
+        ed.push_back(e);
+        ++j;
+    }
+    env->desc2.alloc(std::max<size_t>(ed.size() * sizeof(ExtractDesc), 16), st);
+    if (!ed.empty())
+        TN_CUDA(cudaMemcpyAsync(env->desc2.p, ed.data(), ed.size() * sizeof(ExtractDesc),
+                                cudaMemcpyHostToDevice, st));
+    const double inv = (prm->normalize && D.norm > 0) ? 1.0 / D.norm : 1.0;
+    const int e0 = ctx->timer.mark();
+    launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), 0, 0, env->svdX.d(),
+                       env->svdV.d(), env->svdS.d(), env->svdP.as<int>(), left.buf.d(),
+                       right.buf.d(), ortho, inv, st);
+    ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    psi->sites[p] = std::move(left);
+    psi->sites[p + 1] = std::move(right);
+    psi->links[p + 1] = nl;
+    psi->center = (ortho == TN_ORTHO_LEFT) ? p + 1 : p;
+    env->lpos = std::min(env->lpos, p);
+    env->rpos = std::max(env->rpos, p + 1);
+    env->hp_pos = -1;
+    res->truncerr = D.truncerr;
+    res->newdim = nl.total();
+    eigs = D.eigs;
+}
+
+void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
+                     tn_update_result* res, std::vector<double>& eigs) {
+    check_params(prm);
+    tn_mps* psi = env->psi.get();
+    TN_REQUIRE(p >= 0 && p < psi->N - 1, "bond position out of range");
+    TN_REQUIRE((ortho == TN_ORTHO_LEFT && psi->center == p) ||
+                   (ortho == TN_ORTHO_RIGHT && psi->center == p + 1),
+               "orthogonality center must be at pos (ortho left) or pos+1 (ortho right)");
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    position(env, p, 2);
+    Heff2Plan& P = heff_plan(env);
+    const int64_t n = P.ph.size;
+    env->vecA.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
+    env->vecB.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
+    form_phi(env, p, P.ph, env->vecA.d());
+    EigOut eo = lanczos_lowest(env, P, env->vecA.d(), env->vecB.d(), prm);
+    if (prm->check_convergence && eo.converged < 1)
+        throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
+    res->energy = eo.energy;
+    res->matvecs = eo.matvecs;
+    res->converged = eo.converged;
+    replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
+    res->neigs = (int)eigs.size();
+}
+
+std::unique_ptr<tn_mps> copy_mps(const tn_mps* src) {
+    auto m = std::make_unique<tn_mps>();
+    m->ctx = src->ctx;
+    m->N = src->N;
+    m->d = src->d;
+    m->pq = src->pq;
+    m->links = src->links;
+    m->center = src->center;
+    m->sites.resize(src->N);
+    for (int i = 0; i < src->N; ++i) {
+        m->sites[i].lay = src->sites[i].lay;
+        const size_t nb = size_t(std::max<int64_t>(src->sites[i].lay.size, 1)) * 8;
+        m->sites[i].buf.alloc(nb, src->ctx->stream);
+        TN_CUDA(cudaMemcpyAsync(m->sites[i].buf.p, src->sites[i].buf.p, nb,
+                                cudaMemcpyDeviceToDevice, src->ctx->stream));
+    }
+    return m;
+}
+
+// dense (Dl, d, Dr) column-major <-> site blocks
+void site_from_dense(const SiteLayout& lay, const Link& lk, const Link& rk, int d,
+                     const double* dense, std::vector<double>& blocks) {
+    blocks.assign(size_t(lay.size), 0.0);
+    const int Dl = lk.total();
+    auto lo = lk.offsets(), ro = rk.offsets();
+    std::vector<char> used(size_t(Dl) * d * rk.total(), 0);
+    for (int b = 0; b < lay.nblk(); ++b)
+        for (int s = 0; s < d; ++s) {
+            const int sub = lay.sub[size_t(b) * d + s];
+            if (sub < 0) continue;
+            const int oth = lay.subsec[size_t(b) * d + s];
+            const int il = (lay.layout == LG) ? oth : b;
+            const int ir = (lay.layout == LG) ? b : oth;
+            for (int r = 0; r < rk.dim[ir]; ++r)
+                for (int l = 0; l < lk.dim[il]; ++l) {
+                    const size_t di = size_t(lo[il] + l) + size_t(Dl) * (s + size_t(d) * (ro[ir] + r));
+                    used[di] = 1;
+                    size_t bi;
+                    if (lay.layout == LG) bi = lay.off[b] + (sub + l) + size_t(lay.rows[b]) * r;
+                    else bi = lay.off[b] + l + size_t(lay.rows[b]) * (sub + r);
+                    blocks[bi] = dense[di];
+                }
+        }
+    for (size_t i = 0; i < used.size(); ++i)
+        if (!used[i] && std::fabs(dense[i]) > 1e-12)
+            throw Error(TN_E_INVALID, "site tensor has weight outside its charge sectors");
+}
+
+void site_to_dense(const SiteLayout& lay, const Link& lk, const Link& rk, int d,
+                   const std::vector<double>& blocks, double* dense) {
+    const int Dl = lk.total();
+    auto lo = lk.offsets(), ro = rk.offsets();
+    std::fill(dense, dense + size_t(Dl) * d * rk.total(), 0.0);
+    for (int b = 0; b < lay.nblk(); ++b)
+        for (int s = 0; s < d; ++s) {
+            const int sub = lay.sub[size_t(b) * d + s];
+            if (sub < 0) continue;
+            const int oth = lay.subsec[size_t(b) * d + s];
+            const int il = (lay.layout == LG) ? oth : b;
+            const int ir = (lay.layout == LG) ? b : oth;
+            for (int r = 0; r < rk.dim[ir]; ++r)
+                for (int l = 0; l < lk.dim[il]; ++l) {
+                    const size_t di = size_t(lo[il] + l) + size_t(Dl) * (s + size_t(d) * (ro[ir] + r));
+                    size_t bi;
+                    if (lay.layout == LG) bi = lay.off[b] + (sub + l) + size_t(lay.rows[b]) * r;
+                    else bi = lay.off[b] + l + size_t(lay.rows[b]) * (sub + r);
+                    dense[di] = blocks[bi];
+                }
+        }
+}
+
+// dense two-site (Dl, d, d, Dr) <-> phi layout
+void phi_dense_map(const PhiLayout& ph, const Link& lk, const Link& rk, int d,
+                   std::vector<int64_t>& map) {
+    // map[block element] = dense index
+    map.assign(size_t(ph.size), -1);
+    const int Dl = lk.total();
+    auto lo = lk.offsets(), ro = rk.offsets();
+    for (int b = 0; b < ph.nblk(); ++b)
+        for (int s1 = 0; s1 < d; ++s1) {
+            const int rs = ph.rsub[size_t(b) * d + s1];
+            if (rs < 0) continue;
+            const int il = ph.rsec[size_t(b) * d + s1];
+            for (int s2 = 0; s2 < d; ++s2) {
+                const int cs = ph.csub[size_t(b) * d + s2];
+                if (cs < 0) continue;
+                const int ir = ph.csec[size_t(b) * d + s2];
+                for (int r = 0; r < rk.dim[ir]; ++r)
+                    for (int l = 0; l < lk.dim[il]; ++l) {
+                        const int64_t bi = ph.off[b] + (rs + l) + int64_t(ph.rows[b]) * (cs + r);
+                        const int64_t di = int64_t(lo[il] + l) +
+                                           int64_t(Dl) * (s1 + int64_t(d) * (s2 + int64_t(d) * (ro[ir] + r)));
+                        map[bi] = di;
+                    }
+            }
+        }
+}
+
+}  // namespace
+
+// -------------------------------------------------------------------------------------
+// EventTimer
+// -------------------------------------------------------------------------------------
+namespace tn {
+int EventTimer::mark() {
+    if (used == pool.size()) {
+        cudaEvent_t e;
+        TN_CUDA(cudaEventCreate(&e));
+        pool.push_back(e);
+    }
+    TN_CUDA(cudaEventRecord(pool[used], s));
+    return int(used++);
+}
+void EventTimer::collect(double* acc) {
+    for (const auto& iv : ivs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, pool[iv.a], pool[iv.b]) == cudaSuccess) acc[iv.cat] += ms;
+    }
+    ivs.clear();
+    used = 0;
+}
+EventTimer::~EventTimer() {
+    for (auto e : pool) cudaEventDestroy(e);
+}
+}  // namespace tn
+
+// -------------------------------------------------------------------------------------
+// C ABI
+// -------------------------------------------------------------------------------------
+extern "C" {
+
+const char* tn_last_error(void) { return g_err.c_str(); }
+const char* tn_version(void) { return "tennet-gb300 0.1 (sm_103a)"; }
+
+int tn_ctx_create(int device, tn_ctx** out) {
+    return guarded([&] {
+        TN_REQUIRE(out != nullptr, "null output handle");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0)
+            throw Error(TN_E_NOGPU, "no CUDA device " + std::to_string(device));
+        cudaDeviceProp pr;
+        TN_CUDA(cudaGetDeviceProperties(&pr, device));
+        if (!(pr.major == 10 && pr.minor == 3))
+            throw Error(TN_E_NOGPU, std::string("device is not sm_103 (GB300): ") + pr.name);
+        TN_CUDA(cudaSetDevice(device));
+        auto c = std::make_unique<tn_ctx>();
+        c->device = device;
+        TN_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->timer.s = c->stream;
+        cudaMemPool_t mp;
+        TN_CUDA(cudaDeviceGetDefaultMemPool(&mp, device));
+        uint64_t thr = UINT64_MAX;
+        TN_CUDA(cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &thr));
+        *out = c.release();
+    });
+}
+
+int tn_ctx_destroy(tn_ctx* ctx) {
+    return guarded([&] {
+        if (!ctx) return;
+        cudaStreamSynchronize(ctx->stream);
+        cudaStream_t s = ctx->stream;
+        delete ctx;
+        cudaStreamDestroy(s);
+    });
+}
+
+int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices) {
+    return guarded([&] {
+        TN_REQUIRE(ctx, "null context");
+        TN_REQUIRE(mode == TN_PREC_FP64 || mode == TN_PREC_SPLIT, "unknown precision mode");
+        TN_REQUIRE(slices >= 2 && slices <= 7, "slices must be in [2, 7]");
+        if (mode == TN_PREC_SPLIT)
+            throw Error(TN_E_INVALID, "split-precision contractions are not built in this library");
+        ctx->prec = mode;
+        ctx->slices = slices;
+    });
+}
+
+int tn_mpo_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q, const int32_t* wdims,
+                  const int32_t* wq, const double* W, tn_mpo** out) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && out && phys_q && wdims && wq && W, "null argument");
+        TN_REQUIRE(nsites >= 2 && d >= 1, "need at least two sites");
+        auto m = std::make_unique<tn_mpo>();
+        m->ctx = ctx;
+        m->N = nsites;
+        m->d = d;
+        m->pq.assign(phys_q, phys_q + d);
+        m->wd.assign(wdims, wdims + nsites + 1);
+        TN_REQUIRE(m->wd[0] == 1 && m->wd[nsites] == 1, "boundary MPO links must have dimension 1");
+        size_t qo = 0, wo = 0;
+        for (int i = 0; i <= nsites; ++i) {
+            TN_REQUIRE(m->wd[i] >= 1, "MPO link dimension must be >= 1");
+            m->delta.emplace_back(wq + qo, wq + qo + m->wd[i]);
+            qo += m->wd[i];
+        }
+        for (int i = 0; i < nsites; ++i) {
+            const size_t n = size_t(m->wd[i]) * m->wd[i + 1] * d * d;
+            m->W.emplace_back(W + wo, W + wo + n);
+            wo += n;
+            for (int a = 0; a < m->wd[i]; ++a)
+                for (int b = 0; b < m->wd[i + 1]; ++b)
+                    for (int sp = 0; sp < d; ++sp)
+                        for (int s = 0; s < d; ++s)
+                            if (m->at(i, a, b, sp, s) != 0.0 &&
+                                m->pq[sp] - m->pq[s] != m->delta[i + 1][b] - m->delta[i][a])
+                                throw Error(TN_E_INVALID, "MPO entry violates charge conservation at site " +
+                                                              std::to_string(i));
+        }
+        *out = m.release();
+    });
+}
+
+int tn_mpo_destroy(tn_mpo* mpo) {
+    delete mpo;
+    return TN_OK;
+}
+
+int tn_mps_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q, const int32_t* nsec,
+                  const int32_t* sec_q, const int32_t* sec_dim, const double* site_data,
+                  int center, tn_mps** out) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && out && phys_q && nsec && sec_q && sec_dim && site_data, "null argument");
+        TN_REQUIRE(nsites >= 2, "need at least two sites");
+        TN_REQUIRE(center >= 0 && center < nsites, "center out of range");
+        auto m = std::make_unique<tn_mps>();
+        m->ctx = ctx;
+        m->N = nsites;
+        m->d = d;
+        m->pq.assign(phys_q, phys_q + d);
+        m->center = center;
+        size_t so = 0;
+        for (int i = 0; i <= nsites; ++i) {
+            Link L;
+            for (int k = 0; k < nsec[i]; ++k) {
+                L.q.push_back(sec_q[so + k]);
+                L.dim.push_back(sec_dim[so + k]);
+                TN_REQUIRE(sec_dim[so + k] >= 1, "sector dimension must be >= 1");
+                if (k) TN_REQUIRE(sec_q[so + k] > sec_q[so + k - 1], "sectors must be sorted by charge");
+            }
+            so += nsec[i];
+            TN_REQUIRE(L.nsec() >= 1, "every link needs a sector");
+            m->links.push_back(L);
+        }
+        TN_REQUIRE(m->links[0].total() == 1 && m->links[nsites].total() == 1,
+                   "boundary links must have dimension 1");
+        m->sites.resize(nsites);
+        size_t off = 0;
+        std::vector<double> blocks;
+        for (int i = 0; i < nsites; ++i) {
+            const Link& lk = m->links[i];
+            const Link& rk = m->links[i + 1];
+            m->sites[i].lay = make_site_layout(i < center ? LG : RG, lk, rk, m->pq);
+            site_from_dense(m->sites[i].lay, lk, rk, d, site_data + off, blocks);
+            off += size_t(lk.total()) * d * rk.total();
+            m->sites[i].buf.alloc(std::max<size_t>(blocks.size(), 1) * 8, ctx->stream);
+            if (!blocks.empty())
+                TN_CUDA(cudaMemcpyAsync(m->sites[i].buf.p, blocks.data(), blocks.size() * 8,
+                                        cudaMemcpyHostToDevice, ctx->stream));
+            sync(ctx);
+        }
+        *out = m.release();
+    });
+}
+
+int tn_mps_destroy(tn_mps* mps) {
+    if (mps) cudaStreamSynchronize(mps->ctx->stream);
+    delete mps;
+    return TN_OK;
+}
+
+int tn_mps_link(const tn_mps* mps, int link, int32_t* nsec, int32_t* q, int32_t* dim, int cap) {
+    return guarded([&] {
+        TN_REQUIRE(mps && nsec, "null argument");
+        TN_REQUIRE(link >= 0 && link <= mps->N, "link out of range");
+        const Link& L = mps->links[link];
+        *nsec = L.nsec();
+        if (q || dim) {
+            TN_REQUIRE(cap >= L.nsec(), "capacity too small");
+            for (int k = 0; k < L.nsec(); ++k) {
+                if (q) q[k] = L.q[k];
+                if (dim) dim[k] = L.dim[k];
+            }
+        }
+    });
+}
+
+int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap) {
+    return guarded([&] {
+        TN_REQUIRE(mps && out, "null argument");
+        TN_REQUIRE(site >= 0 && site < mps->N, "site out of range");
+        const Link& lk = mps->links[site];
+        const Link& rk = mps->links[site + 1];
+        TN_REQUIRE(cap >= int64_t(lk.total()) * mps->d * rk.total(), "capacity too small");
+        const tn_site& S = mps->sites[site];
+        std::vector<double> blocks(size_t(S.lay.size));
+        if (!blocks.empty())
+            TN_CUDA(cudaMemcpyAsync(blocks.data(), S.buf.p, blocks.size() * 8,
+                                    cudaMemcpyDeviceToHost, mps->ctx->stream));
+        TN_CUDA(cudaStreamSynchronize(mps->ctx->stream));
+        site_to_dense(S.lay, lk, rk, mps->d, blocks, out);
+    });
+}
+
+int tn_mps_center(const tn_mps* mps) { return mps ? mps->center : TN_E_INVALID; }
+
+int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out) {
+    return guarded([&] {
+        TN_REQUIRE(psi && H && out, "null argument");
+        TN_REQUIRE(psi->N == H->N && psi->d == H->d && psi->pq == H->pq,
+                   "MPS and MPO site indices differ");
+        auto e = std::make_unique<tn_env>();
+        e->ctx = psi->ctx;
+        e->psi = copy_mps(psi);
+        e->H = H;
+        const int N = psi->N;
+        e->L.resize(N);
+        e->R.resize(N);
+        make_trivial_env(e->ctx, e->L[0], psi->links[0], H->delta[0]);
+        make_trivial_env(e->ctx, e->R[N - 1], psi->links[N], H->delta[N]);
+        e->lpos = 0;
+        e->rpos = N - 1;
+        e->pos = 0;
+        e->nsite = 2;
+        *out = e.release();
+    });
+}
+
+int tn_env_destroy(tn_env* env) {
+    if (env) cudaStreamSynchronize(env->ctx->stream);
+    delete env;
+    return TN_OK;
+}
+
+int tn_env_getpsi(tn_env* env, tn_mps** out) {
+    return guarded([&] {
+        TN_REQUIRE(env && out, "null argument");
+        auto m = copy_mps(env->psi.get());
+        sync(env->ctx);
+        *out = m.release();
+    });
+}
+
+int tn_env_position(tn_env* env, int pos, int nsite) {
+    return guarded([&] {
+        TN_REQUIRE(env, "null argument");
+        position(env, pos, nsite);
+        sync(env->ctx);
+        env->ctx->timer.collect(env->acc_ms);
+    });
+}
+
+int tn_env_product_flops(tn_env* env, double* flops) {
+    return guarded([&] {
+        TN_REQUIRE(env && flops, "null argument");
+        Heff2Plan& P = heff_plan(env);
+        *flops = P.flops;
+    });
+}
+
+int tn_env_product(tn_env* env, const double* v, double* out, int64_t n) {
+    return guarded([&] {
+        TN_REQUIRE(env && v && out, "null argument");
+        TN_REQUIRE(env->nsite == 2, "only nsite = 2 products are built");
+        const int p = env->pos;
+        position(env, p, 2);
+        Heff2Plan& P = heff_plan(env);
+        const tn_mps* psi = env->psi.get();
+        const Link& lk = psi->links[p];
+        const Link& rk = psi->links[p + 2];
+        const int64_t nd = int64_t(lk.total()) * psi->d * psi->d * rk.total();
+        TN_REQUIRE(n == nd, "dense two-site tensor has the wrong size");
+        std::vector<int64_t> map;
+        phi_dense_map(P.ph, lk, rk, psi->d, map);
+        std::vector<double> hb(size_t(P.ph.size));
+        for (size_t i = 0; i < hb.size(); ++i) hb[i] = v[map[i]];
+        cudaStream_t st = env->ctx->stream;
+        env->vecA.alloc(std::max<size_t>(hb.size(), 1) * 8, st);
+        env->vecB.alloc(std::max<size_t>(hb.size(), 1) * 8, st);
+        if (!hb.empty())
+            TN_CUDA(cudaMemcpyAsync(env->vecA.p, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
+        heff_apply(env, P, env->vecA.d(), env->vecB.d());
+        if (!hb.empty())
+            TN_CUDA(cudaMemcpyAsync(hb.data(), env->vecB.p, hb.size() * 8, cudaMemcpyDeviceToHost, st));
+        sync(env->ctx);
+        env->ctx->timer.collect(env->acc_ms);
+        std::fill(out, out + nd, 0.0);
+        for (size_t i = 0; i < hb.size(); ++i) out[map[i]] = hb[i];
+    });
+}
+
+int tn_env_update_position(tn_env* env, int pos, int ortho, const tn_update_params* p,
+                           tn_update_result* res, double* eigs, int eigs_cap) {
+    return guarded([&] {
+        TN_REQUIRE(env && res, "null argument");
+        TN_REQUIRE(ortho == TN_ORTHO_LEFT || ortho == TN_ORTHO_RIGHT, "ortho must be left or right");
+        std::vector<double> ev;
+        *res = tn_update_result{};
+        update_two_site(env, pos, ortho, p, res, ev);
+        if (eigs) {
+            const int k = std::min<int>(eigs_cap, (int)ev.size());
+            std::copy(ev.begin(), ev.begin() + k, eigs);
+        }
+        sync(env->ctx);
+        env->ctx->timer.collect(env->acc_ms);
+    });
+}
+
+int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res,
+                     double* mid_eigs, int mid_cap, int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(env && res, "null argument");
+        check_params(p);
+        tn_mps* psi = env->psi.get();
+        TN_REQUIRE(psi->center == 0, "fullsweep! needs the orthogonality center at site 1");
+        const int N = psi->N;
+        tn_ctx* ctx = env->ctx;
+        ctx->timer.collect(env->acc_ms);
+        double acc0[T_NCAT];
+        std::copy(env->acc_ms, env->acc_ms + T_NCAT, acc0);
+        const int64_t mv0 = env->matvecs;
+        const double fl0 = env->heff_flops;
+        *res = tn_sweep_result{};
+        const int es = ctx->timer.mark();
+        double maxerr = 0.0, energy = NAN;
+        std::vector<double> ev, mid;
+        for (int b = 0; b < N - 1; ++b) {
+            tn_update_result r{};
+            update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+        }
+        for (int b = N - 2; b >= 0; --b) {
+            tn_update_result r{};
+            update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+            if (b == N / 2 - 1) mid = ev;
+        }
+        ctx->timer.add(T_SWEEP, es, ctx->timer.mark());
+        sync(ctx);
+        ctx->timer.collect(env->acc_ms);
+        int maxd = 0;
+        for (const auto& L : psi->links) maxd = std::max(maxd, L.total());
+        res->energy = energy;
+        res->maxtruncerr = maxerr;
+        res->maxlinkdim = maxd;
+        res->matvecs = int32_t(env->matvecs - mv0);
+        res->heff_flops = env->heff_flops - fl0;
+        res->heff_ms = env->acc_ms[T_HEFF] - acc0[T_HEFF];
+        res->env_ms = env->acc_ms[T_ENV] - acc0[T_ENV];
+        res->svd_ms = env->acc_ms[T_SVD] - acc0[T_SVD];
+        res->lanczos_ms = env->acc_ms[T_LANCZOS] - acc0[T_LANCZOS];
+        res->sweep_ms = env->acc_ms[T_SWEEP] - acc0[T_SWEEP];
+        if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
+        if (mid_eigs) {
+            const int k = std::min<int>(mid_cap, (int)mid.size());
+            std::copy(mid.begin(), mid.begin() + k, mid_eigs);
+        }
+    });
+}
+
+int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t* cols,
+                    const double* data, int32_t maxdim, int32_t mindim, double cutoff,
+                    int32_t* kept, double* svals, double* truncerr) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && rows && cols && data && kept, "null argument");
+        TN_REQUIRE(nblocks >= 1, "need at least one block");
+        TN_REQUIRE(maxdim >= 1 && mindim >= 1, "maxdim and mindim must be >= 1");
+        std::vector<int> r(rows, rows + nblocks), c(cols, cols + nblocks);
+        std::vector<int64_t> offs(nblocks);
+        int64_t tot = 0;
+        for (int b = 0; b < nblocks; ++b) {
+            TN_REQUIRE(r[b] >= 1 && c[b] >= 1, "block dimensions must be >= 1");
+            offs[b] = tot;
+            tot += int64_t(r[b]) * c[b];
+        }
+        cudaStream_t st = ctx->stream;
+        DevBuf src, X, V, S, P, desc;
+        src.alloc(size_t(tot) * 8, st);
+        TN_CUDA(cudaMemcpyAsync(src.p, data, size_t(tot) * 8, cudaMemcpyHostToDevice, st));
+        SvdResult R;
+        block_svd(ctx, X, V, S, P, desc, r, c, offs, src.d(), R);
+        TruncDecision D = decide(R, maxdim, mindim, cutoff);
+        for (int b = 0; b < nblocks; ++b) kept[b] = D.kept[b];
+        if (svals) std::copy(R.S.begin(), R.S.end(), svals);
+        if (truncerr) *truncerr = D.truncerr;
+        sync(ctx);
+        double scratch_ms[T_NCAT] = {0, 0, 0, 0, 0};
+        ctx->timer.collect(scratch_ms);
+    });
+}
+
+}  // extern "C"

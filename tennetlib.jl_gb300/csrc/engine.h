@@ -1,0 +1,97 @@
+// Host-side objects of the sweep engine (behind the opaque handles of tennet.h).
+#pragma once
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/tennet.h"
+#include "tn_internal.h"
+
+namespace tn {
+
+// CUDA-event interval timer: intervals are recorded on the stream and resolved only at the
+// next synchronisation point, so timing adds no host round trips.
+enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_NCAT };
+struct EventTimer {
+    cudaStream_t s = nullptr;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    struct Iv { int cat; int a, b; };
+    std::vector<Iv> ivs;
+    int mark();
+    void add(int cat, int a, int b) { ivs.push_back(Iv{cat, a, b}); }
+    // sums the recorded intervals (ms) per category into acc and forgets them; the caller
+    // must have synchronised the stream.
+    void collect(double* acc);
+    ~EventTimer();
+};
+
+struct Scratch;  // fixed-capacity device scratch used by the allocation-free entry points
+
+}  // namespace tn
+
+struct tn_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int prec = TN_PREC_FP64;
+    int slices = 4;
+    tn::EventTimer timer;
+};
+
+struct tn_mpo {
+    tn_ctx* ctx = nullptr;
+    int N = 0, d = 0;
+    std::vector<int> pq;
+    std::vector<int> wd;                   // N+1
+    std::vector<std::vector<int>> delta;   // N+1
+    std::vector<std::vector<double>> W;    // per site, column-major (wl, wr, d, d)
+    double at(int i, int a, int b, int sp, int s) const {
+        const int wl = wd[i], wr = wd[i + 1];
+        return W[i][size_t(a) + size_t(wl) * (size_t(b) + size_t(wr) * (size_t(sp) + size_t(d) * s))];
+    }
+};
+
+struct tn_site {
+    tn::SiteLayout lay;
+    tn::DevBuf buf;
+};
+
+struct tn_mps {
+    tn_ctx* ctx = nullptr;
+    int N = 0, d = 0;
+    std::vector<int> pq;
+    std::vector<tn::Link> links;   // N+1
+    std::vector<tn_site> sites;    // N
+    int center = 0;
+};
+
+struct tn_envt {
+    tn::EnvLayout lay;
+    tn::DevBuf buf;
+};
+
+// contraction plans of the two-site effective Hamiltonian at one position
+struct Heff2Plan {
+    tn::PhiLayout ph;
+    tn::GemmPlan g1, g3;
+    tn::CombPlan cb;
+    int64_t ysize = 0, zsize = 0;
+    double flops = 0;
+};
+
+struct tn_env {
+    tn_ctx* ctx = nullptr;
+    std::unique_ptr<tn_mps> psi;
+    const tn_mpo* H = nullptr;
+    std::vector<tn_envt> L, R;
+    int lpos = 0, rpos = 0;
+    int pos = 0, nsite = 2;
+    // work buffers
+    tn::DevBuf t1, t2, kry, part, dots, svdX, svdV, svdS, svdP, desc, desc2, vecA, vecB;
+    std::unique_ptr<Heff2Plan> hp;
+    int hp_pos = -1;
+    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0};
+    int64_t matvecs = 0;
+    double heff_flops = 0;
+};

@@ -1,0 +1,231 @@
+// Internal declarations of libtennet_cuda.so: block layouts of U(1) tensors, contraction
+// plans, device buffers and kernel launchers.  Host code is C++17; kernels are CUDA for
+// sm_103a.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace tn {
+
+// ------------------------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+#define TN_CUDA(x)                                                          \
+    do {                                                                    \
+        cudaError_t _e = (x);                                               \
+        if (_e != cudaSuccess) ::tn::cuda_fail(_e, #x, __FILE__, __LINE__); \
+    } while (0)
+#define TN_REQUIRE(cond, msg)                                     \
+    do {                                                          \
+        if (!(cond)) throw ::tn::Error(-1, std::string(msg));     \
+    } while (0)
+
+// ------------------------------------------------------------------------------------
+// device buffers (stream-ordered pool allocation)
+// ------------------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p; bytes = o.bytes; stream = o.stream;
+            o.p = nullptr; o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t nbytes, cudaStream_t s);     // reallocates only when growing
+    void release();
+    double* d() const { return static_cast<double*>(p); }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ------------------------------------------------------------------------------------
+// links and block layouts
+// ------------------------------------------------------------------------------------
+struct Link {
+    std::vector<int> q, dim;  // sectors sorted by q ascending
+    int nsec() const { return (int)q.size(); }
+    int find(int charge) const;  // sector index or -1
+    int total() const;
+    int maxdim() const;
+    std::vector<int> offsets() const;  // basis offset of each sector
+};
+
+enum Layout { LG = 0, RG = 1 };
+
+// Site tensor A[l, s, r] (charge rule q_r = q_l + q_s).
+//  LG (left-grouped): one block per right sector r; rows = (s, l) slabs, s-major,
+//      l = r - q_s; cols = D_r.  A left isometry is an LG tensor with orthonormal columns.
+//  RG (right-grouped): one block per left sector l; rows = D_l; cols = (s, r) slabs,
+//      r = l + q_s.  A right isometry is an RG tensor with orthonormal rows.
+// Blocks are column-major and packed back to back.
+struct SiteLayout {
+    Layout layout = RG;
+    int d = 0;
+    std::vector<int> rows, cols;
+    std::vector<int64_t> off;
+    std::vector<int> sub;     // [nblk*d] slab offset (row for LG, column for RG), -1 absent
+    std::vector<int> subsec;  // [nblk*d] sector of the other link, -1 absent
+    int64_t size = 0;
+    int nblk() const { return (int)rows.size(); }
+};
+SiteLayout make_site_layout(Layout lay, const Link& left, const Link& right,
+                            const std::vector<int>& pq);
+
+// Two-site tensor phi[l, s1, s2, r] grouped by the middle charge m = q_l + q_s1 = q_r - q_s2:
+// block m has rows (s1, l) slabs (s1-major) and cols (s2, r) slabs (s2-major).  The rows of
+// block m are the LG rows of a left tensor with right sector m; the columns are the RG
+// columns of a right tensor with left sector m.  The same layout with one physical leg
+// (nsite = 1, the one-site tensor (l, s, r) grouped by m = q_r) is not used by this build.
+struct PhiLayout {
+    int d = 0;
+    std::vector<int> m, rows, cols;
+    std::vector<int64_t> off;
+    std::vector<int> rsub, rsec;  // [nblk*d] row offset / left sector of slab s1
+    std::vector<int> csub, csec;  // [nblk*d] col offset / right sector of slab s2
+    int64_t size = 0;
+    int nblk() const { return (int)m.size(); }
+    int find(int charge) const;
+};
+PhiLayout make_phi_layout(const Link& left, const Link& right, const std::vector<int>& pq);
+
+// Environment E[x', a, x] on one link: block (a, ket sector x) of size D_{x'} x D_x with
+// the bra sector x' = x + delta_a.
+struct EnvLayout {
+    int w = 0, nsec = 0;
+    std::vector<int64_t> off;  // [w*nsec], -1 absent
+    std::vector<int> bra;      // [w*nsec]
+    int64_t size = 0;
+};
+EnvLayout make_env_layout(const Link& link, const std::vector<int>& delta);
+
+// ------------------------------------------------------------------------------------
+// contraction plans (device-visible PODs)
+// ------------------------------------------------------------------------------------
+enum BufSlot {
+    S_L = 0,   // left environment
+    S_R = 1,   // right environment
+    S_X = 2,   // input vector / site tensor
+    S_Y = 3,   // output
+    S_T1 = 4,  // intermediates
+    S_T2 = 5,
+    S_A = 6,   // second site tensor
+    S_B = 7,
+    NSLOT = 8
+};
+struct Bases {
+    double* p[NSLOT];
+};
+
+// C[task] = sum over its segments of op(A) * op(B); op = transpose when t* = 1.
+struct Seg {
+    int64_t aoff, boff;
+    int32_t abuf, bbuf, lda, ldb, k, ta, tb;
+};
+struct Task {
+    int64_t coff;
+    int32_t cbuf, m, n, ldc, seg0, nseg;
+};
+struct Tile {
+    int32_t task, m0, n0;
+};
+// dst sub-block = sum_t coef_t * src_t (all rows x cols, column-major)
+struct CombOut {
+    int64_t doff;
+    int32_t dbuf, ldd, rows, cols, t0, nt;
+};
+struct CombTerm {
+    int64_t soff;
+    int32_t sbuf, lds;
+    double coef;
+};
+struct CombTile {
+    int32_t out, r0, c0;
+};
+
+struct GemmPlan {
+    std::vector<Seg> segs;
+    std::vector<Task> tasks;
+    std::vector<Tile> tiles;
+    double flops = 0;
+    DevBuf dsegs, dtasks, dtiles;
+    void add_task(int cbuf, int64_t coff, int m, int n, int ldc);
+    void add_seg(int abuf, int64_t aoff, int lda, int ta, int bbuf, int64_t boff, int ldb,
+                 int tb, int k);
+    void finalize(cudaStream_t s);  // builds tiles, uploads
+};
+struct CombPlan {
+    std::vector<CombOut> outs;
+    std::vector<CombTerm> terms;
+    std::vector<CombTile> tiles;
+    double flops = 0;
+    DevBuf douts, dterms, dtiles;
+    void finalize(cudaStream_t s);
+};
+
+constexpr int GEMM_BM = 64, GEMM_BN = 64;
+constexpr int COMB_TR = 32, COMB_TC = 32;
+
+// ------------------------------------------------------------------------------------
+// kernel launchers (kernels_*.cu)
+// ------------------------------------------------------------------------------------
+void launch_gemm_f64(const GemmPlan& p, const Bases& b, cudaStream_t s);
+void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s);
+
+// Krylov vector kernels.  Partial sums go to `part` (>= K * nparts doubles) and the
+// finalized results to `out` (K doubles), all on the device.
+int blas_nparts();
+void launch_multi_dot(const double* const* V, int K, const double* w, int64_t n,
+                      double* part, double* out, cudaStream_t s);
+void launch_multi_axpy(double* w, const double* const* V, int K, const double* h,
+                       double sign, int64_t n, cudaStream_t s);
+void launch_scale_into(double* dst, const double* src, const double* denom_sq_or_null,
+                       double host_scale, int64_t n, cudaStream_t s);
+void launch_lincomb(double* dst, const double* const* V, int K, const double* coef,
+                    int64_t n, cudaStream_t s);
+
+// Block SVD: for each block b with rows x cols matrix at src + off[b], compute its SVD by
+// one-sided Jacobi.  Results are kept in the SVD workspace (see svd.cu).
+struct SvdWork;
+struct SvdBlockDesc {
+    int64_t src_off;   // offset of the block in the source buffer
+    int64_t x_off;     // offset of the work matrix X (m x n, m >= n)
+    int64_t v_off;     // offset of V (n x n)
+    int64_t s_off;     // offset of the singular values (n) and permutation
+    int32_t rows, cols, m, n, trans, pad;
+};
+void launch_svd_prepare(const SvdBlockDesc* d, int nb, const double* src, double* X,
+                        double* V, cudaStream_t s);
+void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, double* X, double* V,
+                       double* S, int* perm, int* sweeps_out, cudaStream_t s);
+
+// extraction of truncated factors into site tensors
+struct ExtractDesc {
+    int64_t x_off, v_off, s_off;
+    int64_t left_off, right_off;  // destination block offsets
+    int32_t rows, cols, n, trans, k, pad;
+};
+void launch_svd_extract(const ExtractDesc* d, int nb, int max_rows, int max_cols,
+                        const double* X, const double* V, const double* S, const int* perm,
+                        double* left, double* right, int ortho, double inv_norm,
+                        cudaStream_t s);
+
+}  // namespace tn

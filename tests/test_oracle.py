@@ -1,0 +1,151 @@
+"""The oracle pinned against exact results (CPU only).
+
+The reference's own tests assert nothing (test/*.jl contain no @test), so the oracle is
+pinned against exact diagonalisation (tests/golden/ed_energies.json), against dense
+linear algebra and against invariants.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ed
+from oracle import tn_oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
+
+
+@pytest.mark.parametrize("N", [6, 8, 10, 12])
+def test_ed_fixture_reproduces(N):
+    e = ed.ground_energy(N, ed.heisenberg_chain_terms(N))
+    assert abs(e - GOLD["heisenberg_chain"][str(N)]) < 1e-12
+
+
+def test_ed_known_values():
+    # literature values of the open S=1/2 Heisenberg chain
+    assert abs(GOLD["heisenberg_chain"]["12"] - (-5.142090632840)) < 1e-11
+    assert abs(GOLD["heisenberg_chain"]["20"] - (-8.682473334398)) < 1e-11
+
+
+@pytest.mark.parametrize("N", [8, 12])
+def test_oracle_dmrg_matches_ed(N):
+    H = O.heisenberg_mpo(N)
+    psi = O.product_mps([0 if i % 2 == 0 else 1 for i in range(N)], O.SPIN_HALF_Q)
+    sw, env = O.dmrg(psi, H, maxdim=[16, 32, 64], nsweeps=[2, 2, 3], cutoff=1e-14,
+                     krylovdim=5)
+    assert abs(sw.energy[-1] - GOLD["heisenberg_chain"][str(N)]) < 1e-10
+    # the state stays in the S^z = 0 sector, right-canonical at the end
+    assert env.psi.links[N][0] == 0 and env.psi.center == 0
+
+
+def test_oracle_dmrg_no_qn_random_start():
+    N = 10
+    H = O.heisenberg_mpo(N, qn=False)
+    v = O.random_product_vectors(N, 2, 1234)
+    psi = O.product_mps(None, np.zeros(2, dtype=np.int64), vectors=v)
+    sw, _ = O.dmrg(psi, H, maxdim=[16, 32], nsweeps=[3, 3], cutoff=1e-12, krylovdim=3)
+    assert abs(sw.energy[-1] - GOLD["heisenberg_chain"]["10"]) < 1e-9
+
+
+def test_oracle_j1j2_cylinder_matches_ed():
+    Lx, Ly = 3, 4
+    N = Lx * Ly
+    H = O.mpo_from_terms(N, O.j1j2_cylinder_terms(Lx, Ly, 1.0, 0.5))
+    psi = O.product_mps([0 if i % 2 == 0 else 1 for i in range(N)], O.SPIN_HALF_Q)
+    sw, _ = O.dmrg(psi, H, maxdim=[32, 64, 64], nsweeps=[2, 2, 3], cutoff=1e-14, krylovdim=5)
+    assert abs(sw.energy[-1] - GOLD["j1j2_cylinder"]["3x4"]) < 1e-9
+
+
+def _dense_h(H):
+    """Contract an MPO to a dense matrix (small N only)."""
+    acc = H.W[0][0]  # (b, s', s)
+    for W in H.W[1:]:
+        # acc: (b, S', S) with S multi-index; W: (b, c, s', s)
+        b, Sp, S = acc.shape
+        acc = np.einsum("bxy,bcuv->cxuyv", acc, W).reshape(W.shape[1], Sp * 2, S * 2)
+    return acc[0]
+
+
+def test_mpo_builders_agree_with_exact_hamiltonian():
+    N = 6
+    H1 = O.heisenberg_mpo(N)
+    H2 = O.mpo_from_terms(N, ed.heisenberg_chain_terms(N))
+    D1, D2 = _dense_h(H1), _dense_h(H2)
+    assert np.allclose(D1, D2, atol=1e-14)
+    e = np.linalg.eigvalsh(D1)[0]
+    assert abs(e - GOLD["heisenberg_chain"]["6"]) < 1e-12
+
+
+def test_mpo_charges_conserved():
+    N = 12
+    H = O.mpo_from_terms(N, O.j1j2_cylinder_terms(3, 4))
+    for i, W in enumerate(H.W):
+        a, b, sp, s = np.nonzero(W)
+        assert np.all(H.phys_q[sp] - H.phys_q[s] == H.delta[i + 1][b] - H.delta[i][a])
+
+
+def test_truncation_rule_maxdim_and_cutoff():
+    P = np.array([0.5, 0.3, 0.1, 0.05, 0.03, 0.02])
+    n, err, docut = O.truncation_rule(P, maxdim=3, mindim=1, cutoff=1e-12)
+    assert n == 3 and abs(err - 0.1) < 1e-15 and 0.05 < docut < 0.1
+    n, err, docut = O.truncation_rule(P, maxdim=10, mindim=1, cutoff=0.06)
+    # discard 0.02 + 0.03 = 0.05 <= 0.06, adding 0.05 would exceed
+    assert n == 4 and abs(err - 0.05) < 1e-15
+    n, err, docut = O.truncation_rule(P, maxdim=10, mindim=5, cutoff=0.5)
+    assert n == 5
+    n, err, docut = O.truncation_rule(P, maxdim=10, mindim=1, cutoff=0.0)
+    assert n == 6 and docut == 0.0
+
+
+def test_truncation_rule_degenerate_multiplet_is_cut_whole():
+    P = np.array([0.4, 0.2, 0.2, 0.2])
+    n, err, docut = O.truncation_rule(P, maxdim=2, mindim=1, cutoff=1e-15)
+    # cut falls inside a degenerate triplet: the cut value is raised above it
+    assert docut > 0.2
+    blocks = [np.diag(np.sqrt([0.4, 0.2])), np.diag(np.sqrt([0.2])), np.diag(np.sqrt([0.2]))]
+    _, spec, kept = O.svd_blocks_truncate(blocks, 2, 1, 1e-15)
+    assert kept == [1, 0, 0]
+
+
+def test_lanczos_restart_matches_eigh():
+    rng = np.random.default_rng(7)
+    n = 60
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    x0 = rng.standard_normal(n)
+    e, v, info = O.eigsolve_lowest(lambda x: A @ x, x0, krylovdim=20, maxiter=30, tol=1e-12)
+    w, U = np.linalg.eigh(A)
+    assert abs(e - w[0]) < 1e-9
+    assert abs(abs(v @ U[:, 0]) - 1.0) < 1e-8
+
+
+def test_lanczos_matvec_count_follows_restart_schedule():
+    rng = np.random.default_rng(3)
+    n = 200
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    x0 = rng.standard_normal(n)
+    _, _, info = O.eigsolve_lowest(lambda x: A @ x, x0, krylovdim=3, maxiter=2, tol=1e-14)
+    # 3 vectors, restart keeping (3*3+0)//5 = 1 Ritz vector, 2 more expansions
+    assert info.matvecs == 5 and info.numiter == 2
+
+
+def test_heff_is_hermitian():
+    rng = np.random.default_rng(11)
+    N = 6
+    H = O.heisenberg_mpo(N)
+    psi = O.product_mps([0, 1, 0, 1, 0, 1], O.SPIN_HALF_Q)
+    sw, env = O.dmrg(psi, H, maxdim=[8], nsweeps=[1], cutoff=1e-14)
+    env.position(2, 2)
+    sh = (len(env.psi.links[2]), 2, 2, len(env.psi.links[4]))
+    mask = (env.psi.links[2][:, None, None, None] + O.SPIN_HALF_Q[None, :, None, None]
+            + O.SPIN_HALF_Q[None, None, :, None]) == env.psi.links[4][None, None, None, :]
+    x = rng.standard_normal(sh) * mask
+    y = rng.standard_normal(sh) * mask
+    assert abs(np.vdot(x, env.product2(2, y)) - np.vdot(env.product2(2, x), y)) < 1e-12
+
+
+def test_entropy():
+    assert O.entropy([1.0]) == 0.0
+    assert abs(O.entropy([0.5, 0.5]) - np.log(2)) < 1e-15
