@@ -131,6 +131,11 @@ int tn_env_position(tn_env* env, int pos, int nsite);
 /* product(sysenv, v) = H_eff * v at the current position (state_envs.jl:376-378).
  * v/out dense (Dl, d, Dr) for nsite = 1 or (Dl, d, d, Dr) for nsite = 2. */
 int tn_env_product(tn_env* env, const double* v, double* out, int64_t n);
+/* dense copy of environment L[i] (side 0: contracts sites < i) or R[i] (side 1: contracts
+ * sites > i) as (D, w, D) [bra, MPO state, ket] column-major; dims[3] receives (D, w, D).
+ * With out == NULL only dims are written.  The environment must have been built by a
+ * position call (ProjMPO's cached LR[i], used via src/mps/state_envs.jl:364-367). */
+int tn_env_environment(tn_env* env, int side, int i, double* out, int64_t cap, int32_t* dims);
 /* algorithmic flops of one product at the current position */
 int tn_env_product_flops(tn_env* env, double* flops);
 /* update_position!(sysenv, eig_solver, pos, 2, ortho; kwargs...)

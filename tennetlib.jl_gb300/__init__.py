@@ -252,6 +252,17 @@ class StateEnvs:
 
     __call__ = product
 
+    def environment(self, side: str, i: int):
+        """Dense environment L[i] ("left") or R[i] ("right") as [bra, MPO state, ket]."""
+        sd = {"left": 0, "right": 1}[side]
+        dims = np.zeros(3, dtype=np.int32)
+        L.check(self.ctx.lib.tn_env_environment(self.h, sd, i, None, 0,
+                                                dims.ctypes.data_as(L.i32p)))
+        out = np.zeros(int(np.prod(dims.astype(np.int64))))
+        L.check(self.ctx.lib.tn_env_environment(self.h, sd, i, out.ctypes.data_as(L.f64p),
+                                                out.size, dims.ctypes.data_as(L.i32p)))
+        return out.reshape(tuple(int(x) for x in dims), order="F")
+
     def product_flops(self) -> float:
         f = C.c_double()
         L.check(self.ctx.lib.tn_env_product_flops(self.h, C.byref(f)))

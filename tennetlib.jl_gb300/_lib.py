@@ -89,6 +89,7 @@ PROTOS = {
     "tn_env_getpsi": (C.c_int, [vp, C.POINTER(vp)]),
     "tn_env_position": (C.c_int, [vp, C.c_int, C.c_int]),
     "tn_env_product": (C.c_int, [vp, f64p, f64p, C.c_int64]),
+    "tn_env_environment": (C.c_int, [vp, C.c_int, C.c_int, f64p, C.c_int64, i32p]),
     "tn_env_product_flops": (C.c_int, [vp, f64p]),
     "tn_env_update_position": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(UpdateParams),
                                          C.POINTER(UpdateResult), f64p, C.c_int]),

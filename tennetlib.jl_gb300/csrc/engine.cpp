@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -720,9 +722,10 @@ struct SvdResult {
 };
 
 // SVD of the listed blocks of src (device); results stay in the env work buffers.
-void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dV, DevBuf& dS, DevBuf& dP, DevBuf& ddesc,
-               const std::vector<int>& rows, const std::vector<int>& cols,
-               const std::vector<int64_t>& offs, const double* src, SvdResult& R) {
+void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevBuf& dS,
+               DevBuf& dPerm, DevBuf& ddesc, const std::vector<int>& rows,
+               const std::vector<int>& cols, const std::vector<int64_t>& offs, const double* src,
+               SvdResult& R) {
     cudaStream_t st = ctx->stream;
     R.desc.clear();
     int64_t xo = 0, vo = 0, so = 0;
@@ -747,18 +750,30 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dV, DevBuf& dS, DevBuf& dP, DevB
     R.total_n = so;
     const int nb = (int)R.desc.size();
     dX.alloc(size_t(std::max<int64_t>(xo, 1)) * 8, st);
+    dW.alloc(size_t(std::max<int64_t>(xo, 1)) * 8, st);
     dV.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
+    dP.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
     dS.alloc(size_t(std::max<int64_t>(so, 1)) * 8, st);
-    dP.alloc(size_t(std::max<int64_t>(so, 1)) * 4, st);
+    dPerm.alloc(size_t(std::max<int64_t>(so, 1)) * 4, st);
     ddesc.alloc(std::max<size_t>(size_t(nb) * sizeof(SvdBlockDesc), 16), st);
     if (nb)
         TN_CUDA(cudaMemcpyAsync(ddesc.p, R.desc.data(), nb * sizeof(SvdBlockDesc),
                                 cudaMemcpyHostToDevice, st));
+    static const bool dbg = std::getenv("TENNET_DEBUG_SVD") != nullptr;
+    DevBuf dsw;
+    if (dbg) dsw.alloc(size_t(std::max(nb, 1)) * 4, st);
     const int e0 = ctx->timer.mark();
-    launch_svd_prepare(ddesc.as<SvdBlockDesc>(), nb, src, dX.d(), dV.d(), st);
-    launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nb, maxn, dX.d(), dV.d(), dS.d(), dP.as<int>(),
-                      nullptr, st);
+    launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nb, maxn, src, dX.d(), dW.d(), dV.d(), dP.d(),
+                      dS.d(), dPerm.as<int>(), dbg ? dsw.as<int>() : nullptr, st);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    if (dbg && nb) {
+        std::vector<int> sw(nb);
+        TN_CUDA(cudaMemcpyAsync(sw.data(), dsw.p, nb * 4, cudaMemcpyDeviceToHost, st));
+        TN_CUDA(cudaStreamSynchronize(st));
+        for (int b = 0; b < nb; ++b)
+            std::fprintf(stderr, "svd block %d: %dx%d sweeps fp32=%d fp64=%d\n", b, R.desc[b].m,
+                         R.desc[b].n, sw[b] >> 16, sw[b] & 0xffff);
+    }
     R.S.resize(size_t(so));
     if (so)
         TN_CUDA(cudaMemcpyAsync(R.S.data(), dS.p, size_t(so) * 8, cudaMemcpyDeviceToHost, st));
@@ -820,8 +835,8 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
     cudaStream_t st = ctx->stream;
     tn_mps* psi = env->psi.get();
     SvdResult R;
-    block_svd(ctx, env->svdX, env->svdV, env->svdS, env->svdP, env->desc, ph.rows, ph.cols,
-              ph.off, phi, R);
+    block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm,
+              env->desc, ph.rows, ph.cols, ph.off, phi, R);
     TruncDecision D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
     Link nl;
     for (int b = 0; b < ph.nblk(); ++b)
@@ -861,8 +876,8 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
                                 cudaMemcpyHostToDevice, st));
     const double inv = (prm->normalize && D.norm > 0) ? 1.0 / D.norm : 1.0;
     const int e0 = ctx->timer.mark();
-    launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), 0, 0, env->svdX.d(),
-                       env->svdV.d(), env->svdS.d(), env->svdP.as<int>(), left.buf.d(),
+    launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(),
+                       env->svdV.d(), env->svdS.d(), env->svdPerm.as<int>(), left.buf.d(),
                        right.buf.d(), ortho, inv, st);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
     psi->sites[p] = std::move(left);
@@ -1256,6 +1271,44 @@ int tn_env_position(tn_env* env, int pos, int nsite) {
     });
 }
 
+int tn_env_environment(tn_env* env, int side, int i, double* out, int64_t cap,
+                       int32_t* dims) {
+    return guarded([&] {
+        TN_REQUIRE(env && dims, "null argument");
+        const tn_mps* psi = env->psi.get();
+        const int N = psi->N;
+        TN_REQUIRE(i >= 0 && i < N, "environment index out of range");
+        TN_REQUIRE(side == 0 ? i <= env->lpos : i >= env->rpos,
+                   "environment is not built; call tn_env_position first");
+        const tn_envt& E = side == 0 ? env->L[i] : env->R[i];
+        const Link& lk = psi->links[side == 0 ? i : i + 1];
+        const int w = env->H->wd[side == 0 ? i : i + 1];
+        const int D = lk.total();
+        dims[0] = D;
+        dims[1] = w;
+        dims[2] = D;
+        if (!out) return;
+        TN_REQUIRE(cap >= int64_t(D) * w * D, "capacity too small");
+        std::vector<double> blocks(size_t(E.lay.size));
+        if (!blocks.empty())
+            TN_CUDA(cudaMemcpyAsync(blocks.data(), E.buf.p, blocks.size() * 8,
+                                    cudaMemcpyDeviceToHost, env->ctx->stream));
+        sync(env->ctx);
+        std::fill(out, out + int64_t(D) * w * D, 0.0);
+        const auto off = lk.offsets();
+        for (int a = 0; a < w; ++a)
+            for (int x = 0; x < lk.nsec(); ++x) {
+                const int64_t bo = E.lay.off[size_t(a) * E.lay.nsec + x];
+                if (bo < 0) continue;
+                const int xb = E.lay.bra[size_t(a) * E.lay.nsec + x];
+                for (int c = 0; c < lk.dim[x]; ++c)
+                    for (int r = 0; r < lk.dim[xb]; ++r)
+                        out[int64_t(off[xb] + r) + int64_t(D) * (a + int64_t(w) * (off[x] + c))] =
+                            blocks[size_t(bo + r + int64_t(lk.dim[xb]) * c)];
+            }
+    });
+}
+
 int tn_env_product_flops(tn_env* env, double* flops) {
     return guarded([&] {
         TN_REQUIRE(env && flops, "null argument");
@@ -1382,11 +1435,11 @@ int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t
             tot += int64_t(r[b]) * c[b];
         }
         cudaStream_t st = ctx->stream;
-        DevBuf src, X, V, S, P, desc;
+        DevBuf src, X, W, V, P, S, Pm, desc;
         src.alloc(size_t(tot) * 8, st);
         TN_CUDA(cudaMemcpyAsync(src.p, data, size_t(tot) * 8, cudaMemcpyHostToDevice, st));
         SvdResult R;
-        block_svd(ctx, X, V, S, P, desc, r, c, offs, src.d(), R);
+        block_svd(ctx, X, W, V, P, S, Pm, desc, r, c, offs, src.d(), R);
         TruncDecision D = decide(R, maxdim, mindim, cutoff);
         for (int b = 0; b < nblocks; ++b) kept[b] = D.kept[b];
         if (svals) std::copy(R.S.begin(), R.S.end(), svals);

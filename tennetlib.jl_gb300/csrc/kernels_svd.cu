@@ -1,6 +1,6 @@
-// Batched FP64 one-sided Jacobi SVD of the charge blocks of a two-site tensor
-// (Hestenes' method with round-robin parallel ordering), followed by the extraction of the
-// truncated factors into the left/right site tensors.  The truncation decision itself is
+// Batched one-sided Jacobi SVD of the charge blocks of a two-site tensor (Hestenes' method
+// with round-robin parallel ordering; FP32 presolve, FP64 polish), followed by the
+// extraction of the truncated factors into the left/right site tensors.  The truncation decision itself is
 // made on the host from the sorted singular values (tiny, integer-valued result).
 #include <cuda_runtime.h>
 
@@ -10,27 +10,6 @@ namespace tn {
 namespace {
 
 constexpr int SVD_THREADS = 512;
-constexpr int SVD_MAX_SWEEPS = 40;
-
-__global__ void svd_prepare_kernel(const SvdBlockDesc* __restrict__ desc,
-                                   const double* __restrict__ src, double* __restrict__ X,
-                                   double* __restrict__ V) {
-    const SvdBlockDesc d = desc[blockIdx.x];
-    const double* M = src + d.src_off;
-    double* x = X + d.x_off;
-    double* v = V + d.v_off;
-    const int64_t mn = int64_t(d.m) * d.n;
-    for (int64_t e = threadIdx.x; e < mn; e += blockDim.x) {
-        const int i = int(e % d.m), j = int(e / d.m);
-        x[e] = d.trans ? M[j + int64_t(i) * d.rows] : M[i + int64_t(j) * d.rows];
-    }
-    const int64_t nn = int64_t(d.n) * d.n;
-    for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) {
-        const int i = int(e % d.n), j = int(e / d.n);
-        v[e] = (i == j) ? 1.0 : 0.0;
-    }
-}
-
 __device__ __forceinline__ double wsum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -45,130 +24,364 @@ __device__ __forceinline__ void rr_pair(int nn, int r, int k, int& i, int& j) {
     if (i > j) { int t = i; i = j; j = t; }
 }
 
-__global__ void __launch_bounds__(SVD_THREADS)
-svd_jacobi_kernel(const SvdBlockDesc* __restrict__ desc, double* __restrict__ X,
-                  double* __restrict__ V, double* __restrict__ S, int* __restrict__ perm,
-                  int* __restrict__ sweeps_out) {
-    extern __shared__ double raw[];  // n column norms
-    __shared__ int rotated;
-    const SvdBlockDesc d = desc[blockIdx.x];
-    const int m = d.m, n = d.n;
-    double* x = X + d.x_off;
-    double* v = V + d.v_off;
+// Reduction over the 8 lanes of a pair group (xor offsets stay inside the group).
+template <class T>
+__device__ __forceinline__ T gsum8(T v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
+}
+
+// One-sided Jacobi sweeps on the columns of x (m x n, column-major, leading dim m) with
+// the rotations accumulated into v (n x n).  T is the working precision of every operation
+// (on GB300 one warp-wide FP64 instruction occupies the SM's FP64 pipe for many cycles,
+// so the FP32 presolve must not touch FP64).  Each warp works on 4 disjoint column pairs
+// at a time, 8 lanes per pair.  Returns the number of sweeps run; all threads must call it.
+template <class T>
+__device__ int jacobi_sweeps(T* x, T* v, int m, int n, T tol, int max_sweeps, int* rotated) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const double tol = 2.220446049250313e-16 * sqrt(double(m > 1 ? m : 1)) * 2.0;
+    const int grp = lane >> 3, sub = lane & 7;
     const int nn = n + (n & 1);
+    const int npairs = nn / 2;
+    const int slots = nwarps * 4;
     int sweep = 0;
-    if (n > 1) {
-        for (sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
-            if (threadIdx.x == 0) rotated = 0;
-            __syncthreads();
-            for (int r = 0; r < nn - 1; ++r) {
-                for (int k = warp; k < nn / 2; k += nwarps) {
-                    int i, j;
-                    rr_pair(nn, r, k, i, j);
-                    if (j >= n) continue;
-                    double* xi = x + int64_t(i) * m;
-                    double* xj = x + int64_t(j) * m;
-                    double a = 0.0, bb = 0.0, g = 0.0;
-                    for (int t = lane; t < m; t += 32) {
-                        const double p = xi[t], q = xj[t];
+    if (n < 2) return 0;
+    for (sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) *rotated = 0;
+        __syncthreads();
+        for (int r = 0; r < nn - 1; ++r) {
+            for (int base = 0; base < npairs; base += slots) {
+                const int k = base + warp * 4 + grp;
+                int i = 0, j = 0;
+                const bool live = k < npairs;
+                if (live) rr_pair(nn, r, k, i, j);
+                const bool act = live && j < n;
+                T a = 0, bb = 0, g = 0;
+                T* xi = x + int64_t(i) * m;
+                T* xj = x + int64_t(j) * m;
+                if (act)
+                    for (int t = sub; t < m; t += 8) {
+                        const T p = xi[t], q = xj[t];
                         a = fma(p, p, a);
                         bb = fma(q, q, bb);
                         g = fma(p, q, g);
                     }
-                    a = wsum(a);
-                    bb = wsum(bb);
-                    g = wsum(g);
-                    if (!(fabs(g) > tol * sqrt(a) * sqrt(bb))) continue;
-                    const double zeta = (bb - a) / (2.0 * g);
-                    const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    const double c = 1.0 / sqrt(1.0 + tt * tt);
-                    const double s = c * tt;
-                    for (int t = lane; t < m; t += 32) {
-                        const double p = xi[t], q = xj[t];
-                        xi[t] = c * p - s * q;
-                        xj[t] = s * p + c * q;
+                a = gsum8(a);
+                bb = gsum8(bb);
+                g = gsum8(g);
+                const bool rot = act && (fabs(g) > tol * sqrt(a) * sqrt(bb));
+                if (rot) {
+                    const T zeta = (bb - a) / (T(2) * g);
+                    const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+                    const T c = T(1) / sqrt(T(1) + tt * tt);
+                    const T sn = c * tt;
+                    for (int t = sub; t < m; t += 8) {
+                        const T p = xi[t], q = xj[t];
+                        xi[t] = c * p - sn * q;
+                        xj[t] = sn * p + c * q;
                     }
-                    double* vi = v + int64_t(i) * n;
-                    double* vj = v + int64_t(j) * n;
-                    for (int t = lane; t < n; t += 32) {
-                        const double p = vi[t], q = vj[t];
-                        vi[t] = c * p - s * q;
-                        vj[t] = s * p + c * q;
+                    T* vi = v + int64_t(i) * n;
+                    T* vj = v + int64_t(j) * n;
+                    for (int t = sub; t < n; t += 8) {
+                        const T p = vi[t], q = vj[t];
+                        vi[t] = c * p - sn * q;
+                        vj[t] = sn * p + c * q;
                     }
-                    if (lane == 0) rotated = 1;
+                    if (sub == 0) *rotated = 1;
                 }
-                __syncthreads();
             }
-            const int done = !rotated;
             __syncthreads();
-            if (done) break;
         }
+        const int done = !*rotated;
+        __syncthreads();
+        if (done) break;
     }
-    // column norms
+    return sweep;
+}
+
+__device__ double block_sum(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    v = wsum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nwarps; ++w) s += red[w];
+    return s;
+}
+
+// Preconditioned mixed-precision one-sided Jacobi SVD, one CTA per block (work matrix
+// A = M or M^T, m x n with m >= n):
+//  1. QR with column pivoting A P = Q R (FP64 Householder, A and the reflectors stay in the
+//     global work buffer X);
+//  2. FP32 one-sided Jacobi on R^T, accumulating V in float: graded R^T makes cyclic Jacobi
+//     converge in a few sweeps (Drmac & Veselic, SIMAX 29, 2008);
+//  3. V re-orthonormalised in FP64 (two-pass classical Gram-Schmidt);
+//  4. Y = R^T V and FP64 one-sided Jacobi polish of Y with V accumulation (quadratic
+//     convergence from the FP32 start: Higham, Tisseur, Webb & Zhou, SIMAX 42, 2021);
+//  5. QV = Q [V; 0] (reflectors applied in reverse order) and PY = P Y.
+// Then A = QV * diag(s) * (PY / s)^T: QV is the orthonormal factor on the A-row side,
+// PY = (A-column side) * diag(s).  Outputs: QV in W (m x n), PY in V (n x n), singular
+// values sorted descending in S with the sorting permutation in perm.  The n x n Jacobi
+// matrices live in shared memory when 2 n^2 doubles fit, else in the global scratch P/V.
+__global__ void __launch_bounds__(SVD_THREADS)
+svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__ src,
+               double* __restrict__ X, double* __restrict__ W, double* __restrict__ V,
+               double* __restrict__ P, double* __restrict__ S, int* __restrict__ perm,
+               int* __restrict__ sweeps_out, int smem_region) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int rotated;
+    __shared__ int piv;
+    __shared__ double red[SVD_THREADS / 32];
+    __shared__ double hh[3];  // tau, beta, scale of the current reflector
+    const SvdBlockDesc d = desc[blockIdx.x];
+    const int m = d.m, n = d.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // aux: column norms / tau / Gram-Schmidt coefficients (3n doubles) + column perm (n ints)
+    double* cn = reinterpret_cast<double*>(smem + smem_region);
+    double* tau = cn + n;
+    double* h = tau + n;
+    int* cp = reinterpret_cast<int*>(h + n);
+    const bool in_smem = int64_t(2) * n * n * 8 <= smem_region;
+    double* A = X + d.x_off;
+    double* Pm = in_smem ? reinterpret_cast<double*>(smem) : P + d.v_off;
+    double* Qm = in_smem ? reinterpret_cast<double*>(smem) + int64_t(n) * n : V + d.v_off;
+    const double* M = src + d.src_off;
+    // 0. A = M (or M^T), column norms
+    for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
+        const int i = int(e % m), k = int(e / m);
+        A[e] = d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows];
+    }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) cp[j] = j;
+    __syncthreads();
     for (int j = warp; j < n; j += nwarps) {
-        const double* xj = x + int64_t(j) * m;
-        double a = 0.0;
-        for (int t = lane; t < m; t += 32) a = fma(xj[t], xj[t], a);
-        a = wsum(a);
-        if (lane == 0) raw[j] = sqrt(a);
+        const double* a = A + int64_t(j) * m;
+        double t = 0.0;
+        for (int i = lane; i < m; i += 32) t = fma(a[i], a[i], t);
+        t = wsum(t);
+        if (lane == 0) cn[j] = t;
     }
     __syncthreads();
-    // sort descending by rank counting (stable on ties)
+    // 1. Householder QR with column pivoting
+    for (int k = 0; k < n; ++k) {
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = k;
+            for (int j = k + lane; j < n; j += 32)
+                if (cn[j] > best) { best = cn[j]; bi = j; }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) piv = bi;
+        }
+        __syncthreads();
+        const int p = piv;
+        if (p != k) {
+            double* a = A + int64_t(k) * m;
+            double* b = A + int64_t(p) * m;
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const double t = a[i]; a[i] = b[i]; b[i] = t;
+            }
+            if (threadIdx.x == 0) {
+                const double t = cn[k]; cn[k] = cn[p]; cn[p] = t;
+                const int u = cp[k]; cp[k] = cp[p]; cp[p] = u;
+            }
+        }
+        __syncthreads();
+        double* ak = A + int64_t(k) * m;
+        if (warp == 0) {
+            double sq = 0.0;
+            for (int i = k + 1 + lane; i < m; i += 32) sq = fma(ak[i], ak[i], sq);
+            sq = wsum(sq);
+            if (lane == 0) {
+                const double alpha = ak[k];
+                if (sq == 0.0) {
+                    hh[0] = 0.0; hh[1] = alpha; hh[2] = 0.0;
+                } else {
+                    const double beta = -copysign(sqrt(alpha * alpha + sq), alpha);
+                    hh[0] = (beta - alpha) / beta;
+                    hh[1] = beta;
+                    hh[2] = 1.0 / (alpha - beta);
+                }
+                tau[k] = hh[0];
+            }
+        }
+        __syncthreads();
+        const double tk = hh[0], sc = hh[2];
+        for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) ak[i] *= sc;
+        __syncthreads();
+        if (threadIdx.x == 0) ak[k] = hh[1];
+        for (int j = k + 1 + warp; j < n; j += nwarps) {
+            double* aj = A + int64_t(j) * m;
+            double w = 0.0;
+            for (int i = k + 1 + lane; i < m; i += 32) w = fma(ak[i], aj[i], w);
+            w = wsum(w) + aj[k];
+            w *= tk;
+            double nrm = 0.0;
+            __syncwarp();  // every lane has read aj[k] before lane 0 updates it
+            if (lane == 0) aj[k] -= w;
+            for (int i = k + 1 + lane; i < m; i += 32) {
+                const double x = fma(-w, ak[i], aj[i]);
+                aj[i] = x;
+                nrm = fma(x, x, nrm);
+            }
+            nrm = wsum(nrm);
+            if (lane == 0) cn[j] = nrm;
+        }
+        __syncthreads();
+    }
+    // 2. FP32 Jacobi on R^T (n x n lower triangular) in the P region
+    float* x32 = reinterpret_cast<float*>(Pm);
+    float* v32 = x32 + int64_t(n) * n;
+    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
+        const int i = int(e % n), j = int(e / n);
+        x32[e] = (j <= i) ? float(A[j + int64_t(i) * m]) : 0.f;  // R^T[i, j] = R[j, i]
+        v32[e] = (i == j) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    const int sw32 = jacobi_sweeps<float>(x32, v32, n, n, 2.0e-5f, 30, &rotated);
+    __syncthreads();
+    // 3. V (FP64) in the Q region, two-pass Gram-Schmidt
+    double* v = Qm;
+    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) v[e] = double(v32[e]);
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        double* vj = v + int64_t(j) * n;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int i = warp; i < j; i += nwarps) {
+                const double* vi = v + int64_t(i) * n;
+                double a = 0.0;
+                for (int t = lane; t < n; t += 32) a = fma(vi[t], vj[t], a);
+                a = wsum(a);
+                if (lane == 0) h[i] = a;
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                double acc = vj[t];
+                for (int i = 0; i < j; ++i) acc = fma(-h[i], v[t + int64_t(i) * n], acc);
+                vj[t] = acc;
+            }
+            __syncthreads();
+        }
+        double ss = 0.0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) ss = fma(vj[t], vj[t], ss);
+        ss = block_sum(ss, red);
+        const double inv = ss > 0.0 ? 1.0 / sqrt(ss) : 0.0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) vj[t] *= inv;
+        __syncthreads();
+    }
+    // 4. Y = R^T V in the P region (the float arrays there are dead), FP64 polish
+    double* y = Pm;
+    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
+        const int i = int(e % n), j = int(e / n);
+        const double* vj = v + int64_t(j) * n;
+        const double* ri = A + int64_t(i) * m;  // column i of R: R[k, i], k <= i
+        double acc = 0.0;
+        for (int k = 0; k <= i; ++k) acc = fma(ri[k], vj[k], acc);
+        y[e] = acc;
+    }
+    __syncthreads();
+    const double tol = 2.220446049250313e-16 * sqrt(double(n > 1 ? n : 1)) * 32.0;
+    const int sw64 = jacobi_sweeps<double>(y, v, n, n, tol, 30, &rotated);
+    __syncthreads();
+    // singular values and sorting permutation
+    for (int j = warp; j < n; j += nwarps) {
+        const double* yj = y + int64_t(j) * n;
+        double a = 0.0;
+        for (int t = lane; t < n; t += 32) a = fma(yj[t], yj[t], a);
+        a = wsum(a);
+        if (lane == 0) h[j] = sqrt(a);
+    }
+    __syncthreads();
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double sj = raw[j];
+        const double sj = h[j];
         int rank = 0;
         for (int k = 0; k < n; ++k) {
-            const double sk = raw[k];
+            const double sk = h[k];
             rank += (sk > sj) || (sk == sj && k < j);
         }
         S[d.s_off + rank] = sj;
         perm[d.s_off + rank] = j;
     }
-    if (threadIdx.x == 0 && sweeps_out) sweeps_out[blockIdx.x] = sweep;
+    // 5a. QV = Q [V; 0] in W
+    double* qv = W + d.x_off;
+    for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
+        const int i = int(e % m), j = int(e / m);
+        qv[e] = (i < n) ? v[i + int64_t(j) * n] : 0.0;
+    }
+    __syncthreads();
+    for (int k = n - 1; k >= 0; --k) {
+        const double tk = tau[k];
+        if (tk == 0.0) continue;  // uniform: tau lives in shared memory
+        const double* ak = A + int64_t(k) * m;
+        for (int j = warp; j < n; j += nwarps) {
+            double* wj = qv + int64_t(j) * m;
+            double w = 0.0;
+            for (int i = k + 1 + lane; i < m; i += 32) w = fma(ak[i], wj[i], w);
+            w = (wsum(w) + wj[k]) * tk;
+            __syncwarp();
+            if (lane == 0) wj[k] -= w;
+            for (int i = k + 1 + lane; i < m; i += 32) wj[i] = fma(-w, ak[i], wj[i]);
+        }
+        __syncthreads();
+    }
+    // 5b. PY = P Y into the V output (row cp[r] of P Y is row r of Y).  Y lives in shared
+    // memory or in the P scratch, never in V, and V (the FP64 rotations) is dead after 5a.
+    __syncthreads();
+    double* py = V + d.v_off;
+    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
+        const int r = int(e % n), j = int(e / n);
+        py[cp[r] + int64_t(j) * n] = y[e];
+    }
+    if (threadIdx.x == 0 && sweeps_out) sweeps_out[blockIdx.x] = (sw32 << 16) | sw64;
 }
 
+// Truncated factors from (QV, PY): for trans = 0 the block is QV diag(s) (PY/s)^T, for
+// trans = 1 it is (PY/s) diag(s) QV^T.  ortho 0 keeps the left factor orthonormal,
+// ortho 1 the right one; the singular values go to the other side scaled by inv_norm.
 __global__ void svd_extract_kernel(const ExtractDesc* __restrict__ desc,
-                                   const double* __restrict__ X, const double* __restrict__ V,
+                                   const double* __restrict__ QV, const double* __restrict__ PY,
                                    const double* __restrict__ S, const int* __restrict__ perm,
                                    double* __restrict__ left, double* __restrict__ right,
                                    int ortho, double inv_norm) {
     const ExtractDesc d = desc[blockIdx.x];
     const int rows = d.rows, cols = d.cols, n = d.n, k = d.k;
-    const double* x = X + d.x_off;
-    const double* v = V + d.v_off;
+    const double* qv = QV + d.x_off;  // m x n, m = max(rows, cols)
+    const double* py = PY + d.v_off;  // n x n
+    const int m = d.trans ? cols : rows;
     const double* s = S + d.s_off;
     const int* pm = perm + d.s_off;
     double* L = left + d.left_off;
     double* R = right + d.right_off;
-    // left factor: rows x k
     const int64_t nl = int64_t(rows) * k;
     for (int64_t e = threadIdx.x; e < nl; e += blockDim.x) {
         const int i = int(e % rows), c = int(e / rows);
         const int pc = pm[c];
         double u;
         if (!d.trans) {
-            const double xv = x[i + int64_t(pc) * rows];
-            u = (ortho == 0) ? xv / s[c] : xv * inv_norm;
+            const double q = qv[i + int64_t(pc) * m];
+            u = (ortho == 0) ? q : q * s[c] * inv_norm;
         } else {
-            const double vv = v[i + int64_t(pc) * n];
-            u = (ortho == 0) ? vv : vv * s[c] * inv_norm;
+            const double y = py[i + int64_t(pc) * n];
+            u = (ortho == 0) ? y / s[c] : y * inv_norm;
         }
         L[e] = u;
     }
-    // right factor: k x cols
     const int64_t nr = int64_t(k) * cols;
     for (int64_t e = threadIdx.x; e < nr; e += blockDim.x) {
         const int c = int(e % k), j = int(e / k);
         const int pc = pm[c];
         double w;
         if (!d.trans) {
-            const double vv = v[j + int64_t(pc) * n];
-            w = (ortho == 0) ? vv * s[c] * inv_norm : vv;
+            const double y = py[j + int64_t(pc) * n];
+            w = (ortho == 0) ? y * inv_norm : y / s[c];
         } else {
-            const double xv = x[j + int64_t(pc) * cols];
-            w = (ortho == 0) ? xv * inv_norm : xv / s[c];
+            const double q = qv[j + int64_t(pc) * m];
+            w = (ortho == 0) ? q * s[c] * inv_norm : q;
         }
         R[e] = w;
     }
@@ -176,30 +389,28 @@ __global__ void svd_extract_kernel(const ExtractDesc* __restrict__ desc,
 
 }  // namespace
 
-void launch_svd_prepare(const SvdBlockDesc* d, int nb, const double* src, double* X, double* V,
-                        cudaStream_t s) {
+void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, const double* src, double* X,
+                       double* W, double* V, double* P, double* S, int* perm, int* sweeps_out,
+                       cudaStream_t s) {
     if (nb <= 0) return;
-    svd_prepare_kernel<<<nb, 256, 0, s>>>(d, src, X, V);
+    const int64_t limit = 227 * 1024 - 2048;
+    const int64_t aux = int64_t(max_n > 0 ? max_n : 1) * (3 * 8 + 4) + 16;
+    TN_REQUIRE(aux < 96 * 1024, "SVD block too large (more than 3000 columns)");
+    int64_t region = int64_t(2) * max_n * max_n * 8;
+    if (region + aux > limit) region = ((limit - aux) / 16) * 16;  // smaller blocks still fit
+    const size_t shm = size_t(region + aux);
+    TN_CUDA(cudaFuncSetAttribute(svd_qrj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(shm)));
+    svd_qrj_kernel<<<nb, SVD_THREADS, shm, s>>>(d, src, X, W, V, P, S, perm, sweeps_out,
+                                                int(region));
     TN_CUDA(cudaGetLastError());
 }
 
-void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, double* X, double* V,
-                       double* S, int* perm, int* sweeps_out, cudaStream_t s) {
+void launch_svd_extract(const ExtractDesc* d, int nb, const double* QV, const double* PY,
+                        const double* S, const int* perm, double* left, double* right, int ortho,
+                        double inv_norm, cudaStream_t s) {
     if (nb <= 0) return;
-    size_t shm = size_t(max_n > 0 ? max_n : 1) * sizeof(double);
-    TN_REQUIRE(shm <= 200 * 1024, "SVD block too large (more than 25600 columns)");
-    if (shm > 48 * 1024)
-        TN_CUDA(cudaFuncSetAttribute(svd_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(shm)));
-    svd_jacobi_kernel<<<nb, SVD_THREADS, shm, s>>>(d, X, V, S, perm, sweeps_out);
-    TN_CUDA(cudaGetLastError());
-}
-
-void launch_svd_extract(const ExtractDesc* d, int nb, int, int, const double* X,
-                        const double* V, const double* S, const int* perm, double* left,
-                        double* right, int ortho, double inv_norm, cudaStream_t s) {
-    if (nb <= 0) return;
-    svd_extract_kernel<<<nb, 256, 0, s>>>(d, X, V, S, perm, left, right, ortho, inv_norm);
+    svd_extract_kernel<<<nb, 256, 0, s>>>(d, QV, PY, S, perm, left, right, ortho, inv_norm);
     TN_CUDA(cudaGetLastError());
 }
 

@@ -203,8 +203,7 @@ void launch_lincomb(double* dst, const double* const* V, int K, const double* co
                     int64_t n, cudaStream_t s);
 
 // Block SVD: for each block b with rows x cols matrix at src + off[b], compute its SVD by
-// one-sided Jacobi.  Results are kept in the SVD workspace (see svd.cu).
-struct SvdWork;
+// one-sided Jacobi on the m x n work matrix (m >= n; the transpose when rows < cols).
 struct SvdBlockDesc {
     int64_t src_off;   // offset of the block in the source buffer
     int64_t x_off;     // offset of the work matrix X (m x n, m >= n)
@@ -212,10 +211,9 @@ struct SvdBlockDesc {
     int64_t s_off;     // offset of the singular values (n) and permutation
     int32_t rows, cols, m, n, trans, pad;
 };
-void launch_svd_prepare(const SvdBlockDesc* d, int nb, const double* src, double* X,
-                        double* V, cudaStream_t s);
-void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, double* X, double* V,
-                       double* S, int* perm, int* sweeps_out, cudaStream_t s);
+void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, const double* src, double* X,
+                       double* W, double* V, double* P, double* S, int* perm, int* sweeps_out,
+                       cudaStream_t s);
 
 // extraction of truncated factors into site tensors
 struct ExtractDesc {
@@ -223,9 +221,8 @@ struct ExtractDesc {
     int64_t left_off, right_off;  // destination block offsets
     int32_t rows, cols, n, trans, k, pad;
 };
-void launch_svd_extract(const ExtractDesc* d, int nb, int max_rows, int max_cols,
-                        const double* X, const double* V, const double* S, const int* perm,
-                        double* left, double* right, int ortho, double inv_norm,
-                        cudaStream_t s);
+void launch_svd_extract(const ExtractDesc* d, int nb, const double* QV, const double* PY,
+                        const double* S, const int* perm, double* left, double* right, int ortho,
+                        double inv_norm, cudaStream_t s);
 
 }  // namespace tn

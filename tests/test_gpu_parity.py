@@ -162,3 +162,42 @@ def test_update_position_errors(tn, ctx):
         tn.update_position_(env, tn.eig_solver, 0, 2, "left", noise=1e-3)
     e, err, eigs = tn.update_position_(env, tn.eig_solver, 0, 2, "left", maxdim=4)
     assert np.isfinite(e) and len(eigs) >= 1
+
+
+def test_environments_match_oracle(tn, ctx):
+    rng = np.random.default_rng(21)
+    N, p = 10, 5
+    mps = random_qn_mps(N, rng, maxsec_dim=3)
+    H = O.mpo_from_terms(N, ed.heisenberg_chain_terms(N))
+    env = tn.StateEnvs(upload_mps(tn, ctx, mps, center=p), upload_mpo(tn, ctx, H))
+    env.position_(p, 2)
+    eo = O.StateEnvs(mps, H)
+    eo.position(p, 2)
+    for i in range(1, p + 1):
+        ref = eo.L[i]
+        got = env.environment("left", i)
+        assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref), f"L[{i}]"
+    for i in range(p + 1, N - 1):
+        ref = eo.R[i]
+        got = env.environment("right", i)
+        assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref), f"R[{i}]"
+
+
+def test_block_svd_large_blocks_global_path(tn, ctx):
+    # blocks whose work matrices exceed shared memory run on the global-memory path
+    rng = np.random.default_rng(13)
+    blocks = []
+    for (r, c) in [(150, 150), (300, 120), (90, 260), (20, 20)]:
+        U, _ = np.linalg.qr(rng.standard_normal((r, r)))
+        V, _ = np.linalg.qr(rng.standard_normal((c, c)))
+        k = min(r, c)
+        s = np.exp(-np.linspace(0, 30, k)) * rng.uniform(0.5, 1.5, size=k)
+        blocks.append((U[:, :k] * s) @ V[:k, :])
+    kept, sv, err = tn.svd_truncate(blocks, maxdim=200, cutoff=1e-12, ctx=ctx)
+    _, spec, kept_ref = O.svd_blocks_truncate(blocks, 200, 1, 1e-12)
+    assert list(kept) == kept_ref
+    for b, s in zip(blocks, sv):
+        ref = np.linalg.svd(b, compute_uv=False)
+        # LAPACK's gesdd is accurate to ~1e-16 of the largest value (absolute), so that is
+        # the scale of the comparison
+        assert np.allclose(s, ref, rtol=0, atol=1e-13 * ref[0])
