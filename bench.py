@@ -1,0 +1,357 @@
+"""Benchmark of the two-site DMRG sweep (the TenNetLib.jl hot path) on one GB300.
+
+Workload (the U(1) Heisenberg configuration of the metric): open S=1/2 Heisenberg chain,
+N = 100, total S^z = 0, MPO bond dimension 5, Neel start, maxdim ramp 64 -> 1024, cutoff
+1e-12, Lanczos krylovdim 5 / maxiter 2 (eig_solver defaults).  The ramp 64, 128, 256, 512,
+1024 (two sweeps each) prepares the state untimed; a step is then one full two-site sweep
+(left-to-right and right-to-left, 2 (N - 1) bond updates) at maxdim 1024.  The bond
+dimension is limited by the cutoff (about 180 after convergence).
+
+The JSON line reports seconds per sweep (device time from CUDA events inside the library),
+the H_eff contraction throughput, the grouped-GEMM roofline, the end-to-end time through
+the C ABI with host buffers, and the CPU oracle timed on the host cores.
+
+Multi-GPU: sweeps are sequential in the bond position, so N GPUs run N independent
+replicas (no collective on the data path); the value is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sweep s & H_eff TFLOP/s, split-prec vs FP64 GPU at |ΔE/E|≤1e-10"
+N_SITES = 100
+RAMP = [64, 128, 256, 512, 1024]
+MAXDIM = 1024
+CUTOFF = 1e-12
+KRYLOVDIM = 5
+MAXITER = 2
+FP64_PEAK_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 peak on this machine)
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "fallback": True}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def heisenberg(tn, ctx):
+    W, delta, pq = tn.models.mpo_from_terms(N_SITES, tn.models.heisenberg_chain_terms(N_SITES))
+    return tn.MPO(W, delta, pq, ctx), pq
+
+
+def sweep_kwargs(maxdim):
+    return dict(maxdim=maxdim, cutoff=CUTOFF, solver_krylovdim=KRYLOVDIM, solver_maxiter=MAXITER,
+                outputlevel=0)
+
+
+def download_state(psi):
+    """Dense host copy of an engine MPS: (tensors, link charge arrays)."""
+    tensors = [psi.site(i) for i in range(psi.N)]
+    links = [psi.link_charges(i) for i in range(psi.N + 1)]
+    return tensors, links
+
+
+# ------------------------------------------------------------------------------------
+# CPU oracle legs (the checker, timed as the CPU baseline / reference arm)
+# ------------------------------------------------------------------------------------
+
+def oracle_env_from(tensors, links):
+    import numpy as np
+    from oracle import tn_oracle as O
+    H = O.heisenberg_mpo(N_SITES)
+    psi = O.MPS([np.asarray(t) for t in tensors], [np.asarray(q, dtype=np.int64) for q in links],
+                O.SPIN_HALF_Q.copy(), center=0)
+    return O, O.StateEnvs(psi, H)
+
+
+def oracle_halfsweep(O, env, direction):
+    """One half sweep (N - 1 bond updates) of the oracle; returns the last energy."""
+    N = env.N
+    bonds = range(N - 1) if direction == "left" else range(N - 2, -1, -1)
+    e = None
+    for b in bonds:
+        e, _, _ = O.update_two_site(env, b, direction, MAXDIM, 1, CUTOFF, KRYLOVDIM, MAXITER, 1e-14)
+    return e
+
+
+def cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline_from(tensors, links):
+    """Time one full oracle sweep from the GPU-prepared state on the host cores."""
+    O, env = oracle_env_from(tensors, links)
+    env.position(0, 2)  # right environments: setup, not timed
+    t0 = time.perf_counter()
+    oracle_halfsweep(O, env, "left")
+    oracle_halfsweep(O, env, "right")
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s/sweep", "cores": cores(), "kind": "port",
+            "sample": f"one full two-site sweep ({2 * (N_SITES - 1)} bond updates) of the numpy "
+                      "FP64 oracle (dense tensors with charge labels, OpenBLAS threads = all "
+                      "host cores) from the same converged chi~180 state"}
+
+
+def run_reference(args, world, rank, pg):
+    """--impl reference: the oracle port on the host cores (the reference is Julia and
+    cannot run here).  Each step is a bounded sample: one half sweep; value = 2 x its time."""
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import tn_oracle as O
+    H = O.heisenberg_mpo(N_SITES)
+    psi = O.product_mps([0 if i % 2 == 0 else 1 for i in range(N_SITES)], O.SPIN_HALF_Q)
+    env = O.StateEnvs(psi, H)
+    sw = O.SweepData()
+    for md in RAMP:  # prepare (not timed)
+        O.fullsweep(env, sw, md, CUTOFF, 1, KRYLOVDIM, MAXITER, 1e-14)
+    direction = "left"
+    for _ in range(args.warmup):
+        oracle_halfsweep(O, env, direction)
+        direction = "right" if direction == "left" else "left"
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle_halfsweep(O, env, direction)
+        times.append(2.0 * (time.perf_counter() - t0))
+        direction = "right" if direction == "left" else "left"
+    value = statistics.mean(times)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s/sweep",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config(args),
+        "cpu_baseline": {"value": value, "unit": "s/sweep", "cores": cores(), "kind": "port",
+                         "sample": "per step one half sweep (99 bond updates) of the numpy FP64 "
+                                   "oracle from its own converged chi~180 state; value = 2 x time "
+                                   "(TenNetLib.jl itself needs Julia + ITensors, absent here)"},
+        "e2e": {"value": value, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def config(args):
+    return {"workload": "heisenberg_u1_chain_N100_maxdim1024_cutoff1e-12",
+            "model": "S=1/2 Heisenberg OBC, MPO w=5, U(1) Sz=0, Neel start",
+            "sites": N_SITES, "maxdim": MAXDIM, "ramp": RAMP, "cutoff": CUTOFF,
+            "krylovdim": KRYLOVDIM, "maxiter": MAXITER, "precision": args.precision,
+            "parallelism": f"replicas{args.gpus}",
+            "l2": "working set (environments of all 100 sites, ~0.3 GB) larger than L2"}
+
+
+# ------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------
+
+def run_ours(args, world, rank, local, pg):
+    import __graft_entry__ as g
+    g.build()
+    tn = g.load_package()
+    ctx = tn.Context(local)
+    if args.precision == "split":
+        ctx.set_precision("split", args.slices)
+    H, pq = heisenberg(tn, ctx)
+    psi0 = tn.MPS.product(tn.models.neel_states(N_SITES), pq, ctx)
+    env = tn.StateEnvs(psi0, H)
+    sw = tn.SweepData()
+    for md in RAMP:  # prepare the converged state (not timed)
+        tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(md))
+    for _ in range(args.warmup):
+        tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(MAXDIM))
+    n0 = len(sw.stats)
+    # kernels launched before the timed region (lets a profiler skip the preparation)
+    print(f"launches_before_timed={ctx.lib.tn_kernel_launches()}", file=sys.stderr, flush=True)
+    barrier(pg)
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(MAXDIM))
+    wall = time.perf_counter() - t0
+    barrier(pg)
+    st = sw.stats[n0:]
+    dev_s = sum(s["sweep_ms"] for s in st) / 1e3 / args.steps
+    dev_s = allmax(pg, dev_s)
+    heff_ms = sum(s["heff_ms"] for s in st)
+    heff_fl = sum(s["heff_flops"] for s in st)
+    gemm_ms = sum(s["gemm_ms"] for s in st)
+    gemm_fl = sum(s["gemm_flops"] for s in st)
+    gemm_n = sum(s["gemm_launches"] for s in st)
+    launches = sum(s["kernel_launches"] for s in st)
+    energy = sw.energy[-1]
+    chi = sw.maxchi[-1]
+
+    # end to end through the C ABI with host buffers: upload the MPS, build the
+    # environments, sweep, download the MPS
+    tensors, links = download_state(env.getpsi())
+    h2d = sum(t.size * 8 for t in tensors)
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 2))):
+        t1 = time.perf_counter()
+        p2 = tn.MPS(tensors, links, pq, 0, ctx)
+        e2 = tn.StateEnvs(p2, H)
+        s2 = tn.SweepData()
+        tn.fullsweep_(e2, tn.eig_solver, 2, s2, **sweep_kwargs(MAXDIM))
+        out = download_state(e2.getpsi())
+        e2e_times.append(time.perf_counter() - t1)
+        d2h = sum(t.size * 8 for t in out[0])
+        del e2, p2
+    e2e = allmax(pg, statistics.mean(e2e_times))
+
+    if rank != 0:
+        return
+    pk = peaks()
+    gemm_tflops = gemm_fl / max(gemm_ms, 1e-9) / 1e9
+    if args.precision == "split":
+        roof = {"bound": "tensor", "achieved": gemm_tflops, "peak": pk["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": gemm_tflops / pk["bf16_tflops"],
+                "peak_note": "of measured bf16 (algorithmic FP64-equivalent flops, slice "
+                             "products not counted)"}
+    else:
+        roof = {"bound": "fp64", "achieved": gemm_tflops, "peak": FP64_PEAK_NOMINAL_TFLOPS,
+                "unit": "TFLOP/s", "frac": gemm_tflops / FP64_PEAK_NOMINAL_TFLOPS,
+                "peak_note": "of nominal GB300 FP64 (no measured FP64 peak on this pool)"}
+    roof["kernel"] = "grouped block-sparse GEMM of H_eff (two launches per matvec)"
+    roof["flops_per_launch"] = gemm_fl / max(gemm_n, 1)
+    roof["ms_per_launch"] = gemm_ms / max(gemm_n, 1)
+    roof["traffic"] = None
+    share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
+             for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms")}
+    res = {
+        "metric": METRIC, "value": dev_s, "unit": "s/sweep", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64 (bf16-slice tensor-core GEMMs)",
+        "data": "synthetic", "config": config(args),
+        "heff_tflops": heff_fl / max(heff_ms, 1e-9) / 1e9,
+        "heff_ms_per_sweep": heff_ms / args.steps,
+        "time_share": share,
+        "matvecs_per_sweep": sum(s["matvecs"] for s in st) / args.steps,
+        "energy": energy, "maxlinkdim": chi, "wall_s_per_sweep": wall / args.steps,
+        "gpu_launches": launches,
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e, "unit": "s/sweep", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "what": "upload MPS from host + build environments + one sweep + download MPS"},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline_from(tensors, links)
+    print(json.dumps(res), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--slices", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

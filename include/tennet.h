@@ -84,6 +84,10 @@ typedef struct tn_sweep_result {
     double svd_ms;             /* device time of the block SVDs */
     double lanczos_ms;         /* device time of the Krylov vector kernels */
     double sweep_ms;           /* device time of the whole sweep */
+    double gemm_ms;            /* device time of the grouped-GEMM launches of H_eff */
+    double gemm_flops;         /* algorithmic flops of those launches */
+    int64_t gemm_launches;     /* number of those launches */
+    int64_t kernel_launches;   /* all kernels this library launched during the sweep */
 } tn_sweep_result;
 
 /* ---- context ------------------------------------------------------------------- */
@@ -94,6 +98,8 @@ int tn_ctx_destroy(tn_ctx* ctx);
 int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices);
 const char* tn_last_error(void);
 const char* tn_version(void);
+/* number of CUDA kernels this library has launched since it was loaded (diagnostics) */
+int64_t tn_kernel_launches(void);
 
 /* ---- MPO --------------------------------------------------------------------------
  * Replaces the ITensorMPS MPO handed to StateEnvs(psi, H::MPO)

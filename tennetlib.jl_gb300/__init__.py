@@ -368,7 +368,9 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
     swdata.stats.append({
         "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
-        "sweep_ms": res.sweep_ms, "wall_s": wall})
+        "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops,
+        "gemm_launches": res.gemm_launches, "kernel_launches": res.kernel_launches,
+        "wall_s": wall})
     if swdata.sweepcount > 1:
         enerr = swdata.energy[-1] - swdata.energy[-2]
         enterr = swdata.entropy[-1] - swdata.entropy[-2]

@@ -66,6 +66,10 @@ class SweepResult(C.Structure):
         ("svd_ms", C.c_double),
         ("lanczos_ms", C.c_double),
         ("sweep_ms", C.c_double),
+        ("gemm_ms", C.c_double),
+        ("gemm_flops", C.c_double),
+        ("gemm_launches", C.c_int64),
+        ("kernel_launches", C.c_int64),
     ]
 
 
@@ -76,6 +80,7 @@ PROTOS = {
     "tn_ctx_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
     "tn_last_error": (C.c_char_p, []),
     "tn_version": (C.c_char_p, []),
+    "tn_kernel_launches": (C.c_int64, []),
     "tn_mpo_create": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, f64p, C.POINTER(vp)]),
     "tn_mpo_destroy": (C.c_int, [vp]),
     "tn_mps_create": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p, C.c_int,

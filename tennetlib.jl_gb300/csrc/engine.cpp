@@ -515,11 +515,18 @@ void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
     launch_gemm_f64(P.g1, bs, ctx->stream);
+    const int e1 = ctx->timer.mark();
     launch_combine(P.cb, bs, ctx->stream);
+    const int e2 = ctx->timer.mark();
     launch_gemm_f64(P.g3, bs, ctx->stream);
-    ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+    const int e3 = ctx->timer.mark();
+    ctx->timer.add(T_HEFF, e0, e3);
+    ctx->timer.add(T_GEMM, e0, e1);
+    ctx->timer.add(T_GEMM, e2, e3);
     env->matvecs++;
     env->heff_flops += P.flops;
+    env->gemm_flops += P.g1.flops + P.g3.flops;
+    env->gemm_launches += (P.g1.tiles.empty() ? 0 : 1) + (P.g3.tiles.empty() ? 0 : 1);
 }
 
 // phi = site p * site p+1 in the phi layout
@@ -1051,6 +1058,7 @@ extern "C" {
 
 const char* tn_last_error(void) { return g_err.c_str(); }
 const char* tn_version(void) { return "tennet-gb300 0.1 (sm_103a)"; }
+int64_t tn_kernel_launches(void) { return launch_count(); }
 
 int tn_ctx_create(int device, tn_ctx** out) {
     return guarded([&] {
@@ -1379,6 +1387,9 @@ int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* re
         std::copy(env->acc_ms, env->acc_ms + T_NCAT, acc0);
         const int64_t mv0 = env->matvecs;
         const double fl0 = env->heff_flops;
+        const double gf0 = env->gemm_flops;
+        const int64_t gl0 = env->gemm_launches;
+        const int64_t kl0 = launch_count();
         *res = tn_sweep_result{};
         const int es = ctx->timer.mark();
         double maxerr = 0.0, energy = NAN;
@@ -1411,6 +1422,10 @@ int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* re
         res->svd_ms = env->acc_ms[T_SVD] - acc0[T_SVD];
         res->lanczos_ms = env->acc_ms[T_LANCZOS] - acc0[T_LANCZOS];
         res->sweep_ms = env->acc_ms[T_SWEEP] - acc0[T_SWEEP];
+        res->gemm_ms = env->acc_ms[T_GEMM] - acc0[T_GEMM];
+        res->gemm_flops = env->gemm_flops - gf0;
+        res->gemm_launches = env->gemm_launches - gl0;
+        res->kernel_launches = launch_count() - kl0;
         if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
         if (mid_eigs) {
             const int k = std::min<int>(mid_cap, (int)mid.size());
@@ -1445,7 +1460,7 @@ int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t
         if (svals) std::copy(R.S.begin(), R.S.end(), svals);
         if (truncerr) *truncerr = D.truncerr;
         sync(ctx);
-        double scratch_ms[T_NCAT] = {0, 0, 0, 0, 0};
+        double scratch_ms[T_NCAT] = {0, 0, 0, 0, 0, 0};
         ctx->timer.collect(scratch_ms);
     });
 }

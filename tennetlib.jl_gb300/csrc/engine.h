@@ -12,7 +12,7 @@ namespace tn {
 
 // CUDA-event interval timer: intervals are recorded on the stream and resolved only at the
 // next synchronisation point, so timing adds no host round trips.
-enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_NCAT };
+enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_GEMM, T_NCAT };
 struct EventTimer {
     cudaStream_t s = nullptr;
     std::vector<cudaEvent_t> pool;
@@ -92,7 +92,9 @@ struct tn_env {
         vecB;
     std::unique_ptr<Heff2Plan> hp;
     int hp_pos = -1;
-    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0};
+    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0};
+    double gemm_flops = 0;
+    int64_t gemm_launches = 0;
     int64_t matvecs = 0;
     double heff_flops = 0;
 };

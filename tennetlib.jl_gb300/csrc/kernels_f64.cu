@@ -225,6 +225,7 @@ void launch_gemm_f64(const GemmPlan& p, const Bases& b, cudaStream_t s) {
     gemm_f64_kernel<<<unsigned(p.tiles.size()), 256, 0, s>>>(
         p.dsegs.as<Seg>(), p.dtasks.as<Task>(), p.dtiles.as<Tile>(), b);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s) {
@@ -232,6 +233,7 @@ void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s) {
     combine_kernel<<<unsigned(p.tiles.size()), 256, 0, s>>>(
         p.douts.as<CombOut>(), p.dterms.as<CombTerm>(), p.dtiles.as<CombTile>(), b);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 int blas_nparts() { return BLAS_PARTS; }
@@ -250,8 +252,10 @@ void launch_multi_dot(const double* const* V, int K, const double* w, int64_t n,
     else
         multi_dot_kernel<32><<<g, BLAS_THREADS, 0, s>>>(P, K, w, n, part);
     TN_CUDA(cudaGetLastError());
+    count_launch();
     finalize_dot_kernel<<<K, 32, 0, s>>>(part, g, K, out);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_multi_axpy(double* w, const double* const* V, int K, const double* h, double sign,
@@ -259,6 +263,7 @@ void launch_multi_axpy(double* w, const double* const* V, int K, const double* h
     if (K <= 0 || n <= 0) return;
     multi_axpy_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(w, make_ptrs(V, K), K, h, sign, n);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_scale_into(double* dst, const double* src, const double* denom_sq,
@@ -266,6 +271,7 @@ void launch_scale_into(double* dst, const double* src, const double* denom_sq,
     if (n <= 0) return;
     scale_into_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(dst, src, denom_sq, host_scale, n);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_lincomb(double* dst, const double* const* V, int K, const double* coef, int64_t n,
@@ -273,6 +279,7 @@ void launch_lincomb(double* dst, const double* const* V, int K, const double* co
     if (n <= 0) return;
     lincomb_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(dst, make_ptrs(V, K), K, coef, n);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace tn

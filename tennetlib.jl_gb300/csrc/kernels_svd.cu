@@ -404,6 +404,7 @@ void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, const double* s
     svd_qrj_kernel<<<nb, SVD_THREADS, shm, s>>>(d, src, X, W, V, P, S, perm, sweeps_out,
                                                 int(region));
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_svd_extract(const ExtractDesc* d, int nb, const double* QV, const double* PY,
@@ -412,6 +413,7 @@ void launch_svd_extract(const ExtractDesc* d, int nb, const double* QV, const do
     if (nb <= 0) return;
     svd_extract_kernel<<<nb, 256, 0, s>>>(d, QV, PY, S, perm, left, right, ortho, inv_norm);
     TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace tn

@@ -1,6 +1,7 @@
 // Block layouts of U(1) charge-conserving tensors and the small host-side containers of
 // contraction plans.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "tn_internal.h"
@@ -12,6 +13,10 @@ void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     throw Error(code, std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what +
                           " at " + file + ":" + std::to_string(line));
 }
+
+static std::atomic<int64_t> g_launches{0};
+int64_t launch_count() { return g_launches.load(); }
+void count_launch(int n) { g_launches += n; }
 
 void DevBuf::alloc(size_t nbytes, cudaStream_t s) {
     if (nbytes <= bytes && p) return;

@@ -188,6 +188,9 @@ constexpr int COMB_TR = 32, COMB_TC = 32;
 // kernel launchers (kernels_*.cu)
 // ------------------------------------------------------------------------------------
 void launch_gemm_f64(const GemmPlan& p, const Bases& b, cudaStream_t s);
+// number of kernel launches issued by this library since load (all kernels)
+int64_t launch_count();
+void count_launch(int n = 1);
 void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s);
 
 // Krylov vector kernels.  Partial sums go to `part` (>= K * nparts doubles) and the
