@@ -86,6 +86,7 @@ typedef struct tn_sweep_result {
     double sweep_ms;           /* device time of the whole sweep */
     double gemm_ms;            /* device time of the grouped-GEMM launches of H_eff */
     double gemm_flops;         /* algorithmic flops of those launches */
+    double pack_ms;            /* device time of the bf16 slice packing (split precision) */
     int64_t gemm_launches;     /* number of those launches */
     int64_t kernel_launches;   /* all kernels this library launched during the sweep */
 } tn_sweep_result;

@@ -58,14 +58,14 @@ class Context:
 
     _default = None
 
-    def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 4):
+    def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 5):
         self.lib = L.load()
         h = L.vp()
         L.check(self.lib.tn_ctx_create(device, C.byref(h)))
         self.h = h
         self.set_precision(precision, slices)
 
-    def set_precision(self, precision: str, slices: int = 4):
+    def set_precision(self, precision: str, slices: int = 5):
         mode = {"fp64": L.TN_PREC_FP64, "split": L.TN_PREC_SPLIT}[precision]
         L.check(self.lib.tn_ctx_set_precision(self.h, mode, slices))
         self.precision = precision
@@ -368,7 +368,7 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
     swdata.stats.append({
         "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
-        "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops,
+        "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops, "pack_ms": res.pack_ms,
         "gemm_launches": res.gemm_launches, "kernel_launches": res.kernel_launches,
         "wall_s": wall})
     if swdata.sweepcount > 1:

@@ -68,6 +68,7 @@ class SweepResult(C.Structure):
         ("sweep_ms", C.c_double),
         ("gemm_ms", C.c_double),
         ("gemm_flops", C.c_double),
+        ("pack_ms", C.c_double),
         ("gemm_launches", C.c_int64),
         ("kernel_launches", C.c_int64),
     ]

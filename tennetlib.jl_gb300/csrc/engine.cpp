@@ -163,6 +163,144 @@ bool need_right(const tn_mpo* H, int site, int c, int s) {
     return false;
 }
 
+// -------------------------------------------------------------------------------------
+// split-precision GEMM plans
+// -------------------------------------------------------------------------------------
+template <class T>
+void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+    b.alloc(std::max<size_t>(v.size() * sizeof(T), 16), s);
+    if (!v.empty())
+        TN_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_static,
+                                      bool b_static, cudaStream_t st) {
+    auto sp = std::make_unique<SplitPlan>();
+    sp->slices = slices;
+    sp->a_static = a_static;
+    sp->b_static = b_static;
+    const int KT = split_ktile(), RA = split_tile_rows_a(), RB = split_tile_rows_b();
+    const int64_t TA = split_tile_bytes_a(), TB = split_tile_bytes_b();
+    int64_t aoff = 0, boff = 0, eao = 0, ebo = 0;
+    std::vector<std::pair<int, int>> order;  // (nkt, task) for scheduling heavy first
+    for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
+        const Task& t = g.tasks[ti];
+        struct KT3 { int seg, k0, kv; };
+        std::vector<KT3> kts;
+        for (int j = 0; j < t.nseg; ++j) {
+            const Seg& sg = g.segs[t.seg0 + j];
+            for (int k0 = 0; k0 < sg.k; k0 += KT) kts.push_back(KT3{t.seg0 + j, k0, std::min(KT, sg.k - k0)});
+        }
+        const int nkt = (int)kts.size();
+        const int mt = (t.m + RA - 1) / RA, nt = (t.n + RB - 1) / RB;
+        SplitTask stsk{};
+        stsk.coff = t.coff;
+        stsk.a_off = aoff;
+        stsk.b_off = boff;
+        stsk.cbuf = t.cbuf;
+        stsk.m = t.m;
+        stsk.n = t.n;
+        stsk.ldc = t.ldc;
+        stsk.nkt = nkt;
+        stsk.ea_off = int32_t(eao);
+        stsk.eb_off = int32_t(ebo);
+        sp->tasks.push_back(stsk);
+        const int akt0 = (int)sp->aks.size(), bkt0 = (int)sp->bks.size();
+        for (const auto& k : kts) {
+            const Seg& sg = g.segs[k.seg];
+            KTileSrc a{};
+            a.buf = sg.abuf;
+            a.sr = sg.ta ? sg.lda : 1;
+            a.sk = sg.ta ? 1 : sg.lda;
+            a.off = sg.aoff + int64_t(k.k0) * a.sk;
+            a.kvalid = k.kv;
+            sp->aks.push_back(a);
+            KTileSrc bsrc{};
+            bsrc.buf = sg.bbuf;
+            bsrc.sr = sg.tb ? 1 : sg.ldb;
+            bsrc.sk = sg.tb ? sg.ldb : 1;
+            bsrc.off = sg.boff + int64_t(k.k0) * bsrc.sk;
+            bsrc.kvalid = k.kv;
+            sp->bks.push_back(bsrc);
+        }
+        for (int mi = 0; mi < mt; ++mi)
+            sp->ajobs.push_back(PackJob{aoff + int64_t(mi) * nkt * slices * TA, akt0, nkt,
+                                        std::min(RA, t.m - mi * RA), mi * RA, int32_t(eao + mi * RA), 0});
+        for (int ni = 0; ni < nt; ++ni)
+            sp->bjobs.push_back(PackJob{boff + int64_t(ni) * nkt * slices * TB, bkt0, nkt,
+                                        std::min(RB, t.n - ni * RB), ni * RB, int32_t(ebo + ni * RB), 0});
+        for (int mi = 0; mi < mt; ++mi)
+            for (int ni = 0; ni < nt; ++ni) sp->items.push_back(SplitItem{int32_t(ti), mi, ni, 0});
+        aoff += int64_t(mt) * nkt * slices * TA;
+        boff += int64_t(nt) * nkt * slices * TB;
+        eao += int64_t(mt) * RA;
+        ebo += int64_t(nt) * RB;
+    }
+    std::stable_sort(sp->items.begin(), sp->items.end(), [&](const SplitItem& x, const SplitItem& y) {
+        return sp->tasks[x.task].nkt > sp->tasks[y.task].nkt;
+    });
+    sp->abytes = aoff;
+    sp->bbytes = boff;
+    sp->ea_n = eao;
+    sp->eb_n = ebo;
+    upload_vec(sp->dtasks, sp->tasks, st);
+    upload_vec(sp->ditems, sp->items, st);
+    upload_vec(sp->dajobs, sp->ajobs, st);
+    upload_vec(sp->dbjobs, sp->bjobs, st);
+    upload_vec(sp->daks, sp->aks, st);
+    upload_vec(sp->dbks, sp->bks, st);
+    sp->apack.alloc(size_t(std::max<int64_t>(aoff, 1024)), st);
+    sp->bpack.alloc(size_t(std::max<int64_t>(boff, 1024)), st);
+    sp->ea.alloc(size_t(std::max<int64_t>(eao, 4)) * 4, st);
+    sp->eb.alloc(size_t(std::max<int64_t>(ebo, 4)) * 4, st);
+    return sp;
+}
+
+// pack the operands that need it, then run the tensor-core GEMM; times packs and MMA
+void run_split(tn_ctx* ctx, SplitPlan& sp, const Bases& bs, int* mma_ev0, int* mma_ev1) {
+    cudaStream_t st = ctx->stream;
+    const int p0 = ctx->timer.mark();
+    if (!sp.a_static || !sp.a_packed) {
+        launch_split_pack(sp.dajobs.as<PackJob>(), (int)sp.ajobs.size(), sp.daks.as<KTileSrc>(), bs,
+                          sp.apack.as<uint8_t>(), sp.ea.as<int>(), sp.slices, split_tile_rows_a(), st);
+        sp.a_packed = true;
+    }
+    if (!sp.b_static || !sp.b_packed) {
+        launch_split_pack(sp.dbjobs.as<PackJob>(), (int)sp.bjobs.size(), sp.dbks.as<KTileSrc>(), bs,
+                          sp.bpack.as<uint8_t>(), sp.eb.as<int>(), sp.slices, split_tile_rows_b(), st);
+        sp.b_packed = true;
+    }
+    const int p1 = ctx->timer.mark();
+    ctx->timer.add(T_PACK, p0, p1);
+    launch_split_gemm(sp.ditems.as<SplitItem>(), (int)sp.items.size(), sp.dtasks.as<SplitTask>(),
+                      sp.apack.as<uint8_t>(), sp.bpack.as<uint8_t>(), sp.ea.as<int>(),
+                      sp.eb.as<int>(), bs, sp.slices, ctx->err.as<int>(), ctx->nsm, st);
+    const int p2 = ctx->timer.mark();
+    if (mma_ev0) *mma_ev0 = p1;
+    if (mma_ev1) *mma_ev1 = p2;
+}
+
+// grouped GEMM in the context's precision (one-shot plans: every operand packed)
+void run_gemm(tn_ctx* ctx, const GemmPlan& g, const Bases& bs) {
+    if (g.tasks.empty()) return;
+    if (ctx->prec == TN_PREC_SPLIT) {
+        auto sp = make_split(g, ctx->slices, false, false, ctx->stream);
+        run_split(ctx, *sp, bs, nullptr, nullptr);
+    } else {
+        launch_gemm_f64(g, bs, ctx->stream);
+    }
+}
+
+void check_device_error(tn_ctx* ctx) {
+    int e = 0;
+    TN_CUDA(cudaMemcpyAsync(&e, ctx->err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    TN_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (e) {
+        TN_CUDA(cudaMemsetAsync(ctx->err.p, 0, sizeof(int), ctx->stream));
+        throw Error(TN_E_TIMEOUT, "a bounded device wait gave up in the tensor-core GEMM");
+    }
+}
+
 // L[i+1] from L[i] and the left isometry at site i.
 void env_left_step(tn_env* env, int i) {
     tn_ctx* ctx = env->ctx;
@@ -253,9 +391,9 @@ void env_left_step(tn_env* env, int i) {
     bs.p[S_T2] = env->t2.d();
     bs.p[S_Y] = Lout.buf.d();
     const int e0 = ctx->timer.mark();
-    launch_gemm_f64(g1, bs, st);
+    run_gemm(ctx, g1, bs);
     launch_combine(cb, bs, st);
-    launch_gemm_f64(g3, bs, st);
+    run_gemm(ctx, g3, bs);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
 
@@ -347,9 +485,9 @@ void env_right_step(tn_env* env, int i) {
     bs.p[S_T2] = env->t2.d();
     bs.p[S_Y] = Rout.buf.d();
     const int e0 = ctx->timer.mark();
-    launch_gemm_f64(g1, bs, st);
+    run_gemm(ctx, g1, bs);
     launch_combine(cb, bs, st);
-    launch_gemm_f64(g3, bs, st);
+    run_gemm(ctx, g3, bs);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
 
@@ -514,15 +652,27 @@ void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
     bs.p[S_T1] = env->t1.d();
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
-    launch_gemm_f64(P.g1, bs, ctx->stream);
-    const int e1 = ctx->timer.mark();
-    launch_combine(P.cb, bs, ctx->stream);
-    const int e2 = ctx->timer.mark();
-    launch_gemm_f64(P.g3, bs, ctx->stream);
-    const int e3 = ctx->timer.mark();
-    ctx->timer.add(T_HEFF, e0, e3);
-    ctx->timer.add(T_GEMM, e0, e1);
-    ctx->timer.add(T_GEMM, e2, e3);
+    if (ctx->prec == TN_PREC_SPLIT) {
+        if (!P.s1) P.s1 = make_split(P.g1, ctx->slices, true, false, ctx->stream);   // A = L
+        if (!P.s3) P.s3 = make_split(P.g3, ctx->slices, false, true, ctx->stream);   // B = R
+        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+        run_split(ctx, *P.s1, bs, &a0, &a1);
+        launch_combine(P.cb, bs, ctx->stream);
+        run_split(ctx, *P.s3, bs, &b0, &b1);
+        ctx->timer.add(T_GEMM, a0, a1);
+        ctx->timer.add(T_GEMM, b0, b1);
+        ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+    } else {
+        launch_gemm_f64(P.g1, bs, ctx->stream);
+        const int e1 = ctx->timer.mark();
+        launch_combine(P.cb, bs, ctx->stream);
+        const int e2 = ctx->timer.mark();
+        launch_gemm_f64(P.g3, bs, ctx->stream);
+        const int e3 = ctx->timer.mark();
+        ctx->timer.add(T_HEFF, e0, e3);
+        ctx->timer.add(T_GEMM, e0, e1);
+        ctx->timer.add(T_GEMM, e2, e3);
+    }
     env->matvecs++;
     env->heff_flops += P.flops;
     env->gemm_flops += P.g1.flops + P.g3.flops;
@@ -923,6 +1073,7 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     res->converged = eo.converged;
     replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
     res->neigs = (int)eigs.size();
+    if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
 }
 
 std::unique_ptr<tn_mps> copy_mps(const tn_mps* src) {
@@ -1075,6 +1226,10 @@ int tn_ctx_create(int device, tn_ctx** out) {
         c->device = device;
         TN_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         c->timer.s = c->stream;
+        c->nsm = pr.multiProcessorCount;
+        c->err.alloc(sizeof(int), c->stream);
+        TN_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+        TN_CUDA(cudaStreamSynchronize(c->stream));
         cudaMemPool_t mp;
         TN_CUDA(cudaDeviceGetDefaultMemPool(&mp, device));
         uint64_t thr = UINT64_MAX;
@@ -1098,8 +1253,8 @@ int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices) {
         TN_REQUIRE(ctx, "null context");
         TN_REQUIRE(mode == TN_PREC_FP64 || mode == TN_PREC_SPLIT, "unknown precision mode");
         TN_REQUIRE(slices >= 2 && slices <= 7, "slices must be in [2, 7]");
-        if (mode == TN_PREC_SPLIT)
-            throw Error(TN_E_INVALID, "split-precision contractions are not built in this library");
+        TN_REQUIRE(mode == TN_PREC_FP64 || (slices >= 4 && slices <= 7),
+                   "split precision needs 4..7 slices");
         ctx->prec = mode;
         ctx->slices = slices;
     });
@@ -1275,6 +1430,7 @@ int tn_env_position(tn_env* env, int pos, int nsite) {
         TN_REQUIRE(env, "null argument");
         position(env, pos, nsite);
         sync(env->ctx);
+        check_device_error(env->ctx);
         env->ctx->timer.collect(env->acc_ms);
     });
 }
@@ -1350,6 +1506,7 @@ int tn_env_product(tn_env* env, const double* v, double* out, int64_t n) {
         if (!hb.empty())
             TN_CUDA(cudaMemcpyAsync(hb.data(), env->vecB.p, hb.size() * 8, cudaMemcpyDeviceToHost, st));
         sync(env->ctx);
+        check_device_error(env->ctx);
         env->ctx->timer.collect(env->acc_ms);
         std::fill(out, out + nd, 0.0);
         for (size_t i = 0; i < hb.size(); ++i) out[map[i]] = hb[i];
@@ -1423,6 +1580,7 @@ int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* re
         res->lanczos_ms = env->acc_ms[T_LANCZOS] - acc0[T_LANCZOS];
         res->sweep_ms = env->acc_ms[T_SWEEP] - acc0[T_SWEEP];
         res->gemm_ms = env->acc_ms[T_GEMM] - acc0[T_GEMM];
+        res->pack_ms = env->acc_ms[T_PACK] - acc0[T_PACK];
         res->gemm_flops = env->gemm_flops - gf0;
         res->gemm_launches = env->gemm_launches - gl0;
         res->kernel_launches = launch_count() - kl0;
@@ -1460,7 +1618,7 @@ int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t
         if (svals) std::copy(R.S.begin(), R.S.end(), svals);
         if (truncerr) *truncerr = D.truncerr;
         sync(ctx);
-        double scratch_ms[T_NCAT] = {0, 0, 0, 0, 0, 0};
+        double scratch_ms[T_NCAT] = {0, 0, 0, 0, 0, 0, 0};
         ctx->timer.collect(scratch_ms);
     });
 }

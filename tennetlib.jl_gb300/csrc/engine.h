@@ -12,7 +12,7 @@ namespace tn {
 
 // CUDA-event interval timer: intervals are recorded on the stream and resolved only at the
 // next synchronisation point, so timing adds no host round trips.
-enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_GEMM, T_NCAT };
+enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_GEMM, T_PACK, T_NCAT };
 struct EventTimer {
     cudaStream_t s = nullptr;
     std::vector<cudaEvent_t> pool;
@@ -33,10 +33,12 @@ struct Scratch;  // fixed-capacity device scratch used by the allocation-free en
 
 struct tn_ctx {
     int device = 0;
+    int nsm = 0;
     cudaStream_t stream = nullptr;
     int prec = TN_PREC_FP64;
-    int slices = 4;
+    int slices = 5;
     tn::EventTimer timer;
+    tn::DevBuf err;  // device error word of bounded waits (0 = ok)
 };
 
 struct tn_mpo {
@@ -75,6 +77,7 @@ struct tn_envt {
 struct Heff2Plan {
     tn::PhiLayout ph;
     tn::GemmPlan g1, g3;
+    std::unique_ptr<tn::SplitPlan> s1, s3;  // split-precision plans (built on first use)
     tn::CombPlan cb;
     int64_t ysize = 0, zsize = 0;
     double flops = 0;
@@ -92,7 +95,7 @@ struct tn_env {
         vecB;
     std::unique_ptr<Heff2Plan> hp;
     int hp_pos = -1;
-    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0};
+    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0, 0};
     double gemm_flops = 0;
     int64_t gemm_launches = 0;
     int64_t matvecs = 0;

@@ -181,6 +181,44 @@ struct CombPlan {
     void finalize(cudaStream_t s);
 };
 
+// split-precision (bf16 slice) GEMM descriptors.  A packed operand is a list of tiles
+// (row tile, k tile, slice) of the canonical K-major SWIZZLE_128B layout.
+struct KTileSrc {        // one k tile of one task's operand: element (r, k) at
+    int64_t off;         // p[buf][off + r * sr + k * sk]
+    int32_t buf, sr, sk, kvalid;
+};
+struct PackJob {         // one row tile of one task's operand
+    int64_t out_off;     // byte offset of (this row tile, k tile 0, slice 0)
+    int32_t kt0, nkt, rows, row0, eoff, pad;
+};
+struct SplitTask {
+    int64_t coff, a_off, b_off;
+    int32_t cbuf, m, n, ldc, nkt, ea_off, eb_off, pad;
+};
+struct SplitItem {
+    int32_t task, mt, nt, pad;
+};
+struct SplitPlan {
+    std::vector<SplitTask> tasks;
+    std::vector<SplitItem> items;
+    std::vector<PackJob> ajobs, bjobs;
+    std::vector<KTileSrc> aks, bks;
+    int64_t abytes = 0, bbytes = 0, ea_n = 0, eb_n = 0;
+    int slices = 0;
+    bool a_static = false, b_static = false, a_packed = false, b_packed = false;
+    DevBuf dtasks, ditems, dajobs, dbjobs, daks, dbks, apack, bpack, ea, eb;
+};
+int split_tile_bytes_a();
+int split_tile_bytes_b();
+int split_tile_rows_a();
+int split_tile_rows_b();
+int split_ktile();
+void launch_split_pack(const PackJob* jobs, int njobs, const KTileSrc* ksrc, const Bases& b,
+                       uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s);
+void launch_split_gemm(const SplitItem* items, int nitems, const SplitTask* tasks,
+                       const uint8_t* apack, const uint8_t* bpack, const int* ea, const int* eb,
+                       const Bases& b, int slices, int* err, int nsm, cudaStream_t s);
+
 constexpr int GEMM_BM = 64, GEMM_BN = 64;
 constexpr int COMB_TR = 32, COMB_TC = 32;
 
