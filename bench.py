@@ -305,12 +305,14 @@ def run_ours(args, world, rank, local, pg):
         roof = {"bound": "fp64", "achieved": gemm_tflops, "peak": FP64_PEAK_NOMINAL_TFLOPS,
                 "unit": "TFLOP/s", "frac": gemm_tflops / FP64_PEAK_NOMINAL_TFLOPS,
                 "peak_note": "of nominal GB300 FP64 (no measured FP64 peak on this pool)"}
-    roof["kernel"] = "grouped block-sparse GEMM of H_eff (two launches per matvec)"
+    roof["kernel"] = ("tcgen05 split-precision grouped GEMM of H_eff (two launches per matvec)"
+                      if args.precision == "split" else
+                      "FP64 grouped block-sparse GEMM of H_eff (two launches per matvec)")
     roof["flops_per_launch"] = gemm_fl / max(gemm_n, 1)
     roof["ms_per_launch"] = gemm_ms / max(gemm_n, 1)
     roof["traffic"] = None
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
-             for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms")}
+             for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
     res = {
         "metric": METRIC, "value": dev_s, "unit": "s/sweep", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
@@ -329,9 +331,31 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": d2h,
                 "what": "upload MPS from host + build environments + one sweep + download MPS"},
     }
+    if args.precision == "split" and not args.no_fp64_compare:
+        res["fp64_compare"] = fp64_compare(tn, ctx, H, pq, tensors, links, local)
     if world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline_from(tensors, links)
     print(json.dumps(res), flush=True)
+
+
+def fp64_compare(tn, ctx, H, pq, tensors, links, local):
+    """One sweep from the same state on the split path and on the FP64 GPU path."""
+    out = {}
+    ctx64 = tn.Context(local, precision="fp64")
+    H64, _ = heisenberg(tn, ctx64)
+    for name, c, h in (("split", ctx, H), ("fp64", ctx64, H64)):
+        e = tn.StateEnvs(tn.MPS(tensors, links, pq, 0, c), h)
+        sw = tn.SweepData()
+        tn.fullsweep_(e, tn.eig_solver, 2, sw, **sweep_kwargs(MAXDIM))
+        st = sw.stats[-1]
+        out[name] = {"sweep_s": st["sweep_ms"] / 1e3, "energy": sw.energy[-1],
+                     "heff_ms": st["heff_ms"], "svd_ms": st["svd_ms"], "maxlinkdim": sw.maxchi[-1]}
+        del e
+    out["speedup_split_vs_fp64"] = out["fp64"]["sweep_s"] / out["split"]["sweep_s"]
+    out["heff_speedup_split_vs_fp64"] = out["fp64"]["heff_ms"] / max(out["split"]["heff_ms"], 1e-9)
+    out["dE_rel"] = abs(out["split"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])
+    out["same_bond_dims"] = out["split"]["maxlinkdim"] == out["fp64"]["maxlinkdim"]
+    return out
 
 
 def main():
@@ -340,9 +364,10 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
-    ap.add_argument("--slices", type=int, default=4)
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"])
+    ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
