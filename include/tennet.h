@@ -165,6 +165,24 @@ int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t
                     const double* data, int32_t maxdim, int32_t mindim, double cutoff,
                     int32_t* kept, double* svals, double* truncerr);
 
+/* ---- allocation-free block singular values ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot let the library allocate
+ * device memory (a host framework that owns all device memory through its own pool, a
+ * process with a fixed memory budget): singular values of nblocks dense column-major
+ * blocks that already live on the device (concatenated at `blocks`, dimensions in the
+ * host arrays rows/cols), sorted descending per block into the device buffer `svals`
+ * (sum of min(rows, cols) doubles), computed on `stream` (a cudaStream_t, NULL = legacy
+ * default stream) with the same kernel as tn_svd_truncate.  Allocates nothing: its work
+ * space is a file-scope device array of about 16.3 MiB that every GPU on which the
+ * library is loaded holds until the process exits.  Limits: sum rows*cols <= 524288,
+ * sum min(rows, cols) <= 65536, nblocks <= 1024, min(rows, cols) <= 3000 per block;
+ * larger requests return TN_E_INVALID.  The first call on a device looks up the work
+ * array's address with that device current, so make it before any stream capture.  All
+ * calls share the work array: calls that overlap on the GPU race and must be serialised
+ * by the caller.  The call is asynchronous; synchronise `stream` before reading svals. */
+int tn_block_svals_noalloc(int device, const double* blocks, int nblocks, const int32_t* rows,
+                           const int32_t* cols, double* svals, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

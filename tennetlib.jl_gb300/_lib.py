@@ -103,6 +103,7 @@ PROTOS = {
                                    C.c_int, i32p]),
     "tn_svd_truncate": (C.c_int, [vp, C.c_int, i32p, i32p, f64p, C.c_int32, C.c_int32,
                                   C.c_double, i32p, f64p, f64p]),
+    "tn_block_svals_noalloc": (C.c_int, [C.c_int, vp, C.c_int, i32p, i32p, vp, vp]),
 }
 
 _lib = None

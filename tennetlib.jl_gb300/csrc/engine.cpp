@@ -1176,6 +1176,8 @@ void phi_dense_map(const PhiLayout& ph, const Link& lk, const Link& rk, int d,
 
 }  // namespace
 
+void tn::set_last_error(const char* msg) { g_err = msg; }
+
 // -------------------------------------------------------------------------------------
 // EventTimer
 // -------------------------------------------------------------------------------------

@@ -21,6 +21,7 @@ struct Error : std::runtime_error {
 };
 
 void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+void set_last_error(const char* msg);  // message returned by tn_last_error() on this thread
 #define TN_CUDA(x)                                                          \
     do {                                                                    \
         cudaError_t _e = (x);                                               \
