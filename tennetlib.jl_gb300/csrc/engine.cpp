@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <numeric>
 
 using namespace tn;
@@ -182,7 +183,7 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
     const int KT = split_ktile(), RA = split_tile_rows_a(), RB = split_tile_rows_b();
     const int64_t TA = split_tile_bytes_a(), TB = split_tile_bytes_b();
     int64_t aoff = 0, boff = 0, eao = 0, ebo = 0;
-    std::vector<std::pair<int, int>> order;  // (nkt, task) for scheduling heavy first
+    std::map<std::vector<int64_t>, std::pair<int64_t, int64_t>> bseen;  // B signature -> offsets
     for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
         const Task& t = g.tasks[ti];
         struct KT3 { int seg, k0, kv; };
@@ -193,17 +194,28 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
         }
         const int nkt = (int)kts.size();
         const int mt = (t.m + RA - 1) / RA, nt = (t.n + RB - 1) / RB;
+        // tasks whose B operand is the same matrix (e.g. one two-site slab multiplied by
+        // the environment blocks of every MPO state) share one packed copy
+        std::vector<int64_t> bsig;
+        bsig.push_back(t.n);
+        for (int j = 0; j < t.nseg; ++j) {
+            const Seg& sg = g.segs[t.seg0 + j];
+            bsig.insert(bsig.end(), {int64_t(sg.bbuf), sg.boff, int64_t(sg.ldb), int64_t(sg.tb),
+                                     int64_t(sg.k)});
+        }
+        auto bit = bseen.find(bsig);
+        const bool bnew = bit == bseen.end();
         SplitTask stsk{};
         stsk.coff = t.coff;
         stsk.a_off = aoff;
-        stsk.b_off = boff;
+        stsk.b_off = bnew ? boff : bit->second.first;
         stsk.cbuf = t.cbuf;
         stsk.m = t.m;
         stsk.n = t.n;
         stsk.ldc = t.ldc;
         stsk.nkt = nkt;
         stsk.ea_off = int32_t(eao);
-        stsk.eb_off = int32_t(ebo);
+        stsk.eb_off = bnew ? int32_t(ebo) : int32_t(bit->second.second);
         sp->tasks.push_back(stsk);
         const int akt0 = (int)sp->aks.size(), bkt0 = (int)sp->bks.size();
         for (const auto& k : kts) {
@@ -215,6 +227,7 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
             a.off = sg.aoff + int64_t(k.k0) * a.sk;
             a.kvalid = k.kv;
             sp->aks.push_back(a);
+            if (!bnew) continue;
             KTileSrc bsrc{};
             bsrc.buf = sg.bbuf;
             bsrc.sr = sg.tb ? 1 : sg.ldb;
@@ -226,15 +239,20 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
         for (int mi = 0; mi < mt; ++mi)
             sp->ajobs.push_back(PackJob{aoff + int64_t(mi) * nkt * slices * TA, akt0, nkt,
                                         std::min(RA, t.m - mi * RA), mi * RA, int32_t(eao + mi * RA), 0});
-        for (int ni = 0; ni < nt; ++ni)
-            sp->bjobs.push_back(PackJob{boff + int64_t(ni) * nkt * slices * TB, bkt0, nkt,
-                                        std::min(RB, t.n - ni * RB), ni * RB, int32_t(ebo + ni * RB), 0});
+        if (bnew)
+            for (int ni = 0; ni < nt; ++ni)
+                sp->bjobs.push_back(PackJob{boff + int64_t(ni) * nkt * slices * TB, bkt0, nkt,
+                                            std::min(RB, t.n - ni * RB), ni * RB,
+                                            int32_t(ebo + ni * RB), 0});
         for (int mi = 0; mi < mt; ++mi)
             for (int ni = 0; ni < nt; ++ni) sp->items.push_back(SplitItem{int32_t(ti), mi, ni, 0});
         aoff += int64_t(mt) * nkt * slices * TA;
-        boff += int64_t(nt) * nkt * slices * TB;
         eao += int64_t(mt) * RA;
-        ebo += int64_t(nt) * RB;
+        if (bnew) {
+            bseen.emplace(bsig, std::make_pair(boff, ebo));
+            boff += int64_t(nt) * nkt * slices * TB;
+            ebo += int64_t(nt) * RB;
+        }
     }
     std::stable_sort(sp->items.begin(), sp->items.end(), [&](const SplitItem& x, const SplitItem& y) {
         return sp->tasks[x.task].nkt > sp->tasks[y.task].nkt;

@@ -163,57 +163,93 @@ __device__ __forceinline__ double pow2(int e) {
 }
 
 // ------------------------------------------------------------------------------------
-// pack kernel: one CTA per row tile (128 rows for A, 64 for B), one thread per row
+// pack kernel: one CTA per row tile (128 rows for A, 64 for B)
 // ------------------------------------------------------------------------------------
-__global__ void split_pack_kernel(const PackJob* __restrict__ jobs,
-                                  const KTileSrc* __restrict__ ksrc, Bases b,
-                                  uint8_t* __restrict__ out, int* __restrict__ expo,
-                                  int slices, int tile_rows) {
+constexpr int PACK_THREADS = 256;
+
+// Work item of the pack kernel: row r of the tile and one 8-wide chunk (16 bytes of bf16)
+// of one k tile; consecutive threads take consecutive rows so that the loads of a column-
+// major operand coalesce, and each thread keeps 8 independent loads in flight.
+__global__ void __launch_bounds__(PACK_THREADS)
+split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__ ksrc, Bases b,
+                  uint8_t* __restrict__ out, int* __restrict__ expo, int slices, int tile_rows) {
+    __shared__ unsigned long long rowmax[BM];
     const PackJob jb = jobs[blockIdx.x];
-    const int r = threadIdx.x;
-    const bool live = r < jb.rows;
     const int tile_bytes = tile_rows * BKT * 2;
-    // pass 1: row maximum over all k tiles
-    double mx = 0.0;
-    if (live)
-        for (int t = 0; t < jb.nkt; ++t) {
-            const KTileSrc ks = ksrc[jb.kt0 + t];
-            if (ks.kvalid <= 0) continue;
-            const double* x = b.p[ks.buf] + ks.off + int64_t(jb.row0 + r) * ks.sr;
-            for (int k = 0; k < ks.kvalid; ++k) mx = fmax(mx, fabs(x[int64_t(k) * ks.sk]));
-        }
-    int E = 0;
-    if (mx > 0.0) E = int((__double_as_longlong(mx) >> 52) & 0x7ff) - 1022;
-    if (live) expo[jb.eoff + r] = E;
-    const double scale = (mx > 0.0) ? pow2(8 * slices - E) : 0.0;
-    // pass 2: digits, 8 k values (one 16-byte chunk) at a time
-    for (int t = 0; t < jb.nkt; ++t) {
+    const int per_tile = tile_rows * 8;             // (row, chunk) items per k tile
+    const int nitems = per_tile * jb.nkt;
+    for (int r = threadIdx.x; r < tile_rows; r += blockDim.x) rowmax[r] = 0ull;
+    __syncthreads();
+    // pass 1: row maxima of |x| as IEEE bit patterns (integer compare, no FP64 pipe)
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+        const int t = it / per_tile, rem = it % per_tile;
+        const int r = rem % tile_rows, ch = rem / tile_rows;
+        if (r >= jb.rows) continue;
         const KTileSrc ks = ksrc[jb.kt0 + t];
-        const double* x =
-            live && ks.kvalid > 0 ? b.p[ks.buf] + ks.off + int64_t(jb.row0 + r) * ks.sr : nullptr;
-        uint8_t* tile0 = out + jb.out_off + int64_t(t) * slices * tile_bytes;
-        for (int ch = 0; ch < 8; ++ch) {
-            __nv_bfloat16 dig[7][8];
+        const long long* x = reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
+                             int64_t(jb.row0 + r) * ks.sr;
+        unsigned long long mx = 0ull;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int k = ch * 8 + q;
-                long long X = 0;
-                if (x && k < ks.kvalid) X = llrint(x[int64_t(k) * ks.sk] * scale);
-                for (int i = slices - 1; i >= 1; --i) {
-                    int d = int(X & 255);
-                    if (d > 128) d -= 256;
-                    X = (X - d) >> 8;
-                    dig[i][q] = __float2bfloat16_rn(ldexpf(float(d), -8 * i));
+        for (int q = 0; q < 8; ++q) {
+            const int k = ch * 8 + q;
+            if (k < ks.kvalid) {
+                const unsigned long long v = (unsigned long long)(x[int64_t(k) * ks.sk]) & 0x7fffffffffffffffull;
+                mx = v > mx ? v : mx;
+            }
+        }
+        if (mx) atomicMax(&rowmax[r], mx);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < jb.rows; r += blockDim.x) {
+        const unsigned long long m = rowmax[r];
+        expo[jb.eoff + r] = m ? int((m >> 52) & 0x7ff) - 1022 : 0;
+    }
+    // pass 2: balanced base-256 digits.  x * 2^(8s - E) = sig * 2^(ex - 1075 + 8s - E), sig
+    // the 53-bit significand: the rounded integer is sig shifted right by
+    // sh = 1075 + E - 8s - ex (round half away from zero), integer pipe only.
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+        const int t = it / per_tile, rem = it % per_tile;
+        const int r = rem % tile_rows, ch = rem / tile_rows;
+        const KTileSrc ks = ksrc[jb.kt0 + t];
+        const bool live = r < jb.rows && ks.kvalid > 0;
+        const unsigned long long mxb = live ? rowmax[r] : 0ull;
+        const int E = mxb ? int((mxb >> 52) & 0x7ff) - 1022 : 0;
+        const int base_sh = 1075 + E - 8 * slices;
+        const long long* x = live ? reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
+                                        int64_t(jb.row0 + r) * ks.sr
+                                  : nullptr;
+        __nv_bfloat16 dig[7][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = ch * 8 + q;
+            long long X = 0;
+            if (mxb && k < ks.kvalid) {
+                const long long v = x[int64_t(k) * ks.sk];
+                const int ex = int((v >> 52) & 0x7ff);
+                if (ex) {  // subnormals are far below the row scale: they round to 0
+                    const long long m = (v & 0xfffffffffffffLL) | (1LL << 52);
+                    const int sh = base_sh - ex;
+                    long long a = 0;
+                    if (sh <= 0) a = m << (-sh);
+                    else if (sh < 63) a = (m + (1LL << (sh - 1))) >> sh;
+                    X = v < 0 ? -a : a;
                 }
-                dig[0][q] = __float2bfloat16_rn(float(X));
             }
-            // swizzled position of (row r, chunk ch): 8-row atoms of 1024 bytes
-            const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((ch ^ (r & 7)) << 4);
-            for (int i = 0; i < slices; ++i) {
-                uint4 v;
-                __builtin_memcpy(&v, dig[i], 16);
-                *reinterpret_cast<uint4*>(tile0 + int64_t(i) * tile_bytes + off) = v;
+            for (int i = slices - 1; i >= 1; --i) {
+                int d = int(X & 255);
+                if (d > 128) d -= 256;
+                X = (X - d) >> 8;
+                dig[i][q] = __float2bfloat16_rn(ldexpf(float(d), -8 * i));
             }
+            dig[0][q] = __float2bfloat16_rn(float(X));
+        }
+        // swizzled position of (row r, chunk ch): 8-row atoms of 1024 bytes
+        uint8_t* tile0 = out + jb.out_off + int64_t(t) * slices * tile_bytes;
+        const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((ch ^ (r & 7)) << 4);
+        for (int i = 0; i < slices; ++i) {
+            uint4 v;
+            __builtin_memcpy(&v, dig[i], 16);
+            *reinterpret_cast<uint4*>(tile0 + int64_t(i) * tile_bytes + off) = v;
         }
     }
 }
@@ -426,7 +462,8 @@ void launch_split_pack(const PackJob* jobs, int njobs, const KTileSrc* ksrc, con
                        uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s) {
     if (njobs <= 0) return;
     TN_REQUIRE(slices >= 4 && slices <= 7, "split precision needs 4..7 slices");
-    split_pack_kernel<<<njobs, tile_rows, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
+    TN_REQUIRE(tile_rows <= BM, "pack tile taller than the A tile");
+    split_pack_kernel<<<njobs, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
     TN_CUDA(cudaGetLastError());
     count_launch();
 }

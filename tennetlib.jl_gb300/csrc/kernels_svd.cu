@@ -117,7 +117,7 @@ __device__ double block_sum(double v, double* red) {
 //     global work buffer X);
 //  2. FP32 one-sided Jacobi on R^T, accumulating V in float: graded R^T makes cyclic Jacobi
 //     converge in a few sweeps (Drmac & Veselic, SIMAX 29, 2008);
-//  3. V re-orthonormalised in FP64 (two-pass classical Gram-Schmidt);
+//  3. V re-orthonormalised in FP64 (one classical Gram-Schmidt pass);
 //  4. Y = R^T V and FP64 one-sided Jacobi polish of Y with V accumulation (quadratic
 //     convergence from the FP32 start: Higham, Tisseur, Webb & Zhou, SIMAX 42, 2021);
 //  5. QV = Q [V; 0] (reflectors applied in reverse order) and PY = P Y.
@@ -245,13 +245,14 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     __syncthreads();
     const int sw32 = jacobi_sweeps<float>(x32, v32, n, n, 2.0e-5f, 30, &rotated);
     __syncthreads();
-    // 3. V (FP64) in the Q region, two-pass Gram-Schmidt
+    // 3. V (FP64) in the Q region, one Gram-Schmidt pass (V32 is orthogonal to ~1e-6, so a
+    //    single classical pass already reaches FP64 orthogonality)
     double* v = Qm;
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) v[e] = double(v32[e]);
     __syncthreads();
     for (int j = 0; j < n; ++j) {
         double* vj = v + int64_t(j) * n;
-        for (int pass = 0; pass < 2; ++pass) {
+        for (int pass = 0; pass < 1; ++pass) {
             for (int i = warp; i < j; i += nwarps) {
                 const double* vi = v + int64_t(i) * n;
                 double a = 0.0;
