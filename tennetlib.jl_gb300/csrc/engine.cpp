@@ -772,6 +772,11 @@ EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
     env->kry.alloc(size_t(nvec) * size_t(std::max<int64_t>(n, 1)) * 8, st);
     env->part.alloc(size_t(32) * blas_nparts() * 8, st);
     env->dots.alloc(128 * 8, st);
+    if (!env->ticket.p) {
+        env->ticket.alloc(sizeof(unsigned), st);
+        TN_CUDA(cudaMemsetAsync(env->ticket.p, 0, sizeof(unsigned), st));
+    }
+    unsigned* tk = env->ticket.as<unsigned>();
     std::vector<double*> pool;
     for (int i = 0; i < nvec; ++i) pool.push_back(env->kry.d() + int64_t(i) * n);
     double* dv = env->dots.d();
@@ -790,12 +795,9 @@ EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
     auto gs2 = [&](int K, std::vector<double>& h, double& beta) {
         // h = V^T w ; w -= V h ; twice ; beta = |w|
         const int e0 = ctx->timer.mark();
-        launch_multi_dot(V.data(), K, w, n, env->part.d(), dv, st);
-        launch_multi_axpy(w, V.data(), K, dv, -1.0, n, st);
-        launch_multi_dot(V.data(), K, w, n, env->part.d(), dv + 32, st);
-        launch_multi_axpy(w, V.data(), K, dv + 32, -1.0, n, st);
-        const double* wp = w;
-        launch_multi_dot(&wp, 1, w, n, env->part.d(), dv + 64, st);
+        launch_gs_pass(V.data(), K, w, nullptr, 0.0, n, true, false, env->part.d(), dv, tk, st);
+        launch_gs_pass(V.data(), K, w, dv, -1.0, n, true, false, env->part.d(), dv + 32, tk, st);
+        launch_gs_pass(V.data(), K, w, dv + 32, -1.0, n, false, true, env->part.d(), dv + 64, tk, st);
         ctx->timer.add(T_LANCZOS, e0, ctx->timer.mark());
         TN_CUDA(cudaMemcpyAsync(hostd.data(), dv, 65 * 8, cudaMemcpyDeviceToHost, st));
         sync(ctx);

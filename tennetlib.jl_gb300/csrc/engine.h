@@ -91,8 +91,8 @@ struct tn_env {
     int lpos = 0, rpos = 0;
     int pos = 0, nsite = 2;
     // work buffers
-    tn::DevBuf t1, t2, kry, part, dots, svdX, svdW, svdV, svdP, svdS, svdPerm, desc, desc2, vecA,
-        vecB;
+    tn::DevBuf t1, t2, kry, part, dots, ticket, svdX, svdW, svdV, svdP, svdS, svdPerm, desc, desc2,
+        vecA, vecB;
     std::unique_ptr<Heff2Plan> hp;
     int hp_pos = -1;
     double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0, 0};

@@ -205,6 +205,69 @@ lincomb_kernel(double* __restrict__ dst, VecPtrs V, int kk, const double* __rest
     }
 }
 
+// One fused Gram-Schmidt pass over a Krylov residual w:
+//   (optional)  w += sign * sum_k hin[k] V_k
+//   (optional)  out[k] = V_k . w   for k < kk          (with the updated w)
+//   (optional)  out[kk or 0] = w . w
+// Partial sums of every block go to `part`; the last block to finish (atomic ticket)
+// adds them in block order, so results are deterministic, and resets the ticket.
+template <int K>
+__global__ void __launch_bounds__(BLAS_THREADS)
+gs_pass_kernel(VecPtrs V, int kk, double* __restrict__ w, const double* __restrict__ hin,
+               double sign, int64_t n, int dots, int norm, double* __restrict__ part,
+               double* __restrict__ out, unsigned* __restrict__ ticket) {
+    __shared__ double hs[KMAX];
+    __shared__ double red[BLAS_THREADS / 32][K + 1];
+    __shared__ int last;
+    if (hin && threadIdx.x < kk) hs[threadIdx.x] = sign * hin[threadIdx.x];
+    __syncthreads();
+    double acc[K + 1];
+#pragma unroll
+    for (int k = 0; k <= K; ++k) acc[k] = 0.0;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double x = w[i];
+        if (hin) {
+            for (int k = 0; k < kk; ++k) x = fma(hs[k], V.p[k][i], x);
+            w[i] = x;
+        }
+        if (dots) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (k < kk) acc[k] = fma(V.p[k][i], x, acc[k]);
+        }
+        if (norm) acc[K] = fma(x, x, acc[K]);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nres = (dots ? kk : 0) + (norm ? 1 : 0);
+#pragma unroll
+    for (int k = 0; k <= K; ++k) {
+        const double v = warp_sum(acc[k]);
+        if (lane == 0) red[wid][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nres) {
+        const int src = (dots && threadIdx.x < kk) ? threadIdx.x : K;
+        double sum = 0.0;
+        for (int j = 0; j < BLAS_THREADS / 32; ++j) sum += red[j][src];
+        part[int64_t(threadIdx.x) * gridDim.x + blockIdx.x] = sum;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int j = wid; j < nres; j += BLAS_THREADS / 32) {
+        double sum = 0.0;
+        for (int bb = lane; bb < (int)gridDim.x; bb += 32)
+            sum += reinterpret_cast<volatile double*>(part)[int64_t(j) * gridDim.x + bb];
+        sum = warp_sum(sum);
+        if (lane == 0) out[j] = sum;
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
 int grid_for(int64_t n) {
     int64_t g = (n + BLAS_THREADS - 1) / BLAS_THREADS;
     if (g > BLAS_PARTS) g = BLAS_PARTS;
@@ -262,6 +325,24 @@ void launch_multi_axpy(double* w, const double* const* V, int K, const double* h
                        int64_t n, cudaStream_t s) {
     if (K <= 0 || n <= 0) return;
     multi_axpy_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(w, make_ptrs(V, K), K, h, sign, n);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void launch_gs_pass(const double* const* V, int K, double* w, const double* hin, double sign,
+                    int64_t n, bool dots, bool norm, double* part, double* out, unsigned* ticket,
+                    cudaStream_t s) {
+    VecPtrs P = K > 0 ? make_ptrs(V, K) : VecPtrs{};
+    const int g = BLAS_PARTS;
+    const int d = dots ? 1 : 0, nm = norm ? 1 : 0;
+    if (K <= 4)
+        gs_pass_kernel<4><<<g, BLAS_THREADS, 0, s>>>(P, K, w, hin, sign, n, d, nm, part, out, ticket);
+    else if (K <= 8)
+        gs_pass_kernel<8><<<g, BLAS_THREADS, 0, s>>>(P, K, w, hin, sign, n, d, nm, part, out, ticket);
+    else if (K <= 16)
+        gs_pass_kernel<16><<<g, BLAS_THREADS, 0, s>>>(P, K, w, hin, sign, n, d, nm, part, out, ticket);
+    else
+        gs_pass_kernel<32><<<g, BLAS_THREADS, 0, s>>>(P, K, w, hin, sign, n, d, nm, part, out, ticket);
     TN_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -239,6 +239,11 @@ void launch_multi_dot(const double* const* V, int K, const double* w, int64_t n,
                       double* part, double* out, cudaStream_t s);
 void launch_multi_axpy(double* w, const double* const* V, int K, const double* h,
                        double sign, int64_t n, cudaStream_t s);
+// Fused Gram-Schmidt pass (see kernels_f64.cu): optional w += sign * V hin, optional dots
+// V^T w into out[0..K), optional |w|^2 into out[K or 0]; one launch, deterministic.
+void launch_gs_pass(const double* const* V, int K, double* w, const double* hin, double sign,
+                    int64_t n, bool dots, bool norm, double* part, double* out, unsigned* ticket,
+                    cudaStream_t s);
 void launch_scale_into(double* dst, const double* src, const double* denom_sq_or_null,
                        double host_scale, int64_t n, cudaStream_t s);
 void launch_lincomb(double* dst, const double* const* V, int K, const double* coef,
