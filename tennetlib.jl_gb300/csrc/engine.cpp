@@ -938,18 +938,28 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
                                 cudaMemcpyHostToDevice, st));
     static const bool dbg = std::getenv("TENNET_DEBUG_SVD") != nullptr;
     DevBuf dsw;
-    if (dbg) dsw.alloc(size_t(std::max(nb, 1)) * 4, st);
+    const size_t clk_off = size_t((nb + 1) & ~1) * 4;  // 8-byte aligned clock area
+    if (dbg) dsw.alloc(clk_off + size_t(std::max(nb, 1)) * 8 * 8, st);
     const int e0 = ctx->timer.mark();
     launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nb, maxn, src, dX.d(), dW.d(), dV.d(), dP.d(),
                       dS.d(), dPerm.as<int>(), dbg ? dsw.as<int>() : nullptr, st);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
     if (dbg && nb) {
         std::vector<int> sw(nb);
+        std::vector<long long> ck(size_t(nb) * 8);
         TN_CUDA(cudaMemcpyAsync(sw.data(), dsw.p, nb * 4, cudaMemcpyDeviceToHost, st));
+        TN_CUDA(cudaMemcpyAsync(ck.data(), static_cast<char*>(dsw.p) + clk_off, ck.size() * 8,
+                                cudaMemcpyDeviceToHost, st));
         TN_CUDA(cudaStreamSynchronize(st));
-        for (int b = 0; b < nb; ++b)
-            std::fprintf(stderr, "svd block %d: %dx%d sweeps fp32=%d fp64=%d\n", b, R.desc[b].m,
-                         R.desc[b].n, sw[b] >> 16, sw[b] & 0xffff);
+        for (int b = 0; b < nb; ++b) {
+            const long long* c = &ck[size_t(b) * 8];
+            std::fprintf(stderr,
+                         "svd block %d: %dx%d sweeps fp32=%d fp64=%d kcycles qr=%lld fp32=%lld "
+                         "gs=%lld y=%lld polish=%lld norms=%lld qv=%lld\n",
+                         b, R.desc[b].m, R.desc[b].n, sw[b] >> 16, sw[b] & 0xffff, (c[1] - c[0]) / 1000,
+                         (c[2] - c[1]) / 1000, (c[3] - c[2]) / 1000, (c[4] - c[3]) / 1000,
+                         (c[5] - c[4]) / 1000, (c[6] - c[5]) / 1000, (c[7] - c[6]) / 1000);
+        }
     }
     R.S.resize(size_t(so));
     if (so)

@@ -70,10 +70,17 @@ __device__ int jacobi_sweeps(T* x, T* v, int m, int n, T tol, int max_sweeps, in
                 a = gsum8(a);
                 bb = gsum8(bb);
                 g = gsum8(g);
-                const bool rot = act && (fabs(g) > tol * sqrt(a) * sqrt(bb));
+                bool rot = act && a > T(0) && bb > T(0) && (fabs(g) > tol * sqrt(a) * sqrt(bb));
+                T tt = T(0);
                 if (rot) {
                     const T zeta = (bb - a) / (T(2) * g);
-                    const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+                    const T az = fabs(zeta);
+                    // |zeta| large (graded columns): tan = 1/(2 zeta) avoids zeta^2 overflow
+                    tt = az > T(1e15) ? T(0.5) / zeta
+                                      : (zeta >= T(0) ? T(1) : T(-1)) / (az + sqrt(T(1) + zeta * zeta));
+                    rot = isfinite(tt) && tt != T(0);  // a no-op rotation is not a rotation
+                }
+                if (rot) {
                     const T c = T(1) / sqrt(T(1) + tt * tt);
                     const T sn = c * tt;
                     for (int t = sub; t < m; t += 8) {
@@ -100,14 +107,138 @@ __device__ int jacobi_sweeps(T* x, T* v, int m, int n, T tol, int max_sweeps, in
     return sweep;
 }
 
-__device__ double block_sum(double v, double* red) {
+// ------------------------------------------------------------------------------------
+// double-float (FP32 pair) arithmetic: about 48 significant bits on the FP32 pipe, which
+// on GB300 issues 64 times the FP64 rate (Dekker 1971; TwoSum/TwoProd via FMA)
+// ------------------------------------------------------------------------------------
+struct __align__(8) df2 {
+    float hi, lo;
+};
+__device__ __forceinline__ df2 fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return df2{s, b - (s - a)};
+}
+__device__ __forceinline__ df2 df_add(df2 a, df2 b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    return fast_two_sum(s, e);
+}
+__device__ __forceinline__ df2 df_neg(df2 a) { return df2{-a.hi, -a.lo}; }
+__device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df2 df_fma(df2 a, df2 b, df2 c) { return df_add(df_mul(a, b), c); }
+__device__ __forceinline__ df2 df_shfl_xor(df2 a, int o) {
+    return df2{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
+__device__ __forceinline__ df2 df_from_double(double x) {
+    const float h = __double2float_rn(x);
+    return df2{h, __double2float_rn(x - double(h))};
+}
+__device__ __forceinline__ double df_to_double(df2 a) { return double(a.hi) + double(a.lo); }
+// 1 / sqrt(u) in double-float: FP32 estimate + one Newton step
+__device__ __forceinline__ df2 df_rsqrt(df2 u) {
+    const df2 y0{rsqrtf(u.hi), 0.f};
+    const df2 e = df_add(df2{1.f, 0.f}, df_neg(df_mul(u, df_mul(y0, y0))));
+    return df_add(y0, df_mul(df_mul(y0, e), df2{0.5f, 0.f}));
+}
+
+// One-sided Jacobi sweeps in double-float on the columns of x (m x n) with rotations
+// accumulated into v (n x n); same pairing and layout as jacobi_sweeps.  The rotation
+// angle comes from FP32 (it only has to zero the pair to ~1e-7 of itself, which a sweep
+// squares), while c and s are formed in double-float from that angle so that every
+// rotation is orthogonal to double-float precision.  No FP64 instruction is executed.
+__device__ int jacobi_sweeps_df(df2* x, df2* v, int m, int n, float tol, int max_sweeps,
+                                int* rotated) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    v = wsum(v);
+    const int grp = lane >> 3, sub = lane & 7;
+    const int nn = n + (n & 1);
+    const int npairs = nn / 2;
+    const int slots = nwarps * 4;
+    int sweep = 0;
+    if (n < 2) return 0;
+    for (sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) *rotated = 0;
+        __syncthreads();
+        for (int r = 0; r < nn - 1; ++r) {
+            for (int base = 0; base < npairs; base += slots) {
+                const int k = base + warp * 4 + grp;
+                int i = 0, j = 0;
+                const bool live = k < npairs;
+                if (live) rr_pair(nn, r, k, i, j);
+                const bool act = live && j < n;
+                df2 a{0.f, 0.f}, bb{0.f, 0.f}, g{0.f, 0.f};
+                df2* xi = x + int64_t(i) * m;
+                df2* xj = x + int64_t(j) * m;
+                if (act)
+                    for (int t = sub; t < m; t += 8) {
+                        const df2 p = xi[t], q = xj[t];
+                        a = df_fma(p, p, a);
+                        bb = df_fma(q, q, bb);
+                        g = df_fma(p, q, g);
+                    }
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) {
+                    a = df_add(a, df_shfl_xor(a, o));
+                    bb = df_add(bb, df_shfl_xor(bb, o));
+                    g = df_add(g, df_shfl_xor(g, o));
+                }
+                bool rot = act && a.hi > 0.f && bb.hi > 0.f &&
+                           (fabsf(g.hi) > tol * sqrtf(a.hi) * sqrtf(bb.hi));
+                float tt = 0.f;
+                if (rot) {
+                    const df2 d = df_add(bb, df_neg(a));
+                    const float zeta = (d.hi + d.lo) / (2.f * g.hi);
+                    const float az = fabsf(zeta);
+                    // |zeta| large (graded columns): tan = 1/(2 zeta) avoids zeta^2 overflow
+                    tt = az > 1e15f ? 0.5f / zeta
+                                    : (zeta >= 0.f ? 1.f : -1.f) / (az + sqrtf(1.f + zeta * zeta));
+                    rot = isfinite(tt) && tt != 0.f;  // a no-op rotation is not a rotation
+                }
+                if (rot) {
+                    const df2 t2{tt, 0.f};
+                    const df2 c = df_rsqrt(df_add(df2{1.f, 0.f}, df_mul(t2, t2)));
+                    const df2 sn = df_mul(c, t2);
+                    for (int t = sub; t < m; t += 8) {
+                        const df2 p = xi[t], q = xj[t];
+                        xi[t] = df_add(df_mul(c, p), df_neg(df_mul(sn, q)));
+                        xj[t] = df_add(df_mul(sn, p), df_mul(c, q));
+                    }
+                    df2* vi = v + int64_t(i) * n;
+                    df2* vj = v + int64_t(j) * n;
+                    for (int t = sub; t < n; t += 8) {
+                        const df2 p = vi[t], q = vj[t];
+                        vi[t] = df_add(df_mul(c, p), df_neg(df_mul(sn, q)));
+                        vj[t] = df_add(df_mul(sn, p), df_mul(c, q));
+                    }
+                    if (sub == 0) *rotated = 1;
+                }
+            }
+            __syncthreads();
+        }
+        const int done = !*rotated;
+        __syncthreads();
+        if (done) break;
+    }
+    return sweep;
+}
+
+// sum of one double-float per thread over the CTA (fixed order)
+__device__ df2 df_block_sum(df2 v, df2* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_xor(v, o));
     __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    double s = 0.0;
-    for (int w = 0; w < nwarps; ++w) s += red[w];
+    df2 s{0.f, 0.f};
+    for (int w = 0; w < nwarps; ++w) s = df_add(s, red[w]);
     return s;
 }
 
@@ -117,9 +248,11 @@ __device__ double block_sum(double v, double* red) {
 //     global work buffer X);
 //  2. FP32 one-sided Jacobi on R^T, accumulating V in float: graded R^T makes cyclic Jacobi
 //     converge in a few sweeps (Drmac & Veselic, SIMAX 29, 2008);
-//  3. V re-orthonormalised in FP64 (one classical Gram-Schmidt pass);
-//  4. Y = R^T V and FP64 one-sided Jacobi polish of Y with V accumulation (quadratic
-//     convergence from the FP32 start: Higham, Tisseur, Webb & Zhou, SIMAX 42, 2021);
+//  3. V re-orthonormalised in double-float (one classical Gram-Schmidt pass);
+//  4. Y = R^T V and a double-float one-sided Jacobi polish of Y with V accumulation
+//     (quadratic convergence from the FP32 start: Higham, Tisseur, Webb & Zhou, SIMAX 42,
+//     2021); double-float (FP32 pairs, ~48 bits) runs on the FP32 pipe, which issues 64
+//     times the FP64 rate of GB300;
 //  5. QV = Q [V; 0] (reflectors applied in reverse order) and PY = P Y.
 // Then A = QV * diag(s) * (PY / s)^T: QV is the orthonormal factor on the A-row side,
 // PY = (A-column side) * diag(s).  Outputs: QV in W (m x n), PY in V (n x n), singular
@@ -138,6 +271,14 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     const SvdBlockDesc d = desc[blockIdx.x];
     const int m = d.m, n = d.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // optional phase clocks (diagnostics): 8 stamps per block after the sweep counters
+    long long* clk = sweeps_out ? reinterpret_cast<long long*>(sweeps_out + ((gridDim.x + 1) & ~1)) +
+                                      blockIdx.x * 8
+                                : nullptr;
+    auto stamp = [&](int i) {
+        if (clk && threadIdx.x == 0) clk[i] = clock64();
+    };
+    stamp(0);
     // aux: column norms / tau / Gram-Schmidt coefficients (3n doubles) + column perm (n ints)
     double* cn = reinterpret_cast<double*>(smem + smem_region);
     double* tau = cn + n;
@@ -234,68 +375,79 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         }
         __syncthreads();
     }
-    // 2. FP32 Jacobi on R^T (n x n lower triangular) in the P region
+    stamp(1);
+    // 2. R^T as double-float into the W scratch (unused until step 5); FP32 Jacobi on
+    //    R^T (n x n lower triangular) in the P region
+    df2* rt = reinterpret_cast<df2*>(W + d.x_off);
     float* x32 = reinterpret_cast<float*>(Pm);
     float* v32 = x32 + int64_t(n) * n;
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
         const int i = int(e % n), j = int(e / n);
-        x32[e] = (j <= i) ? float(A[j + int64_t(i) * m]) : 0.f;  // R^T[i, j] = R[j, i]
+        const df2 r = (j <= i) ? df_from_double(A[j + int64_t(i) * m]) : df2{0.f, 0.f};  // R^T[i,j] = R[j,i]
+        rt[e] = r;
+        x32[e] = r.hi;
         v32[e] = (i == j) ? 1.f : 0.f;
     }
     __syncthreads();
     const int sw32 = jacobi_sweeps<float>(x32, v32, n, n, 2.0e-5f, 30, &rotated);
     __syncthreads();
-    // 3. V (FP64) in the Q region, one Gram-Schmidt pass (V32 is orthogonal to ~1e-6, so a
-    //    single classical pass already reaches FP64 orthogonality)
-    double* v = Qm;
-    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) v[e] = double(v32[e]);
+    stamp(2);
+    // 3. V in double-float in the Q region, one classical Gram-Schmidt pass (V32 is
+    //    orthogonal to ~1e-6, so one pass reaches double-float orthogonality)
+    df2* v = reinterpret_cast<df2*>(Qm);
+    df2* hd = reinterpret_cast<df2*>(h);
+    df2* redd = reinterpret_cast<df2*>(red);
+    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) v[e] = df2{v32[e], 0.f};
     __syncthreads();
     for (int j = 0; j < n; ++j) {
-        double* vj = v + int64_t(j) * n;
-        for (int pass = 0; pass < 1; ++pass) {
-            for (int i = warp; i < j; i += nwarps) {
-                const double* vi = v + int64_t(i) * n;
-                double a = 0.0;
-                for (int t = lane; t < n; t += 32) a = fma(vi[t], vj[t], a);
-                a = wsum(a);
-                if (lane == 0) h[i] = a;
-            }
-            __syncthreads();
-            for (int t = threadIdx.x; t < n; t += blockDim.x) {
-                double acc = vj[t];
-                for (int i = 0; i < j; ++i) acc = fma(-h[i], v[t + int64_t(i) * n], acc);
-                vj[t] = acc;
-            }
-            __syncthreads();
+        df2* vj = v + int64_t(j) * n;
+        for (int i = warp; i < j; i += nwarps) {
+            const df2* vi = v + int64_t(i) * n;
+            df2 a{0.f, 0.f};
+            for (int t = lane; t < n; t += 32) a = df_fma(vi[t], vj[t], a);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a = df_add(a, df_shfl_xor(a, o));
+            if (lane == 0) hd[i] = a;
         }
-        double ss = 0.0;
-        for (int t = threadIdx.x; t < n; t += blockDim.x) ss = fma(vj[t], vj[t], ss);
-        ss = block_sum(ss, red);
-        const double inv = ss > 0.0 ? 1.0 / sqrt(ss) : 0.0;
-        for (int t = threadIdx.x; t < n; t += blockDim.x) vj[t] *= inv;
+        __syncthreads();
+        df2 ss{0.f, 0.f};
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            df2 acc = vj[t];
+            for (int i = 0; i < j; ++i) acc = df_add(acc, df_neg(df_mul(hd[i], v[t + int64_t(i) * n])));
+            vj[t] = acc;
+            ss = df_fma(acc, acc, ss);
+        }
+        ss = df_block_sum(ss, redd);
+        const df2 inv = ss.hi > 0.f ? df_rsqrt(ss) : df2{0.f, 0.f};
+        for (int t = threadIdx.x; t < n; t += blockDim.x) vj[t] = df_mul(vj[t], inv);
         __syncthreads();
     }
-    // 4. Y = R^T V in the P region (the float arrays there are dead), FP64 polish
-    double* y = Pm;
+    stamp(3);
+    // 4. Y = R^T V (double-float) in the P region (the float arrays there are dead), then
+    //    the double-float Jacobi polish
+    df2* y = reinterpret_cast<df2*>(Pm);
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
         const int i = int(e % n), j = int(e / n);
-        const double* vj = v + int64_t(j) * n;
-        const double* ri = A + int64_t(i) * m;  // column i of R: R[k, i], k <= i
-        double acc = 0.0;
-        for (int k = 0; k <= i; ++k) acc = fma(ri[k], vj[k], acc);
+        const df2* vj = v + int64_t(j) * n;
+        df2 acc{0.f, 0.f};
+        for (int k = 0; k <= i; ++k) acc = df_fma(rt[i + int64_t(k) * n], vj[k], acc);
         y[e] = acc;
     }
     __syncthreads();
-    const double tol = 2.220446049250313e-16 * sqrt(double(n > 1 ? n : 1)) * 32.0;
-    const int sw64 = jacobi_sweeps<double>(y, v, n, n, tol, 30, &rotated);
+    stamp(4);
+    // rotation threshold above the rounding noise of a double-float dot product
+    const float tol = 3.55e-15f * sqrtf(float(n > 1 ? n : 1)) * 32.f;
+    const int sw64 = jacobi_sweeps_df(y, v, n, n, tol, 30, &rotated);
+    stamp(5);
     __syncthreads();
     // singular values and sorting permutation
     for (int j = warp; j < n; j += nwarps) {
-        const double* yj = y + int64_t(j) * n;
-        double a = 0.0;
-        for (int t = lane; t < n; t += 32) a = fma(yj[t], yj[t], a);
-        a = wsum(a);
-        if (lane == 0) h[j] = sqrt(a);
+        const df2* yj = y + int64_t(j) * n;
+        df2 a{0.f, 0.f};
+        for (int t = lane; t < n; t += 32) a = df_fma(yj[t], yj[t], a);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a = df_add(a, df_shfl_xor(a, o));
+        if (lane == 0) h[j] = sqrt(df_to_double(a));
     }
     __syncthreads();
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -308,11 +460,12 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         S[d.s_off + rank] = sj;
         perm[d.s_off + rank] = j;
     }
+    stamp(6);
     // 5a. QV = Q [V; 0] in W
     double* qv = W + d.x_off;
     for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
         const int i = int(e % m), j = int(e / m);
-        qv[e] = (i < n) ? v[i + int64_t(j) * n] : 0.0;
+        qv[e] = (i < n) ? df_to_double(v[i + int64_t(j) * n]) : 0.0;
     }
     __syncthreads();
     for (int k = n - 1; k >= 0; --k) {
@@ -336,8 +489,9 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     double* py = V + d.v_off;
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
         const int r = int(e % n), j = int(e / n);
-        py[cp[r] + int64_t(j) * n] = y[e];
+        py[cp[r] + int64_t(j) * n] = df_to_double(y[e]);
     }
+    stamp(7);
     if (threadIdx.x == 0 && sweeps_out) sweeps_out[blockIdx.x] = (sw32 << 16) | sw64;
 }
 
