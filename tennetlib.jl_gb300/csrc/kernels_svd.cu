@@ -149,6 +149,16 @@ __device__ __forceinline__ df2 df_rsqrt(df2 u) {
     return df_add(y0, df_mul(df_mul(y0, e), df2{0.5f, 0.f}));
 }
 
+__device__ __forceinline__ df2 df_recip(df2 b) {
+    const df2 y0{1.f / b.hi, 0.f};
+    const df2 e = df_add(df2{1.f, 0.f}, df_neg(df_mul(b, y0)));
+    return df_add(y0, df_mul(y0, e));
+}
+__device__ __forceinline__ df2 df_sqrt(df2 x) {
+    if (!(x.hi > 0.f)) return df2{0.f, 0.f};
+    return df_mul(x, df_rsqrt(x));
+}
+
 // One-sided Jacobi sweeps in double-float on the columns of x (m x n) with rotations
 // accumulated into v (n x n); same pairing and layout as jacobi_sweeps.  The rotation
 // angle comes from FP32 (it only has to zero the pair to ~1e-7 of itself, which a sweep
@@ -244,8 +254,8 @@ __device__ df2 df_block_sum(df2 v, df2* red) {
 
 // Preconditioned mixed-precision one-sided Jacobi SVD, one CTA per block (work matrix
 // A = M or M^T, m x n with m >= n):
-//  1. QR with column pivoting A P = Q R (FP64 Householder, A and the reflectors stay in the
-//     global work buffer X);
+//  1. QR with column pivoting A P = Q R (double-float Householder; A and the reflectors
+//     stay in the global work buffer X);
 //  2. FP32 one-sided Jacobi on R^T, accumulating V in float: graded R^T makes cyclic Jacobi
 //     converge in a few sweeps (Drmac & Veselic, SIMAX 29, 2008);
 //  3. V re-orthonormalised in double-float (one classical Gram-Schmidt pass);
@@ -267,7 +277,6 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     __shared__ int rotated;
     __shared__ int piv;
     __shared__ double red[SVD_THREADS / 32];
-    __shared__ double hh[3];  // tau, beta, scale of the current reflector
     const SvdBlockDesc d = desc[blockIdx.x];
     const int m = d.m, n = d.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -284,36 +293,40 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     double* tau = cn + n;
     double* h = tau + n;
     int* cp = reinterpret_cast<int*>(h + n);
+    float* cnf = reinterpret_cast<float*>(cn);      // column norms (pivoting only needs FP32)
+    df2* taud = reinterpret_cast<df2*>(tau);        // Householder tau in double-float
+    __shared__ df2 hhd[3];                          // tau, beta, scale of the current reflector
     const bool in_smem = int64_t(2) * n * n * 8 <= smem_region;
-    double* A = X + d.x_off;
+    df2* A = reinterpret_cast<df2*>(X + d.x_off);    // work matrix and reflectors (double-float)
     double* Pm = in_smem ? reinterpret_cast<double*>(smem) : P + d.v_off;
     double* Qm = in_smem ? reinterpret_cast<double*>(smem) + int64_t(n) * n : V + d.v_off;
     const double* M = src + d.src_off;
-    // 0. A = M (or M^T), column norms
+    // 0. A = M (or M^T) in double-float, column norms
     for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
         const int i = int(e % m), k = int(e / m);
-        A[e] = d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows];
+        A[e] = df_from_double(d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows]);
     }
     for (int j = threadIdx.x; j < n; j += blockDim.x) cp[j] = j;
     __syncthreads();
     for (int j = warp; j < n; j += nwarps) {
-        const double* a = A + int64_t(j) * m;
-        double t = 0.0;
-        for (int i = lane; i < m; i += 32) t = fma(a[i], a[i], t);
-        t = wsum(t);
-        if (lane == 0) cn[j] = t;
+        const df2* a = A + int64_t(j) * m;
+        df2 t{0.f, 0.f};
+        for (int i = lane; i < m; i += 32) t = df_fma(a[i], a[i], t);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_xor(t, o));
+        if (lane == 0) cnf[j] = t.hi;
     }
     __syncthreads();
-    // 1. Householder QR with column pivoting
+    // 1. Householder QR with column pivoting, double-float
     for (int k = 0; k < n; ++k) {
         if (warp == 0) {
-            double best = -1.0;
+            float best = -1.f;
             int bi = k;
             for (int j = k + lane; j < n; j += 32)
-                if (cn[j] > best) { best = cn[j]; bi = j; }
+                if (cnf[j] > best) { best = cnf[j]; bi = j; }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
@@ -322,56 +335,60 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         __syncthreads();
         const int p = piv;
         if (p != k) {
-            double* a = A + int64_t(k) * m;
-            double* b = A + int64_t(p) * m;
+            df2* a = A + int64_t(k) * m;
+            df2* b2 = A + int64_t(p) * m;
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const double t = a[i]; a[i] = b[i]; b[i] = t;
+                const df2 t = a[i]; a[i] = b2[i]; b2[i] = t;
             }
             if (threadIdx.x == 0) {
-                const double t = cn[k]; cn[k] = cn[p]; cn[p] = t;
+                const float t = cnf[k]; cnf[k] = cnf[p]; cnf[p] = t;
                 const int u = cp[k]; cp[k] = cp[p]; cp[p] = u;
             }
         }
         __syncthreads();
-        double* ak = A + int64_t(k) * m;
+        df2* ak = A + int64_t(k) * m;
         if (warp == 0) {
-            double sq = 0.0;
-            for (int i = k + 1 + lane; i < m; i += 32) sq = fma(ak[i], ak[i], sq);
-            sq = wsum(sq);
+            df2 sq{0.f, 0.f};
+            for (int i = k + 1 + lane; i < m; i += 32) sq = df_fma(ak[i], ak[i], sq);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sq = df_add(sq, df_shfl_xor(sq, o));
             if (lane == 0) {
-                const double alpha = ak[k];
-                if (sq == 0.0) {
-                    hh[0] = 0.0; hh[1] = alpha; hh[2] = 0.0;
+                const df2 alpha = ak[k];
+                if (sq.hi == 0.f) {
+                    hhd[0] = df2{0.f, 0.f}; hhd[1] = alpha; hhd[2] = df2{0.f, 0.f};
                 } else {
-                    const double beta = -copysign(sqrt(alpha * alpha + sq), alpha);
-                    hh[0] = (beta - alpha) / beta;
-                    hh[1] = beta;
-                    hh[2] = 1.0 / (alpha - beta);
+                    df2 beta = df_sqrt(df_fma(alpha, alpha, sq));
+                    if (alpha.hi >= 0.f) beta = df_neg(beta);
+                    hhd[0] = df_mul(df_add(beta, df_neg(alpha)), df_recip(beta));
+                    hhd[1] = beta;
+                    hhd[2] = df_recip(df_add(alpha, df_neg(beta)));
                 }
-                tau[k] = hh[0];
+                taud[k] = hhd[0];
             }
         }
         __syncthreads();
-        const double tk = hh[0], sc = hh[2];
-        for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) ak[i] *= sc;
+        const df2 tk = hhd[0], sc = hhd[2];
+        for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) ak[i] = df_mul(ak[i], sc);
         __syncthreads();
-        if (threadIdx.x == 0) ak[k] = hh[1];
+        if (threadIdx.x == 0) ak[k] = hhd[1];
         for (int j = k + 1 + warp; j < n; j += nwarps) {
-            double* aj = A + int64_t(j) * m;
-            double w = 0.0;
-            for (int i = k + 1 + lane; i < m; i += 32) w = fma(ak[i], aj[i], w);
-            w = wsum(w) + aj[k];
-            w *= tk;
-            double nrm = 0.0;
+            df2* aj = A + int64_t(j) * m;
+            df2 w{0.f, 0.f};
+            for (int i = k + 1 + lane; i < m; i += 32) w = df_fma(ak[i], aj[i], w);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w = df_add(w, df_shfl_xor(w, o));
+            w = df_mul(df_add(w, aj[k]), tk);
+            df2 nrm{0.f, 0.f};
             __syncwarp();  // every lane has read aj[k] before lane 0 updates it
-            if (lane == 0) aj[k] -= w;
+            if (lane == 0) aj[k] = df_add(aj[k], df_neg(w));
             for (int i = k + 1 + lane; i < m; i += 32) {
-                const double x = fma(-w, ak[i], aj[i]);
+                const df2 x = df_add(aj[i], df_neg(df_mul(w, ak[i])));
                 aj[i] = x;
-                nrm = fma(x, x, nrm);
+                nrm = df_fma(x, x, nrm);
             }
-            nrm = wsum(nrm);
-            if (lane == 0) cn[j] = nrm;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) nrm = df_add(nrm, df_shfl_xor(nrm, o));
+            if (lane == 0) cnf[j] = nrm.hi;
         }
         __syncthreads();
     }
@@ -383,7 +400,7 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     float* v32 = x32 + int64_t(n) * n;
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
         const int i = int(e % n), j = int(e / n);
-        const df2 r = (j <= i) ? df_from_double(A[j + int64_t(i) * m]) : df2{0.f, 0.f};  // R^T[i,j] = R[j,i]
+        const df2 r = (j <= i) ? A[j + int64_t(i) * m] : df2{0.f, 0.f};  // R^T[i,j] = R[j,i]
         rt[e] = r;
         x32[e] = r.hi;
         v32[e] = (i == j) ? 1.f : 0.f;
@@ -461,27 +478,36 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         perm[d.s_off + rank] = j;
     }
     stamp(6);
-    // 5a. QV = Q [V; 0] in W
-    double* qv = W + d.x_off;
+    // 5a. QV = Q [V; 0] in W (double-float; R^T stored there is dead), then FP64 in place
+    df2* qv = reinterpret_cast<df2*>(W + d.x_off);
     for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
         const int i = int(e % m), j = int(e / m);
-        qv[e] = (i < n) ? df_to_double(v[i + int64_t(j) * n]) : 0.0;
+        qv[e] = (i < n) ? v[i + int64_t(j) * n] : df2{0.f, 0.f};
     }
     __syncthreads();
     for (int k = n - 1; k >= 0; --k) {
-        const double tk = tau[k];
-        if (tk == 0.0) continue;  // uniform: tau lives in shared memory
-        const double* ak = A + int64_t(k) * m;
+        const df2 tk = taud[k];
+        if (tk.hi == 0.f) continue;  // uniform: tau lives in shared memory
+        const df2* ak = A + int64_t(k) * m;
         for (int j = warp; j < n; j += nwarps) {
-            double* wj = qv + int64_t(j) * m;
-            double w = 0.0;
-            for (int i = k + 1 + lane; i < m; i += 32) w = fma(ak[i], wj[i], w);
-            w = (wsum(w) + wj[k]) * tk;
+            df2* wj = qv + int64_t(j) * m;
+            df2 w{0.f, 0.f};
+            for (int i = k + 1 + lane; i < m; i += 32) w = df_fma(ak[i], wj[i], w);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w = df_add(w, df_shfl_xor(w, o));
+            w = df_mul(df_add(w, wj[k]), tk);
             __syncwarp();
-            if (lane == 0) wj[k] -= w;
-            for (int i = k + 1 + lane; i < m; i += 32) wj[i] = fma(-w, ak[i], wj[i]);
+            if (lane == 0) wj[k] = df_add(wj[k], df_neg(w));
+            for (int i = k + 1 + lane; i < m; i += 32) wj[i] = df_add(wj[i], df_neg(df_mul(w, ak[i])));
         }
         __syncthreads();
+    }
+    {
+        double* qvd = W + d.x_off;  // same bytes, element by element
+        for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
+            const df2 t = qv[e];
+            qvd[e] = df_to_double(t);
+        }
     }
     // 5b. PY = P Y into the V output (row cp[r] of P Y is row r of Y).  Y lives in shared
     // memory or in the P scratch, never in V, and V (the FP64 rotations) is dead after 5a.
