@@ -313,6 +313,16 @@ def run_ours(args, world, rank, local, pg):
     roof["traffic"] = None
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
              for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
+    dominant = max(("svd_ms", "heff_ms", "lanczos_ms", "env_ms"), key=lambda k: share[k])
+    dom = {"svd_ms": {"kernel": "svd_qrj_kernel (block SVD: double-float QR with pivoting, FP32 "
+                                "Jacobi presolve, double-float polish)",
+                      "bound": "FP32 and FP64 pipes of one SM per charge block (latency-bound at "
+                               "chi~180: 7-9 blocks of <= ~103 columns per bond)"},
+           "heff_ms": {"kernel": "split_pack_kernel + split_gemm_kernel + combine_kernel",
+                       "bound": "tensor (see roofline)"},
+           "lanczos_ms": {"kernel": "gs_pass_kernel", "bound": "hbm"},
+           "env_ms": {"kernel": "environment GEMMs", "bound": "tensor"}}[dominant]
+    dom["share"] = share[dominant]
     res = {
         "metric": METRIC, "value": dev_s, "unit": "s/sweep", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
@@ -326,6 +336,7 @@ def run_ours(args, world, rank, local, pg):
         "energy": energy, "maxlinkdim": chi, "wall_s_per_sweep": wall / args.steps,
         "gpu_launches": launches,
         "roofline": roof,
+        "dominant_kernel": dom,
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": "s/sweep", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,

@@ -396,7 +396,10 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     // 2. R^T as double-float into the W scratch (unused until step 5); FP32 Jacobi on
     //    R^T (n x n lower triangular) in the P region
     df2* rt = reinterpret_cast<df2*>(W + d.x_off);
-    float* x32 = reinterpret_cast<float*>(Pm);
+    // the FP32 pair of n x n arrays fits shared memory up to twice the size the
+    // double-float phases need
+    const bool f32_smem = int64_t(2) * n * n * 4 <= smem_region;
+    float* x32 = f32_smem ? reinterpret_cast<float*>(smem) : reinterpret_cast<float*>(Pm);
     float* v32 = x32 + int64_t(n) * n;
     for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
         const int i = int(e % n), j = int(e / n);
