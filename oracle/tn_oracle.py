@@ -378,6 +378,65 @@ def eigsolve_lowest(apply, x0, krylovdim=5, maxiter=2, tol=1e-14, eager=False):
     return float(D[0]), vec, info
 
 
+def exponentiate(apply, t, x0, krylovdim=30, maxiter=100, tol=1e-12):
+    """exp(t A) x0 for Hermitian A (``exp_solver``, ``src/base/solver.jl:66-88``, restating
+    KrylovKit's ``exponentiate`` with eager Lanczos and full re-orthogonalisation).
+
+    Step control of this restatement: the Krylov space grows one vector at a time; after
+    each expansion y = exp(dt T) e1 is formed from the projected matrix T and the step is
+    accepted when |dt| * beta * |y[K-1]| <= tol (or beta <= tol, or the space is
+    exhausted).  If krylovdim vectors do not reach the tolerance, the largest step dt/2^j
+    that does is taken and the iteration restarts from the evolved vector for the rest of
+    t; at most maxiter restarts.  Returns (vector, info) with info = number of matvecs.
+    """
+    x = np.array(x0, dtype=np.result_type(x0, t, np.float64))
+    remaining = t
+    matvecs = 0
+    for _ in range(maxiter):
+        if remaining == 0:
+            break
+        nrm = np.linalg.norm(x)
+        if nrm == 0:
+            break
+        V = [x / nrm]
+        H = np.zeros((krylovdim + 1, krylovdim + 1), dtype=V[0].dtype)
+        w = apply(V[0])
+        matvecs += 1
+        h, r = _gs2(V, w)
+        H[0, 0] = h[0].real
+        beta = np.linalg.norm(r)
+        dt = remaining
+        while True:
+            K = len(V)
+            Hk = H[:K, :K]
+            Hk = 0.5 * (Hk + Hk.conj().T)
+            lam, U = np.linalg.eigh(Hk)
+            y = U @ (np.exp(dt * lam) * U[0, :].conj())
+            err = abs(dt) * beta * abs(y[K - 1])
+            if err <= tol or beta <= tol or K >= x.size:
+                x = nrm * (y @ np.stack(V, axis=0))
+                remaining = remaining - dt
+                break
+            if K == krylovdim:
+                while err > tol and abs(dt) > 1e-300:
+                    dt = dt / 2
+                    y = U @ (np.exp(dt * lam) * U[0, :].conj())
+                    err = abs(dt) * beta * abs(y[K - 1])
+                x = nrm * (y @ np.stack(V, axis=0))
+                remaining = remaining - dt
+                break
+            v = r / beta
+            V.append(v)
+            w = apply(v)
+            matvecs += 1
+            h, r = _gs2(V, w)
+            H[: K + 1, K] = h
+            H[K, : K + 1] = h.conj()
+            H[K, K] = h[K].real
+            beta = np.linalg.norm(r)
+    return x, matvecs
+
+
 # --------------------------------------------------------------------------------------
 # SVD with ITensors-style global truncation
 # --------------------------------------------------------------------------------------
@@ -586,6 +645,117 @@ def update_two_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
     env.lpos = min(env.lpos, pos)
     env.rpos = max(env.rpos, pos + 1)
     return energy, spec, info
+
+
+def halfsweep_done(N, pos, nsite, ortho):
+    """``halfsweep_done`` (``src/mps/update_site.jl:13-23``), 0-based positions."""
+    if pos == 0 and ortho == "right":
+        return True
+    if pos == N - 1 and ortho == "left" and nsite == 1:
+        return True
+    if pos == N - 2 and ortho == "left" and nsite == 2:
+        return True
+    return False
+
+
+def update_two_site_tdvp(env: StateEnvs, pos, ortho, time_step, maxdim, mindim, cutoff,
+                         krylovdim=30, maxiter=100, tol=1e-12, normalize=True):
+    """``_update_two_site!`` with ``exp_solver`` and ``reverse_step = true``
+    (``src/mps/update_site.jl:27-90``): forward two-site evolution by ``time_step``,
+    ``replacebond!``, then the one-site backward evolution by ``-time_step`` on the new
+    orthogonality center unless the half sweep is done."""
+    psi = env.psi
+    N = psi.N
+    phi = np.tensordot(psi.A[pos], psi.A[pos + 1], axes=([2], [0]))
+    env.position(pos, 2)
+    shape = phi.shape
+
+    def apply2(v):
+        return env.product2(pos, v.reshape(shape)).reshape(-1)
+
+    vec, _ = exponentiate(apply2, time_step, phi.reshape(-1), krylovdim, maxiter, tol)
+    if normalize:
+        vec = vec / np.linalg.norm(vec)
+    energy = float(np.real(np.vdot(vec, apply2(vec))))
+    phi = vec.reshape(shape)
+    A, B, qmid, spec = split_two_site(phi, psi.links[pos], psi.phys_q, psi.links[pos + 2],
+                                      maxdim, mindim, cutoff, ortho, normalize)
+    psi.A[pos] = A
+    psi.A[pos + 1] = B
+    psi.links[pos + 1] = qmid
+    psi.center = pos + 1 if ortho == "left" else pos
+    env.lpos = min(env.lpos, pos)
+    env.rpos = max(env.rpos, pos + 1)
+    if not halfsweep_done(N, pos, 2, ortho):
+        p1 = pos + 1 if ortho == "left" else pos
+        env.position(p1, 1)
+        t1 = psi.A[p1]
+        sh1 = t1.shape
+
+        def apply1(v):
+            return heff1_apply(env.L[p1], env.H.W[p1], env.R[p1], v.reshape(sh1)).reshape(-1)
+
+        v1, _ = exponentiate(apply1, -time_step, t1.reshape(-1), krylovdim, maxiter, tol)
+        if normalize:
+            v1 = v1 / np.linalg.norm(v1)
+        energy = float(np.real(np.vdot(v1, apply1(v1))))
+        psi.A[p1] = v1.reshape(sh1)
+        env.lpos = min(env.lpos, p1)
+        env.rpos = max(env.rpos, p1)
+    return energy, spec
+
+
+def tdvp_sweep(env: StateEnvs, swdata: SweepData, tau, maxdim, cutoff, mindim=1, krylovdim=30,
+               maxiter=100, tol=1e-12, normalize=True):
+    """``tdvpsweep!`` with nsite = 2 (``src/mps/tdvp.jl:247-277``): a full sweep with
+    ``exp_solver`` at time step tau/2 and reverse steps."""
+    N = env.N
+    assert env.psi.center == 0
+    swdata.sweepcount += 1
+    energy = float("nan")
+    maxtruncerr = 0.0
+    lasteigs = [None] * (N - 1)
+    for b in range(N - 1):
+        energy, spec = update_two_site_tdvp(env, b, "left", 0.5 * tau, maxdim, mindim, cutoff,
+                                            krylovdim, maxiter, tol, normalize)
+        maxtruncerr = max(maxtruncerr, spec.truncerr)
+    for b in range(N - 2, -1, -1):
+        energy, spec = update_two_site_tdvp(env, b, "right", 0.5 * tau, maxdim, mindim, cutoff,
+                                            krylovdim, maxiter, tol, normalize)
+        lasteigs[b] = spec.eigs
+        maxtruncerr = max(maxtruncerr, spec.truncerr)
+    swdata.maxchi.append(env.psi.maxlinkdim())
+    swdata.energy.append(energy)
+    mid = lasteigs[N // 2 - 1]
+    swdata.entropy.append(entropy(mid / np.sum(mid)))
+    swdata.maxtruncerr.append(maxtruncerr)
+    swdata.lasteigs = lasteigs
+    return energy
+
+
+def expect_local(psi: MPS, op):
+    """<psi| op_i |psi> for every site i (``measure(T, psi, opstr)``, restated by moving the
+    orthogonality center with dense QR; ``src/mps/measure.jl:150-177``)."""
+    N = psi.N
+    # left-canonicalise a copy site by site; the center then runs left to right
+    A = [a.copy() for a in psi.A]
+    # bring to right-canonical form first (copy may already be, be safe)
+    for i in range(N - 1, 0, -1):
+        Dl, d, Dr = A[i].shape
+        M = A[i].reshape(Dl, d * Dr)
+        Q, R = np.linalg.qr(M.T.conj())
+        A[i] = Q.T.conj().reshape(-1, d, Dr)
+        A[i - 1] = np.tensordot(A[i - 1], R.T.conj(), axes=([2], [0]))
+    out = np.zeros(N)
+    for i in range(N):
+        c = A[i]
+        out[i] = float(np.real(np.einsum("lsr,ts,ltr->", c.conj(), op, c)))
+        if i < N - 1:
+            Dl, d, Dr = c.shape
+            Q, R = np.linalg.qr(c.reshape(Dl * d, Dr))
+            A[i] = Q.reshape(Dl, d, -1)
+            A[i + 1] = np.tensordot(R, A[i + 1], axes=([1], [0]))
+    return out
 
 
 def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,

@@ -15,6 +15,8 @@ Python                          TenNetLib (file:line)
 ``DMRGParams``                  ``DMRGParams``                      src/mps/dmrg.jl:26-102
 ``dmrg_`` / ``dmrg`` / ``dmrg2`` ``dmrg!`` / ``dmrg`` / ``dmrg2``    src/mps/dmrg.jl:148-301
 ``eig_solver``                  ``eig_solver``                      src/base/solver.jl:23-43
+``exp_solver``                  ``exp_solver``                      src/base/solver.jl:66-88
+``TDVPEngine`` / ``tdvpsweep_``  ``TDVPEngine`` / ``tdvpsweep!``      src/mps/tdvp.jl:17-277
 ``entropy``                     ``_entropy``                        src/mps/measure.jl:4-20
 =============================  ==============================================================
 
@@ -40,7 +42,7 @@ INT32_MAX = 2**31 - 1
 __all__ = [
     "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
     "update_position_", "fullsweep_", "dmrg_", "dmrg", "dmrg2", "entropy", "svd_truncate",
-    "Float64_threshold", "TenNetError", "models",
+    "Float64_threshold", "TenNetError", "models", "TDVPEngine", "tdvpsweep_", "exp_solver",
 ]
 
 _threshold = [FLOAT64_THRESHOLD]
@@ -276,29 +278,35 @@ class StateEnvs:
             pass
 
 
+def exp_solver(*_args, **_kwargs):
+    """Token for the Krylov exponential solver (``src/base/solver.jl:66-88``); the solve
+    runs inside libtennet_cuda.so as part of each TDVP update step."""
+    raise TypeError("exp_solver is passed to tdvpsweep_, not called")
+
+
 def eig_solver(*_args, **_kwargs):
     """Token for the Lanczos ground-state solver (``src/base/solver.jl:23-43``).  The solve
     itself runs inside libtennet_cuda.so as part of each update step."""
     raise TypeError("eig_solver is passed to update_position_/fullsweep_, not called")
 
 
-def _params(kwargs) -> L.UpdateParams:
+def _params(kwargs, exp=False) -> L.UpdateParams:
     p = L.UpdateParams()
     maxdim = kwargs.get("maxdim", INT32_MAX)
     p.maxdim = int(min(maxdim, INT32_MAX))
     p.mindim = int(kwargs.get("mindim", 1))
     p.cutoff = float(kwargs.get("cutoff", Float64_threshold()))
     p.normalize = int(bool(kwargs.get("normalize", True)))
-    p.krylovdim = int(kwargs.get("solver_krylovdim", 5))
-    p.maxiter = int(kwargs.get("solver_maxiter", 2))
-    p.tol = float(kwargs.get("solver_tol", 1e-14))
-    p.eager = int(bool(kwargs.get("solver_eager", False)))
+    p.krylovdim = int(kwargs.get("solver_krylovdim", 30 if exp else 5))
+    p.maxiter = int(kwargs.get("solver_maxiter", 100 if exp else 2))
+    p.tol = float(kwargs.get("solver_tol", 1e-12 if exp else 1e-14))
+    p.eager = int(bool(kwargs.get("solver_eager", exp)))
     p.check_convergence = int(bool(kwargs.get("solver_check_convergence", False)))
     p.noise = float(kwargs.get("noise", 0.0))
     if not kwargs.get("ishermitian", True):
         raise ValueError("only Hermitian effective Hamiltonians are built")
-    if kwargs.get("time_step") is not None:
-        raise ValueError("time evolution (exp_solver) is not built in this engine")
+    if kwargs.get("time_step") is not None and not exp:
+        raise ValueError("time evolution goes through tdvpsweep_")
     return p
 
 
@@ -384,6 +392,86 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
               f"MaxErr={swdata.maxtruncerr[-1]:.2g}, Time={round(wall, 3)}")
         print("-" * 83)
     return enerr, enterr
+
+
+def _record_sweep(swdata, res, mid, wall, noise=0.0, outputlevel=0):
+    mid = np.asarray(mid)
+    swdata.sweepcount += 1
+    swdata.maxchi.append(int(res.maxlinkdim))
+    swdata.energy.append(float(res.energy))
+    swdata.entropy.append(entropy(mid / mid.sum()) if mid.size else 0.0)
+    swdata.maxtruncerr.append(float(res.maxtruncerr))
+    swdata.lasteigs = [mid]
+    swdata.stats.append({
+        "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
+        "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
+        "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops,
+        "pack_ms": res.pack_ms, "gemm_launches": res.gemm_launches,
+        "kernel_launches": res.kernel_launches, "wall_s": wall})
+
+
+class TDVPEngine:
+    """``TDVPEngine(psi, H)`` (``src/mps/tdvp.jl:17-64``): environments, sweep history and
+    the absolute elapsed time of a TDVP run."""
+
+    def __init__(self, psi: MPS, H: MPO):
+        self.sysenv = StateEnvs(psi, H)
+        self.swdata = SweepData()
+        self.abstime = 0.0
+
+    def getpsi(self) -> MPS:
+        return self.sysenv.getpsi()
+
+    def sweepcount(self):
+        return self.swdata.sweepcount
+
+    def getenergy(self):
+        return self.swdata.energy[-1]
+
+    def getentropy(self):
+        return self.swdata.entropy[-1]
+
+    def maxchi(self):
+        return self.swdata.maxchi[-1]
+
+    def totalerror(self):
+        return float(sum(self.swdata.maxtruncerr))
+
+    def sweeperror(self):
+        return self.swdata.maxtruncerr[-1]
+
+    def sweepdata(self):
+        return self.swdata
+
+
+def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwargs):
+    """``tdvpsweep!`` (``src/mps/tdvp.jl:247-277``) with nsite = 2: one full sweep with
+    ``exp_solver`` at time_step/2 and reverse one-site steps; ``abstime += |time_step|``.
+
+    This build evolves with real time steps (imaginary-time evolution exp(time_step H));
+    complex steps and ``nsite = "dynamic"`` are not built.
+    """
+    if solver is not exp_solver:
+        raise ValueError("`tdvpsweep!()`: `solver` must be `exp_solver` !!")
+    if nsite != 2:
+        raise ValueError("only nsite = 2 TDVP sweeps are built")
+    if isinstance(time_step, complex) or np.iscomplexobj(time_step):
+        raise NotImplementedError("complex time steps are not built in this engine")
+    if kwargs.get("noise", 0.0):
+        raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
+                         "`reverse_step=true` !!")
+    p = _params(kwargs, exp=True)
+    res = L.SweepResult()
+    cap = max(int(p.maxdim if p.maxdim < 1 << 20 else 1 << 16), 1)
+    mid = np.zeros(cap)
+    nmid = C.c_int32()
+    sysenv = engine.sysenv
+    t0 = time.perf_counter()
+    L.check(sysenv.ctx.lib.tn_env_tdvpsweep(sysenv.h, float(time_step), C.byref(p), C.byref(res),
+                                            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    _record_sweep(engine.swdata, res, mid[: nmid.value], time.perf_counter() - t0)
+    engine.abstime += abs(time_step)
+    return None
 
 
 @dataclass

@@ -511,7 +511,7 @@ void env_right_step(tn_env* env, int i) {
 
 void position(tn_env* env, int pos, int nsite) {
     const int N = env->psi->N;
-    TN_REQUIRE(nsite == 2, "this engine builds the two-site effective Hamiltonian only");
+    TN_REQUIRE(nsite == 1 || nsite == 2, "nsite must be 1 or 2");
     TN_REQUIRE(pos >= 0 && pos + nsite - 1 < N, "position out of range");
     while (env->lpos < pos) {
         env_left_step(env, env->lpos);
@@ -524,7 +524,10 @@ void position(tn_env* env, int pos, int nsite) {
         env->rpos--;
     }
     env->rpos = last;
-    if (env->pos != pos || env->nsite != nsite) env->hp_pos = -1;
+    if (env->pos != pos || env->nsite != nsite) {
+        env->hp_pos = -1;
+        env->h1p_pos = -1;
+    }
     env->pos = pos;
     env->nsite = nsite;
 }
@@ -695,6 +698,190 @@ void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
     env->heff_flops += P.flops;
     env->gemm_flops += P.g1.flops + P.g3.flops;
     env->gemm_launches += (P.g1.tiles.empty() ? 0 : 1) + (P.g3.tiles.empty() ? 0 : 1);
+}
+
+// -------------------------------------------------------------------------------------
+// one-site effective Hamiltonian (right-grouped one-site tensor)
+// -------------------------------------------------------------------------------------
+std::unique_ptr<Heff1Plan> build_heff1(tn_env* env, int p) {
+    auto P = std::make_unique<Heff1Plan>();
+    const tn_mpo* H = env->H;
+    const tn_mps* psi = env->psi.get();
+    const int d = psi->d;
+    const Link& lk = psi->links[p];
+    const Link& rk = psi->links[p + 1];
+    const EnvLayout& Lin = env->L[p].lay;
+    const EnvLayout& Rin = env->R[p].lay;
+    P->lay = make_site_layout(RG, lk, rk, psi->pq);
+    const SiteLayout& lay = P->lay;
+    const int wl = H->wd[p], wr = H->wd[p + 1];
+    // step 1: Y(a, il) = L(a, il) * v block il  (D_l' x cols(il))
+    std::vector<int64_t> yoff(size_t(wl) * lk.nsec(), -1);
+    int64_t y = 0;
+    for (int il = 0; il < lk.nsec(); ++il) {
+        if (lay.cols[il] == 0) continue;
+        for (int a = 0; a < wl; ++a) {
+            const int64_t lo = Lin.off[size_t(a) * Lin.nsec + il];
+            if (lo < 0) continue;
+            bool need = false;
+            for (int s2 = 0; s2 < d; ++s2) need = need || need_left(H, p, a, s2);
+            if (!need) continue;
+            const int Db = lk.dim[Lin.bra[size_t(a) * Lin.nsec + il]];
+            yoff[size_t(a) * lk.nsec() + il] = y;
+            P->g1.add_task(S_T1, y, Db, lay.cols[il], Db);
+            P->g1.add_seg(S_L, lo, Db, 0, S_X, lay.off[il], lk.dim[il], 0, lk.dim[il]);
+            y += int64_t(Db) * lay.cols[il];
+        }
+    }
+    // steps 2/3: Z(b, il', s') then out(il')[:, slab (s', r')] = sum_b Z * R(b)^T
+    int64_t z = 0;
+    for (int ilp = 0; ilp < lk.nsec(); ++ilp)
+        for (int sp = 0; sp < d; ++sp) {
+            const int csub = lay.sub[size_t(ilp) * d + sp];
+            if (csub < 0) continue;
+            const int irp = lay.subsec[size_t(ilp) * d + sp];
+            const int Dlp = lk.dim[ilp];
+            P->g3.add_task(S_Y, lay.off[ilp] + int64_t(csub) * Dlp, Dlp, rk.dim[irp], Dlp);
+            struct PendingSeg { int64_t zo, ro; int Drp, Dr; };
+            std::vector<PendingSeg> segs;
+            for (int b = 0; b < wr; ++b) {
+                const int ir = rk.find(rk.q[irp] - H->delta[p + 1][b]);
+                if (ir < 0) continue;
+                const int64_t ro = Rin.off[size_t(b) * Rin.nsec + ir];
+                if (ro < 0 || Rin.bra[size_t(b) * Rin.nsec + ir] != irp) continue;
+                const int Dr = rk.dim[ir];
+                CombOut o;
+                o.doff = z;
+                o.dbuf = S_T2;
+                o.ldd = Dlp;
+                o.rows = Dlp;
+                o.cols = Dr;
+                o.t0 = (int)P->cb.terms.size();
+                o.nt = 0;
+                for (int a = 0; a < wl; ++a) {
+                    const int il = lk.find(lk.q[ilp] - H->delta[p][a]);
+                    if (il < 0) continue;
+                    const int64_t yo = yoff[size_t(a) * lk.nsec() + il];
+                    if (yo < 0 || Lin.bra[size_t(a) * Lin.nsec + il] != ilp) continue;
+                    for (int s = 0; s < d; ++s) {
+                        const double wv = H->at(p, a, b, sp, s);
+                        if (wv == 0.0) continue;
+                        const int ys = lay.sub[size_t(il) * d + s];
+                        if (ys < 0 || lay.subsec[size_t(il) * d + s] != ir) continue;
+                        P->cb.terms.push_back(CombTerm{yo + int64_t(ys) * Dlp, S_T1, Dlp, wv});
+                        o.nt++;
+                    }
+                }
+                if (o.nt == 0) {
+                    P->cb.terms.resize(o.t0);
+                    continue;
+                }
+                P->cb.flops += 2.0 * o.nt * double(o.rows) * o.cols;
+                P->cb.outs.push_back(o);
+                segs.push_back(PendingSeg{z, ro, rk.dim[irp], Dr});
+                z += int64_t(Dlp) * Dr;
+            }
+            for (const auto& sg : segs)
+                P->g3.add_seg(S_T2, sg.zo, Dlp, 0, S_R, sg.ro, sg.Drp, 1, sg.Dr);
+        }
+    cudaStream_t st = env->ctx->stream;
+    P->g1.finalize(st);
+    P->g3.finalize(st);
+    P->cb.finalize(st);
+    P->ysize = y;
+    P->zsize = z;
+    P->flops = P->g1.flops + P->g3.flops + P->cb.flops;
+    return P;
+}
+
+Heff1Plan& heff1_plan(tn_env* env) {
+    if (env->h1p_pos != env->pos || !env->h1p) {
+        env->h1p = build_heff1(env, env->pos);
+        env->h1p_pos = env->pos;
+        cudaStream_t st = env->ctx->stream;
+        env->t1.alloc(size_t(std::max<int64_t>(env->h1p->ysize, 1)) * 8, st);
+        env->t2.alloc(size_t(std::max<int64_t>(env->h1p->zsize, 1)) * 8, st);
+    }
+    return *env->h1p;
+}
+
+void heff1_apply(tn_env* env, Heff1Plan& P, const double* x, double* y) {
+    tn_ctx* ctx = env->ctx;
+    Bases bs{};
+    bs.p[S_L] = env->L[env->pos].buf.d();
+    bs.p[S_R] = env->R[env->pos].buf.d();
+    bs.p[S_X] = const_cast<double*>(x);
+    bs.p[S_Y] = y;
+    bs.p[S_T1] = env->t1.d();
+    bs.p[S_T2] = env->t2.d();
+    const int e0 = ctx->timer.mark();
+    if (ctx->prec == TN_PREC_SPLIT) {
+        if (!P.s1) P.s1 = make_split(P.g1, ctx->slices, true, false, ctx->stream);
+        if (!P.s3) P.s3 = make_split(P.g3, ctx->slices, false, true, ctx->stream);
+        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+        run_split(ctx, *P.s1, bs, &a0, &a1);
+        launch_combine(P.cb, bs, ctx->stream);
+        run_split(ctx, *P.s3, bs, &b0, &b1);
+        ctx->timer.add(T_GEMM, a0, a1);
+        ctx->timer.add(T_GEMM, b0, b1);
+    } else {
+        launch_gemm_f64(P.g1, bs, ctx->stream);
+        launch_combine(P.cb, bs, ctx->stream);
+        launch_gemm_f64(P.g3, bs, ctx->stream);
+    }
+    ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+    env->matvecs++;
+    env->heff_flops += P.flops;
+    env->gemm_flops += P.g1.flops + P.g3.flops;
+    env->gemm_launches += (P.g1.tiles.empty() ? 0 : 1) + (P.g3.tiles.empty() ? 0 : 1);
+}
+
+// copy a site tensor between the left-grouped and right-grouped layouts (block copies)
+void regroup(tn_ctx* ctx, const SiteLayout& src, const double* sp, const SiteLayout& dst,
+             double* dp, const Link& lk, const Link& rk) {
+    CombPlan cb;
+    const int d = src.d;
+    for (int b = 0; b < src.nblk(); ++b)
+        for (int s = 0; s < d; ++s) {
+            const int sub = src.sub[size_t(b) * d + s];
+            if (sub < 0) continue;
+            const int oth = src.subsec[size_t(b) * d + s];
+            const int il = src.layout == LG ? oth : b;
+            const int ir = src.layout == LG ? b : oth;
+            const int db = dst.layout == LG ? ir : il;
+            const int dsub = dst.sub[size_t(db) * d + s];
+            TN_REQUIRE(dsub >= 0, "internal: regroup layout mismatch");
+            CombOut o;
+            o.rows = lk.dim[il];
+            o.cols = rk.dim[ir];
+            o.dbuf = S_Y;
+            if (dst.layout == LG) {
+                o.doff = dst.off[db] + dsub;
+                o.ldd = dst.rows[db];
+            } else {
+                o.doff = dst.off[db] + int64_t(dsub) * lk.dim[il];
+                o.ldd = lk.dim[il];
+            }
+            o.t0 = (int)cb.terms.size();
+            o.nt = 1;
+            CombTerm t;
+            t.sbuf = S_X;
+            t.coef = 1.0;
+            if (src.layout == LG) {
+                t.soff = src.off[b] + sub;
+                t.lds = src.rows[b];
+            } else {
+                t.soff = src.off[b] + int64_t(sub) * lk.dim[il];
+                t.lds = lk.dim[il];
+            }
+            cb.terms.push_back(t);
+            cb.outs.push_back(o);
+        }
+    cb.finalize(ctx->stream);
+    Bases bs{};
+    bs.p[S_X] = const_cast<double*>(sp);
+    bs.p[S_Y] = dp;
+    launch_combine(cb, bs, ctx->stream);
 }
 
 // phi = site p * site p+1 in the phi layout
@@ -890,6 +1077,145 @@ EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
 }
 
 // -------------------------------------------------------------------------------------
+// Krylov exponentiation exp(t H_eff) x (KrylovKit exponentiate semantics restated): eager
+// Lanczos with full re-orthogonalisation; after each expansion y = exp(dt T) e1 and the
+// step is accepted when |dt| * beta * |y[K-1]| <= tol (or beta <= tol, or the space is
+// exhausted); a full Krylov space that misses the tolerance takes the largest dt / 2^j
+// that meets it and restarts from the evolved vector for the remaining time.
+// -------------------------------------------------------------------------------------
+template <class MV>
+int krylov_exp(tn_env* env, MV&& apply, int64_t n, double t, const double* x0, double* out,
+               const tn_update_params* prm) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    const int kd = prm->krylovdim;
+    const int nvec = kd + 2;  // basis + residual + current vector
+    env->kry.alloc(size_t(nvec) * size_t(std::max<int64_t>(n, 1)) * 8, st);
+    env->part.alloc(size_t(32) * blas_nparts() * 8, st);
+    env->dots.alloc(128 * 8, st);
+    if (!env->ticket.p) {
+        env->ticket.alloc(sizeof(unsigned), st);
+        TN_CUDA(cudaMemsetAsync(env->ticket.p, 0, sizeof(unsigned), st));
+    }
+    unsigned* tk = env->ticket.as<unsigned>();
+    double* dv = env->dots.d();
+    std::vector<double*> pool;
+    for (int i = 0; i < nvec; ++i) pool.push_back(env->kry.d() + int64_t(i) * n);
+    double* cur = pool.back();
+    pool.pop_back();
+    double* w = pool.back();
+    pool.pop_back();
+    TN_CUDA(cudaMemcpyAsync(cur, x0, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
+    std::vector<double> hostd(65);
+    int matvecs = 0;
+    double remaining = t;
+    auto norm2 = [&](double* v) {
+        const double* vp = v;
+        launch_gs_pass(&vp, 0, v, nullptr, 0.0, n, false, true, env->part.d(), dv + 64, tk, st);
+        double r = 0;
+        TN_CUDA(cudaMemcpyAsync(&r, dv + 64, 8, cudaMemcpyDeviceToHost, st));
+        sync(ctx);
+        return r;
+    };
+    for (int it = 0; it < prm->maxiter && remaining != 0.0; ++it) {
+        const double nrm = std::sqrt(std::max(norm2(cur), 0.0));
+        if (nrm == 0.0) break;
+        std::vector<double*> V;
+        V.push_back(pool[0]);
+        launch_scale_into(V[0], cur, nullptr, 1.0 / nrm, n, st);
+        std::vector<double> Hm(size_t(kd + 1) * (kd + 1), 0.0);
+        auto Hat = [&](int i, int j) -> double& { return Hm[size_t(i) * (kd + 1) + j]; };
+        auto gs = [&](int K, std::vector<double>& h, double& beta) {
+            const int e0 = ctx->timer.mark();
+            launch_gs_pass(V.data(), K, w, nullptr, 0.0, n, true, false, env->part.d(), dv, tk, st);
+            launch_gs_pass(V.data(), K, w, dv, -1.0, n, true, false, env->part.d(), dv + 32, tk, st);
+            launch_gs_pass(V.data(), K, w, dv + 32, -1.0, n, false, true, env->part.d(), dv + 64, tk, st);
+            ctx->timer.add(T_LANCZOS, e0, ctx->timer.mark());
+            TN_CUDA(cudaMemcpyAsync(hostd.data(), dv, 65 * 8, cudaMemcpyDeviceToHost, st));
+            sync(ctx);
+            h.resize(K);
+            for (int i = 0; i < K; ++i) h[i] = hostd[i] + hostd[32 + i];
+            beta = std::sqrt(std::max(hostd[64], 0.0));
+        };
+        std::vector<double> h, D, U;
+        double beta = 0.0;
+        apply(V[0], w);
+        matvecs++;
+        gs(1, h, beta);
+        Hat(0, 0) = h[0];
+        double dt = remaining;
+        while (true) {
+            const int K = (int)V.size();
+            std::vector<double> A(size_t(K) * K);
+            for (int i = 0; i < K; ++i)
+                for (int j = 0; j < K; ++j) A[size_t(i) * K + j] = 0.5 * (Hat(i, j) + Hat(j, i));
+            sym_eig(K, A, D, U);
+            auto expv = [&](double tau, std::vector<double>& y) {
+                y.assign(K, 0.0);
+                for (int j = 0; j < K; ++j) {
+                    const double c = std::exp(tau * D[j]) * U[size_t(0) * K + j];
+                    for (int i = 0; i < K; ++i) y[i] += U[size_t(i) * K + j] * c;
+                }
+            };
+            std::vector<double> y;
+            expv(dt, y);
+            double err = std::fabs(dt) * beta * std::fabs(y[K - 1]);
+            const bool exhausted = int64_t(K) >= n;
+            bool accept = err <= prm->tol || beta <= prm->tol || exhausted;
+            if (!accept && K == kd) {
+                while (err > prm->tol && std::fabs(dt) > 1e-300) {
+                    dt *= 0.5;
+                    expv(dt, y);
+                    err = std::fabs(dt) * beta * std::fabs(y[K - 1]);
+                }
+                accept = true;
+            }
+            if (accept) {
+                for (double& c : y) c *= nrm;
+                TN_CUDA(cudaMemcpyAsync(dv + 96, y.data(), K * 8, cudaMemcpyHostToDevice, st));
+                launch_lincomb(cur, V.data(), K, dv + 96, n, st);
+                sync(ctx);
+                remaining -= dt;
+                break;
+            }
+            double* v = pool[K];
+            launch_scale_into(v, w, nullptr, 1.0 / beta, n, st);
+            V.push_back(v);
+            apply(v, w);
+            matvecs++;
+            gs(K + 1, h, beta);
+            for (int i = 0; i <= K; ++i) {
+                Hat(i, K) = h[i];
+                Hat(K, i) = h[i];
+            }
+        }
+    }
+    TN_CUDA(cudaMemcpyAsync(out, cur, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
+    return matvecs;
+}
+
+// normalise x in place (when asked) and return <x|H x> using y as scratch
+template <class MV>
+double normalize_and_energy(tn_env* env, MV&& apply, int64_t n, double* x, double* y,
+                            bool normalize) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    unsigned* tk = env->ticket.as<unsigned>();
+    double* dv = env->dots.d();
+    const double* xp = x;
+    if (normalize) {
+        launch_gs_pass(&xp, 0, x, nullptr, 0.0, n, false, true, env->part.d(), dv + 64, tk, st);
+        launch_scale_into(x, x, dv + 64, 1.0, n, st);
+    }
+    apply(x, y);
+    launch_gs_pass(&xp, 1, y, nullptr, 0.0, n, true, false, env->part.d(), dv + 64, tk, st);
+    double e = 0.0;
+    TN_CUDA(cudaMemcpyAsync(&e, dv + 64, 8, cudaMemcpyDeviceToHost, st));
+    sync(ctx);
+    return e;
+}
+
+// -------------------------------------------------------------------------------------
 // block SVD + truncation
 // -------------------------------------------------------------------------------------
 struct SvdResult {
@@ -1079,8 +1405,16 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
     eigs = D.eigs;
 }
 
+// halfsweep_done (TenNetLib src/mps/update_site.jl:13-23), 0-based, nsite = 2
+bool halfsweep_done2(int N, int pos, int ortho) {
+    return (pos == 0 && ortho == TN_ORTHO_RIGHT) || (pos == N - 2 && ortho == TN_ORTHO_LEFT);
+}
+
+// _update_two_site! (TenNetLib src/mps/update_site.jl:27-90).  time_step == nullptr: the
+// eigensolver; otherwise the exponential solver with the reverse one-site step.
 void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
-                     tn_update_result* res, std::vector<double>& eigs) {
+                     tn_update_result* res, std::vector<double>& eigs,
+                     const double* time_step = nullptr) {
     check_params(prm);
     tn_mps* psi = env->psi.get();
     TN_REQUIRE(p >= 0 && p < psi->N - 1, "bond position out of range");
@@ -1095,14 +1429,56 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     env->vecA.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     env->vecB.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     form_phi(env, p, P.ph, env->vecA.d());
-    EigOut eo = lanczos_lowest(env, P, env->vecA.d(), env->vecB.d(), prm);
-    if (prm->check_convergence && eo.converged < 1)
-        throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
-    res->energy = eo.energy;
-    res->matvecs = eo.matvecs;
-    res->converged = eo.converged;
+    auto apply2 = [&](const double* x, double* y) { heff_apply(env, P, x, y); };
+    if (!time_step) {
+        EigOut eo = lanczos_lowest(env, P, env->vecA.d(), env->vecB.d(), prm);
+        if (prm->check_convergence && eo.converged < 1)
+            throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
+        res->energy = eo.energy;
+        res->matvecs = eo.matvecs;
+        res->converged = eo.converged;
+    } else {
+        const int64_t mv0 = env->matvecs;
+        krylov_exp(env, apply2, n, *time_step, env->vecA.d(), env->vecB.d(), prm);
+        res->energy = normalize_and_energy(env, apply2, n, env->vecB.d(), env->vecA.d(),
+                                           prm->normalize != 0);
+        res->matvecs = int32_t(env->matvecs - mv0);
+        res->converged = 1;
+    }
     replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
     res->neigs = (int)eigs.size();
+    if (time_step && !halfsweep_done2(psi->N, p, ortho)) {
+        // reverse step: evolve the new orthogonality center back by -time_step
+        const int p1 = (ortho == TN_ORTHO_LEFT) ? p + 1 : p;
+        position(env, p1, 1);
+        Heff1Plan& P1 = heff1_plan(env);
+        const int64_t n1 = P1.lay.size;
+        env->vecC.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
+        env->vecD.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
+        tn_site& site = psi->sites[p1];
+        const Link& lk = psi->links[p1];
+        const Link& rk = psi->links[p1 + 1];
+        if (site.lay.layout == RG)
+            TN_CUDA(cudaMemcpyAsync(env->vecC.p, site.buf.p, size_t(n1) * 8,
+                                    cudaMemcpyDeviceToDevice, st));
+        else
+            regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk);
+        auto apply1 = [&](const double* x, double* y) { heff1_apply(env, P1, x, y); };
+        const double back = -*time_step;
+        const int64_t mv0 = env->matvecs;
+        krylov_exp(env, apply1, n1, back, env->vecC.d(), env->vecD.d(), prm);
+        res->energy = normalize_and_energy(env, apply1, n1, env->vecD.d(), env->vecC.d(),
+                                           prm->normalize != 0);
+        res->matvecs += int32_t(env->matvecs - mv0);
+        if (site.lay.layout == RG)
+            TN_CUDA(cudaMemcpyAsync(site.buf.p, env->vecD.p, size_t(n1) * 8,
+                                    cudaMemcpyDeviceToDevice, st));
+        else
+            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk);
+        env->lpos = std::min(env->lpos, p1);
+        env->rpos = std::max(env->rpos, p1);
+        env->hp_pos = -1;
+    }
     if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
 }
 
@@ -1562,65 +1938,85 @@ int tn_env_update_position(tn_env* env, int pos, int ortho, const tn_update_para
     });
 }
 
+}  // extern "C"
+
+namespace {
+// fullsweep! (TenNetLib src/mps/sweep.jl:94-196) with the eigensolver (time_step null) or
+// the exponential solver at time_step with reverse steps (tdvpsweep!, src/mps/tdvp.jl:268)
+void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
+                int mid_cap, int32_t* n_mid_eigs, const double* time_step) {
+    TN_REQUIRE(env && res, "null argument");
+    check_params(p);
+    tn_mps* psi = env->psi.get();
+    TN_REQUIRE(psi->center == 0, "fullsweep! needs the orthogonality center at site 1");
+    const int N = psi->N;
+    tn_ctx* ctx = env->ctx;
+    ctx->timer.collect(env->acc_ms);
+    double acc0[T_NCAT];
+    std::copy(env->acc_ms, env->acc_ms + T_NCAT, acc0);
+    const int64_t mv0 = env->matvecs;
+    const double fl0 = env->heff_flops;
+    const double gf0 = env->gemm_flops;
+    const int64_t gl0 = env->gemm_launches;
+    const int64_t kl0 = launch_count();
+    *res = tn_sweep_result{};
+    const int es = ctx->timer.mark();
+    double maxerr = 0.0, energy = NAN;
+    std::vector<double> ev, mid;
+    for (int b = 0; b < N - 1; ++b) {
+        tn_update_result r{};
+        update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step);
+        energy = r.energy;
+        maxerr = std::max(maxerr, r.truncerr);
+    }
+    for (int b = N - 2; b >= 0; --b) {
+        tn_update_result r{};
+        update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step);
+        energy = r.energy;
+        maxerr = std::max(maxerr, r.truncerr);
+        if (b == N / 2 - 1) mid = ev;
+    }
+    ctx->timer.add(T_SWEEP, es, ctx->timer.mark());
+    sync(ctx);
+    ctx->timer.collect(env->acc_ms);
+    int maxd = 0;
+    for (const auto& L : psi->links) maxd = std::max(maxd, L.total());
+    res->energy = energy;
+    res->maxtruncerr = maxerr;
+    res->maxlinkdim = maxd;
+    res->matvecs = int32_t(env->matvecs - mv0);
+    res->heff_flops = env->heff_flops - fl0;
+    res->heff_ms = env->acc_ms[T_HEFF] - acc0[T_HEFF];
+    res->env_ms = env->acc_ms[T_ENV] - acc0[T_ENV];
+    res->svd_ms = env->acc_ms[T_SVD] - acc0[T_SVD];
+    res->lanczos_ms = env->acc_ms[T_LANCZOS] - acc0[T_LANCZOS];
+    res->sweep_ms = env->acc_ms[T_SWEEP] - acc0[T_SWEEP];
+    res->gemm_ms = env->acc_ms[T_GEMM] - acc0[T_GEMM];
+    res->pack_ms = env->acc_ms[T_PACK] - acc0[T_PACK];
+    res->gemm_flops = env->gemm_flops - gf0;
+    res->gemm_launches = env->gemm_launches - gl0;
+    res->kernel_launches = launch_count() - kl0;
+    if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
+    if (mid_eigs) {
+        const int k = std::min<int>(mid_cap, (int)mid.size());
+        std::copy(mid.begin(), mid.begin() + k, mid_eigs);
+    }
+}
+}  // namespace
+
+extern "C" {
+
 int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res,
                      double* mid_eigs, int mid_cap, int32_t* n_mid_eigs) {
+    return guarded([&] { full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, nullptr); });
+}
+
+int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_sweep_result* res,
+                     double* mid_eigs, int mid_cap, int32_t* n_mid_eigs) {
     return guarded([&] {
-        TN_REQUIRE(env && res, "null argument");
-        check_params(p);
-        tn_mps* psi = env->psi.get();
-        TN_REQUIRE(psi->center == 0, "fullsweep! needs the orthogonality center at site 1");
-        const int N = psi->N;
-        tn_ctx* ctx = env->ctx;
-        ctx->timer.collect(env->acc_ms);
-        double acc0[T_NCAT];
-        std::copy(env->acc_ms, env->acc_ms + T_NCAT, acc0);
-        const int64_t mv0 = env->matvecs;
-        const double fl0 = env->heff_flops;
-        const double gf0 = env->gemm_flops;
-        const int64_t gl0 = env->gemm_launches;
-        const int64_t kl0 = launch_count();
-        *res = tn_sweep_result{};
-        const int es = ctx->timer.mark();
-        double maxerr = 0.0, energy = NAN;
-        std::vector<double> ev, mid;
-        for (int b = 0; b < N - 1; ++b) {
-            tn_update_result r{};
-            update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev);
-            energy = r.energy;
-            maxerr = std::max(maxerr, r.truncerr);
-        }
-        for (int b = N - 2; b >= 0; --b) {
-            tn_update_result r{};
-            update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev);
-            energy = r.energy;
-            maxerr = std::max(maxerr, r.truncerr);
-            if (b == N / 2 - 1) mid = ev;
-        }
-        ctx->timer.add(T_SWEEP, es, ctx->timer.mark());
-        sync(ctx);
-        ctx->timer.collect(env->acc_ms);
-        int maxd = 0;
-        for (const auto& L : psi->links) maxd = std::max(maxd, L.total());
-        res->energy = energy;
-        res->maxtruncerr = maxerr;
-        res->maxlinkdim = maxd;
-        res->matvecs = int32_t(env->matvecs - mv0);
-        res->heff_flops = env->heff_flops - fl0;
-        res->heff_ms = env->acc_ms[T_HEFF] - acc0[T_HEFF];
-        res->env_ms = env->acc_ms[T_ENV] - acc0[T_ENV];
-        res->svd_ms = env->acc_ms[T_SVD] - acc0[T_SVD];
-        res->lanczos_ms = env->acc_ms[T_LANCZOS] - acc0[T_LANCZOS];
-        res->sweep_ms = env->acc_ms[T_SWEEP] - acc0[T_SWEEP];
-        res->gemm_ms = env->acc_ms[T_GEMM] - acc0[T_GEMM];
-        res->pack_ms = env->acc_ms[T_PACK] - acc0[T_PACK];
-        res->gemm_flops = env->gemm_flops - gf0;
-        res->gemm_launches = env->gemm_launches - gl0;
-        res->kernel_launches = launch_count() - kl0;
-        if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
-        if (mid_eigs) {
-            const int k = std::min<int>(mid_cap, (int)mid.size());
-            std::copy(mid.begin(), mid.begin() + k, mid_eigs);
-        }
+        TN_REQUIRE(std::isfinite(tau), "time step must be finite");
+        const double half = 0.5 * tau;
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half);
     });
 }
 

@@ -83,6 +83,17 @@ struct Heff2Plan {
     double flops = 0;
 };
 
+// contraction plans of the one-site effective Hamiltonian at one position; the one-site
+// tensor is taken in the right-grouped layout
+struct Heff1Plan {
+    tn::SiteLayout lay;
+    tn::GemmPlan g1, g3;
+    tn::CombPlan cb;
+    std::unique_ptr<tn::SplitPlan> s1, s3;
+    int64_t ysize = 0, zsize = 0;
+    double flops = 0;
+};
+
 struct tn_env {
     tn_ctx* ctx = nullptr;
     std::unique_ptr<tn_mps> psi;
@@ -95,6 +106,9 @@ struct tn_env {
         vecA, vecB;
     std::unique_ptr<Heff2Plan> hp;
     int hp_pos = -1;
+    std::unique_ptr<Heff1Plan> h1p;
+    int h1p_pos = -1;
+    tn::DevBuf vecC, vecD;
     double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0, 0};
     double gemm_flops = 0;
     int64_t gemm_launches = 0;

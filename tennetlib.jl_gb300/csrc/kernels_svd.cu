@@ -10,12 +10,6 @@ namespace tn {
 namespace {
 
 constexpr int SVD_THREADS = 512;
-__device__ __forceinline__ double wsum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 // Round-robin tournament: nn (even) players, round r in [0, nn-1), pair k in [0, nn/2).
 __device__ __forceinline__ void rr_pair(int nn, int r, int k, int& i, int& j) {
     auto player = [&](int pos) { return pos == 0 ? 0 : 1 + ((pos - 1 + r) % (nn - 1)); };

@@ -149,3 +149,25 @@ def test_heff_is_hermitian():
 def test_entropy():
     assert O.entropy([1.0]) == 0.0
     assert abs(O.entropy([0.5, 0.5]) - np.log(2)) < 1e-15
+
+
+def test_exponentiate_matches_expm():
+    import scipy.linalg as sla
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((40, 40))
+    A = A + A.T
+    x = rng.standard_normal(40)
+    for t, kd in ((-0.3, 30), (-0.3, 10), (-2.0, 8)):   # the last two restart
+        y, mv = O.exponentiate(lambda v: A @ v, t, x, krylovdim=kd)
+        ref = sla.expm(t * A) @ x
+        assert np.linalg.norm(y - ref) <= 1e-11 * np.linalg.norm(ref)
+
+
+def test_oracle_tdvp_imaginary_time_lowers_energy():
+    N = 8
+    H = O.heisenberg_mpo(N)
+    env = O.StateEnvs(O.product_mps([0, 1] * 4, O.SPIN_HALF_Q), H)
+    sw = O.SweepData()
+    es = [O.tdvp_sweep(env, sw, -1.0, 16, 1e-14) for _ in range(40)]
+    assert all(b <= a + 1e-12 for a, b in zip(es, es[1:]))
+    assert abs(es[-1] - GOLD["heisenberg_chain"]["8"]) < 1e-8
