@@ -173,6 +173,75 @@ int tn_svd_truncate(tn_ctx* ctx, int nblocks, const int32_t* rows, const int32_t
                     const double* data, int32_t maxdim, int32_t mindim, double cutoff,
                     int32_t* kept, double* svals, double* truncerr);
 
+/* ---- tree tensor networks (TTN) ----------------------------------------------------
+ * A tree of nnodes nodes numbered 0..nnodes-1, given by nedges edges (node pairs), with
+ * nsites physical sites of dimension d attached (site_node[nsites]).  The legs of a node
+ * tensor are its sites in ascending order, then its neighbours in ascending node number;
+ * node tensors cross the ABI dense and column-major in that leg order.  TenNetLib labels
+ * nodes (layer, index) (src/ttn/ttn.jl:1-30, src/ttn/ttn_generators.jl:69-96): the caller
+ * numbers the sorted labels.  No charge conservation (dense node tensors). */
+typedef struct tn_ttn tn_ttn;
+typedef struct tn_ttn_model tn_ttn_model;
+typedef struct tn_ttn_env tn_ttn_env;
+
+/* TTN(sites, graph, tensors, orthocenter) (src/ttn/ttn.jl:21-26).  link_dims[nedges]: bond
+ * dimension of each edge in the order given; data: node tensors concatenated in node
+ * order; center: the orthogonality centre (every other node an isometry toward it), or -1
+ * for arbitrary tensors. */
+int tn_ttn_create(tn_ctx* ctx, int nsites, int d, int nnodes, int nedges, const int32_t* edges,
+                  const int32_t* site_node, const int32_t* link_dims, const double* data,
+                  int center, tn_ttn** out);
+int tn_ttn_destroy(tn_ttn* psi);
+int tn_ttn_center(const tn_ttn* psi);
+/* number of legs of `node` and (dims != NULL, capacity 64) their dimensions in leg order */
+int tn_ttn_node_dims(const tn_ttn* psi, int node, int32_t* nlegs, int32_t* dims);
+/* dense node tensor, column-major in leg order */
+int tn_ttn_node(const tn_ttn* psi, int node, double* out, int64_t cap);
+/* maxlinkdim(ttn) (src/ttn/ttn.jl:199-209) */
+int tn_ttn_maxlinkdim(const tn_ttn* psi);
+/* isometrize!(ttn, node; normalize) (src/ttn/ttn.jl:326-382) with QR moves on the GPU: from
+ * scratch (isometrize_full!) when the TTN has no centre, else along the path from it. */
+int tn_ttn_isometrize(tn_ttn* psi, int node, int normalize);
+
+/* CouplingModel (src/base/couplingmodel.jl:153-230) from product terms, unmerged: term t is
+ * coef[t] * prod_j op_{t,j}, term_nops[t] operators on distinct sites (term_sites, all terms
+ * concatenated); ops: d x d column-major matrices [s', s] in the same order. */
+int tn_ttn_model_create(int nsites, int d, int nterms, const int32_t* term_nops,
+                        const int32_t* term_sites, const double* ops, const double* coef,
+                        tn_ttn_model** out);
+int tn_ttn_model_destroy(tn_ttn_model* model);
+
+/* StateEnvsTTN(psi, H) (src/ttn/state_envs_ttn.jl:27-31, link tensors built as in
+ * LinkTensorsTTN(psi, M), src/ttn/linktensors.jl:233-261) for `count` states at once: the
+ * environments share one device arena and are swept together by tn_ttn_envs_fullsweep.
+ * All states share one tree and one orthogonality centre; each has its own model. */
+int tn_ttn_envs_create(int count, tn_ttn* const* psis, tn_ttn_model* const* models,
+                       tn_ttn_env** out);
+int tn_ttn_env_destroy(tn_ttn_env* env);
+/* getpsi(sysenv) (state_envs_ttn.jl:87): a copy of the current state */
+int tn_ttn_env_getpsi(tn_ttn_env* env, tn_ttn** out);
+int tn_ttn_env_center(const tn_ttn_env* env);
+/* position!(sysenv, node) (state_envs_ttn.jl:120-141): QR moves, normalisation, link
+ * tensors moved along the same path (move_linktensors!, src/ttn/linktensors.jl:130-156) */
+int tn_ttn_env_position(tn_ttn_env* env, int node);
+/* product(sysenv, v) at the orthogonality centre (src/ttn/linktensors.jl:183-221); v and
+ * out are dense node tensors of the centre */
+int tn_ttn_env_product(tn_ttn_env* env, const double* v, double* out, int64_t n);
+/* algorithmic flops of one product at the centre */
+int tn_ttn_env_product_flops(tn_ttn_env* env, double* flops);
+/* update_position!(sysenv, eig_solver, node; kwargs...) (src/ttn/update_site_ttn.jl:42-63);
+ * p->maxdim bounds the links moved through (a larger link would need the truncating SVD
+ * move, which is not built: TN_E_INVALID); p->noise must be 0 */
+int tn_ttn_env_update_position(tn_ttn_env* env, int node, const tn_update_params* p,
+                               tn_update_result* res);
+/* fullsweep!(sysenv, sweeppath, eig_solver, swdata; kwargs...), noise = 0 branch
+ * (src/ttn/sweep_ttn.jl:117-274): update_position! along path, then along the reversed
+ * path, for the `count` environments created together (envs in creation order), in
+ * lockstep: each contraction stage of all of them is one grouped launch.  res[count]
+ * receives each environment's energy and maxlinkdim; the timings are of the whole group. */
+int tn_ttn_envs_fullsweep(int count, tn_ttn_env* const* envs, int npath, const int32_t* path,
+                          const tn_update_params* p, tn_sweep_result* res);
+
 /* ---- allocation-free block singular values ----------------------------------------
  * No counterpart in the reference.  For callers that cannot let the library allocate
  * device memory (a host framework that owns all device memory through its own pool, a

@@ -18,6 +18,7 @@ Python                          TenNetLib (file:line)
 ``exp_solver``                  ``exp_solver``                      src/base/solver.jl:66-88
 ``TDVPEngine`` / ``tdvpsweep_``  ``TDVPEngine`` / ``tdvpsweep!``      src/mps/tdvp.jl:17-277
 ``entropy``                     ``_entropy``                        src/mps/measure.jl:4-20
+``ttn.*``                       the TTN path (``TTN``, ``StateEnvsTTN``, ``optimize!``; see ttn.py)
 =============================  ==============================================================
 
 All arithmetic runs in libtennet_cuda.so; this module only moves host arrays across the C
@@ -34,6 +35,7 @@ import numpy as np
 
 from . import _lib as L
 from . import models  # noqa: F401
+from . import ttn  # noqa: F401
 from ._lib import TenNetError
 
 FLOAT64_THRESHOLD = 1e-15
@@ -43,6 +45,7 @@ __all__ = [
     "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
     "update_position_", "fullsweep_", "dmrg_", "dmrg", "dmrg2", "entropy", "svd_truncate",
     "Float64_threshold", "TenNetError", "models", "TDVPEngine", "tdvpsweep_", "exp_solver",
+    "ttn",
 ]
 
 _threshold = [FLOAT64_THRESHOLD]

@@ -106,6 +106,28 @@ PROTOS = {
     "tn_svd_truncate": (C.c_int, [vp, C.c_int, i32p, i32p, f64p, C.c_int32, C.c_int32,
                                   C.c_double, i32p, f64p, f64p]),
     "tn_block_svals_noalloc": (C.c_int, [C.c_int, vp, C.c_int, i32p, i32p, vp, vp]),
+    "tn_ttn_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, i32p, i32p, i32p, f64p,
+                                C.c_int, C.POINTER(vp)]),
+    "tn_ttn_destroy": (C.c_int, [vp]),
+    "tn_ttn_center": (C.c_int, [vp]),
+    "tn_ttn_node_dims": (C.c_int, [vp, C.c_int, i32p, i32p]),
+    "tn_ttn_node": (C.c_int, [vp, C.c_int, f64p, C.c_int64]),
+    "tn_ttn_maxlinkdim": (C.c_int, [vp]),
+    "tn_ttn_isometrize": (C.c_int, [vp, C.c_int, C.c_int]),
+    "tn_ttn_model_create": (C.c_int, [C.c_int, C.c_int, C.c_int, i32p, i32p, f64p, f64p,
+                                      C.POINTER(vp)]),
+    "tn_ttn_model_destroy": (C.c_int, [vp]),
+    "tn_ttn_envs_create": (C.c_int, [C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "tn_ttn_env_destroy": (C.c_int, [vp]),
+    "tn_ttn_env_getpsi": (C.c_int, [vp, C.POINTER(vp)]),
+    "tn_ttn_env_center": (C.c_int, [vp]),
+    "tn_ttn_env_position": (C.c_int, [vp, C.c_int]),
+    "tn_ttn_env_product": (C.c_int, [vp, f64p, f64p, C.c_int64]),
+    "tn_ttn_env_product_flops": (C.c_int, [vp, f64p]),
+    "tn_ttn_env_update_position": (C.c_int, [vp, C.c_int, C.POINTER(UpdateParams),
+                                             C.POINTER(UpdateResult)]),
+    "tn_ttn_envs_fullsweep": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, i32p,
+                                        C.POINTER(UpdateParams), C.POINTER(SweepResult)]),
 }
 
 _lib = None

@@ -175,7 +175,7 @@ void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 }
 
 std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_static,
-                                      bool b_static, cudaStream_t st) {
+                                      bool b_static, cudaStream_t st, bool own_packs = true) {
     auto sp = std::make_unique<SplitPlan>();
     sp->slices = slices;
     sp->a_static = a_static;
@@ -216,6 +216,7 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
         stsk.nkt = nkt;
         stsk.ea_off = int32_t(eao);
         stsk.eb_off = bnew ? int32_t(ebo) : int32_t(bit->second.second);
+        stsk.accum = t.accum;
         sp->tasks.push_back(stsk);
         const int akt0 = (int)sp->aks.size(), bkt0 = (int)sp->bks.size();
         for (const auto& k : kts) {
@@ -267,10 +268,16 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
     upload_vec(sp->dbjobs, sp->bjobs, st);
     upload_vec(sp->daks, sp->aks, st);
     upload_vec(sp->dbks, sp->bks, st);
-    sp->apack.alloc(size_t(std::max<int64_t>(aoff, 1024)), st);
-    sp->bpack.alloc(size_t(std::max<int64_t>(boff, 1024)), st);
-    sp->ea.alloc(size_t(std::max<int64_t>(eao, 4)) * 4, st);
-    sp->eb.alloc(size_t(std::max<int64_t>(ebo, 4)) * 4, st);
+    if (own_packs) {
+        sp->apack.alloc(size_t(std::max<int64_t>(aoff, 1024)), st);
+        sp->bpack.alloc(size_t(std::max<int64_t>(boff, 1024)), st);
+        sp->ea.alloc(size_t(std::max<int64_t>(eao, 4)) * 4, st);
+        sp->eb.alloc(size_t(std::max<int64_t>(ebo, 4)) * 4, st);
+        sp->ap = sp->apack.as<uint8_t>();
+        sp->bp = sp->bpack.as<uint8_t>();
+        sp->eap = sp->ea.as<int>();
+        sp->ebp = sp->eb.as<int>();
+    }
     return sp;
 }
 
@@ -280,19 +287,18 @@ void run_split(tn_ctx* ctx, SplitPlan& sp, const Bases& bs, int* mma_ev0, int* m
     const int p0 = ctx->timer.mark();
     if (!sp.a_static || !sp.a_packed) {
         launch_split_pack(sp.dajobs.as<PackJob>(), (int)sp.ajobs.size(), sp.daks.as<KTileSrc>(), bs,
-                          sp.apack.as<uint8_t>(), sp.ea.as<int>(), sp.slices, split_tile_rows_a(), st);
+                          sp.ap, sp.eap, sp.slices, split_tile_rows_a(), st);
         sp.a_packed = true;
     }
     if (!sp.b_static || !sp.b_packed) {
         launch_split_pack(sp.dbjobs.as<PackJob>(), (int)sp.bjobs.size(), sp.dbks.as<KTileSrc>(), bs,
-                          sp.bpack.as<uint8_t>(), sp.eb.as<int>(), sp.slices, split_tile_rows_b(), st);
+                          sp.bp, sp.ebp, sp.slices, split_tile_rows_b(), st);
         sp.b_packed = true;
     }
     const int p1 = ctx->timer.mark();
     ctx->timer.add(T_PACK, p0, p1);
     launch_split_gemm(sp.ditems.as<SplitItem>(), (int)sp.items.size(), sp.dtasks.as<SplitTask>(),
-                      sp.apack.as<uint8_t>(), sp.bpack.as<uint8_t>(), sp.ea.as<int>(),
-                      sp.eb.as<int>(), bs, sp.slices, ctx->err.as<int>(), ctx->nsm, st);
+                      sp.ap, sp.bp, sp.eap, sp.ebp, bs, sp.slices, ctx->err.as<int>(), ctx->nsm, st);
     const int p2 = ctx->timer.mark();
     if (mma_ev0) *mma_ev0 = p1;
     if (mma_ev1) *mma_ev1 = p2;
@@ -1583,6 +1589,21 @@ void phi_dense_map(const PhiLayout& ph, const Link& lk, const Link& rk, int d,
 }  // namespace
 
 void tn::set_last_error(const char* msg) { g_err = msg; }
+
+// helpers shared with the tree tensor network sweep (ttn.cpp)
+void tn::sym_eig_host(int n, const std::vector<double>& A, std::vector<double>& D,
+                      std::vector<double>& U) {
+    sym_eig(n, A, D, U);
+}
+std::unique_ptr<SplitPlan> tn::make_split_plan(const GemmPlan& g, int slices, cudaStream_t st,
+                                               bool own_packs) {
+    return make_split(g, slices, false, false, st, own_packs);
+}
+void tn::run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs) {
+    sp.a_packed = sp.b_packed = false;
+    run_split(ctx, sp, bs, nullptr, nullptr);
+}
+void tn::check_device_error_public(tn_ctx* ctx) { check_device_error(ctx); }
 
 // -------------------------------------------------------------------------------------
 // EventTimer

@@ -31,6 +31,17 @@ struct Scratch;  // fixed-capacity device scratch used by the allocation-free en
 
 }  // namespace tn
 
+struct tn_ctx;
+namespace tn {
+// helpers of engine.cpp shared with the tree tensor network sweep
+void sym_eig_host(int n, const std::vector<double>& A, std::vector<double>& D,
+                  std::vector<double>& U);  // ascending; A, U row-major
+std::unique_ptr<SplitPlan> make_split_plan(const GemmPlan& g, int slices, cudaStream_t st,
+                                           bool own_packs);
+void run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs);
+void check_device_error_public(tn_ctx* ctx);
+}  // namespace tn
+
 struct tn_ctx {
     int device = 0;
     int nsm = 0;

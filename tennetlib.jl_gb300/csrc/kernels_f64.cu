@@ -80,7 +80,10 @@ gemm_f64_kernel(const Seg* __restrict__ segs, const Task* __restrict__ tasks,
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int gi = t.m0 + tx + 16 * i;
-            if (gi < tk.m) C[gi + int64_t(gj) * tk.ldc] = acc[i][j];
+            if (gi < tk.m) {
+                double* c = C + gi + int64_t(gj) * tk.ldc;
+                *c = tk.accum ? *c + acc[i][j] : acc[i][j];
+            }
         }
     }
 }

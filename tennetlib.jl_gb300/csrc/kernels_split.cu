@@ -436,7 +436,8 @@ split_gemm_kernel(const SplitItem* __restrict__ items, int nitems,
                     if (gc < tk.n) {
                         const int ec = eb[tk.eb_off + gc];
                         const double v = (double(hi[c]) + double(lo[c])) * pow2(er + ec - 16);
-                        C[gr + int64_t(gc) * tk.ldc] = v;
+                        double* c = C + gr + int64_t(gc) * tk.ldc;
+                        *c = tk.accum ? *c + v : v;
                     }
                 }
             }

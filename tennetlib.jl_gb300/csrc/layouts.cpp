@@ -172,8 +172,9 @@ EnvLayout make_env_layout(const Link& link, const std::vector<int>& delta) {
 // ------------------------------------------------------------------------------------
 // plan containers
 // ------------------------------------------------------------------------------------
-void GemmPlan::add_task(int cbuf, int64_t coff, int m, int n, int ldc) {
+void GemmPlan::add_task(int cbuf, int64_t coff, int m, int n, int ldc, int accum) {
     Task t;
+    t.accum = accum;
     t.coff = coff;
     t.cbuf = cbuf;
     t.m = m;

@@ -144,6 +144,7 @@ struct Seg {
 struct Task {
     int64_t coff;
     int32_t cbuf, m, n, ldc, seg0, nseg;
+    int32_t accum;  // 1: C += result (tasks of one launch must not overlap), 0: C = result
 };
 struct Tile {
     int32_t task, m0, n0;
@@ -168,7 +169,7 @@ struct GemmPlan {
     std::vector<Tile> tiles;
     double flops = 0;
     DevBuf dsegs, dtasks, dtiles;
-    void add_task(int cbuf, int64_t coff, int m, int n, int ldc);
+    void add_task(int cbuf, int64_t coff, int m, int n, int ldc, int accum = 0);
     void add_seg(int abuf, int64_t aoff, int lda, int ta, int bbuf, int64_t boff, int ldb,
                  int tb, int k);
     void finalize(cudaStream_t s);  // builds tiles, uploads
@@ -194,7 +195,7 @@ struct PackJob {         // one row tile of one task's operand
 };
 struct SplitTask {
     int64_t coff, a_off, b_off;
-    int32_t cbuf, m, n, ldc, nkt, ea_off, eb_off, pad;
+    int32_t cbuf, m, n, ldc, nkt, ea_off, eb_off, accum;
 };
 struct SplitItem {
     int32_t task, mt, nt, pad;
@@ -208,6 +209,10 @@ struct SplitPlan {
     int slices = 0;
     bool a_static = false, b_static = false, a_packed = false, b_packed = false;
     DevBuf dtasks, ditems, dajobs, dbjobs, daks, dbks, apack, bpack, ea, eb;
+    // pack buffers used by the launches: the owned buffers above, or caller-provided
+    // scratch (make_split with own_packs = false) of abytes / bbytes / 4 ea_n / 4 eb_n bytes
+    uint8_t *ap = nullptr, *bp = nullptr;
+    int *eap = nullptr, *ebp = nullptr;
 };
 int split_tile_bytes_a();
 int split_tile_bytes_b();

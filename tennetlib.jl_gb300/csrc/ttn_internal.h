@@ -1,0 +1,103 @@
+// Internal declarations of the tree tensor network (TTN) sweep: the tree, the batched
+// kernel descriptors and their launchers.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "tn_internal.h"
+
+namespace tn {
+
+constexpr int BK_MAX = 32;      // Krylov vectors per batched kernel
+constexpr int TTN_PARTS = 152;  // partial sums per instance of the batched reductions
+constexpr int HH_B = 32;        // panel width of the blocked Householder QR
+
+// A tree of nodes 0..nn-1 with physical sites attached.  The legs of node v are its sites
+// (ascending), then its neighbours (ascending).
+struct TtnTree {
+    int N = 0, d = 0, nn = 0;
+    std::vector<std::vector<int>> nbr, sites;
+    std::vector<int> site_node;
+    std::vector<std::pair<int, int>> edges;  // (a, b), a < b
+    std::map<std::pair<int, int>, int> eidx;
+    int nlegs(int v) const { return int(sites[v].size() + nbr[v].size()); }
+    int leg_nbr(int v, int u) const;
+    int leg_site(int v, int n) const;
+    int edge(int a, int b) const;
+    std::vector<int> path(int a, int b) const;   // shortest path a .. b
+    std::vector<char> side(int v, int u) const;  // sites on v's side of the edge (v, u)
+};
+
+// ---- batched Krylov descriptors -----------------------------------------------------
+struct BGsDesc {                 // one instance of a fused Gram-Schmidt pass
+    const double* V[BK_MAX];
+    double* w;
+    const double* hin;           // w += sign * V hin first (device, or null)
+    double* out;                 // dots V^T w (kk values), then |w|^2
+    int64_t n;
+    int32_t kk, pad;
+};
+struct BScaleDesc {              // dst (and dst2) = src * scale [/ sqrt(*denom_sq)]
+    const double* src;
+    double* dst;
+    double* dst2;
+    const double* denom_sq;
+    double scale;
+    int64_t n;
+};
+struct BLinDesc {                // dst = sum_k coef[k] V[k]
+    const double* V[BK_MAX];
+    const double* coef;
+    double* dst;
+    int64_t n;
+    int32_t kk, pad;
+};
+struct PermDesc {                // (P, D, Q) <-> (P, Q, D)
+    const double* src;
+    double* dst;
+    int64_t P, D, Q;
+    int32_t to_end, pad;
+};
+struct QrDesc {                  // small QR: A (m x n, ld m) -> Q in place, R out
+    double* A;
+    double* R;
+    double* tau;
+    int32_t m, n;
+};
+struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m >= n)
+    double* A;                   // factored in place; then overwritten by Q (= Q below)
+    double* Q;
+    double* R;                   // kmin x n
+    double* V;                   // panels of explicit reflectors, see hh_panel_voff
+    double* T;                   // per panel -T (HH_B x HH_B)
+    double* tau;                 // kmin
+    double* scal;                // current column: tau, scale, beta
+    double* wv;                  // current column: tau * w_k of the panel columns
+    double* part;                // partial sums (>= HH_B*HH_B*TTN_PARTS)
+    unsigned* ticket;
+    int32_t m, n, kmin, pad;
+};
+
+// offset of the explicit V of the panel starting at column p0 (panels of HH_B columns,
+// panel P has (m - P*HH_B) rows)
+__host__ __device__ inline int64_t hh_panel_voff(int m, int p0) {
+    const int64_t P = p0 / HH_B;
+    return P * HH_B * int64_t(m) - int64_t(HH_B) * HH_B * P * (P - 1) / 2;
+}
+
+int ttn_parts();
+void launch_bgs_pass(const BGsDesc* d, int ninst, int kmax, int64_t nmax, double sign, bool dots,
+                     bool norm, double* part, unsigned* tickets, cudaStream_t s);
+void launch_bscale(const BScaleDesc* d, int ninst, int64_t nmax, cudaStream_t s);
+void launch_blincomb(const BLinDesc* d, int ninst, int64_t nmax, cudaStream_t s);
+void launch_permute(const PermDesc* d, int ninst, int64_t nmax, cudaStream_t s);
+void launch_qr_small(const QrDesc* d, int ninst, cudaStream_t s);
+void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int pend, cudaStream_t s);
+void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,
+                         cudaStream_t s);
+void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s);
+
+}  // namespace tn
