@@ -65,10 +65,27 @@ class Context:
 
     def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 5):
         self.lib = L.load()
+        self._users = 0
+        self._closing = False
         h = L.vp()
         L.check(self.lib.tn_ctx_create(device, C.byref(h)))
         self.h = h
         self.set_precision(precision, slices)
+
+    # Objects that own device handles of this context hold it; the context is destroyed
+    # only after the last of them, whatever order the garbage collector finalises them in.
+    def _hold(self):
+        self._users += 1
+
+    def _drop(self):
+        self._users -= 1
+        if self._closing and self._users <= 0:
+            self._destroy()
+
+    def _destroy(self):
+        if getattr(self, "h", None):
+            self.lib.tn_ctx_destroy(self.h)
+            self.h = None
 
     def set_precision(self, precision: str, slices: int = 5):
         mode = {"fp64": L.TN_PREC_FP64, "split": L.TN_PREC_SPLIT}[precision]
@@ -83,15 +100,30 @@ class Context:
         return cls._default
 
     def close(self):
-        if getattr(self, "h", None):
-            self.lib.tn_ctx_destroy(self.h)
-            self.h = None
+        self._closing = True
+        if self._users <= 0:
+            self._destroy()
 
     def __del__(self):
         try:
             self.close()
         except Exception:
             pass
+
+
+def _own(obj, handle):
+    """Record that obj owns a device handle of obj.ctx."""
+    obj.h = handle
+    obj.ctx._hold()
+
+
+def _release(obj, destroy_name: str):
+    """Destroy obj's device handle, then release its hold on the context."""
+    h = getattr(obj, "h", None)
+    if h:
+        obj.h = None
+        getattr(obj.ctx.lib, destroy_name)(h)
+        obj.ctx._drop()
 
 
 def _links_to_sectors(links):
@@ -124,7 +156,7 @@ class MPO:
         a4, p4 = L.as_f64(flat)
         h = L.vp()
         L.check(self.ctx.lib.tn_mpo_create(self.ctx.h, self.N, self.d, p1, p2, p3, p4, C.byref(h)))
-        self.h = h
+        _own(self, h)
 
     @classmethod
     def from_terms(cls, N, terms, conserve_qns=True, ctx=None):
@@ -133,8 +165,7 @@ class MPO:
 
     def __del__(self):
         try:
-            if self.h:
-                self.ctx.lib.tn_mpo_destroy(self.h)
+            _release(self, "tn_mpo_destroy")
         except Exception:
             pass
 
@@ -146,7 +177,7 @@ class MPS:
                  ctx: Context | None = None, _handle=None, _N=None, _d=None):
         self.ctx = ctx or Context.default()
         if _handle is not None:
-            self.h = _handle
+            _own(self, _handle)
             self.N = _N
             self.d = _d
             self.phys_q = np.asarray(phys_q, dtype=np.int32)
@@ -161,7 +192,7 @@ class MPS:
         L.check(self.ctx.lib.tn_mps_create(self.ctx.h, self.N, self.d, bufs[0][1], bufs[1][1],
                                            bufs[2][1], bufs[3][1], bufs[4][1], center,
                                            C.byref(h)))
-        self.h = h
+        _own(self, h)
 
     @classmethod
     def product(cls, states, phys_q, ctx=None):
@@ -209,8 +240,7 @@ class MPS:
 
     def __del__(self):
         try:
-            if self.h:
-                self.ctx.lib.tn_mps_destroy(self.h)
+            _release(self, "tn_mps_destroy")
         except Exception:
             pass
 
@@ -226,7 +256,7 @@ class StateEnvs:
         self.d = psi.d
         h = L.vp()
         L.check(self.ctx.lib.tn_env_create(psi.h, H.h, C.byref(h)))
-        self.h = h
+        _own(self, h)
 
     def __len__(self):
         return self.N
@@ -275,8 +305,7 @@ class StateEnvs:
 
     def __del__(self):
         try:
-            if self.h:
-                self.ctx.lib.tn_env_destroy(self.h)
+            _release(self, "tn_env_destroy")
         except Exception:
             pass
 

@@ -38,6 +38,16 @@ import numpy as np
 
 from . import _lib as L
 
+
+def _own(obj, handle):
+    from . import _own as own
+    own(obj, handle)
+
+
+def _release(obj, name):
+    from . import _release as rel
+    rel(obj, name)
+
 INT32_MAX = 2**31 - 1
 PAULI_X = np.array([[0.0, 1.0], [1.0, 0.0]])
 PAULI_Z = np.array([[1.0, 0.0], [0.0, -1.0]])
@@ -159,7 +169,7 @@ class TTN:
     tensor legs: the node's sites ascending, then its neighbours in label order."""
 
     def __init__(self, graph, sitenodes, d, tensors=None, center=None, ctx=None, _handle=None):
-        from . import Context
+        from . import Context  # noqa: F811
         self.ctx = ctx or Context.default()
         self.graph = {k: list(v) for k, v in graph.items()}
         self.labels = sorted(self.graph)
@@ -170,7 +180,7 @@ class TTN:
         self.edges = sorted({tuple(sorted((self.index[a], self.index[b])))
                              for a in self.graph for b in self.graph[a]})
         if _handle is not None:
-            self.h = _handle
+            _own(self, _handle)
             return
         dims = {}
         for e in self.edges:
@@ -188,7 +198,7 @@ class TTN:
         L.check(self.ctx.lib.tn_ttn_create(self.ctx.h, self.N, d, len(self.labels), len(self.edges),
                                            bufs[0][1], bufs[1][1], bufs[2][1], bufs[3][1], c,
                                            C.byref(h)))
-        self.h = h
+        _own(self, h)
 
     def sites_of(self, v):
         return [n for n, x in enumerate(self.sitenodes) if x == v]
@@ -228,8 +238,7 @@ class TTN:
 
     def __del__(self):
         try:
-            if self.h:
-                self.ctx.lib.tn_ttn_destroy(self.h)
+            _release(self, "tn_ttn_destroy")
         except Exception:
             pass
 
@@ -346,11 +355,11 @@ class StateEnvsTTN:
         self.template = psi
         self.H = H
         if _handle is not None:
-            self.h = _handle
+            _own(self, _handle)
             return
         hs = (L.vp * 1)()
         L.check(self.ctx.lib.tn_ttn_envs_create(1, (L.vp * 1)(psi.h), (L.vp * 1)(H.h), hs))
-        self.h = L.vp(hs[0])
+        _own(self, L.vp(hs[0]))
 
     @classmethod
     def batch(cls, psis, models):
@@ -397,8 +406,7 @@ class StateEnvsTTN:
 
     def __del__(self):
         try:
-            if self.h:
-                self.ctx.lib.tn_ttn_env_destroy(self.h)
+            _release(self, "tn_ttn_env_destroy")
         except Exception:
             pass
 
