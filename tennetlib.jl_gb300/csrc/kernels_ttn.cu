@@ -179,7 +179,7 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // One CTA factors one m x n matrix A (lda = m): R (kmin x n) is written out, A is
 // overwritten by the explicit Q (m x kmin), kmin = min(m, n).  Unblocked Householder QR
 // (LAPACK dgeqr2) followed by the backward accumulation of Q (dorg2r).
-__global__ void __launch_bounds__(256) qr_small_kernel(const QrDesc* __restrict__ descs) {
+__global__ void __launch_bounds__(1024) qr_small_kernel(const QrDesc* __restrict__ descs) {
     __shared__ double red[33];
     __shared__ double sc[3];
     const QrDesc& D = descs[blockIdx.x];
@@ -275,9 +275,10 @@ __global__ void __launch_bounds__(BT) hh_norm_kernel(const HhDesc* __restrict__ 
     if (threadIdx.x == 0) {
         double tau, scale, beta;
         make_reflector(col[j], t, tau, scale, beta);
-        D.scal[0] = tau;
-        D.scal[1] = scale;
-        D.scal[2] = beta;
+        double* sc = D.scal + 4 * (j & 1);
+        sc[0] = tau;
+        sc[1] = scale;
+        sc[2] = beta;
         D.tau[j] = tau;
         *D.ticket = 0u;
     }
@@ -322,7 +323,8 @@ __global__ void __launch_bounds__(BT) hh_dots_kernel(const HhDesc* __restrict__ 
     __syncthreads();
     if (!last) return;
     __threadfence();
-    const double tau = D.scal[0], scale = D.scal[1];
+    const double* sc = D.scal + 4 * (j & 1);
+    const double tau = sc[0], scale = sc[1];
     for (int c = wid; c < nk; c += BT / 32) {
         double s = 0.0;
         for (int b = lane; b < (int)gridDim.x; b += 32)
@@ -335,23 +337,55 @@ __global__ void __launch_bounds__(BT) hh_dots_kernel(const HhDesc* __restrict__ 
 }
 
 // A[i, k] -= v_i (tau w_k) for i >= j, k in (j, pend); then column j holds v (scaled) below
-// the diagonal and beta on it
+// the diagonal and beta on it.  When column j + 1 is in the panel, the same pass sums the
+// squares of its updated entries below the diagonal and the last block forms its reflector
+// (the work of hh_norm_kernel for column j + 1).
 __global__ void __launch_bounds__(BT) hh_update_kernel(const HhDesc* __restrict__ descs, int j,
                                                        int pend) {
+    __shared__ double red[33];
+    __shared__ int last;
     const HhDesc& D = descs[blockIdx.y];
     if (j >= D.kmin) return;
     const int pe = pend < D.kmin ? pend : D.kmin;
     const int nk = pe - j - 1;
     double* col = D.A + int64_t(j) * D.m;
-    const double scale = D.scal[1], beta = D.scal[2];
+    const double* sc = D.scal + 4 * (j & 1);
+    const double scale = sc[1], beta = sc[2];
+    double nrm = 0.0;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t i = j + int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < D.m; i += stride) {
         const double v = i == j ? 1.0 : col[i] * scale;
         for (int c = 0; c < nk; ++c) {
             double* a = D.A + i + int64_t(j + 1 + c) * D.m;
-            *a = fma(-v, D.wv[c], *a);
+            const double x = fma(-v, D.wv[c], *a);
+            *a = x;
+            if (c == 0 && i > j + 1) nrm = fma(x, x, nrm);
         }
         col[i] = i == j ? beta : v;
+    }
+    if (nk <= 0) return;
+    nrm = block_sum(nrm, red);
+    if (threadIdx.x == 0) D.part[blockIdx.x] = nrm;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(D.ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last || threadIdx.x >= 32) return;
+    __threadfence();
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32)
+        t += reinterpret_cast<volatile double*>(D.part)[b];
+    t = warp_sum(t);
+    if (threadIdx.x == 0) {
+        const double alpha = reinterpret_cast<volatile double*>(D.A)[(j + 1) + int64_t(j + 1) * D.m];
+        double tau, sca, bet;
+        make_reflector(alpha, t, tau, sca, bet);
+        double* sn = D.scal + 4 * ((j + 1) & 1);
+        sn[0] = tau;
+        sn[1] = sca;
+        sn[2] = bet;
+        D.tau[j + 1] = tau;
+        *D.ticket = 0u;
     }
 }
 
@@ -403,7 +437,7 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
 #pragma unroll 8
         for (int rr = 0; rr < 64; ++rr) acc = fma(tile[rr][a], tile[rr][b], acc);
     }
-    D.part[int64_t(threadIdx.x) * gridDim.x + blockIdx.x] = acc;
+    D.part[int64_t(blockIdx.x) * (HH_B * HH_B) + threadIdx.x] = acc;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = (atomicAdd(D.ticket, 1u) == gridDim.x - 1);
@@ -412,7 +446,7 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     __threadfence();
     double s = 0.0;
     for (int bb = 0; bb < (int)gridDim.x; ++bb)
-        s += reinterpret_cast<volatile double*>(D.part)[int64_t(threadIdx.x) * gridDim.x + bb];
+        s += reinterpret_cast<volatile double*>(D.part)[int64_t(bb) * (HH_B * HH_B) + threadIdx.x];
     G[a][b] = s;
     T[a][b] = 0.0;
     __syncthreads();
@@ -506,20 +540,24 @@ void launch_permute(const PermDesc* d, int ninst, int64_t nmax, cudaStream_t s) 
 
 void launch_qr_small(const QrDesc* d, int ninst, cudaStream_t s) {
     if (ninst <= 0) return;
-    qr_small_kernel<<<ninst, 256, 0, s>>>(d);
+    qr_small_kernel<<<ninst, 1024, 0, s>>>(d);
     TN_CUDA(cudaGetLastError());
     count_launch();
 }
 
-void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int pend, cudaStream_t s) {
-    const int g = grid_x(mmax, TTN_PARTS);
-    hh_norm_kernel<<<dim3(g, ninst), BT, 0, s>>>(d, j);
-    TN_CUDA(cudaGetLastError());
+void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, int pend,
+                      cudaStream_t s) {
+    const int g = grid_x(mmax, 4 * TTN_PARTS);
+    if (j == p0) {  // inside a panel the update of column j - 1 formed this reflector
+        hh_norm_kernel<<<dim3(g, ninst), BT, 0, s>>>(d, j);
+        TN_CUDA(cudaGetLastError());
+        count_launch();
+    }
     hh_dots_kernel<<<dim3(g, ninst), BT, 0, s>>>(d, j, pend);
     TN_CUDA(cudaGetLastError());
     hh_update_kernel<<<dim3(g, ninst), BT, 0, s>>>(d, j, pend);
     TN_CUDA(cudaGetLastError());
-    count_launch(3);
+    count_launch(2);
 }
 
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,

@@ -277,7 +277,8 @@ struct tn_ttn_env {
             w_rt = 0, w_tt = 0, w_tau = 0, w_small = 0, w_wp = 0, w_w = 0, w_w2 = 0, w_hpart = 0,
             w_coef = 0, w_end = 0;
     int kry_vecs = 0;
-    int nchunk_t = 1;
+    int nchunk_t = 1;                 // k chunks of the link-tensor contractions
+    int nchunk_q = 1;                 // k chunks of the QR panel products
     // statistics of the last solve
     double energy = 0;
     int matvecs = 0, converged = 0;
@@ -396,7 +397,7 @@ void add_env_contraction(GemmPlan& g, CombPlan& comb, const std::vector<int>& di
     const int64_t per_unit = Q == 1 || P == 1 ? 1 : P;
     const int64_t ktot = units * per_unit;
     int nch = 1;
-    if (ktot >= 8192 && D >= 16) nch = int(std::min<int64_t>(nchunk_max, ktot / 4096));
+    if (ktot >= 4096 && D >= 16) nch = int(std::min<int64_t>(nchunk_max, ktot / 2048));
     nch = std::max(1, std::min<int>(nch, int(units)));
     const int64_t per = (units + nch - 1) / nch;
     std::vector<int64_t> parts;
@@ -559,7 +560,8 @@ void build_work_layout(tn_ttn_env* e, int kd) {
         return o;
     };
     e->kry_vecs = 2 * kd + 1;
-    e->nchunk_t = 16;
+    e->nchunk_t = 32;
+    e->nchunk_q = 128;
     e->w_x = take(S);
     e->w_y = take(S);
     e->w_kry = take(S * e->kry_vecs);
@@ -572,7 +574,7 @@ void build_work_layout(tn_ttn_env* e, int kd) {
     e->w_tt = take((e->dmax / HH_B + 2) * int64_t(HH_B) * HH_B);
     e->w_tau = take(e->dmax + 32);
     e->w_small = take(64);
-    e->w_wp = take(int64_t(e->nchunk_t) * HH_B * e->dmax);
+    e->w_wp = take(int64_t(e->nchunk_q) * HH_B * e->dmax);
     e->w_w = take(int64_t(HH_B) * e->dmax);
     e->w_w2 = take(int64_t(HH_B) * e->dmax);
     e->w_hpart = take(int64_t(HH_B) * HH_B * TTN_PARTS);
@@ -874,7 +876,7 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                 if (nt > 0) {
                     // W = V^T A_trail (split over rows), W2 = (-T)^T W, A_trail += V W2
                     const int64_t atr = aoff + p0 + int64_t(p0 + pb) * m;
-                    const int nch = int(std::min<int64_t>(e->nchunk_t, std::max<int64_t>(1, rows / 2048)));
+                    const int nch = int(std::min<int64_t>(e->nchunk_q, std::max<int64_t>(1, rows / 512)));
                     const int64_t per = (rows + nch - 1) / nch;
                     std::vector<int64_t> parts;
                     for (int c = 0; c < nch; ++c) {
@@ -907,7 +909,7 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                 // Q formation for this panel: Qsub = Q[p0:, p0:kmin]
                 const int nq = kmin - p0;
                 const int64_t qs = aoff + p0 + int64_t(p0) * m;
-                const int nch = int(std::min<int64_t>(e->nchunk_t, std::max<int64_t>(1, rows / 2048)));
+                const int nch = int(std::min<int64_t>(e->nchunk_q, std::max<int64_t>(1, rows / 512)));
                 const int64_t per = (rows + nch - 1) / nch;
                 std::vector<int64_t> parts;
                 for (int c = 0; c < nch; ++c) {
@@ -988,7 +990,7 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
             h.T = wptr(G, e, e->w_tt);
             h.tau = wptr(G, e, e->w_tau);
             h.scal = wptr(G, e, e->w_small);
-            h.wv = wptr(G, e, e->w_small) + 8;
+            h.wv = wptr(G, e, e->w_small) + 16;
             h.part = wptr(G, e, e->w_hpart);
             h.ticket = hh_ticket(G, e->idx);
             h.m = int(m);
@@ -1016,7 +1018,8 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
         const int sl = qr_slices(G);
         for (int p = 0; p * HH_B < kmax; ++p) {
             const int p0 = p * HH_B, pend = p0 + HH_B;
-            for (int j = p0; j < std::min(pend, kmax); ++j) launch_hh_column(dh, nh, mmax, j, pend, st);
+            for (int j = p0; j < std::min(pend, kmax); ++j)
+                launch_hh_column(dh, nh, mmax, j, p0, pend, st);
             launch_hh_panel_end(dh, nh, mmax, p0, HH_B, st);
             tplan_run(G, QP.w[p], sl, T_SVD);
             comb_run(G, QP.wc[p]);

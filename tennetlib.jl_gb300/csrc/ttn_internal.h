@@ -74,7 +74,7 @@ struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m 
     double* V;                   // panels of explicit reflectors, see hh_panel_voff
     double* T;                   // per panel -T (HH_B x HH_B)
     double* tau;                 // kmin
-    double* scal;                // current column: tau, scale, beta
+    double* scal;                // tau, scale, beta of column j at scal + 4 (j & 1)
     double* wv;                  // current column: tau * w_k of the panel columns
     double* part;                // partial sums (>= HH_B*HH_B*TTN_PARTS)
     unsigned* ticket;
@@ -95,7 +95,8 @@ void launch_bscale(const BScaleDesc* d, int ninst, int64_t nmax, cudaStream_t s)
 void launch_blincomb(const BLinDesc* d, int ninst, int64_t nmax, cudaStream_t s);
 void launch_permute(const PermDesc* d, int ninst, int64_t nmax, cudaStream_t s);
 void launch_qr_small(const QrDesc* d, int ninst, cudaStream_t s);
-void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int pend, cudaStream_t s);
+void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, int pend,
+                      cudaStream_t s);
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,
                          cudaStream_t s);
 void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s);
