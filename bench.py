@@ -225,6 +225,83 @@ def run_reference(args, world, rank, pg):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------------------------------
+# TTN leg: 32 transverse-field Ising instances on the 64-site binary tree
+# ------------------------------------------------------------------------------------
+TTN_SITES = 64
+TTN_INSTANCES = 32
+TTN_CHIS = [64, 128, 256]
+
+
+def tfim_ground_energy(J, h):
+    """Open TFIM ground energy by Jordan-Wigner: minus the sum of the singular values of
+    the bidiagonal matrix (h_i on the diagonal, J_i above it)."""
+    import numpy as np
+    B = np.diag(np.asarray(h, dtype=float)) + np.diag(np.asarray(J, dtype=float), 1)
+    return -float(np.linalg.svd(B, compute_uv=False).sum())
+
+
+def run_ttn(tn, device, args, world):
+    """One lockstep sweep of all instances (after one warm-up sweep); device time."""
+    ctx = tn.Context(device, precision=args.precision, slices=args.slices)
+    T = tn.ttn
+    chis, psis, models, exact = [], [], [], []
+    t0 = time.perf_counter()
+    for i in range(TTN_INSTANCES):
+        chi = TTN_CHIS[i % len(TTN_CHIS)]
+        J, h = T.tfim_instance(TTN_SITES, 1000 + i)
+        chis.append(chi)
+        psis.append(T.default_randomTTN(TTN_SITES, chi, 2000 + i, ctx=ctx))
+        models.append(T.CouplingModel(T.tfim_terms(J, h), TTN_SITES))
+        exact.append(tfim_ground_energy(J, h))
+    envs = T.StateEnvsTTN.batch(psis, models)
+    prep = time.perf_counter() - t0
+    path = T.default_sweeppath(TTN_SITES)
+    sws = [T.SweepDataTTN() for _ in envs]
+    kw = dict(maxdim=max(TTN_CHIS), outputlevel=0)
+    T.fullsweep_batch_(envs, path, tn.eig_solver, sws, **kw)      # warm-up
+    t1 = time.perf_counter()
+    T.fullsweep_batch_(envs, path, tn.eig_solver, sws, **kw)      # timed
+    wall = time.perf_counter() - t1
+    st = sws[0].stats[-1]
+    dev_s = st["sweep_ms"] / 1e3
+    rel = [abs(sw.energy[-1] - e) / abs(e) for sw, e in zip(sws, exact)]
+    out = {
+        "workload": "tfim_binary_tree_64_sites_32_instances_maxdim_64_128_256",
+        "instances": TTN_INSTANCES, "maxdim_cycle": TTN_CHIS, "sweeps_before_timed": 1,
+        "value": dev_s, "unit": "s/sweep (all instances, lockstep)",
+        "wall_s": wall, "prepare_s": prep,
+        "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
+        "heff_flops_per_sweep": st["heff_flops"],
+        "time_share": {k: st[k] / max(st["sweep_ms"], 1e-9)
+                       for k in ("heff_ms", "env_ms", "svd_ms", "lanczos_ms", "pack_ms")},
+        "time_share_note": "svd_ms = QR isometry moves; env_ms = link-tensor moves",
+        "matvecs": st["matvecs"], "gpu_launches": st["kernel_launches"],
+        "max_rel_energy_error_vs_free_fermion_after_2_sweeps": max(rel),
+        "median_rel_energy_error_after_2_sweeps": statistics.median(rel),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = ttn_cpu_baseline()
+    return out
+
+
+def ttn_cpu_baseline():
+    """The numpy oracle on a bounded sample: one sweep of instance 0 (maxdim 64)."""
+    from oracle import ttn_oracle as O
+    J, h = O.tfim_instance(TTN_SITES, 1000)
+    se = O.StateEnvsTTN(O.random_ttn(TTN_SITES, TTN_CHIS[0], 2000), O.tfim_terms(J, h))
+    g, _ = O.default_graph_sitenodes(TTN_SITES)
+    sw = O.SweepDataTTN()
+    t0 = time.perf_counter()
+    O.fullsweep(se, O.default_sweeppath(TTN_SITES, g.keys()), sw, maxdim=TTN_CHIS[0])
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s/sweep of one maxdim-64 instance", "cores": cores(),
+            "kind": "port",
+            "sample": "one sweep (124 node updates) of instance 0 (maxdim 64) by the numpy "
+                      "FP64 TTN oracle; maxdim-128 and -256 instances cost about 8x and 100x "
+                      "more each on the CPU"}
+
+
 def config(args):
     return {"workload": "heisenberg_u1_chain_N100_maxdim1024_cutoff1e-12",
             "model": "S=1/2 Heisenberg OBC, MPO w=5, U(1) Sz=0, Neel start",
@@ -346,6 +423,8 @@ def run_ours(args, world, rank, local, pg):
         res["fp64_compare"] = fp64_compare(tn, ctx, H, pq, tensors, links, local)
     if world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline_from(tensors, links)
+    if not args.no_ttn:
+        res["ttn"] = run_ttn(tn, local, args, world)
     print(json.dumps(res), flush=True)
 
 
@@ -379,6 +458,7 @@ def main():
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-ttn", action="store_true", help="skip the TTN (32-instance) leg")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":

@@ -89,6 +89,8 @@ typedef struct tn_sweep_result {
     double pack_ms;            /* device time of the bf16 slice packing (split precision) */
     int64_t gemm_launches;     /* number of those launches */
     int64_t kernel_launches;   /* all kernels this library launched during the sweep */
+    double qr_panel_ms;        /* TTN: device time of the Householder column/panel kernels */
+    double qr_gemm_ms;         /* TTN: device time of the QR's grouped GEMMs (with packing) */
 } tn_sweep_result;
 
 /* ---- context ------------------------------------------------------------------- */

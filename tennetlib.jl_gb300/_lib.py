@@ -71,6 +71,8 @@ class SweepResult(C.Structure):
         ("pack_ms", C.c_double),
         ("gemm_launches", C.c_int64),
         ("kernel_launches", C.c_int64),
+        ("qr_panel_ms", C.c_double),
+        ("qr_gemm_ms", C.c_double),
     ]
 
 

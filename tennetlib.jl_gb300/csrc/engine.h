@@ -12,7 +12,8 @@ namespace tn {
 
 // CUDA-event interval timer: intervals are recorded on the stream and resolved only at the
 // next synchronisation point, so timing adds no host round trips.
-enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_GEMM, T_PACK, T_NCAT };
+enum TimeCat { T_HEFF = 0, T_ENV, T_SVD, T_LANCZOS, T_SWEEP, T_GEMM, T_PACK, T_QRPANEL, T_QRGEMM,
+               T_NCAT };
 struct EventTimer {
     cudaStream_t s = nullptr;
     std::vector<cudaEvent_t> pool;
@@ -120,7 +121,7 @@ struct tn_env {
     std::unique_ptr<Heff1Plan> h1p;
     int h1p_pos = -1;
     tn::DevBuf vecC, vecD;
-    double acc_ms[tn::T_NCAT] = {0, 0, 0, 0, 0, 0, 0};
+    double acc_ms[tn::T_NCAT] = {};
     double gemm_flops = 0;
     int64_t gemm_launches = 0;
     int64_t matvecs = 0;

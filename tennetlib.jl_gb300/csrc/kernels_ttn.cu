@@ -389,6 +389,135 @@ __global__ void __launch_bounds__(BT) hh_update_kernel(const HhDesc* __restrict_
     }
 }
 
+// ---- cooperative panel factorisation -------------------------------------------------
+// All CTAs of one launch are co-resident (cooperative launch).  Instance i owns the CTAs
+// [cta0, cta0 + ncta), each a contiguous chunk of the rows [p0, m).  Per column: partial
+// norms -> barrier -> every CTA forms the same reflector -> partial dots -> barrier ->
+// every CTA sums the same partials in the same order -> local update.  Waits are bounded
+// (about a second of clocks); a wait that gives up sets *err and the kernel returns.
+constexpr long long COOP_WAIT = 2000000000LL;
+
+__device__ __forceinline__ bool inst_barrier(unsigned* bar, unsigned target, int* err,
+                                             int* s_fail) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        const long long t0 = clock64();
+        while (true) {
+            if (*reinterpret_cast<volatile unsigned*>(bar) >= target) break;
+            if (*reinterpret_cast<volatile int*>(err) != 0 || clock64() - t0 > COOP_WAIT) {
+                atomicExch(err, 2);
+                *s_fail = 1;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *reinterpret_cast<volatile int*>(s_fail) == 0;
+}
+
+__global__ void __launch_bounds__(BT)
+hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* err) {
+    __shared__ double red[BT / 32][HH_B];
+    __shared__ double red1[33];
+    __shared__ double wsh[HH_B];
+    __shared__ double sc[3];
+    __shared__ int s_fail;
+    int inst = -1;
+    for (int i = 0; i < ninst; ++i)
+        if (int(blockIdx.x) >= descs[i].cta0 && int(blockIdx.x) < descs[i].cta0 + descs[i].ncta) inst = i;
+    if (inst < 0) return;
+    const HhDesc& D = descs[inst];
+    if (p0 >= D.kmin) return;  // uniform over the instance's CTAs
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+    const int G = D.ncta, g = int(blockIdx.x) - D.cta0;
+    const int pe = (p0 + HH_B) < D.kmin ? (p0 + HH_B) : D.kmin;
+    const int64_t m = D.m;
+    const int64_t chunk = (m - p0 + G - 1) / G;
+    const int64_t r0 = p0 + int64_t(g) * chunk;
+    const int64_t r1 = (r0 + chunk) < m ? (r0 + chunk) : m;
+    double* part1 = D.part;        // G norm partials
+    double* part2 = D.part + G;    // G x HH_B dot partials
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned nb = 0;
+    for (int j = p0; j < pe; ++j) {
+        double* col = D.A + int64_t(j) * m;
+        double s = 0.0;
+        for (int64_t i = (r0 > j + 1 ? r0 : j + 1) + threadIdx.x; i < r1; i += BT) s = fma(col[i], col[i], s);
+        s = block_sum(s, red1);
+        if (threadIdx.x == 0) part1[g] = s;
+        if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
+        // every CTA sums the G partials in the same fixed order (lane-strided, then a
+        // warp tree): identical reflectors everywhere
+        if (wid == 0) {
+            double t = 0.0;
+            for (int b = lane; b < G; b += 32) t += reinterpret_cast<volatile double*>(part1)[b];
+            t = warp_sum(t);
+            if (lane == 0) {
+                const double alpha = reinterpret_cast<volatile double*>(col)[j];
+                double tau, scale, beta;
+                make_reflector(alpha, t, tau, scale, beta);
+                sc[0] = tau;
+                sc[1] = scale;
+                sc[2] = beta;
+            }
+        }
+        __syncthreads();
+        const double tau = sc[0], scale = sc[1], beta = sc[2];
+        const int nk = pe - j - 1;
+        const int64_t i0 = r0 > j ? r0 : j;
+        if (nk > 0) {
+            double acc[HH_B];
+#pragma unroll
+            for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
+            for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
+                const double v = i == j ? 1.0 : col[i] * scale;
+#pragma unroll
+                for (int c = 0; c < HH_B; ++c)
+                    if (c < nk) acc[c] = fma(v, D.A[i + int64_t(j + 1 + c) * m], acc[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < HH_B; ++c) {
+                const double v = warp_sum(acc[c]);
+                if (lane == 0) red[wid][c] = v;
+            }
+            __syncthreads();
+            if (threadIdx.x < nk) {
+                double t = 0.0;
+                for (int w = 0; w < BT / 32; ++w) t += red[w][threadIdx.x];
+                part2[int64_t(g) * HH_B + threadIdx.x] = t;
+            }
+            if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
+            for (int c = wid; c < nk; c += BT / 32) {
+                double t = 0.0;
+                for (int b = lane; b < G; b += 32)
+                    t += reinterpret_cast<volatile double*>(part2)[int64_t(b) * HH_B + c];
+                t = warp_sum(t);
+                if (lane == 0) wsh[c] = tau * t;  // the partials include row j (v_j = 1)
+            }
+            __syncthreads();
+            for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
+                const double v = i == j ? 1.0 : col[i] * scale;
+                for (int c = 0; c < nk; ++c) {
+                    double* a = D.A + i + int64_t(j + 1 + c) * m;
+                    *a = fma(-v, wsh[c], *a);
+                }
+            }
+        } else {
+            // last column of the panel: every CTA must have read alpha (= A[j, j]) before
+            // its owner overwrites it with beta below
+            if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
+        }
+        for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) col[i] = i == j ? beta : col[i] * scale;
+        if (g == 0 && threadIdx.x == 0) D.tau[j] = tau;
+        __syncthreads();
+    }
+}
+
 // explicit unit lower-trapezoidal V of the panel [p0, p0 + pb): V (m - p0) x pb, ld m - p0
 __global__ void __launch_bounds__(BT) hh_build_v_kernel(const HhDesc* __restrict__ descs, int p0,
                                                         int pb_max) {
@@ -558,6 +687,26 @@ void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, i
     hh_update_kernel<<<dim3(g, ninst), BT, 0, s>>>(d, j, pend);
     TN_CUDA(cudaGetLastError());
     count_launch(2);
+}
+
+int hh_coop_capacity() {
+    static int cap = -1;
+    if (cap < 0) {
+        int dev = 0, nsm = 0, per = 0;
+        TN_CUDA(cudaGetDevice(&dev));
+        TN_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        TN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, hh_panel_coop_kernel, BT, 0));
+        cap = nsm * per;
+    }
+    return cap;
+}
+
+void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int p0, int* err,
+                          cudaStream_t s) {
+    void* args[] = {(void*)&d, (void*)&ninst, (void*)&p0, (void*)&err};
+    TN_CUDA(cudaLaunchCooperativeKernel((const void*)hh_panel_coop_kernel, dim3(nctas), dim3(BT),
+                                        args, 0, s));
+    count_launch();
 }
 
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,

@@ -288,14 +288,14 @@ struct TtnGroup {
     tn_ctx* ctx = nullptr;
     std::vector<tn_ttn_env*> envs;  // members in creation order (null once destroyed)
     int alive = 0;
-    DevBuf arena, work, packs, tickets, scal, bpart;
+    DevBuf arena, work, packs, tickets, scal, bpart, bars;
     DevBuf d_gs, d_sc, d_lin, d_perm, d_qr, d_hh;  // descriptor tables of the batched kernels
     int work_kd = 0;
     std::map<int, std::unique_ptr<ProductPlan>> pcache;
     std::map<std::pair<int, int>, std::unique_ptr<MovePlan>> mcache;
     std::map<std::pair<int, int>, std::unique_ptr<QrPlan>> qcache;
     int dims_version = 0, cache_version = -1;
-    double acc_ms[T_NCAT] = {0, 0, 0, 0, 0, 0, 0};
+    double acc_ms[T_NCAT] = {};
     double heff_flops = 0, gemm_flops = 0;
     int64_t gemm_launches = 0, matvecs = 0;
 };
@@ -874,7 +874,8 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                 const int64_t toff = e->wbase + e->w_tt + int64_t(p) * HH_B * HH_B;
                 const int nt = n - p0 - pb;
                 if (nt > 0) {
-                    // W = V^T A_trail (split over rows), W2 = (-T)^T W, A_trail += V W2
+                    // Wt = A_trail^T V (split over rows; nt x pb so that the long side is M),
+                    // W2 = (-T)^T Wt^T, A_trail += V W2
                     const int64_t atr = aoff + p0 + int64_t(p0 + pb) * m;
                     const int nch = int(std::min<int64_t>(e->nchunk_q, std::max<int64_t>(1, rows / 512)));
                     const int64_t per = (rows + nch - 1) / nch;
@@ -884,8 +885,8 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                         if (r0 >= r1) break;
                         const int64_t wo = nch > 1 ? e->wbase + e->w_wp + int64_t(c) * HH_B * nt
                                                    : e->wbase + e->w_w;
-                        Q.w[p].g.add_task(S_R, wo, pb, nt, pb, 0);
-                        Q.w[p].g.add_seg(S_R, voff + r0, int(rows), 1, abuf, atr + r0, int(m), 0,
+                        Q.w[p].g.add_task(S_R, wo, nt, pb, nt, 0);
+                        Q.w[p].g.add_seg(abuf, atr + r0, int(m), 1, S_R, voff + r0, int(rows), 0,
                                          int(r1 - r0));
                         if (nch > 1) parts.push_back(wo);
                     }
@@ -893,20 +894,21 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                         CombOut o{};
                         o.doff = e->wbase + e->w_w;
                         o.dbuf = S_R;
-                        o.ldd = pb;
-                        o.rows = pb;
-                        o.cols = nt;
+                        o.ldd = nt;
+                        o.rows = nt;
+                        o.cols = pb;
                         o.t0 = int(Q.wc[p].terms.size());
                         o.nt = int(parts.size());
-                        for (int64_t po : parts) Q.wc[p].terms.push_back(CombTerm{po, S_R, pb, 1.0});
+                        for (int64_t po : parts) Q.wc[p].terms.push_back(CombTerm{po, S_R, nt, 1.0});
                         Q.wc[p].outs.push_back(o);
                     }
                     Q.w2[p].g.add_task(S_R, e->wbase + e->w_w2, pb, nt, pb, 0);
-                    Q.w2[p].g.add_seg(S_R, toff, HH_B, 1, S_R, e->wbase + e->w_w, pb, 0, pb);
+                    Q.w2[p].g.add_seg(S_R, toff, HH_B, 1, S_R, e->wbase + e->w_w, nt, 1, pb);
                     Q.upd[p].g.add_task(abuf, atr, int(rows), nt, int(m), 1);
                     Q.upd[p].g.add_seg(S_R, voff, int(rows), 0, S_R, e->wbase + e->w_w2, pb, 0, pb);
                 }
-                // Q formation for this panel: Qsub = Q[p0:, p0:kmin]
+                // Q formation for this panel: Qsub = Q[p0:, p0:kmin]; Wt = Qsub^T V,
+                // W2 = (-T) Wt^T, Qsub += V W2
                 const int nq = kmin - p0;
                 const int64_t qs = aoff + p0 + int64_t(p0) * m;
                 const int nch = int(std::min<int64_t>(e->nchunk_q, std::max<int64_t>(1, rows / 512)));
@@ -917,24 +919,24 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
                     if (r0 >= r1) break;
                     const int64_t wo = nch > 1 ? e->wbase + e->w_wp + int64_t(c) * HH_B * nq
                                                : e->wbase + e->w_w;
-                    Q.qw[p].g.add_task(S_R, wo, pb, nq, pb, 0);
-                    Q.qw[p].g.add_seg(S_R, voff + r0, int(rows), 1, abuf, qs + r0, int(m), 0, int(r1 - r0));
+                    Q.qw[p].g.add_task(S_R, wo, nq, pb, nq, 0);
+                    Q.qw[p].g.add_seg(abuf, qs + r0, int(m), 1, S_R, voff + r0, int(rows), 0, int(r1 - r0));
                     if (nch > 1) parts.push_back(wo);
                 }
                 if (parts.size() > 1) {
                     CombOut o{};
                     o.doff = e->wbase + e->w_w;
                     o.dbuf = S_R;
-                    o.ldd = pb;
-                    o.rows = pb;
-                    o.cols = nq;
+                    o.ldd = nq;
+                    o.rows = nq;
+                    o.cols = pb;
                     o.t0 = int(Q.qwc[p].terms.size());
                     o.nt = int(parts.size());
-                    for (int64_t po : parts) Q.qwc[p].terms.push_back(CombTerm{po, S_R, pb, 1.0});
+                    for (int64_t po : parts) Q.qwc[p].terms.push_back(CombTerm{po, S_R, nq, 1.0});
                     Q.qwc[p].outs.push_back(o);
                 }
                 Q.qw2[p].g.add_task(S_R, e->wbase + e->w_w2, pb, nq, pb, 0);
-                Q.qw2[p].g.add_seg(S_R, toff, HH_B, 0, S_R, e->wbase + e->w_w, pb, 0, pb);
+                Q.qw2[p].g.add_seg(S_R, toff, HH_B, 0, S_R, e->wbase + e->w_w, nq, 1, pb);
                 Q.qupd[p].g.add_task(abuf, qs, int(rows), nq, int(m), 1);
                 Q.qupd[p].g.add_seg(S_R, voff, int(rows), 0, S_R, e->wbase + e->w_w2, pb, 0, pb);
             }
@@ -1008,31 +1010,68 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
     }
     if (!small.empty()) {
         upload_descs(G, G.d_qr, small);
+        const int q0 = G.ctx->timer.mark();
         launch_qr_small(G.d_qr.as<QrDesc>(), int(small.size()), st);
+        G.ctx->timer.add(T_QRPANEL, q0, G.ctx->timer.mark());
     }
     QrPlan& QP = qr_plan(G, v, u, blocked);
     if (!hh.empty()) {
+        // CTAs of the cooperative panel kernel, in proportion to the rows of each matrix
+        const int cap = hh_coop_capacity();
+        const int nh0 = int(hh.size());
+        bool coop = nh0 <= cap;
+        if (coop) {
+            double tot = 0;
+            for (auto& h : hh) tot += double(h.m);
+            int used = 0;
+            for (auto& h : hh) {
+                h.ncta = std::max(1, int(double(cap - nh0) * double(h.m) / tot));
+                h.ncta = int(std::min<int64_t>(h.ncta, std::max<int64_t>(1, (h.m + 255) / 256)));
+                h.cta0 = used;
+                used += h.ncta;
+            }
+            coop = used <= cap;
+        }
+        if (G.bars.bytes < hh.size() * sizeof(unsigned))
+            G.bars.alloc(std::max<size_t>(hh.size() * sizeof(unsigned), 64), st);
+        int nctas = 0;
+        for (size_t i = 0; i < hh.size(); ++i) {
+            hh[i].bar = G.bars.as<unsigned>() + i;
+            nctas = std::max(nctas, hh[i].cta0 + hh[i].ncta);
+        }
         upload_descs(G, G.d_hh, hh);
         const HhDesc* dh = G.d_hh.as<HhDesc>();
         const int nh = int(hh.size());
         const int sl = qr_slices(G);
+        tn_ctx* ctx = G.ctx;
         for (int p = 0; p * HH_B < kmax; ++p) {
             const int p0 = p * HH_B, pend = p0 + HH_B;
-            for (int j = p0; j < std::min(pend, kmax); ++j)
-                launch_hh_column(dh, nh, mmax, j, p0, pend, st);
+            const int q0 = ctx->timer.mark();
+            if (coop) {
+                TN_CUDA(cudaMemsetAsync(G.bars.p, 0, size_t(nh) * sizeof(unsigned), st));
+                launch_hh_panel_coop(dh, nh, nctas, p0, ctx->err.as<int>(), st);
+            } else {
+                for (int j = p0; j < std::min(pend, kmax); ++j)
+                    launch_hh_column(dh, nh, mmax, j, p0, pend, st);
+            }
             launch_hh_panel_end(dh, nh, mmax, p0, HH_B, st);
+            const int q1 = ctx->timer.mark();
             tplan_run(G, QP.w[p], sl, T_SVD);
             comb_run(G, QP.wc[p]);
             tplan_run(G, QP.w2[p], sl, T_SVD);
             tplan_run(G, QP.upd[p], sl, T_SVD);
+            ctx->timer.add(T_QRPANEL, q0, q1);
+            ctx->timer.add(T_QRGEMM, q1, ctx->timer.mark());
         }
         launch_hh_finish(dh, nh, mnmax, st);
+        const int q2 = ctx->timer.mark();
         for (int p = (kmax + HH_B - 1) / HH_B - 1; p >= 0; --p) {
             tplan_run(G, QP.qw[p], sl, T_SVD);
             comb_run(G, QP.qwc[p]);
             tplan_run(G, QP.qw2[p], sl, T_SVD);
             tplan_run(G, QP.qupd[p], sl, T_SVD);
         }
+        ctx->timer.add(T_QRGEMM, q2, ctx->timer.mark());
     }
     // Q back into the node tensor (leg lu now of size kmin)
     for (size_t i = 0; i < E.size(); ++i) {
@@ -1490,6 +1529,8 @@ void fill_sweep_result(TtnGroup& G, tn_ttn_env* e, tn_sweep_result* r, int64_t l
     r->pack_ms = G.acc_ms[T_PACK];
     r->gemm_launches = G.gemm_launches;
     r->kernel_launches = launches;
+    r->qr_panel_ms = G.acc_ms[T_QRPANEL];
+    r->qr_gemm_ms = G.acc_ms[T_QRGEMM];
 }
 
 }  // namespace
@@ -1621,6 +1662,7 @@ int tn_ttn_isometrize(tn_ttn* psi, int node, int normalize) {
         psi->center = node;
         TN_CUDA(cudaStreamSynchronize(st));
         G->envs.clear();
+        check_device_error_public(psi->ctx);
     });
 }
 
@@ -1707,6 +1749,7 @@ int tn_ttn_env_position(tn_ttn_env* env, int node) {
         TN_REQUIRE(node >= 0 && node < env->tree.nn, "bad node");
         position_group(G, node, true, INT_MAX);
         collect_stats(G);
+        check_device_error_public(env->ctx);
     });
 }
 

@@ -78,7 +78,10 @@ struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m 
     double* wv;                  // current column: tau * w_k of the panel columns
     double* part;                // partial sums (>= HH_B*HH_B*TTN_PARTS)
     unsigned* ticket;
-    int32_t m, n, kmin, pad;
+    unsigned* bar;               // barrier counter of the cooperative panel kernel
+    int32_t m, n, kmin;
+    int32_t cta0, ncta;          // CTAs [cta0, cta0 + ncta) of the cooperative panel kernel
+    int32_t pad;
 };
 
 // offset of the explicit V of the panel starting at column p0 (panels of HH_B columns,
@@ -100,5 +103,11 @@ void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, i
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,
                          cudaStream_t s);
 void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s);
+// CTAs that the cooperative panel kernel may use (all co-resident on the device)
+int hh_coop_capacity();
+// one panel [p0, p0 + HH_B) of every instance in one cooperative launch of nctas CTAs
+// (instance i owns CTAs [cta0, cta0 + ncta)); grid-wide waits are bounded and set *err
+void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int p0, int* err,
+                          cudaStream_t s);
 
 }  // namespace tn

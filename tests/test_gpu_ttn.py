@@ -175,3 +175,25 @@ def test_optimize_api_and_unbuilt_modes(tn, ctx):
     with pytest.raises(tn.TenNetError):
         tn.ttn.fullsweep_(se, tn.ttn.default_sweeppath(N)[:-1], tn.eig_solver,
                           tn.ttn.SweepDataTTN(), outputlevel=0)
+
+
+def test_batched_blocked_qr_matches_single(tn, ctx):
+    """Tall QR moves of several instances share one cooperative panel launch; results equal
+    those of each instance alone (N = 32: the (48|64)^3 top nodes take the blocked path)."""
+    N = 32
+    chis = [64, 48, 64]
+    path = tn.ttn.default_sweeppath(N)
+    insts = [tfim(N, 30 + i) for i in range(3)]
+    psis = [tn.ttn.default_randomTTN(N, c, 40 + i, ctx=ctx) for i, c in enumerate(chis)]
+    models = [model(tn, N, t) for t, _ in insts]
+    batch = tn.ttn.StateEnvsTTN.batch(psis, models)
+    swb = [tn.ttn.SweepDataTTN() for _ in range(3)]
+    for _ in range(2):
+        tn.ttn.fullsweep_batch_(batch, path, tn.eig_solver, swb, maxdim=64, outputlevel=0)
+    for i in range(3):
+        se = tn.ttn.StateEnvsTTN(psis[i], models[i])
+        sw = tn.ttn.SweepDataTTN()
+        for _ in range(2):
+            tn.ttn.fullsweep_(se, path, tn.eig_solver, sw, maxdim=64, outputlevel=0)
+        assert np.allclose(swb[i].energy, sw.energy, rtol=1e-10, atol=0), (i, swb[i].energy, sw.energy)
+    assert _isometric(batch[0].getpsi(), batch[0].orthocenter)
