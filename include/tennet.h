@@ -127,6 +127,12 @@ int tn_mps_link(const tn_mps* mps, int link, int32_t* nsec, int32_t* q, int32_t*
 /* dense site tensor (Dl, d, Dr) column-major */
 int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap);
 int tn_mps_center(const tn_mps* mps);
+/* measure(T, psi, opstr) for every site (TenNetLib src/mps/measure.jl:150-219): out[i] =
+ * <psi|O_i|psi> / <psi|psi> with the single-site operator op (d x d column-major [s', s]),
+ * from GPU transfer matrices instead of moving the orthogonality centre (equal for the
+ * normalised states the sweeps produce).  Entries with q_{s'} != q_s do not contribute
+ * (charge conservation). */
+int tn_mps_expect_local(tn_mps* mps, const double* op, double* out);
 
 /* ---- StateEnvs --------------------------------------------------------------------
  * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO

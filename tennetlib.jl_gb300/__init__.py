@@ -18,6 +18,7 @@ Python                          TenNetLib (file:line)
 ``exp_solver``                  ``exp_solver``                      src/base/solver.jl:66-88
 ``TDVPEngine`` / ``tdvpsweep_``  ``TDVPEngine`` / ``tdvpsweep!``      src/mps/tdvp.jl:17-277
 ``entropy``                     ``_entropy``                        src/mps/measure.jl:4-20
+``measure(psi, "Sz")``          ``measure``                         src/mps/measure.jl:150-219
 ``ttn.*``                       the TTN path (``TTN``, ``StateEnvsTTN``, ``optimize!``; see ttn.py)
 =============================  ==============================================================
 
@@ -45,7 +46,7 @@ __all__ = [
     "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
     "update_position_", "fullsweep_", "dmrg_", "dmrg", "dmrg2", "entropy", "svd_truncate",
     "Float64_threshold", "TenNetError", "models", "TDVPEngine", "tdvpsweep_", "exp_solver",
-    "ttn",
+    "ttn", "measure",
 ]
 
 _threshold = [FLOAT64_THRESHOLD]
@@ -235,6 +236,17 @@ class MPS:
     def center(self):
         return self.ctx.lib.tn_mps_center(self.h)
 
+    def expect_local(self, op):
+        """<psi|O_i|psi> / <psi|psi> for every site i (op: d x d matrix [s', s])."""
+        op = np.asarray(op, dtype=np.float64)
+        if op.shape != (self.d, self.d):
+            raise ValueError("operator must be d x d")
+        flat = np.ascontiguousarray(op.ravel(order="F"))
+        out = np.zeros(self.N)
+        L.check(self.ctx.lib.tn_mps_expect_local(self.h, flat.ctypes.data_as(L.f64p),
+                                                 out.ctypes.data_as(L.f64p)))
+        return out
+
     def __len__(self):
         return self.N
 
@@ -308,6 +320,31 @@ class StateEnvs:
             _release(self, "tn_env_destroy")
         except Exception:
             pass
+
+
+SPIN_HALF_OPS = {
+    "Sz": np.diag([0.5, -0.5]),
+    "Sx": np.array([[0.0, 0.5], [0.5, 0.0]]),
+    "S+": np.array([[0.0, 1.0], [0.0, 0.0]]),
+    "S-": np.array([[0.0, 0.0], [1.0, 0.0]]),
+    "Id": np.eye(2),
+    "Nup": np.diag([1.0, 0.0]),
+    "Ndn": np.diag([0.0, 1.0]),
+}
+
+
+def measure(psi: MPS, op, pos: int | None = None, sites=None):
+    """``measure(Float64, psi, opstr[, pos]; sites)`` (``src/mps/measure.jl:150-219``):
+    local expectation values of a single-site operator, given by S=1/2 name ("Sz", "Sx",
+    "S+", "S-", "Id", "Nup", "Ndn") or as a d x d matrix [s', s].  pos (0-based) returns one
+    value; sites selects a subset; default all sites."""
+    mat = SPIN_HALF_OPS[op] if isinstance(op, str) else np.asarray(op, dtype=np.float64)
+    vals = psi.expect_local(mat)
+    if pos is not None:
+        return float(vals[pos])
+    if sites is not None:
+        return [float(vals[i]) for i in sites]
+    return [float(v) for v in vals]
 
 
 def exp_solver(*_args, **_kwargs):

@@ -271,6 +271,26 @@ gs_pass_kernel(VecPtrs V, int kk, double* __restrict__ w, const double* __restri
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+__global__ void __launch_bounds__(BLAS_THREADS)
+block_dot_kernel(const BlockDot* __restrict__ descs, double* __restrict__ out) {
+    __shared__ double red[BLAS_THREADS / 32];
+    const BlockDot D = descs[blockIdx.x];
+    const int64_t n = int64_t(D.rows) * D.cols;
+    double acc = 0.0;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const int r = int(e % D.rows), c = int(e / D.rows);
+        acc = fma(D.x[r + int64_t(c) * D.ldx], D.y[r + int64_t(c) * D.ldy], acc);
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < BLAS_THREADS / 32; ++w) s += red[w];
+        out[blockIdx.x] = s;
+    }
+}
+
 int grid_for(int64_t n) {
     int64_t g = (n + BLAS_THREADS - 1) / BLAS_THREADS;
     if (g > BLAS_PARTS) g = BLAS_PARTS;
@@ -303,6 +323,13 @@ void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s) {
 }
 
 int blas_nparts() { return BLAS_PARTS; }
+
+void launch_block_dots(const BlockDot* d, int n, double* out, cudaStream_t s) {
+    if (n <= 0) return;
+    block_dot_kernel<<<n, BLAS_THREADS, 0, s>>>(d, out);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+}
 
 void launch_multi_dot(const double* const* V, int K, const double* w, int64_t n,
                       double* part, double* out, cudaStream_t s) {

@@ -254,6 +254,15 @@ void launch_scale_into(double* dst, const double* src, const double* denom_sq_or
 void launch_lincomb(double* dst, const double* const* V, int K, const double* coef,
                     int64_t n, cudaStream_t s);
 
+// sum of x (.) y over one rows x cols block pair (x, y column-major with their leading
+// dimensions), one result per pair, deterministic
+struct BlockDot {
+    const double* x;
+    const double* y;
+    int32_t ldx, ldy, rows, cols;
+};
+void launch_block_dots(const BlockDot* d, int n, double* out, cudaStream_t s);
+
 // Block SVD: for each block b with rows x cols matrix at src + off[b], compute its SVD by
 // one-sided Jacobi on the m x n work matrix (m >= n; the transpose when rows < cols).
 struct SvdBlockDesc {

@@ -1,0 +1,65 @@
+"""Local expectation values on the GPU (tn_mps_expect_local) against the oracle.
+
+Tolerance: 1e-12 absolute per site (values are O(1)); the sum of <S^z_i> over a state of
+total S^z = 0 vanishes to 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import tn_oracle as O
+from tests.helpers import random_qn_mps, upload_mps
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_state(psi, N):
+    A = [psi.site(i) for i in range(N)]
+    links = [psi.link_charges(i).astype(np.int64) for i in range(N + 1)]
+    return O.MPS(A, links, O.SPIN_HALF_Q.copy(), center=psi.center)
+
+
+def test_measure_ground_state_matches_oracle(tn, ctx):
+    N = 12
+    W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
+    H = tn.MPO(W, delta, pq, ctx)
+    env = tn.StateEnvs(tn.MPS.product(tn.models.neel_states(N), pq, ctx), H)
+    sw = tn.SweepData()
+    for md in (8, 16, 32, 32):
+        tn.fullsweep_(env, tn.eig_solver, 2, sw, maxdim=md, cutoff=1e-12, outputlevel=0)
+    psi = env.getpsi()
+    sz = tn.measure(psi, "Sz")
+    ref = O.expect_local(_oracle_state(psi, N), np.diag([0.5, -0.5]))
+    assert np.allclose(sz, ref, atol=1e-12)
+    assert abs(sum(sz)) < 1e-12
+    assert tn.measure(psi, "Sz", pos=3) == pytest.approx(sz[3], abs=1e-15)
+    assert np.allclose(tn.measure(psi, "Id"), 1.0, atol=1e-12)
+    # mirror symmetry of the open chain ground state
+    assert np.allclose(sz, -np.array(sz[::-1]), atol=1e-8)
+
+
+def test_measure_mixed_canonical_random_state(tn, ctx):
+    """A random charge-conserving MPS with the centre in the middle (left- and
+    right-grouped site layouts both present), unnormalised."""
+    rng = np.random.default_rng(7)
+    N = 8
+    mps = random_qn_mps(N, rng, maxsec_dim=3)
+    psi = upload_mps(tn, ctx, mps, center=4)
+    sz = np.diag([0.5, -0.5])
+    # dense reference: contract the whole state
+    v = mps.A[0]
+    for a in mps.A[1:]:
+        v = np.tensordot(v, a, axes=([-1], [0]))
+    v = v.reshape(-1)
+    nrm = v @ v
+    ref = []
+    for i in range(N):
+        op = [np.eye(2)] * N
+        op[i] = sz
+        M = op[0]
+        for o in op[1:]:
+            M = np.kron(M, o)
+        ref.append(v @ (M @ v) / nrm)
+    got = psi.expect_local(sz)
+    assert np.allclose(got, ref, atol=1e-12)
+    nup = psi.expect_local(np.diag([1.0, 0.0]))
+    assert np.allclose(nup, 0.5 + np.array(ref), atol=1e-12)
