@@ -1605,6 +1605,36 @@ void tn::run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs) {
 }
 void tn::check_device_error_public(tn_ctx* ctx) { check_device_error(ctx); }
 
+// SVD with ITensors truncation of one dense m x n matrix A on the device (the block SVD of
+// replacebond! on a single block): U (m x k, ld m) and S V^T (k x n, ld k); returns k.
+int tn::svd_truncate_dense(tn_ctx* ctx, const double* A, int m, int n, int maxdim, int mindim,
+                           double cutoff, double* U, double* SVt, double* truncerr) {
+    cudaStream_t st = ctx->stream;
+    DevBuf dX, dW, dV, dP, dS, dPerm, ddesc, ded;
+    SvdResult R;
+    block_svd(ctx, dX, dW, dV, dP, dS, dPerm, ddesc, {m}, {n}, {0}, A, R);
+    TruncDecision D = decide(R, maxdim, mindim, cutoff);
+    const int k = D.kept[0];
+    ExtractDesc e{};
+    e.x_off = R.desc[0].x_off;
+    e.v_off = R.desc[0].v_off;
+    e.s_off = R.desc[0].s_off;
+    e.left_off = 0;
+    e.right_off = 0;
+    e.rows = m;
+    e.cols = n;
+    e.n = R.desc[0].n;
+    e.trans = R.desc[0].trans;
+    e.k = k;
+    ded.alloc(sizeof(ExtractDesc), st);
+    TN_CUDA(cudaMemcpyAsync(ded.p, &e, sizeof(ExtractDesc), cudaMemcpyHostToDevice, st));
+    launch_svd_extract(ded.as<ExtractDesc>(), 1, dW.d(), dV.d(), dS.d(), dPerm.as<int>(), U, SVt,
+                       TN_ORTHO_LEFT, 1.0, st);
+    TN_CUDA(cudaStreamSynchronize(st));
+    if (truncerr) *truncerr = D.truncerr;
+    return k;
+}
+
 // -------------------------------------------------------------------------------------
 // EventTimer
 // -------------------------------------------------------------------------------------

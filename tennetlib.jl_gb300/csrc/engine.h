@@ -41,6 +41,8 @@ std::unique_ptr<SplitPlan> make_split_plan(const GemmPlan& g, int slices, cudaSt
                                            bool own_packs);
 void run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs);
 void check_device_error_public(tn_ctx* ctx);
+int svd_truncate_dense(tn_ctx* ctx, const double* A, int m, int n, int maxdim, int mindim,
+                       double cutoff, double* U, double* SVt, double* truncerr);
 }  // namespace tn
 
 struct tn_ctx {

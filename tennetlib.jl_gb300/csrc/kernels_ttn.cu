@@ -471,17 +471,24 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
         const int nk = pe - j - 1;
         const int64_t i0 = r0 > j ? r0 : j;
         if (nk > 0) {
+            // panel products v^T A[:, k]; groups of 8 columns past nk are skipped whole
             double acc[HH_B];
 #pragma unroll
             for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
             for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
                 const double v = i == j ? 1.0 : col[i] * scale;
+                const double* arow = D.A + i + int64_t(j + 1) * m;
 #pragma unroll
-                for (int c = 0; c < HH_B; ++c)
-                    if (c < nk) acc[c] = fma(v, D.A[i + int64_t(j + 1 + c) * m], acc[c]);
+                for (int cg = 0; cg < HH_B; cg += 8) {
+                    if (cg >= nk) break;
+#pragma unroll
+                    for (int c = cg; c < cg + 8; ++c)
+                        if (c < nk) acc[c] = fma(v, arow[int64_t(c) * m], acc[c]);
+                }
             }
 #pragma unroll
             for (int c = 0; c < HH_B; ++c) {
+                if (c >= ((nk + 7) & ~7)) break;
                 const double v = warp_sum(acc[c]);
                 if (lane == 0) red[wid][c] = v;
             }

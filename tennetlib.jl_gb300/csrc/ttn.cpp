@@ -832,11 +832,9 @@ void run_link_move(TtnGroup& G, int v, int u) {
 }
 
 // ---- isometry move v -> u (QR; all members) ------------------------------------------------
-QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
-    check_cache(G);
-    auto& slot = G.qcache[{v, u}];
-    if (slot) return *slot;
-    slot = std::make_unique<QrPlan>();
+std::unique_ptr<QrPlan> build_qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked,
+                                      const std::vector<int>& kmins) {
+    auto slot = std::make_unique<QrPlan>();
     QrPlan& Q = *slot;
     auto E = members(G);
     const TtnTree& t = E[0]->tree;
@@ -861,7 +859,7 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
         const auto& dv = e->dims[v];
         const int n = dv[lu];
         const int64_t m = vol(dv) / n;
-        const int kmin = int(std::min<int64_t>(m, n));
+        const int kmin = kmins[i];
         // the factored matrix: the node tensor itself when the leg is last, else the copy
         const bool inplace = lu == int(dv.size()) - 1;
         const int abuf = inplace ? S_L : S_R;
@@ -945,10 +943,18 @@ QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked) {
         add_mode_tasks(Q.rmode.g, e->dims[u], lv, kmin, S_R, e->wbase + e->w_rt,
                        {ModeIn{S_L, e->node_off[u], S_R, e->wbase + e->w_r}}, 0);
     }
-    return Q;
+    return slot;
 }
 
-void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
+QrPlan& qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked,
+                const std::vector<int>& kmins) {
+    check_cache(G);
+    auto& slot = G.qcache[{v, u}];
+    if (!slot) slot = build_qr_plan(G, v, u, blocked, kmins);
+    return *slot;
+}
+
+void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double cutoff = -1.0) {
     auto E = members(G);
     const TtnTree& t = E[0]->tree;
     const int lu = t.leg_nbr(v, u), lv = t.leg_nbr(u, v);
@@ -962,13 +968,11 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
     std::vector<int> kmins(E.size());
     int64_t nmax = 1, mmax = 1, mnmax = 1;
     int kmax = 0;
+    std::vector<char> truncate(E.size(), 0);
     for (size_t i = 0; i < E.size(); ++i) {
         tn_ttn_env* e = E[i];
         const auto& dv = e->dims[v];
         const int n = dv[lu];
-        TN_REQUIRE(n <= maxdim,
-                   "TTN: moving through a link larger than maxdim needs the truncating SVD move "
-                   "(not built)");
         const int64_t m = vol(dv) / n;
         const int kmin = int(std::min<int64_t>(m, n));
         kmins[i] = kmin;
@@ -979,6 +983,9 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
             to.push_back(PermDesc{aptr(G, e->node_off[v]), A, P, n, Qd, 1, 0});
         }
         nmax = std::max(nmax, vol(dv));
+        // a link larger than maxdim: truncating SVD move (moveisometry_to_next!, ttn.jl:292-300)
+        truncate[i] = n > maxdim;
+        if (truncate[i]) continue;
         const bool blk = m * n > SMALL_QR && m >= n;
         blocked[i] = blk;
         if (!blk) {
@@ -1008,13 +1015,32 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim) {
         upload_descs(G, G.d_perm, to);
         launch_permute(G.d_perm.as<PermDesc>(), int(to.size()), nmax, st);
     }
+    for (size_t i = 0; i < E.size(); ++i) {
+        if (!truncate[i]) continue;
+        tn_ttn_env* e = E[i];
+        const auto& dv = e->dims[v];
+        const int n = dv[lu];
+        const int64_t m = vol(dv) / n;
+        const bool inplace = lu == int(dv.size()) - 1;
+        const double* A = inplace ? aptr(G, e->node_off[v]) : wptr(G, e, e->w_qa);
+        // U into the QR work (then like Q), S V^T into the R slot
+        kmins[i] = svd_truncate_dense(G.ctx, A, int(m), n, maxdim, mindim, cutoff,
+                                      wptr(G, e, e->w_qv), wptr(G, e, e->w_r), nullptr);
+        double* dst = inplace ? aptr(G, e->node_off[v]) : wptr(G, e, e->w_qa);
+        TN_CUDA(cudaMemcpyAsync(dst, wptr(G, e, e->w_qv), size_t(m) * kmins[i] * 8,
+                                cudaMemcpyDeviceToDevice, st));
+    }
     if (!small.empty()) {
         upload_descs(G, G.d_qr, small);
         const int q0 = G.ctx->timer.mark();
         launch_qr_small(G.d_qr.as<QrDesc>(), int(small.size()), st);
         G.ctx->timer.add(T_QRPANEL, q0, G.ctx->timer.mark());
     }
-    QrPlan& QP = qr_plan(G, v, u, blocked);
+    // a truncating move changes the dimensions: its plan is built for this move only
+    std::unique_ptr<QrPlan> once;
+    const bool any_trunc = std::find(truncate.begin(), truncate.end(), 1) != truncate.end();
+    if (any_trunc) once = build_qr_plan(G, v, u, blocked, kmins);
+    QrPlan& QP = any_trunc ? *once : qr_plan(G, v, u, blocked, kmins);
     if (!hh.empty()) {
         // CTAs of the cooperative panel kernel, in proportion to the rows of each matrix
         const int cap = hh_coop_capacity();

@@ -197,3 +197,39 @@ def test_batched_blocked_qr_matches_single(tn, ctx):
             tn.ttn.fullsweep_(se, path, tn.eig_solver, sw, maxdim=64, outputlevel=0)
         assert np.allclose(swb[i].energy, sw.energy, rtol=1e-10, atol=0), (i, swb[i].energy, sw.energy)
     assert _isometric(batch[0].getpsi(), batch[0].orthocenter)
+
+
+def test_sweeps_with_blocked_qr_match_oracle(tn, ctx):
+    """N = 32, chi = 64: the isometry moves through the (64, 64, 64) top nodes take the
+    blocked (cooperative, double-float panel) Householder path; per-sweep energies agree
+    with the oracle's host QR to 1e-10."""
+    N, chi = 32, 64
+    terms, _ = tfim(N, 8)
+    psi = T.random_ttn(N, chi, 12)
+    eo = T.StateEnvsTTN(psi, terms)
+    eg = tn.ttn.StateEnvsTTN(upload(tn, ctx, psi), model(tn, N, terms))
+    path = tn.ttn.default_sweeppath(N)
+    so, sg = T.SweepDataTTN(), tn.ttn.SweepDataTTN()
+    for _ in range(2):
+        T.fullsweep(eo, path, so, maxdim=chi)
+        tn.ttn.fullsweep_(eg, path, tn.eig_solver, sg, maxdim=chi, outputlevel=0)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
+    assert _isometric(eg.getpsi(), eg.orthocenter)
+
+
+def test_truncating_isometry_moves_match_oracle(tn, ctx):
+    """Sweeping a chi = 16 TTN with maxdim = 8: every move through a 16-dimensional link
+    takes the truncating SVD path of moveisometry_to_next! (src/ttn/ttn.jl:292-300)."""
+    N = 16
+    terms, _ = tfim(N, 21)
+    psi = T.random_ttn(N, 16, 22)
+    eo = T.StateEnvsTTN(psi, terms)
+    eg = tn.ttn.StateEnvsTTN(upload(tn, ctx, psi), model(tn, N, terms))
+    path = tn.ttn.default_sweeppath(N)
+    so, sg = T.SweepDataTTN(), tn.ttn.SweepDataTTN()
+    for _ in range(2):
+        T.fullsweep(eo, path, so, maxdim=8)
+        tn.ttn.fullsweep_(eg, path, tn.eig_solver, sg, maxdim=8, outputlevel=0)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
+        assert sg.maxchi[-1] == so.maxchi[-1] == 8
+    assert _isometric(eg.getpsi(), eg.orthocenter)
