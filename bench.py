@@ -277,6 +277,8 @@ def run_ttn(tn, device, args, world):
                        for k in ("heff_ms", "env_ms", "svd_ms", "lanczos_ms", "pack_ms")},
         "time_share_note": "svd_ms = QR isometry moves; env_ms = link-tensor moves",
         "matvecs": st["matvecs"], "gpu_launches": st["kernel_launches"],
+        "krylov_hbm_gbs": st["krylov_bytes"] / max(st["lanczos_ms"], 1e-9) / 1e6,
+        "qr_panel_s": st["qr_panel_ms"] / 1e3, "qr_gemm_s": st["qr_gemm_ms"] / 1e3,
         "max_rel_energy_error_vs_free_fermion_after_2_sweeps": max(rel),
         "median_rel_energy_error_after_2_sweeps": statistics.median(rel),
     }
@@ -410,6 +412,10 @@ def run_ours(args, world, rank, local, pg):
         "heff_ms_per_sweep": heff_ms / args.steps,
         "time_share": share,
         "matvecs_per_sweep": sum(s["matvecs"] for s in st) / args.steps,
+        "krylov_hbm_gbs": sum(s["krylov_bytes"] for s in st)
+                          / max(sum(s["lanczos_ms"] for s in st), 1e-9) / 1e6,
+        "krylov_hbm_note": "algorithmic bytes of the Lanczos vector kernels (each element read "
+                           "or written once per launch) over their CUDA-event time",
         "energy": energy, "maxlinkdim": chi, "wall_s_per_sweep": wall / args.steps,
         "gpu_launches": launches,
         "roofline": roof,

@@ -91,6 +91,7 @@ typedef struct tn_sweep_result {
     int64_t kernel_launches;   /* all kernels this library launched during the sweep */
     double qr_panel_ms;        /* TTN: device time of the Householder column/panel kernels */
     double qr_gemm_ms;         /* TTN: device time of the QR's grouped GEMMs (with packing) */
+    double krylov_bytes;       /* algorithmic HBM bytes of the Krylov vector kernels */
 } tn_sweep_result;
 
 /* ---- context ------------------------------------------------------------------- */

@@ -73,6 +73,7 @@ class SweepResult(C.Structure):
         ("kernel_launches", C.c_int64),
         ("qr_panel_ms", C.c_double),
         ("qr_gemm_ms", C.c_double),
+        ("krylov_bytes", C.c_double),
     ]
 
 

@@ -2010,6 +2010,7 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     const double gf0 = env->gemm_flops;
     const int64_t gl0 = env->gemm_launches;
     const int64_t kl0 = launch_count();
+    const int64_t kb0 = krylov_bytes();
     *res = tn_sweep_result{};
     const int es = ctx->timer.mark();
     double maxerr = 0.0, energy = NAN;
@@ -2047,6 +2048,7 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     res->gemm_flops = env->gemm_flops - gf0;
     res->gemm_launches = env->gemm_launches - gl0;
     res->kernel_launches = launch_count() - kl0;
+    res->krylov_bytes = double(krylov_bytes() - kb0);
     if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
     if (mid_eigs) {
         const int k = std::min<int>(mid_cap, (int)mid.size());

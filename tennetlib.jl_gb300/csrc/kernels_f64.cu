@@ -349,6 +349,7 @@ void launch_multi_dot(const double* const* V, int K, const double* w, int64_t n,
     finalize_dot_kernel<<<K, 32, 0, s>>>(part, g, K, out);
     TN_CUDA(cudaGetLastError());
     count_launch();
+    count_krylov_bytes(int64_t(K + 1) * n * 8);
 }
 
 void launch_multi_axpy(double* w, const double* const* V, int K, const double* h, double sign,
@@ -357,6 +358,7 @@ void launch_multi_axpy(double* w, const double* const* V, int K, const double* h
     multi_axpy_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(w, make_ptrs(V, K), K, h, sign, n);
     TN_CUDA(cudaGetLastError());
     count_launch();
+    count_krylov_bytes(int64_t(K + 2) * n * 8);
 }
 
 void launch_gs_pass(const double* const* V, int K, double* w, const double* hin, double sign,
@@ -375,6 +377,7 @@ void launch_gs_pass(const double* const* V, int K, double* w, const double* hin,
         gs_pass_kernel<32><<<g, BLAS_THREADS, 0, s>>>(P, K, w, hin, sign, n, d, nm, part, out, ticket);
     TN_CUDA(cudaGetLastError());
     count_launch();
+    count_krylov_bytes(int64_t(1 + ((hin || dots) ? K : 0) + (hin ? 1 : 0)) * n * 8);
 }
 
 void launch_scale_into(double* dst, const double* src, const double* denom_sq,
@@ -383,6 +386,7 @@ void launch_scale_into(double* dst, const double* src, const double* denom_sq,
     scale_into_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(dst, src, denom_sq, host_scale, n);
     TN_CUDA(cudaGetLastError());
     count_launch();
+    count_krylov_bytes(2 * n * 8);
 }
 
 void launch_lincomb(double* dst, const double* const* V, int K, const double* coef, int64_t n,
@@ -391,6 +395,7 @@ void launch_lincomb(double* dst, const double* const* V, int K, const double* co
     lincomb_kernel<<<grid_for(n), BLAS_THREADS, 0, s>>>(dst, make_ptrs(V, K), K, coef, n);
     TN_CUDA(cudaGetLastError());
     count_launch();
+    count_krylov_bytes(int64_t(K + 1) * n * 8);
 }
 
 }  // namespace tn

@@ -17,6 +17,9 @@ void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 static std::atomic<int64_t> g_launches{0};
 int64_t launch_count() { return g_launches.load(); }
 void count_launch(int n) { g_launches += n; }
+static std::atomic<int64_t> g_krylov_bytes{0};
+int64_t krylov_bytes() { return g_krylov_bytes.load(); }
+void count_krylov_bytes(int64_t b) { g_krylov_bytes += b; }
 
 void DevBuf::alloc(size_t nbytes, cudaStream_t s) {
     if (nbytes <= bytes && p) return;

@@ -235,6 +235,10 @@ void launch_gemm_f64(const GemmPlan& p, const Bases& b, cudaStream_t s);
 // number of kernel launches issued by this library since load (all kernels)
 int64_t launch_count();
 void count_launch(int n = 1);
+// algorithmic HBM bytes moved by the Krylov vector kernels since load (each vector element
+// read or written once per launch)
+int64_t krylov_bytes();
+void count_krylov_bytes(int64_t b);
 void launch_combine(const CombPlan& p, const Bases& b, cudaStream_t s);
 
 // Krylov vector kernels.  Partial sums go to `part` (>= K * nparts doubles) and the

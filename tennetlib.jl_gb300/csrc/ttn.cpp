@@ -296,7 +296,7 @@ struct TtnGroup {
     std::map<std::pair<int, int>, std::unique_ptr<QrPlan>> qcache;
     int dims_version = 0, cache_version = -1;
     double acc_ms[T_NCAT] = {};
-    double heff_flops = 0, gemm_flops = 0;
+    double heff_flops = 0, gemm_flops = 0, krylov_bytes = 0;
     int64_t gemm_launches = 0, matvecs = 0;
 };
 
@@ -772,6 +772,8 @@ void gs_launch(TtnGroup& G, const std::vector<BGsDesc>& d, int kmax, double sign
     upload_descs(G, G.d_gs, d);
     launch_bgs_pass(G.d_gs.as<BGsDesc>(), int(d.size()), std::max(kmax, 1), nmax, sign, dots, norm,
                     G.bpart.d(), G.tickets.as<unsigned>(), G.ctx->stream);
+    for (const auto& x : d)
+        count_krylov_bytes(int64_t(1 + ((x.hin || dots) ? x.kk : 0) + (x.hin ? 1 : 0)) * x.n * 8);
 }
 void scale_launch(TtnGroup& G, const std::vector<BScaleDesc>& d) {
     if (d.empty()) return;
@@ -779,6 +781,7 @@ void scale_launch(TtnGroup& G, const std::vector<BScaleDesc>& d) {
     for (const auto& x : d) nmax = std::max(nmax, x.n);
     upload_descs(G, G.d_sc, d);
     launch_bscale(G.d_sc.as<BScaleDesc>(), int(d.size()), nmax, G.ctx->stream);
+    for (const auto& x : d) count_krylov_bytes(int64_t(x.dst2 ? 3 : 2) * x.n * 8);
 }
 void lin_launch(TtnGroup& G, const std::vector<BLinDesc>& d) {
     if (d.empty()) return;
@@ -786,6 +789,7 @@ void lin_launch(TtnGroup& G, const std::vector<BLinDesc>& d) {
     for (const auto& x : d) nmax = std::max(nmax, x.n);
     upload_descs(G, G.d_lin, d);
     launch_blincomb(G.d_lin.as<BLinDesc>(), int(d.size()), nmax, G.ctx->stream);
+    for (const auto& x : d) count_krylov_bytes(int64_t(x.kk + 1) * x.n * 8);
 }
 
 // x_i /= |x_i| in place for every listed instance (norm into scal[64])
@@ -1419,7 +1423,7 @@ void collect_stats(TtnGroup& G) {
 void reset_stats(TtnGroup& G) {
     collect_stats(G);
     std::fill(G.acc_ms, G.acc_ms + T_NCAT, 0.0);
-    G.heff_flops = G.gemm_flops = 0;
+    G.heff_flops = G.gemm_flops = G.krylov_bytes = 0;
     G.gemm_launches = G.matvecs = 0;
 }
 
@@ -1557,6 +1561,7 @@ void fill_sweep_result(TtnGroup& G, tn_ttn_env* e, tn_sweep_result* r, int64_t l
     r->kernel_launches = launches;
     r->qr_panel_ms = G.acc_ms[T_QRPANEL];
     r->qr_gemm_ms = G.acc_ms[T_QRGEMM];
+    r->krylov_bytes = G.krylov_bytes;
 }
 
 }  // namespace
@@ -1840,6 +1845,7 @@ int tn_ttn_envs_fullsweep(int count, tn_ttn_env* const* envs, int npath, const i
         check_ttn_params(p);
         reset_stats(G);
         const int64_t l0 = launch_count();
+        const int64_t kb0 = krylov_bytes();
         const int s0 = G.ctx->timer.mark();
         for (int k = 0; k < npath; ++k) update_group(G, path[k], p);
         for (int k = npath - 1; k >= 0; --k) update_group(G, path[k], p);
@@ -1847,6 +1853,7 @@ int tn_ttn_envs_fullsweep(int count, tn_ttn_env* const* envs, int npath, const i
         collect_stats(G);
         check_device_error_public(G.ctx);
         const int64_t launches = launch_count() - l0;
+        G.krylov_bytes = double(krylov_bytes() - kb0);
         for (int i = 0; i < count; ++i) fill_sweep_result(G, envs[i], &res[i], launches);
     });
 }
