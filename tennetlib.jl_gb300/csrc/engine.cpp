@@ -262,6 +262,10 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
     sp->bbytes = boff;
     sp->ea_n = eao;
     sp->eb_n = ebo;
+    for (const auto& j : sp->ajobs) sp->a_maxnkt = std::max(sp->a_maxnkt, j.nkt);
+    for (const auto& j : sp->bjobs) sp->b_maxnkt = std::max(sp->b_maxnkt, j.nkt);
+    sp->amax.alloc(size_t(std::max<int64_t>(eao, 1)) * 8, st);
+    sp->bmax.alloc(size_t(std::max<int64_t>(ebo, 1)) * 8, st);
     upload_vec(sp->dtasks, sp->tasks, st);
     upload_vec(sp->ditems, sp->items, st);
     upload_vec(sp->dajobs, sp->ajobs, st);
@@ -287,12 +291,14 @@ void run_split(tn_ctx* ctx, SplitPlan& sp, const Bases& bs, int* mma_ev0, int* m
     const int p0 = ctx->timer.mark();
     if (!sp.a_static || !sp.a_packed) {
         launch_split_pack(sp.dajobs.as<PackJob>(), (int)sp.ajobs.size(), sp.daks.as<KTileSrc>(), bs,
-                          sp.ap, sp.eap, sp.slices, split_tile_rows_a(), st);
+                          sp.ap, sp.eap, sp.slices, split_tile_rows_a(), st, sp.a_maxnkt,
+                          sp.amax.as<unsigned long long>(), sp.ea_n);
         sp.a_packed = true;
     }
     if (!sp.b_static || !sp.b_packed) {
         launch_split_pack(sp.dbjobs.as<PackJob>(), (int)sp.bjobs.size(), sp.dbks.as<KTileSrc>(), bs,
-                          sp.bp, sp.ebp, sp.slices, split_tile_rows_b(), st);
+                          sp.bp, sp.ebp, sp.slices, split_tile_rows_b(), st, sp.b_maxnkt,
+                          sp.bmax.as<unsigned long long>(), sp.eb_n);
         sp.b_packed = true;
     }
     const int p1 = ctx->timer.mark();

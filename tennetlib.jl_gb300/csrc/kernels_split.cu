@@ -254,6 +254,109 @@ split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__
     }
 }
 
+// k-split pack for operands with long k: the k tiles of every job are divided among
+// gridDim.y CTAs (kper tiles each).  Pass 1 (split_rowmax_kernel) folds each row's max |x|
+// (IEEE bit pattern, an exact and order-independent maximum) into gmax with atomicMax;
+// pass 2 (split_pack_part_kernel) writes the digits of its k tiles with the exponents taken
+// from gmax.  Same digits as split_pack_kernel, many more CTAs.
+__global__ void __launch_bounds__(PACK_THREADS)
+split_rowmax_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__ ksrc, Bases b,
+                    unsigned long long* __restrict__ gmax, int tile_rows, int kper) {
+    __shared__ unsigned long long rowmax[BM];
+    const PackJob jb = jobs[blockIdx.x];
+    const int t0 = blockIdx.y * kper;
+    if (t0 >= jb.nkt) return;
+    const int t1 = (t0 + kper) < jb.nkt ? (t0 + kper) : jb.nkt;
+    const int per_tile = tile_rows * 8;
+    const int nitems = per_tile * (t1 - t0);
+    for (int r = threadIdx.x; r < tile_rows; r += blockDim.x) rowmax[r] = 0ull;
+    __syncthreads();
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+        const int t = t0 + it / per_tile, rem = it % per_tile;
+        const int r = rem % tile_rows, ch = rem / tile_rows;
+        if (r >= jb.rows) continue;
+        const KTileSrc ks = ksrc[jb.kt0 + t];
+        const long long* x = reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
+                             int64_t(jb.row0 + r) * ks.sr;
+        unsigned long long mx = 0ull;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = ch * 8 + q;
+            if (k < ks.kvalid) {
+                const unsigned long long v = (unsigned long long)(x[int64_t(k) * ks.sk]) & 0x7fffffffffffffffull;
+                mx = v > mx ? v : mx;
+            }
+        }
+        if (mx) atomicMax(&rowmax[r], mx);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < jb.rows; r += blockDim.x)
+        if (rowmax[r]) atomicMax(&gmax[jb.eoff + r], rowmax[r]);
+}
+
+__global__ void __launch_bounds__(PACK_THREADS)
+split_pack_part_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__ ksrc, Bases b,
+                       uint8_t* __restrict__ out, int* __restrict__ expo,
+                       const unsigned long long* __restrict__ gmax, int slices, int tile_rows,
+                       int kper) {
+    const PackJob jb = jobs[blockIdx.x];
+    const int t0 = blockIdx.y * kper;
+    if (t0 >= jb.nkt) return;
+    const int t1 = (t0 + kper) < jb.nkt ? (t0 + kper) : jb.nkt;
+    const int tile_bytes = tile_rows * BKT * 2;
+    const int per_tile = tile_rows * 8;
+    const int nitems = per_tile * (t1 - t0);
+    if (blockIdx.y == 0)
+        for (int r = threadIdx.x; r < jb.rows; r += blockDim.x) {
+            const unsigned long long m = gmax[jb.eoff + r];
+            expo[jb.eoff + r] = m ? int((m >> 52) & 0x7ff) - 1022 : 0;
+        }
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+        const int t = t0 + it / per_tile, rem = it % per_tile;
+        const int r = rem % tile_rows, ch = rem / tile_rows;
+        const KTileSrc ks = ksrc[jb.kt0 + t];
+        const bool live = r < jb.rows && ks.kvalid > 0;
+        const unsigned long long mxb = live ? gmax[jb.eoff + r] : 0ull;
+        const int E = mxb ? int((mxb >> 52) & 0x7ff) - 1022 : 0;
+        const int base_sh = 1075 + E - 8 * slices;
+        const long long* x = live ? reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
+                                        int64_t(jb.row0 + r) * ks.sr
+                                  : nullptr;
+        __nv_bfloat16 dig[7][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = ch * 8 + q;
+            long long X = 0;
+            if (mxb && k < ks.kvalid) {
+                const long long v = x[int64_t(k) * ks.sk];
+                const int ex = int((v >> 52) & 0x7ff);
+                if (ex) {
+                    const long long m = (v & 0xfffffffffffffLL) | (1LL << 52);
+                    const int sh = base_sh - ex;
+                    long long a = 0;
+                    if (sh <= 0) a = m << (-sh);
+                    else if (sh < 63) a = (m + (1LL << (sh - 1))) >> sh;
+                    X = v < 0 ? -a : a;
+                }
+            }
+            for (int i = slices - 1; i >= 1; --i) {
+                int d = int(X & 255);
+                if (d > 128) d -= 256;
+                X = (X - d) >> 8;
+                dig[i][q] = __float2bfloat16_rn(ldexpf(float(d), -8 * i));
+            }
+            dig[0][q] = __float2bfloat16_rn(float(X));
+        }
+        uint8_t* tile0 = out + jb.out_off + int64_t(t) * slices * tile_bytes;
+        const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((ch ^ (r & 7)) << 4);
+        for (int i = 0; i < slices; ++i) {
+            uint4 v;
+            __builtin_memcpy(&v, dig[i], 16);
+            *reinterpret_cast<uint4*>(tile0 + int64_t(i) * tile_bytes + off) = v;
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // MMA kernel
 // ------------------------------------------------------------------------------------
@@ -460,13 +563,26 @@ int split_tile_rows_b() { return BN; }
 int split_ktile() { return BKT; }
 
 void launch_split_pack(const PackJob* jobs, int njobs, const KTileSrc* ksrc, const Bases& b,
-                       uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s) {
+                       uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s,
+                       int max_nkt, unsigned long long* gmax, int64_t nrows) {
     if (njobs <= 0) return;
     TN_REQUIRE(slices >= 4 && slices <= 7, "split precision needs 4..7 slices");
     TN_REQUIRE(tile_rows <= BM, "pack tile taller than the A tile");
-    split_pack_kernel<<<njobs, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
+    constexpr int KPER = 2;  // k tiles per CTA of the k-split pack
+    if (max_nkt <= 2 * KPER || !gmax) {
+        split_pack_kernel<<<njobs, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
+        TN_CUDA(cudaGetLastError());
+        count_launch();
+        return;
+    }
+    const dim3 g(njobs, (max_nkt + KPER - 1) / KPER);
+    TN_CUDA(cudaMemsetAsync(gmax, 0, size_t(nrows) * sizeof(unsigned long long), s));
+    split_rowmax_kernel<<<g, PACK_THREADS, 0, s>>>(jobs, ksrc, b, gmax, tile_rows, KPER);
     TN_CUDA(cudaGetLastError());
-    count_launch();
+    split_pack_part_kernel<<<g, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, gmax, slices,
+                                                      tile_rows, KPER);
+    TN_CUDA(cudaGetLastError());
+    count_launch(2);
 }
 
 void launch_split_gemm(const SplitItem* items, int nitems, const SplitTask* tasks,

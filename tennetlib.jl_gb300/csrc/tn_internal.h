@@ -213,14 +213,19 @@ struct SplitPlan {
     // scratch (make_split with own_packs = false) of abytes / bbytes / 4 ea_n / 4 eb_n bytes
     uint8_t *ap = nullptr, *bp = nullptr;
     int *eap = nullptr, *ebp = nullptr;
+    int a_maxnkt = 0, b_maxnkt = 0;   // longest k (in tiles) of a pack job
+    DevBuf amax, bmax;                // row maxima scratch of the k-split pack
 };
 int split_tile_bytes_a();
 int split_tile_bytes_b();
 int split_tile_rows_a();
 int split_tile_rows_b();
 int split_ktile();
+// max_nkt: the largest k-tile count of a job; operands with long k are packed by the k-split
+// kernels, which need gmax (nrows 64-bit words of scratch, the exponent count of the operand)
 void launch_split_pack(const PackJob* jobs, int njobs, const KTileSrc* ksrc, const Bases& b,
-                       uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s);
+                       uint8_t* out, int* expo, int slices, int tile_rows, cudaStream_t s,
+                       int max_nkt = 0, unsigned long long* gmax = nullptr, int64_t nrows = 0);
 void launch_split_gemm(const SplitItem* items, int nitems, const SplitTask* tasks,
                        const uint8_t* apack, const uint8_t* bpack, const int* ea, const int* eb,
                        const Bases& b, int slices, int* err, int nsm, cudaStream_t s);
