@@ -447,7 +447,7 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
         "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops, "pack_ms": res.pack_ms,
         "gemm_launches": res.gemm_launches, "kernel_launches": res.kernel_launches,
-        "wall_s": wall})
+        "krylov_bytes": res.krylov_bytes, "wall_s": wall})
     if swdata.sweepcount > 1:
         enerr = swdata.energy[-1] - swdata.energy[-2]
         enterr = swdata.entropy[-1] - swdata.entropy[-2]
@@ -476,7 +476,8 @@ def _record_sweep(swdata, res, mid, wall, noise=0.0, outputlevel=0):
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
         "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops,
         "pack_ms": res.pack_ms, "gemm_launches": res.gemm_launches,
-        "kernel_launches": res.kernel_launches, "wall_s": wall})
+        "kernel_launches": res.kernel_launches, "krylov_bytes": res.krylov_bytes,
+        "wall_s": wall})
 
 
 class TDVPEngine:

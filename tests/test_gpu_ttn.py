@@ -233,3 +233,20 @@ def test_truncating_isometry_moves_match_oracle(tn, ctx):
         assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
         assert sg.maxchi[-1] == so.maxchi[-1] == 8
     assert _isometric(eg.getpsi(), eg.orthocenter)
+
+
+@pytest.mark.parametrize("N", [6, 12])
+def test_ragged_trees_match_oracle(tn, ctx, N):
+    """Site counts that are not powers of two: sites attach to layer-2 nodes
+    (default_graph_sitenodes, src/ttn/ttn_generators.jl:69-96)."""
+    terms, exact = tfim(N, 2)
+    psi = T.random_ttn(N, 8, 3)
+    eo = T.StateEnvsTTN(psi, terms)
+    eg = tn.ttn.StateEnvsTTN(upload(tn, ctx, psi), model(tn, N, terms))
+    path = tn.ttn.default_sweeppath(N)
+    so, sg = T.SweepDataTTN(), tn.ttn.SweepDataTTN()
+    for _ in range(3):
+        T.fullsweep(eo, path, so, maxdim=8)
+        tn.ttn.fullsweep_(eg, path, tn.eig_solver, sg, maxdim=8, outputlevel=0)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
+    assert abs(sg.energy[-1] - exact) < 1e-7 * abs(exact)
