@@ -247,7 +247,7 @@ def run_ttn(tn, device, args, world):
     T = tn.ttn
     chis, psis, models, exact = [], [], [], []
     t0 = time.perf_counter()
-    for i in range(TTN_INSTANCES):
+    for i in range(args.ttn_instances):
         chi = TTN_CHIS[i % len(TTN_CHIS)]
         J, h = T.tfim_instance(TTN_SITES, 1000 + i)
         chis.append(chi)
@@ -267,8 +267,8 @@ def run_ttn(tn, device, args, world):
     dev_s = st["sweep_ms"] / 1e3
     rel = [abs(sw.energy[-1] - e) / abs(e) for sw, e in zip(sws, exact)]
     out = {
-        "workload": "tfim_binary_tree_64_sites_32_instances_maxdim_64_128_256",
-        "instances": TTN_INSTANCES, "maxdim_cycle": TTN_CHIS, "sweeps_before_timed": 1,
+        "workload": f"tfim_binary_tree_64_sites_{args.ttn_instances}_instances_maxdim_64_128_256",
+        "instances": args.ttn_instances, "maxdim_cycle": TTN_CHIS, "sweeps_before_timed": 1,
         "value": dev_s, "unit": "s/sweep (all instances, lockstep)",
         "wall_s": wall, "prepare_s": prep,
         "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
@@ -317,21 +317,57 @@ def config(args):
 # our arm
 # ------------------------------------------------------------------------------------
 
+def save_state(path, psi):
+    import numpy as np
+    t, lk = download_state(psi)
+    np.savez(path, *(t + lk))
+
+
+def load_state(tn, ctx, path, pq):
+    import numpy as np
+    z = np.load(path)
+    arrs = [z[f"arr_{i}"] for i in range(2 * N_SITES + 1)]
+    return tn.MPS(arrs[:N_SITES], arrs[N_SITES:], pq, 0, ctx)
+
+
+def run_partial(tn, ctx, env, args):
+    """Profiling aid: the first K left-to-right bond updates of the timed sweep."""
+    for p in range(args.partial_updates):
+        tn.update_position_(env, tn.eig_solver, p, 2, "left", maxdim=MAXDIM, cutoff=CUTOFF,
+                            solver_krylovdim=KRYLOVDIM, solver_maxiter=MAXITER)
+    print(json.dumps({"partial_updates": args.partial_updates,
+                      "launches": ctx.lib.tn_kernel_launches()}), flush=True)
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__ as g
     g.build()
     tn = g.load_package()
+    if args.ttn_only:
+        if rank == 0:
+            print(json.dumps({"ttn": run_ttn(tn, local, args, world)}), flush=True)
+        return
     ctx = tn.Context(local)
     if args.precision == "split":
         ctx.set_precision("split", args.slices)
     H, pq = heisenberg(tn, ctx)
-    psi0 = tn.MPS.product(tn.models.neel_states(N_SITES), pq, ctx)
-    env = tn.StateEnvs(psi0, H)
     sw = tn.SweepData()
-    for md in RAMP:  # prepare the converged state (not timed)
-        tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(md))
+    if args.load_state:
+        env = tn.StateEnvs(load_state(tn, ctx, args.load_state, pq), H)
+        if args.partial_updates:
+            run_partial(tn, ctx, env, args)
+            return
+    else:
+        psi0 = tn.MPS.product(tn.models.neel_states(N_SITES), pq, ctx)
+        env = tn.StateEnvs(psi0, H)
+        for md in RAMP:  # prepare the converged state (not timed)
+            tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(md))
     for _ in range(args.warmup):
         tn.fullsweep_(env, tn.eig_solver, 2, sw, **sweep_kwargs(MAXDIM))
+    if args.save_state:
+        save_state(args.save_state, env.getpsi())
+        print(json.dumps({"saved": args.save_state, "maxlinkdim": sw.maxchi[-1]}), flush=True)
+        return
     n0 = len(sw.stats)
     # kernels launched before the timed region (lets a profiler skip the preparation)
     print(f"launches_before_timed={ctx.lib.tn_kernel_launches()}", file=sys.stderr, flush=True)
@@ -389,7 +425,11 @@ def run_ours(args, world, rank, local, pg):
                       "FP64 grouped block-sparse GEMM of H_eff (two launches per matvec)")
     roof["flops_per_launch"] = gemm_fl / max(gemm_n, 1)
     roof["ms_per_launch"] = gemm_ms / max(gemm_n, 1)
-    roof["traffic"] = None
+    # DRAM bytes (read + write) of one captured launch of this kernel at this workload
+    # (ncu, dram__bytes_read.sum + dram__bytes_write.sum: split_gemm_kernel 3.99 MB, one
+    # H_eff stage at chi ~ 182); per launch like `achieved`
+    roof["traffic"] = 3.991808e6 if args.precision == "split" else None
+    roof["traffic_unit"] = "bytes per launch (one ncu capture)"
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
              for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
     dominant = max(("svd_ms", "heff_ms", "lanczos_ms", "env_ms"), key=lambda k: share[k])
@@ -465,6 +505,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-ttn", action="store_true", help="skip the TTN (32-instance) leg")
+    ap.add_argument("--ttn-only", action="store_true", help="run only the TTN leg")
+    ap.add_argument("--ttn-instances", type=int, default=TTN_INSTANCES)
+    ap.add_argument("--save-state", default="", help="save the prepared MPS (npz) and exit")
+    ap.add_argument("--load-state", default="", help="start from a saved MPS (no ramp)")
+    ap.add_argument("--partial-updates", type=int, default=0,
+                    help="with --load-state: only the first K bond updates (profiling)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":

@@ -158,8 +158,11 @@ __device__ __forceinline__ df2 df_sqrt(df2 x) {
 // angle comes from FP32 (it only has to zero the pair to ~1e-7 of itself, which a sweep
 // squares), while c and s are formed in double-float from that angle so that every
 // rotation is orthogonal to double-float precision.  No FP64 instruction is executed.
+// A sweep whose largest rotated |cos| (g / sqrt(a b)) stays below 1e-7 leaves, by the
+// quadratic convergence of one-sided Jacobi, nothing above tol for the next sweep: the
+// loop then stops without the confirming sweep.
 __device__ int jacobi_sweeps_df(df2* x, df2* v, int m, int n, float tol, int max_sweeps,
-                                int* rotated) {
+                                int* rotated, unsigned* maxcos_bits) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int grp = lane >> 3, sub = lane & 7;
     const int nn = n + (n & 1);
@@ -168,7 +171,10 @@ __device__ int jacobi_sweeps_df(df2* x, df2* v, int m, int n, float tol, int max
     int sweep = 0;
     if (n < 2) return 0;
     for (sweep = 0; sweep < max_sweeps; ++sweep) {
-        if (threadIdx.x == 0) *rotated = 0;
+        if (threadIdx.x == 0) {
+            *rotated = 0;
+            *maxcos_bits = 0u;
+        }
         __syncthreads();
         for (int r = 0; r < nn - 1; ++r) {
             for (int base = 0; base < npairs; base += slots) {
@@ -221,14 +227,23 @@ __device__ int jacobi_sweeps_df(df2* x, df2* v, int m, int n, float tol, int max
                         vi[t] = df_add(df_mul(c, p), df_neg(df_mul(sn, q)));
                         vj[t] = df_add(df_mul(sn, p), df_mul(c, q));
                     }
-                    if (sub == 0) *rotated = 1;
+                    if (sub == 0) {
+                        *rotated = 1;
+                        const float cosr = fabsf(g.hi) / (sqrtf(a.hi) * sqrtf(bb.hi));
+                        atomicMax(maxcos_bits, __float_as_uint(cosr));  // positive floats order as ints
+                    }
                 }
             }
             __syncthreads();
         }
         const int done = !*rotated;
+        const bool converged = *rotated && __uint_as_float(*maxcos_bits) < 1.0e-7f;
         __syncthreads();
         if (done) break;
+        if (converged) {
+            ++sweep;
+            break;
+        }
     }
     return sweep;
 }
@@ -269,6 +284,7 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
                int* __restrict__ sweeps_out, int smem_region) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int rotated;
+    __shared__ unsigned maxcos;
     __shared__ int piv;
     __shared__ double red[SVD_THREADS / 32];
     const SvdBlockDesc d = desc[blockIdx.x];
@@ -451,7 +467,7 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     stamp(4);
     // rotation threshold above the rounding noise of a double-float dot product
     const float tol = 3.55e-15f * sqrtf(float(n > 1 ? n : 1)) * 32.f;
-    const int sw64 = jacobi_sweeps_df(y, v, n, n, tol, 30, &rotated);
+    const int sw64 = jacobi_sweeps_df(y, v, n, n, tol, 30, &rotated, &maxcos);
     stamp(5);
     __syncthreads();
     // singular values and sorting permutation
