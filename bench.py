@@ -426,9 +426,9 @@ def run_ours(args, world, rank, local, pg):
     roof["flops_per_launch"] = gemm_fl / max(gemm_n, 1)
     roof["ms_per_launch"] = gemm_ms / max(gemm_n, 1)
     # DRAM bytes (read + write) of one captured launch of this kernel at this workload
-    # (ncu, dram__bytes_read.sum + dram__bytes_write.sum: split_gemm_kernel 3.99 MB, one
+    # (ncu, dram__bytes_read.sum + dram__bytes_write.sum: split_gemm_kernel 4.57 MB, one
     # H_eff stage at chi ~ 182); per launch like `achieved`
-    roof["traffic"] = 3.991808e6 if args.precision == "split" else None
+    roof["traffic"] = 4.574208e6 if args.precision == "split" else None
     roof["traffic_unit"] = "bytes per launch (one ncu capture)"
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
              for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
