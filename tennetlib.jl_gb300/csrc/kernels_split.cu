@@ -235,7 +235,10 @@ split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__
                     X = v < 0 ? -a : a;
                 }
             }
-            for (int i = slices - 1; i >= 1; --i) {
+            // compile-time slice indices keep dig[][] in registers
+#pragma unroll
+            for (int i = 6; i >= 1; --i) {
+                if (i >= slices) continue;
                 int d = int(X & 255);
                 if (d > 128) d -= 256;
                 X = (X - d) >> 8;
@@ -246,7 +249,9 @@ split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__
         // swizzled position of (row r, chunk ch): 8-row atoms of 1024 bytes
         uint8_t* tile0 = out + jb.out_off + int64_t(t) * slices * tile_bytes;
         const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((ch ^ (r & 7)) << 4);
-        for (int i = 0; i < slices; ++i) {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            if (i >= slices) continue;
             uint4 v;
             __builtin_memcpy(&v, dig[i], 16);
             *reinterpret_cast<uint4*>(tile0 + int64_t(i) * tile_bytes + off) = v;
@@ -339,7 +344,10 @@ split_pack_part_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restr
                     X = v < 0 ? -a : a;
                 }
             }
-            for (int i = slices - 1; i >= 1; --i) {
+            // compile-time slice indices keep dig[][] in registers
+#pragma unroll
+            for (int i = 6; i >= 1; --i) {
+                if (i >= slices) continue;
                 int d = int(X & 255);
                 if (d > 128) d -= 256;
                 X = (X - d) >> 8;
@@ -349,7 +357,9 @@ split_pack_part_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restr
         }
         uint8_t* tile0 = out + jb.out_off + int64_t(t) * slices * tile_bytes;
         const int off = (r >> 3) * 1024 + (r & 7) * 128 + ((ch ^ (r & 7)) << 4);
-        for (int i = 0; i < slices; ++i) {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            if (i >= slices) continue;
             uint4 v;
             __builtin_memcpy(&v, dig[i], 16);
             *reinterpret_cast<uint4*>(tile0 + int64_t(i) * tile_bytes + off) = v;
