@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -260,6 +261,8 @@ def run_ttn(tn, device, args, world):
     sws = [T.SweepDataTTN() for _ in envs]
     kw = dict(maxdim=max(TTN_CHIS), outputlevel=0)
     T.fullsweep_batch_(envs, path, tn.eig_solver, sws, **kw)      # warm-up
+    print(f"ttn_launches_before_timed={ctx.lib.tn_kernel_launches()}", file=sys.stderr,
+          flush=True)
     t1 = time.perf_counter()
     T.fullsweep_batch_(envs, path, tn.eig_solver, sws, **kw)      # timed
     wall = time.perf_counter() - t1
@@ -479,14 +482,22 @@ def fp64_compare(tn, ctx, H, pq, tensors, links, local):
     out = {}
     ctx64 = tn.Context(local, precision="fp64")
     H64, _ = heisenberg(tn, ctx64)
+    final = {}
     for name, c, h in (("split", ctx, H), ("fp64", ctx64, H64)):
         e = tn.StateEnvs(tn.MPS(tensors, links, pq, 0, c), h)
         sw = tn.SweepData()
         tn.fullsweep_(e, tn.eig_solver, 2, sw, **sweep_kwargs(MAXDIM))
         st = sw.stats[-1]
         out[name] = {"sweep_s": st["sweep_ms"] / 1e3, "energy": sw.energy[-1],
-                     "heff_ms": st["heff_ms"], "svd_ms": st["svd_ms"], "maxlinkdim": sw.maxchi[-1]}
+                     "heff_ms": st["heff_ms"], "svd_ms": st["svd_ms"], "maxlinkdim": sw.maxchi[-1],
+                     "maxtruncerr": sw.maxtruncerr[-1]}
+        final[name] = download_state(e.getpsi())
         del e
+    # state overlap |<psi_split|psi_fp64>| of the two (normalised) results, on the GPU
+    ps = tn.MPS(final["split"][0], final["split"][1], pq, 0, ctx)
+    pd = tn.MPS(final["fp64"][0], final["fp64"][1], pq, 0, ctx)
+    out["overlap_split_fp64"] = abs(ps.inner(pd)) / math.sqrt(ps.inner(ps) * pd.inner(pd))
+    del ps, pd
     out["speedup_split_vs_fp64"] = out["fp64"]["sweep_s"] / out["split"]["sweep_s"]
     out["heff_speedup_split_vs_fp64"] = out["fp64"]["heff_ms"] / max(out["split"]["heff_ms"], 1e-9)
     out["dE_rel"] = abs(out["split"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])

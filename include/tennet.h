@@ -134,6 +134,10 @@ int tn_mps_center(const tn_mps* mps);
  * normalised states the sweeps produce).  Entries with q_{s'} != q_s do not contribute
  * (charge conservation). */
 int tn_mps_expect_local(tn_mps* mps, const double* op, double* out);
+/* inner(a, b) = <a|b> of two states on the same sites (the ITensorMPS inner that users of
+ * TenNetLib call on the states it returns; TenNetLib's own sweep calls no overlap), from GPU
+ * transfer matrices over the charge sectors both states carry. */
+int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out);
 
 /* ---- StateEnvs --------------------------------------------------------------------
  * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO

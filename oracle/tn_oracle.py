@@ -758,6 +758,16 @@ def expect_local(psi: MPS, op):
     return out
 
 
+def inner(a: MPS, b: MPS) -> float:
+    """<a|b> of two MPS on the same sites by dense transfer matrices, left to right (the
+    ITensorMPS ``inner(a, b)`` that users of TenNetLib call on its states; the library itself
+    calls no overlap on the sweep path)."""
+    E = np.ones((1, 1))
+    for x, y in zip(a.A, b.A):
+        E = np.einsum("ab,asc,bsd->cd", E, x.conj(), y)
+    return float(np.real(E[0, 0]))
+
+
 def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,
               maxiter=2, tol=1e-14, normalize=True):
     """``fullsweep!`` with nsite = 2 (``src/mps/sweep.jl:94-196``)."""

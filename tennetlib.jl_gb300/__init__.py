@@ -236,6 +236,12 @@ class MPS:
     def center(self):
         return self.ctx.lib.tn_mps_center(self.h)
 
+    def inner(self, other: "MPS") -> float:
+        """<self|other> (both states on this context, same sites)."""
+        v = C.c_double()
+        L.check(self.ctx.lib.tn_mps_overlap(self.h, other.h, C.byref(v)))
+        return v.value
+
     def expect_local(self, op):
         """<psi|O_i|psi> / <psi|psi> for every site i (op: d x d matrix [s', s])."""
         op = np.asarray(op, dtype=np.float64)

@@ -94,6 +94,7 @@ PROTOS = {
     "tn_mps_site": (C.c_int, [vp, C.c_int, f64p, C.c_int64]),
     "tn_mps_center": (C.c_int, [vp]),
     "tn_mps_expect_local": (C.c_int, [vp, f64p, f64p]),
+    "tn_mps_overlap": (C.c_int, [vp, vp, f64p]),
     "tn_env_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
     "tn_env_destroy": (C.c_int, [vp]),
     "tn_env_getpsi": (C.c_int, [vp, C.POINTER(vp)]),

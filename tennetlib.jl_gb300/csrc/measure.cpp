@@ -10,6 +10,7 @@
 // GEMMs plus one batched Frobenius-dot kernel.
 #include <cstring>
 #include <map>
+#include <tuple>
 
 #include "engine.h"
 
@@ -224,5 +225,122 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
             out[q.i] += op[q.sp + size_t(d) * q.s] * part[k];  // O[s', s], column-major
         }
         for (int i = 0; i < N; ++i) out[i] /= norm;
+    });
+}
+
+// <a|b> of two MPS on the same sites (ITensorMPS inner(psi, phi) on the sweep's states):
+// mixed transfer matrices E_{i+1}[q] (Da_q x Db_q) = sum_s A_s[l, q]^T E_i[l] B_s[l, q] over
+// the charge sectors present in both states, FP64 grouped GEMMs; the result is E_N.
+extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
+    return guarded_m([&] {
+        TN_REQUIRE(a && b && out, "null argument");
+        TN_REQUIRE(a->ctx == b->ctx && a->N == b->N && a->d == b->d && a->pq == b->pq,
+                   "overlap needs two states of one context on the same sites");
+        tn_ctx* ctx = a->ctx;
+        cudaStream_t st = ctx->stream;
+        const int N = a->N, d = a->d;
+        // sub-blocks keyed by (s, left charge, right charge)
+        auto subs_of = [&](const tn_mps* m, int i) {
+            std::map<std::tuple<int, int, int>, SubBlock> out_map;
+            const SiteLayout& L = m->sites[i].lay;
+            for (int bk = 0; bk < L.nblk(); ++bk)
+                for (int s = 0; s < d; ++s) {
+                    const int sub = L.sub[size_t(bk) * d + s];
+                    if (sub < 0) continue;
+                    const int oth = L.subsec[size_t(bk) * d + s];
+                    SubBlock x;
+                    x.s = s;
+                    x.ld = L.rows[bk];
+                    if (L.layout == LG) {
+                        x.l = oth;
+                        x.r = bk;
+                        x.off = L.off[bk] + sub;
+                    } else {
+                        x.l = bk;
+                        x.r = oth;
+                        x.off = L.off[bk] + int64_t(sub) * L.rows[bk];
+                    }
+                    out_map[{s, m->links[i].q[x.l], m->links[i + 1].q[x.r]}] = x;
+                }
+            return out_map;
+        };
+        // E_i blocks for the charges present in both links
+        std::vector<std::map<int, int64_t>> eoff(N + 1);
+        int64_t etot = 0;
+        for (int i = 0; i <= N; ++i) {
+            const Link& la = a->links[i];
+            const Link& lb = b->links[i];
+            for (int x = 0; x < la.nsec(); ++x) {
+                const int y = lb.find(la.q[x]);
+                if (y < 0) continue;
+                eoff[i][la.q[x]] = etot;
+                etot += int64_t(la.dim[x]) * lb.dim[y];
+            }
+        }
+        TN_REQUIRE(!eoff[0].empty() && !eoff[N].empty(), "the states have different total charges");
+        DevBuf E, T;
+        E.alloc(size_t(std::max<int64_t>(etot, 1)) * 8, st);
+        TN_CUDA(cudaMemsetAsync(E.p, 0, E.bytes, st));
+        const double one = 1.0;
+        TN_CUDA(cudaMemcpyAsync(E.d() + eoff[0].begin()->second, &one, 8, cudaMemcpyHostToDevice, st));
+        for (int i = 0; i < N; ++i) {
+            const auto sa = subs_of(a, i), sb = subs_of(b, i);
+            const Link &lka = a->links[i], &lkb = b->links[i], &rka = a->links[i + 1],
+                       &rkb = b->links[i + 1];
+            struct Job { SubBlock xa, xb; int64_t toff, eo, en; int Dla, Dlb, Dra, Drb; int qr; };
+            std::vector<Job> jobs;
+            int64_t t = 0;
+            for (const auto& kv : sa) {
+                auto it = sb.find(kv.first);
+                if (it == sb.end()) continue;
+                const int ql = std::get<1>(kv.first), qr = std::get<2>(kv.first);
+                if (!eoff[i].count(ql) || !eoff[i + 1].count(qr)) continue;
+                Job j;
+                j.xa = kv.second;
+                j.xb = it->second;
+                j.Dla = lka.dim[j.xa.l];
+                j.Dlb = lkb.dim[j.xb.l];
+                j.Dra = rka.dim[j.xa.r];
+                j.Drb = rkb.dim[j.xb.r];
+                j.eo = eoff[i][ql];
+                j.en = eoff[i + 1][qr];
+                j.qr = qr;
+                j.toff = t;
+                t += int64_t(j.Dla) * j.Drb;
+                jobs.push_back(j);
+            }
+            T.alloc(size_t(std::max<int64_t>(t, 1)) * 8, st);
+            Bases bs{};
+            bs.p[S_L] = E.d();
+            bs.p[S_X] = a->sites[i].buf.d();
+            bs.p[S_A] = b->sites[i].buf.d();
+            bs.p[S_T1] = T.d();
+            GemmPlan g1, g2;
+            std::map<int, std::vector<size_t>> byr;
+            for (size_t k = 0; k < jobs.size(); ++k) {
+                const Job& j = jobs[k];
+                // T = E_i[ql] (Da_l x Db_l) * B_s (Db_l x Db_r)
+                g1.add_task(S_T1, j.toff, j.Dla, j.Drb, j.Dla);
+                g1.add_seg(S_L, j.eo, j.Dla, 0, S_A, j.xb.off, j.xb.ld, 0, j.Dlb);
+                byr[j.qr].push_back(k);
+            }
+            for (auto& kv : byr) {
+                const Job& j0 = jobs[kv.second[0]];
+                g2.add_task(S_L, j0.en, j0.Dra, j0.Drb, j0.Dra);
+                for (size_t k : kv.second) {
+                    const Job& j = jobs[k];
+                    g2.add_seg(S_X, j.xa.off, j.xa.ld, 1, S_T1, j.toff, j.Dla, 0, j.Dla);
+                }
+            }
+            g1.finalize(st);
+            g2.finalize(st);
+            launch_gemm_f64(g1, bs, st);
+            launch_gemm_f64(g2, bs, st);
+            TN_CUDA(cudaStreamSynchronize(st));
+        }
+        double v = 0.0;
+        TN_CUDA(cudaMemcpyAsync(&v, E.d() + eoff[N].begin()->second, 8, cudaMemcpyDeviceToHost, st));
+        TN_CUDA(cudaStreamSynchronize(st));
+        *out = v;
     });
 }

@@ -63,3 +63,50 @@ def test_measure_mixed_canonical_random_state(tn, ctx):
     assert np.allclose(got, ref, atol=1e-12)
     nup = psi.expect_local(np.diag([1.0, 0.0]))
     assert np.allclose(nup, 0.5 + np.array(ref), atol=1e-12)
+
+
+def _dense(mps):
+    v = mps.A[0]
+    for a in mps.A[1:]:
+        v = np.tensordot(v, a, axes=([-1], [0]))
+    return v.reshape(-1)
+
+
+def test_overlap_random_states(tn, ctx):
+    """<a|b> of two random charge-conserving states whose link sectors differ (sectors
+    carried by one state only drop out), against the dense contraction and the oracle."""
+    N = 9
+    a = random_qn_mps(N, np.random.default_rng(11), maxsec_dim=3)
+    b = random_qn_mps(N, np.random.default_rng(12), maxsec_dim=4)
+    ga = upload_mps(tn, ctx, a, center=0)
+    gb = upload_mps(tn, ctx, b, center=5)
+    ref = _dense(a) @ _dense(b)
+    assert O.inner(a, b) == pytest.approx(ref, rel=1e-12, abs=1e-12)
+    scale = np.linalg.norm(_dense(a)) * np.linalg.norm(_dense(b))
+    assert abs(ga.inner(gb) - ref) < 1e-12 * scale
+    assert abs(gb.inner(ga) - ref) < 1e-12 * scale
+    assert ga.inner(ga) == pytest.approx(_dense(a) @ _dense(a), rel=1e-12)
+
+
+def test_overlap_split_vs_fp64_ground_state(tn):
+    """The split-precision and FP64 sweeps reach the same ground state: |<psi_s|psi_d>| = 1
+    to 1e-8 (fidelity of two normalised states, both from the same start)."""
+    N = 16
+    states = {}
+    c = tn.Context()
+    try:
+        W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
+        H = tn.MPO(W, delta, pq, c)
+        for mode in ("fp64", "split"):
+            c.set_precision(mode)
+            env = tn.StateEnvs(tn.MPS.product(tn.models.neel_states(N), pq, c), H)
+            sw = tn.SweepData()
+            for md in (8, 16, 32, 64, 64, 64):
+                tn.fullsweep_(env, tn.eig_solver, 2, sw, maxdim=md, cutoff=1e-12, outputlevel=0)
+            states[mode] = env.getpsi()
+        f = states["split"].inner(states["fp64"])
+        assert abs(abs(f) - 1.0) < 1e-8
+        assert states["fp64"].inner(states["fp64"]) == pytest.approx(1.0, abs=1e-12)
+    finally:
+        states.clear()
+        c.close()

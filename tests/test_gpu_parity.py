@@ -125,6 +125,11 @@ def test_dmrg_sweeps_match_oracle_qn(tn, ctx):
         assert abs(sg.entropy[-1] - so.entropy[-1]) < 1e-9
         _same_links(eo, eg)
     assert abs(sg.energy[-1] - GOLD["heisenberg_chain"]["12"]) < 1e-8
+    # state overlap with the oracle's ground state, on the GPU (both normalised)
+    pg = eg.getpsi()
+    po = upload_mps(tn, ctx, eo.psi, center=eo.psi.center)
+    f = abs(pg.inner(po)) / np.sqrt(pg.inner(pg) * po.inner(po))
+    assert abs(f - 1.0) < 1e-9
 
 
 def test_dmrg_config1_random_product_no_qn(tn, ctx):

@@ -171,3 +171,18 @@ def test_oracle_tdvp_imaginary_time_lowers_energy():
     es = [O.tdvp_sweep(env, sw, -1.0, 16, 1e-14) for _ in range(40)]
     assert all(b <= a + 1e-12 for a, b in zip(es, es[1:]))
     assert abs(es[-1] - GOLD["heisenberg_chain"]["8"]) < 1e-8
+
+
+def test_inner_matches_dense():
+    from tests.helpers import random_qn_mps
+    a = random_qn_mps(7, np.random.default_rng(3), maxsec_dim=3)
+    b = random_qn_mps(7, np.random.default_rng(4), maxsec_dim=2)
+
+    def dense(m):
+        v = m.A[0]
+        for t in m.A[1:]:
+            v = np.tensordot(v, t, axes=([-1], [0]))
+        return v.reshape(-1)
+
+    assert O.inner(a, b) == pytest.approx(dense(a) @ dense(b), rel=1e-12, abs=1e-12)
+    assert O.inner(a, a) == pytest.approx(dense(a) @ dense(a), rel=1e-12)
