@@ -525,24 +525,22 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
     }
 }
 
-// explicit unit lower-trapezoidal V of the panel [p0, p0 + pb): V (m - p0) x pb, ld m - p0
+// columns [p0, p0 + pb) of the explicit unit lower-trapezoidal V (m x kmin, ld m): zero above
+// the diagonal, one on it, the stored reflector below
 __global__ void __launch_bounds__(BT) hh_build_v_kernel(const HhDesc* __restrict__ descs, int p0,
                                                         int pb_max) {
     const HhDesc& D = descs[blockIdx.y];
     if (p0 >= D.kmin) return;
     const int pb = (D.kmin - p0) < pb_max ? (D.kmin - p0) : pb_max;
-    const int64_t rows = D.m - p0;
-    const int64_t total = rows * pb;
-    double* V = D.V + hh_panel_voff(D.m, p0);
+    const int64_t m = D.m;
+    const int64_t total = m * pb;
+    double* V = D.V + p0 * m;
+    const double* A = D.A + p0 * m;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t r = e % rows;
-        const int c = int(e / rows);
-        double v;
-        if (r < c) v = 0.0;
-        else if (r == c) v = 1.0;
-        else v = D.A[p0 + r + int64_t(p0 + c) * D.m];
-        V[e] = v;
+        const int64_t r = e % m;
+        const int64_t dg = p0 + e / m;  // the diagonal row of this column
+        V[e] = r < dg ? 0.0 : (r == dg ? 1.0 : A[e]);
     }
 }
 
@@ -560,6 +558,7 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     const int pb = (D.kmin - p0) < pb_max ? (D.kmin - p0) : pb_max;
     const int64_t rows = D.m - p0;
     const double* V = D.V + hh_panel_voff(D.m, p0);
+    const int64_t ldv = D.m;
     const int a = threadIdx.x % HH_B, b = threadIdx.x / HH_B;
     double acc = 0.0;
     for (int64_t r0 = int64_t(blockIdx.x) * 64; r0 < rows; r0 += int64_t(gridDim.x) * 64) {
@@ -567,7 +566,7 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
         for (int e = threadIdx.x; e < 64 * HH_B; e += blockDim.x) {
             const int rr = e % 64, c = e / 64;
             const int64_t r = r0 + rr;
-            tile[rr][c] = (r < rows && c < pb) ? V[r + int64_t(c) * rows] : 0.0;
+            tile[rr][c] = (r < rows && c < pb) ? V[r + int64_t(c) * ldv] : 0.0;
         }
         __syncthreads();
 #pragma unroll 8
@@ -601,6 +600,39 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     }
     D.T[int64_t(p0 / HH_B) * HH_B * HH_B + a + b * HH_B] = (a < pb && b < pb) ? -T[a][b] : 0.0;
     if (threadIdx.x == 0) *D.ticket = 0u;
+}
+
+// -T of the whole block reflector H_0 H_1 ... H_{kmin-1} = I - V T V^T (LAPACK dlarft,
+// forward, columnwise) from G = V^T V: T[0:j, j] = -tau_j T[0:j, 0:j] G[0:j, j], T[j, j] = tau_j.
+// One CTA per instance; the columns are sequential, the rows of a column parallel over the
+// threads (T and G read from global memory through L1/L2; column j of G staged in shared).
+constexpr int TALL_THREADS = 512;
+constexpr int TALL_MAXK = 4096;
+__global__ void __launch_bounds__(TALL_THREADS) hh_tall_kernel(const HhDesc* __restrict__ descs) {
+    const HhDesc& D = descs[blockIdx.x];
+    const int k = D.kmin;
+    __shared__ double gj[TALL_MAXK];
+    double* T = D.Tall;  // holds +T while it is built, negated at the end
+    const double* G = D.G;
+    for (int j = 0; j < k; ++j) {
+        for (int c = threadIdx.x; c < j; c += blockDim.x) gj[c] = G[c + int64_t(j) * k];
+        __syncthreads();
+        const double tj = D.tau[j];
+        for (int r = threadIdx.x; r < j; r += blockDim.x) {
+            double v0 = 0.0, v1 = 0.0;
+            int c = r;
+            for (; c + 1 < j; c += 2) {
+                v0 = fma(T[r + int64_t(c) * k], gj[c], v0);
+                v1 = fma(T[r + int64_t(c + 1) * k], gj[c + 1], v1);
+            }
+            if (c < j) v0 = fma(T[r + int64_t(c) * k], gj[c], v0);
+            T[r + int64_t(j) * k] = -tj * (v0 + v1);
+        }
+        for (int r = j + threadIdx.x; r < k; r += blockDim.x) T[r + int64_t(j) * k] = r == j ? tj : 0.0;
+        __syncthreads();
+    }
+    const int64_t tot = int64_t(k) * k;
+    for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) T[e] = -T[e];
 }
 
 // R (kmin x n) = upper triangle of the factored A; Q (m x kmin, ld m) = [I; 0]
@@ -726,6 +758,13 @@ void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int p
     hh_gram_t_kernel<<<dim3(g, ninst), HH_B * HH_B, 0, s>>>(d, p0, pb);
     TN_CUDA(cudaGetLastError());
     count_launch(2);
+}
+
+void launch_hh_tall(const HhDesc* d, int ninst, cudaStream_t s) {
+    if (ninst <= 0) return;
+    hh_tall_kernel<<<ninst, TALL_THREADS, 0, s>>>(d);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s) {

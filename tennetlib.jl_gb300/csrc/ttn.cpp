@@ -233,8 +233,10 @@ struct MovePlan {       // link tensors of edge (v -> u)
 struct QrPlan {         // isometry move v -> u: blocked-QR GEMMs and the R mode product
     std::vector<TPlan> w, w2, upd;       // per panel (factorisation)
     std::vector<CombPlan> wc;
-    std::vector<TPlan> qw, qw2, qupd;    // per panel (Q formation, reverse order)
-    std::vector<CombPlan> qwc;
+    // Q formation with the whole block reflector: G = V^T V (k split, then combined),
+    // W = (-T) V_top^T, Q = [I; 0] + V W
+    TPlan gram, qw, qfin;
+    CombPlan gramc;
     TPlan rmode;
     int npanel = 0;
 };
@@ -275,7 +277,7 @@ struct tn_ttn_env {
     int64_t wbase = 0;
     int64_t w_x = 0, w_y = 0, w_kry = 0, w_tmp = 0, w_part = 0, w_qa = 0, w_qv = 0, w_r = 0,
             w_rt = 0, w_tt = 0, w_tau = 0, w_small = 0, w_wp = 0, w_w = 0, w_w2 = 0, w_hpart = 0,
-            w_coef = 0, w_end = 0;
+            w_coef = 0, w_g = 0, w_tall = 0, w_wq = 0, w_end = 0;
     int kry_vecs = 0;
     int nchunk_t = 1;                 // k chunks of the link-tensor contractions
     int nchunk_q = 1;                 // k chunks of the QR panel products
@@ -579,6 +581,9 @@ void build_work_layout(tn_ttn_env* e, int kd) {
     e->w_w2 = take(int64_t(HH_B) * e->dmax);
     e->w_hpart = take(int64_t(HH_B) * HH_B * TTN_PARTS);
     e->w_coef = take(int64_t(BK_MAX) * BK_MAX);
+    e->w_g = take(D2);
+    e->w_tall = take(D2);
+    e->w_wq = take(D2);
     e->w_end = c;
 }
 
@@ -854,10 +859,6 @@ std::unique_ptr<QrPlan> build_qr_plan(TtnGroup& G, int v, int u, const std::vect
     Q.w2.resize(npanel);
     Q.upd.resize(npanel);
     Q.wc.resize(npanel);
-    Q.qw.resize(npanel);
-    Q.qw2.resize(npanel);
-    Q.qupd.resize(npanel);
-    Q.qwc.resize(npanel);
     for (size_t i = 0; i < E.size(); ++i) {
         tn_ttn_env* e = E[i];
         const auto& dv = e->dims[v];
@@ -888,7 +889,7 @@ std::unique_ptr<QrPlan> build_qr_plan(TtnGroup& G, int v, int u, const std::vect
                         const int64_t wo = nch > 1 ? e->wbase + e->w_wp + int64_t(c) * HH_B * nt
                                                    : e->wbase + e->w_w;
                         Q.w[p].g.add_task(S_R, wo, nt, pb, nt, 0);
-                        Q.w[p].g.add_seg(abuf, atr + r0, int(m), 1, S_R, voff + r0, int(rows), 0,
+                        Q.w[p].g.add_seg(abuf, atr + r0, int(m), 1, S_R, voff + r0, int(m), 0,
                                          int(r1 - r0));
                         if (nch > 1) parts.push_back(wo);
                     }
@@ -907,41 +908,42 @@ std::unique_ptr<QrPlan> build_qr_plan(TtnGroup& G, int v, int u, const std::vect
                     Q.w2[p].g.add_task(S_R, e->wbase + e->w_w2, pb, nt, pb, 0);
                     Q.w2[p].g.add_seg(S_R, toff, HH_B, 1, S_R, e->wbase + e->w_w, nt, 1, pb);
                     Q.upd[p].g.add_task(abuf, atr, int(rows), nt, int(m), 1);
-                    Q.upd[p].g.add_seg(S_R, voff, int(rows), 0, S_R, e->wbase + e->w_w2, pb, 0, pb);
+                    Q.upd[p].g.add_seg(S_R, voff, int(m), 0, S_R, e->wbase + e->w_w2, pb, 0, pb);
                 }
-                // Q formation for this panel: Qsub = Q[p0:, p0:kmin]; Wt = Qsub^T V,
-                // W2 = (-T) Wt^T, Qsub += V W2
-                const int nq = kmin - p0;
-                const int64_t qs = aoff + p0 + int64_t(p0) * m;
-                const int nch = int(std::min<int64_t>(e->nchunk_q, std::max<int64_t>(1, rows / 512)));
-                const int64_t per = (rows + nch - 1) / nch;
-                std::vector<int64_t> parts;
-                for (int c = 0; c < nch; ++c) {
-                    const int64_t r0 = c * per, r1 = std::min(rows, r0 + per);
-                    if (r0 >= r1) break;
-                    const int64_t wo = nch > 1 ? e->wbase + e->w_wp + int64_t(c) * HH_B * nq
-                                               : e->wbase + e->w_w;
-                    Q.qw[p].g.add_task(S_R, wo, nq, pb, nq, 0);
-                    Q.qw[p].g.add_seg(abuf, qs + r0, int(m), 1, S_R, voff + r0, int(rows), 0, int(r1 - r0));
-                    if (nch > 1) parts.push_back(wo);
-                }
-                if (parts.size() > 1) {
-                    CombOut o{};
-                    o.doff = e->wbase + e->w_w;
-                    o.dbuf = S_R;
-                    o.ldd = nq;
-                    o.rows = nq;
-                    o.cols = pb;
-                    o.t0 = int(Q.qwc[p].terms.size());
-                    o.nt = int(parts.size());
-                    for (int64_t po : parts) Q.qwc[p].terms.push_back(CombTerm{po, S_R, nq, 1.0});
-                    Q.qwc[p].outs.push_back(o);
-                }
-                Q.qw2[p].g.add_task(S_R, e->wbase + e->w_w2, pb, nq, pb, 0);
-                Q.qw2[p].g.add_seg(S_R, toff, HH_B, 0, S_R, e->wbase + e->w_w, nq, 1, pb);
-                Q.qupd[p].g.add_task(abuf, qs, int(rows), nq, int(m), 1);
-                Q.qupd[p].g.add_seg(S_R, voff, int(rows), 0, S_R, e->wbase + e->w_w2, pb, 0, pb);
             }
+            // Q formation: G = V^T V over row chunks (partials combined), W = (-T) V_top^T,
+            // Q (= [I; 0] beforehand) += V W
+            const int64_t vo = e->wbase + e->w_qv;
+            const int64_t cap = std::max<int64_t>(1, int64_t(e->nchunk_q) * HH_B * e->dmax /
+                                                         (int64_t(kmin) * kmin));
+            const int nch = int(std::min<int64_t>(cap, std::max<int64_t>(1, m / 512)));
+            const int64_t per = (m + nch - 1) / nch;
+            std::vector<int64_t> parts;
+            for (int c = 0; c < nch; ++c) {
+                const int64_t r0 = c * per, r1 = std::min<int64_t>(m, r0 + per);
+                if (r0 >= r1) break;
+                const int64_t wo = nch > 1 ? e->wbase + e->w_wp + int64_t(c) * kmin * kmin
+                                           : e->wbase + e->w_g;
+                Q.gram.g.add_task(S_R, wo, kmin, kmin, kmin, 0);
+                Q.gram.g.add_seg(S_R, vo + r0, int(m), 1, S_R, vo + r0, int(m), 0, int(r1 - r0));
+                if (nch > 1) parts.push_back(wo);
+            }
+            if (parts.size() > 1) {
+                CombOut o{};
+                o.doff = e->wbase + e->w_g;
+                o.dbuf = S_R;
+                o.ldd = kmin;
+                o.rows = kmin;
+                o.cols = kmin;
+                o.t0 = int(Q.gramc.terms.size());
+                o.nt = int(parts.size());
+                for (int64_t po : parts) Q.gramc.terms.push_back(CombTerm{po, S_R, kmin, 1.0});
+                Q.gramc.outs.push_back(o);
+            }
+            Q.qw.g.add_task(S_R, e->wbase + e->w_wq, kmin, kmin, kmin, 0);
+            Q.qw.g.add_seg(S_R, e->wbase + e->w_tall, kmin, 0, S_R, vo, int(m), 1, kmin);
+            Q.qfin.g.add_task(abuf, aoff, int(m), kmin, int(m), 1);
+            Q.qfin.g.add_seg(S_R, vo, int(m), 0, S_R, e->wbase + e->w_wq, kmin, 0, kmin);
         }
         // psi_u <- R x_lv psi_u (into the rt temporary, copied back afterwards)
         add_mode_tasks(Q.rmode.g, e->dims[u], lv, kmin, S_R, e->wbase + e->w_rt,
@@ -1005,6 +1007,9 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
             h.scal = wptr(G, e, e->w_small);
             h.wv = wptr(G, e, e->w_small) + 16;
             h.part = wptr(G, e, e->w_hpart);
+            h.G = wptr(G, e, e->w_g);
+            h.Tall = wptr(G, e, e->w_tall);
+            TN_REQUIRE(kmin <= 4096, "blocked QR: more than 4096 columns");
             h.ticket = hh_ticket(G, e->idx);
             h.m = int(m);
             h.n = n;
@@ -1095,12 +1100,11 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
         }
         launch_hh_finish(dh, nh, mnmax, st);
         const int q2 = ctx->timer.mark();
-        for (int p = (kmax + HH_B - 1) / HH_B - 1; p >= 0; --p) {
-            tplan_run(G, QP.qw[p], sl, T_SVD);
-            comb_run(G, QP.qwc[p]);
-            tplan_run(G, QP.qw2[p], sl, T_SVD);
-            tplan_run(G, QP.qupd[p], sl, T_SVD);
-        }
+        tplan_run(G, QP.gram, sl, T_SVD);
+        comb_run(G, QP.gramc);
+        launch_hh_tall(dh, nh, st);
+        tplan_run(G, QP.qw, sl, T_SVD);
+        tplan_run(G, QP.qfin, sl, T_SVD);
         ctx->timer.add(T_QRGEMM, q2, ctx->timer.mark());
     }
     // Q back into the node tensor (leg lu now of size kmin)

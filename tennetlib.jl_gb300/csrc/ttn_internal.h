@@ -71,8 +71,10 @@ struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m 
     double* A;                   // factored in place; then overwritten by Q (= Q below)
     double* Q;
     double* R;                   // kmin x n
-    double* V;                   // panels of explicit reflectors, see hh_panel_voff
+    double* V;                   // explicit reflectors, m x kmin, ld m (see hh_panel_voff)
     double* T;                   // per panel -T (HH_B x HH_B)
+    double* G;                   // V^T V of all reflectors (kmin x kmin, ld kmin)
+    double* Tall;                // -T of the whole block reflector (kmin x kmin, ld kmin)
     double* tau;                 // kmin
     double* scal;                // tau, scale, beta of column j at scal + 4 (j & 1)
     double* wv;                  // current column: tau * w_k of the panel columns
@@ -84,11 +86,11 @@ struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m 
     int32_t pad;
 };
 
-// offset of the explicit V of the panel starting at column p0 (panels of HH_B columns,
-// panel P has (m - P*HH_B) rows)
+// The reflectors form one unit lower-trapezoidal matrix V (m x kmin, ld m; zero above the
+// diagonal, one on it).  Offset of the panel starting at column p0, from its diagonal row:
+// that panel's reflectors are the (m - p0) x HH_B block below, with ld m.
 __host__ __device__ inline int64_t hh_panel_voff(int m, int p0) {
-    const int64_t P = p0 / HH_B;
-    return P * HH_B * int64_t(m) - int64_t(HH_B) * HH_B * P * (P - 1) / 2;
+    return int64_t(p0) + int64_t(p0) * m;
 }
 
 int ttn_parts();
@@ -103,6 +105,8 @@ void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, i
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,
                          cudaStream_t s);
 void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s);
+// -T of the whole block reflector from G = V^T V and tau (one CTA per instance)
+void launch_hh_tall(const HhDesc* d, int ninst, cudaStream_t s);
 // CTAs that the cooperative panel kernel may use (all co-resident on the device)
 int hh_coop_capacity();
 // one panel [p0, p0 + HH_B) of every instance in one cooperative launch of nctas CTAs

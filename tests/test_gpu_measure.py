@@ -72,12 +72,25 @@ def _dense(mps):
     return v.reshape(-1)
 
 
+def _drop_sector(mps, i, rng):
+    """The same kind of random state with the largest charge removed from link i."""
+    links = [q.copy() for q in mps.links]
+    links[i] = links[i][links[i] != links[i].max()]
+    A = []
+    for j in range(len(links) - 1):
+        t = rng.standard_normal((len(links[j]), 2, len(links[j + 1])))
+        A.append(t * O.qn_mask3(links[j], mps.phys_q, links[j + 1]))
+    return O.MPS(A, links, mps.phys_q, center=0)
+
+
 def test_overlap_random_states(tn, ctx):
-    """<a|b> of two random charge-conserving states whose link sectors differ (sectors
-    carried by one state only drop out), against the dense contraction and the oracle."""
-    N = 9
+    """<a|b> of two random charge-conserving states whose link sectors differ (a sector
+    carried by one state only drops out), against the dense contraction and the oracle."""
+    N = 10
     a = random_qn_mps(N, np.random.default_rng(11), maxsec_dim=3)
-    b = random_qn_mps(N, np.random.default_rng(12), maxsec_dim=4)
+    b = _drop_sector(random_qn_mps(N, np.random.default_rng(12), maxsec_dim=4), 5,
+                     np.random.default_rng(13))
+    assert len(set(a.links[5]) - set(b.links[5])) == 1
     ga = upload_mps(tn, ctx, a, center=0)
     gb = upload_mps(tn, ctx, b, center=5)
     ref = _dense(a) @ _dense(b)
