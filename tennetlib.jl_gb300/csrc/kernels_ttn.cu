@@ -560,6 +560,14 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     const double* V = D.V + hh_panel_voff(D.m, p0);
     const int64_t ldv = D.m;
     const int a = threadIdx.x % HH_B, b = threadIdx.x / HH_B;
+    // the Gram is symmetric: threads [0, NPAIR) take the pairs ga <= gb (whole warps idle past)
+    constexpr int NPAIR = HH_B * (HH_B + 1) / 2;
+    const int t = threadIdx.x;
+    int gb = int((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
+    while ((gb + 1) * (gb + 2) / 2 <= t) ++gb;
+    while (gb > 0 && gb * (gb + 1) / 2 > t) --gb;
+    const int ga = t - gb * (gb + 1) / 2;
+    const bool mine = t < NPAIR;
     double acc = 0.0;
     for (int64_t r0 = int64_t(blockIdx.x) * 64; r0 < rows; r0 += int64_t(gridDim.x) * 64) {
         __syncthreads();
@@ -569,8 +577,10 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
             tile[rr][c] = (r < rows && c < pb) ? V[r + int64_t(c) * ldv] : 0.0;
         }
         __syncthreads();
+        if (mine) {
 #pragma unroll 8
-        for (int rr = 0; rr < 64; ++rr) acc = fma(tile[rr][a], tile[rr][b], acc);
+            for (int rr = 0; rr < 64; ++rr) acc = fma(tile[rr][ga], tile[rr][gb], acc);
+        }
     }
     D.part[int64_t(blockIdx.x) * (HH_B * HH_B) + threadIdx.x] = acc;
     __threadfence();
@@ -579,10 +589,13 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double s = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb)
-        s += reinterpret_cast<volatile double*>(D.part)[int64_t(bb) * (HH_B * HH_B) + threadIdx.x];
-    G[a][b] = s;
+    if (mine) {
+        double s = 0.0;
+        for (int bb = 0; bb < (int)gridDim.x; ++bb)
+            s += reinterpret_cast<volatile double*>(D.part)[int64_t(bb) * (HH_B * HH_B) + threadIdx.x];
+        G[ga][gb] = s;
+        G[gb][ga] = s;
+    }
     T[a][b] = 0.0;
     __syncthreads();
     // T[0:j, j] = -tau_j T[0:j, 0:j] G[0:j, j]; T[j, j] = tau_j
@@ -602,37 +615,61 @@ __global__ void __launch_bounds__(HH_B * HH_B) hh_gram_t_kernel(const HhDesc* __
     if (threadIdx.x == 0) *D.ticket = 0u;
 }
 
-// -T of the whole block reflector H_0 H_1 ... H_{kmin-1} = I - V T V^T (LAPACK dlarft,
-// forward, columnwise) from G = V^T V: T[0:j, j] = -tau_j T[0:j, 0:j] G[0:j, j], T[j, j] = tau_j.
-// One CTA per instance; the columns are sequential, the rows of a column parallel over the
-// threads (T and G read from global memory through L1/L2; column j of G staged in shared).
-constexpr int TALL_THREADS = 512;
-constexpr int TALL_MAXK = 4096;
+// -T of the whole block reflector H_0 H_1 ... H_{kmin-1} = I - V T V^T (forward,
+// columnwise) from the per-panel factors T_p and G = V^T V, one 32-column block at a time:
+// T[0:q0, q] = -T[0:q0, 0:q0] (G[0:q0, q] T_q) (Schreiber and Van Loan's merge of two block
+// reflectors).  One CTA per instance; Y = G[0:q0, q] T_q goes through a global scratch
+// (row-major, ld HH_B) so that every row's 32 products come from two cache lines.
+constexpr int TALL_THREADS = 256;
 __global__ void __launch_bounds__(TALL_THREADS) hh_tall_kernel(const HhDesc* __restrict__ descs) {
     const HhDesc& D = descs[blockIdx.x];
     const int k = D.kmin;
-    __shared__ double gj[TALL_MAXK];
     double* T = D.Tall;  // holds +T while it is built, negated at the end
     const double* G = D.G;
-    for (int j = 0; j < k; ++j) {
-        for (int c = threadIdx.x; c < j; c += blockDim.x) gj[c] = G[c + int64_t(j) * k];
+    double* Y = D.Yscr;
+    __shared__ double Tq[HH_B][HH_B + 1];
+    const int np = (k + HH_B - 1) / HH_B;
+    // diagonal blocks +T_p (the per-panel factors hold -T_p), zero elsewhere
+    for (int64_t e = threadIdx.x; e < int64_t(k) * k; e += blockDim.x) {
+        const int r = int(e % k), c = int(e / k), p = c / HH_B;
+        T[e] = r / HH_B == p
+                   ? -D.T[int64_t(p) * HH_B * HH_B + (r % HH_B) + (c % HH_B) * HH_B]
+                   : 0.0;
+    }
+    __syncthreads();
+    for (int q = 1; q < np; ++q) {
+        const int q0 = q * HH_B;
+        const int qb = (k - q0) < HH_B ? (k - q0) : HH_B;
+        for (int e = threadIdx.x; e < HH_B * HH_B; e += blockDim.x)
+            Tq[e % HH_B][e / HH_B] = -D.T[int64_t(q) * HH_B * HH_B + e];
         __syncthreads();
-        const double tj = D.tau[j];
-        for (int r = threadIdx.x; r < j; r += blockDim.x) {
-            double v0 = 0.0, v1 = 0.0;
-            int c = r;
-            for (; c + 1 < j; c += 2) {
-                v0 = fma(T[r + int64_t(c) * k], gj[c], v0);
-                v1 = fma(T[r + int64_t(c + 1) * k], gj[c + 1], v1);
-            }
-            if (c < j) v0 = fma(T[r + int64_t(c) * k], gj[c], v0);
-            T[r + int64_t(j) * k] = -tj * (v0 + v1);
+        // Y (q0 x HH_B) = G[0:q0, q0:q0+qb] T_q (T_q upper triangular; zero columns past qb)
+        for (int e = threadIdx.x; e < q0 * HH_B; e += blockDim.x) {
+            const int r = e % q0, c = e / q0;
+            double y = 0.0;
+            if (c < qb)
+                for (int cc = 0; cc <= c; ++cc) y = fma(G[r + int64_t(q0 + cc) * k], Tq[cc][c], y);
+            Y[int64_t(r) * HH_B + c] = y;
         }
-        for (int r = j + threadIdx.x; r < k; r += blockDim.x) T[r + int64_t(j) * k] = r == j ? tj : 0.0;
+        __syncthreads();
+        // T[0:q0, q0:q0+qb] = -T[0:q0, 0:q0] Y (T upper triangular)
+        for (int r = threadIdx.x; r < q0; r += blockDim.x) {
+            double acc[HH_B];
+#pragma unroll
+            for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
+            for (int cp = r; cp < q0; ++cp) {
+                const double t = T[r + int64_t(cp) * k];
+                const double* y = Y + int64_t(cp) * HH_B;
+#pragma unroll
+                for (int c = 0; c < HH_B; ++c) acc[c] = fma(t, y[c], acc[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < HH_B; ++c)
+                if (c < qb) T[r + int64_t(q0 + c) * k] = -acc[c];
+        }
         __syncthreads();
     }
-    const int64_t tot = int64_t(k) * k;
-    for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) T[e] = -T[e];
+    for (int64_t e = threadIdx.x; e < int64_t(k) * k; e += blockDim.x) T[e] = -T[e];
 }
 
 // R (kmin x n) = upper triangle of the factored A; Q (m x kmin, ld m) = [I; 0]

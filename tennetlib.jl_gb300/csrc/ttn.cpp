@@ -305,7 +305,7 @@ struct TtnGroup {
 namespace {
 
 constexpr int SCAL_PER = 160;   // per-instance scalar area (doubles) of the Krylov kernels
-constexpr int64_t SMALL_QR = 65536;
+constexpr int64_t SMALL_QR = 16384;  // m * n above this: blocked QR (one CTA is FP64-bound)
 
 Bases group_bases(TtnGroup& G) {
     Bases b{};
@@ -1009,7 +1009,7 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
             h.part = wptr(G, e, e->w_hpart);
             h.G = wptr(G, e, e->w_g);
             h.Tall = wptr(G, e, e->w_tall);
-            TN_REQUIRE(kmin <= 4096, "blocked QR: more than 4096 columns");
+            h.Yscr = wptr(G, e, e->w_wq);
             h.ticket = hh_ticket(G, e->idx);
             h.m = int(m);
             h.n = n;

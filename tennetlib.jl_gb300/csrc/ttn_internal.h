@@ -75,6 +75,7 @@ struct HhDesc {                  // blocked Householder QR of A (m x n, ld m, m 
     double* T;                   // per panel -T (HH_B x HH_B)
     double* G;                   // V^T V of all reflectors (kmin x kmin, ld kmin)
     double* Tall;                // -T of the whole block reflector (kmin x kmin, ld kmin)
+    double* Yscr;                // scratch of the -T kernel (>= kmin * HH_B)
     double* tau;                 // kmin
     double* scal;                // tau, scale, beta of column j at scal + 4 (j & 1)
     double* wv;                  // current column: tau * w_k of the panel columns
@@ -105,7 +106,7 @@ void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, i
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,
                          cudaStream_t s);
 void launch_hh_finish(const HhDesc* d, int ninst, int64_t mnmax, cudaStream_t s);
-// -T of the whole block reflector from G = V^T V and tau (one CTA per instance)
+// -T of the whole block reflector from G = V^T V and the per-panel T (one CTA per instance)
 void launch_hh_tall(const HhDesc* d, int ninst, cudaStream_t s);
 // CTAs that the cooperative panel kernel may use (all co-resident on the device)
 int hh_coop_capacity();
