@@ -350,6 +350,10 @@ def run_ours(args, world, rank, local, pg):
         if rank == 0:
             print(json.dumps({"ttn": run_ttn(tn, local, args, world)}), flush=True)
         return
+    if args.j1j2_chi2048:
+        if rank == 0:
+            print(json.dumps({"j1j2_chi2048": run_j1j2(tn, local, args)}), flush=True)
+        return
     ctx = tn.Context(local)
     if args.precision == "split":
         ctx.set_precision("split", args.slices)
@@ -477,6 +481,56 @@ def run_ours(args, world, rank, local, pg):
     print(json.dumps(res), flush=True)
 
 
+# J1-J2 cylinder at chi = 2048: the bond problem of the 6 x 16 cylinder (Ly = 6, MPO bond
+# dimension 26 in the bulk) on a 6 x 4 cylinder, J2/J1 = 0.5, U(1), cutoff 1e-10
+J1J2_LX, J1J2_LY = 4, 6
+J1J2_RAMP = [256, 512, 1024, 2048]
+
+
+def run_j1j2(tn, local, args):
+    """Ramp to chi = 2048 (untimed), then one sweep from the same state on the split path and
+    on the FP64 GPU path: sweep time, H_eff time and TFLOP/s, energy, state overlap."""
+    N = J1J2_LX * J1J2_LY
+    terms = tn.models.j1j2_cylinder_terms(J1J2_LX, J1J2_LY)
+    W, delta, pq = tn.models.mpo_from_terms(N, terms)
+    neel = [((i // J1J2_LY) + (i % J1J2_LY)) % 2 for i in range(N)]
+    ctx = tn.Context(local, precision="split", slices=args.slices)
+    H = tn.MPO(W, delta, pq, ctx)
+    env = tn.StateEnvs(tn.MPS.product(neel, pq, ctx), H)
+    sw = tn.SweepData()
+    t0 = time.perf_counter()
+    for md in J1J2_RAMP:
+        tn.fullsweep_(env, tn.eig_solver, 2, sw, maxdim=md, cutoff=1e-10, outputlevel=0)
+    prep = time.perf_counter() - t0
+    tensors, links = download_state(env.getpsi())
+    del env
+    out = {"workload": f"j1j2_cylinder_{J1J2_LY}x{J1J2_LX}_J2_0.5_u1_chi2048_cutoff1e-10",
+           "sites": N, "mpo_bond_dim": int(max(w.shape[0] for w in W)), "ramp": J1J2_RAMP,
+           "prepare_s": prep, "chi_start": int(max(len(q) for q in links))}
+    final = {}
+    for prec in ("split", "fp64"):
+        c = ctx if prec == "split" else tn.Context(local, precision="fp64")
+        Hc = H if prec == "split" else tn.MPO(W, delta, pq, c)
+        e = tn.StateEnvs(tn.MPS(tensors, links, pq, 0, c), Hc)
+        s = tn.SweepData()
+        tn.fullsweep_(e, tn.eig_solver, 2, s, maxdim=J1J2_RAMP[-1], cutoff=1e-10, outputlevel=0)
+        st = s.stats[-1]
+        out[prec] = {"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
+                     "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
+                     "svd_s": st["svd_ms"] / 1e3, "energy": s.energy[-1],
+                     "maxlinkdim": s.maxchi[-1], "maxtruncerr": s.maxtruncerr[-1]}
+        final[prec] = download_state(e.getpsi())
+        del e
+    ps = tn.MPS(final["split"][0], final["split"][1], pq, 0, ctx)
+    pd = tn.MPS(final["fp64"][0], final["fp64"][1], pq, 0, ctx)
+    out["overlap_split_fp64"] = abs(ps.inner(pd)) / math.sqrt(ps.inner(ps) * pd.inner(pd))
+    out["dE_rel"] = abs(out["split"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])
+    out["speedup_sweep_split_vs_fp64"] = out["fp64"]["sweep_s"] / out["split"]["sweep_s"]
+    out["speedup_heff_split_vs_fp64"] = out["fp64"]["heff_s"] / out["split"]["heff_s"]
+    out["same_bond_dims"] = out["split"]["maxlinkdim"] == out["fp64"]["maxlinkdim"]
+    return out
+
+
 def fp64_compare(tn, ctx, H, pq, tensors, links, local):
     """One sweep from the same state on the split path and on the FP64 GPU path."""
     out = {}
@@ -518,6 +572,8 @@ def main():
     ap.add_argument("--no-ttn", action="store_true", help="skip the TTN (32-instance) leg")
     ap.add_argument("--ttn-only", action="store_true", help="run only the TTN leg")
     ap.add_argument("--ttn-instances", type=int, default=TTN_INSTANCES)
+    ap.add_argument("--j1j2-chi2048", action="store_true",
+                    help="only the J1-J2 cylinder comparison at chi = 2048 (split vs FP64)")
     ap.add_argument("--save-state", default="", help="save the prepared MPS (npz) and exit")
     ap.add_argument("--load-state", default="", help="start from a saved MPS (no ramp)")
     ap.add_argument("--partial-updates", type=int, default=0,

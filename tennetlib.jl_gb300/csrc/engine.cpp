@@ -184,6 +184,7 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
     const int64_t TA = split_tile_bytes_a(), TB = split_tile_bytes_b();
     int64_t aoff = 0, boff = 0, eao = 0, ebo = 0;
     std::map<std::vector<int64_t>, std::pair<int64_t, int64_t>> bseen;  // B signature -> offsets
+    std::map<std::vector<int64_t>, std::pair<int64_t, int64_t>> aseen;  // A signature -> offsets
     for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
         const Task& t = g.tasks[ti];
         struct KT3 { int seg, k0, kv; };
@@ -205,29 +206,41 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
         }
         auto bit = bseen.find(bsig);
         const bool bnew = bit == bseen.end();
+        // likewise for A (e.g. one node tensor multiplied on the same leg by several matrices)
+        std::vector<int64_t> asig;
+        asig.push_back(t.m);
+        for (int j = 0; j < t.nseg; ++j) {
+            const Seg& sg = g.segs[t.seg0 + j];
+            asig.insert(asig.end(), {int64_t(sg.abuf), sg.aoff, int64_t(sg.lda), int64_t(sg.ta),
+                                     int64_t(sg.k)});
+        }
+        auto ait = aseen.find(asig);
+        const bool anew = ait == aseen.end();
         SplitTask stsk{};
         stsk.coff = t.coff;
-        stsk.a_off = aoff;
+        stsk.a_off = anew ? aoff : ait->second.first;
         stsk.b_off = bnew ? boff : bit->second.first;
         stsk.cbuf = t.cbuf;
         stsk.m = t.m;
         stsk.n = t.n;
         stsk.ldc = t.ldc;
         stsk.nkt = nkt;
-        stsk.ea_off = int32_t(eao);
+        stsk.ea_off = anew ? int32_t(eao) : int32_t(ait->second.second);
         stsk.eb_off = bnew ? int32_t(ebo) : int32_t(bit->second.second);
         stsk.accum = t.accum;
         sp->tasks.push_back(stsk);
         const int akt0 = (int)sp->aks.size(), bkt0 = (int)sp->bks.size();
         for (const auto& k : kts) {
             const Seg& sg = g.segs[k.seg];
-            KTileSrc a{};
-            a.buf = sg.abuf;
-            a.sr = sg.ta ? sg.lda : 1;
-            a.sk = sg.ta ? 1 : sg.lda;
-            a.off = sg.aoff + int64_t(k.k0) * a.sk;
-            a.kvalid = k.kv;
-            sp->aks.push_back(a);
+            if (anew) {
+                KTileSrc a{};
+                a.buf = sg.abuf;
+                a.sr = sg.ta ? sg.lda : 1;
+                a.sk = sg.ta ? 1 : sg.lda;
+                a.off = sg.aoff + int64_t(k.k0) * a.sk;
+                a.kvalid = k.kv;
+                sp->aks.push_back(a);
+            }
             if (!bnew) continue;
             KTileSrc bsrc{};
             bsrc.buf = sg.bbuf;
@@ -237,9 +250,11 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
             bsrc.kvalid = k.kv;
             sp->bks.push_back(bsrc);
         }
-        for (int mi = 0; mi < mt; ++mi)
-            sp->ajobs.push_back(PackJob{aoff + int64_t(mi) * nkt * slices * TA, akt0, nkt,
-                                        std::min(RA, t.m - mi * RA), mi * RA, int32_t(eao + mi * RA), 0});
+        if (anew)
+            for (int mi = 0; mi < mt; ++mi)
+                sp->ajobs.push_back(PackJob{aoff + int64_t(mi) * nkt * slices * TA, akt0, nkt,
+                                            std::min(RA, t.m - mi * RA), mi * RA,
+                                            int32_t(eao + mi * RA), 0});
         if (bnew)
             for (int ni = 0; ni < nt; ++ni)
                 sp->bjobs.push_back(PackJob{boff + int64_t(ni) * nkt * slices * TB, bkt0, nkt,
@@ -247,8 +262,11 @@ std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_stat
                                             int32_t(ebo + ni * RB), 0});
         for (int mi = 0; mi < mt; ++mi)
             for (int ni = 0; ni < nt; ++ni) sp->items.push_back(SplitItem{int32_t(ti), mi, ni, 0});
-        aoff += int64_t(mt) * nkt * slices * TA;
-        eao += int64_t(mt) * RA;
+        if (anew) {
+            aseen.emplace(asig, std::make_pair(aoff, eao));
+            aoff += int64_t(mt) * nkt * slices * TA;
+            eao += int64_t(mt) * RA;
+        }
         if (bnew) {
             bseen.emplace(bsig, std::make_pair(boff, ebo));
             boff += int64_t(nt) * nkt * slices * TB;

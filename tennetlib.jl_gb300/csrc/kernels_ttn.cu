@@ -419,10 +419,18 @@ __device__ __forceinline__ bool inst_barrier(unsigned* bar, unsigned target, int
     return *reinterpret_cast<volatile int*>(s_fail) == 0;
 }
 
-__global__ void __launch_bounds__(BT)
+// One grid barrier per column: every CTA reduces, over its own rows below j, sigma^2 = sum x_i^2
+// and s_c = sum x_i A[i, c] for the panel columns c right of j (x = column j), and the owner of
+// row j publishes A[j, j..pe).  After the barrier every CTA forms the same reflector
+// (beta, tau, scale = 1 / (alpha - beta)) and w_c = tau (A[j, c] + scale s_c) = tau v^T A[:, c],
+// then updates its rows.  Partials and the published row are double-buffered by column parity:
+// a CTA can only reuse a buffer after the next barrier, which every CTA reaches only once it
+// has read the totals of the previous column.
+__global__ void __launch_bounds__(BT, 2)
 hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* err) {
-    __shared__ double red[BT / 32][HH_B];
-    __shared__ double red1[33];
+    constexpr int W1 = HH_B + 1;
+    __shared__ double red[BT / 32][W1];
+    __shared__ double tot[W1];
     __shared__ double wsh[HH_B];
     __shared__ double sc[3];
     __shared__ int s_fail;
@@ -440,73 +448,71 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
     const int64_t chunk = (m - p0 + G - 1) / G;
     const int64_t r0 = p0 + int64_t(g) * chunk;
     const int64_t r1 = (r0 + chunk) < m ? (r0 + chunk) : m;
-    double* part1 = D.part;        // G norm partials
-    double* part2 = D.part + G;    // G x HH_B dot partials
+    double* parts = D.part;                          // 2 x G x W1: [sigma^2, s_0, s_1, ...]
+    double* pubs = D.part + 2 * int64_t(G) * W1;     // 2 x W1: A[j, j], A[j, j+1], ...
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned nb = 0;
     for (int j = p0; j < pe; ++j) {
+        const int buf = j & 1;
         double* col = D.A + int64_t(j) * m;
-        double s = 0.0;
-        for (int64_t i = (r0 > j + 1 ? r0 : j + 1) + threadIdx.x; i < r1; i += BT) s = fma(col[i], col[i], s);
-        s = block_sum(s, red1);
-        if (threadIdx.x == 0) part1[g] = s;
-        if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
-        // every CTA sums the G partials in the same fixed order (lane-strided, then a
-        // warp tree): identical reflectors everywhere
-        if (wid == 0) {
-            double t = 0.0;
-            for (int b = lane; b < G; b += 32) t += reinterpret_cast<volatile double*>(part1)[b];
-            t = warp_sum(t);
-            if (lane == 0) {
-                const double alpha = reinterpret_cast<volatile double*>(col)[j];
-                double tau, scale, beta;
-                make_reflector(alpha, t, tau, scale, beta);
-                sc[0] = tau;
-                sc[1] = scale;
-                sc[2] = beta;
+        const int nk = pe - j - 1;
+        double ss = 0.0;
+        double acc[HH_B];
+#pragma unroll
+        for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
+        for (int64_t i = (r0 > j + 1 ? r0 : j + 1) + threadIdx.x; i < r1; i += BT) {
+            const double x = col[i];
+            ss = fma(x, x, ss);
+            const double* arow = D.A + i + int64_t(j + 1) * m;
+            // groups of 8 columns past nk are skipped whole
+#pragma unroll
+            for (int cg = 0; cg < HH_B; cg += 8) {
+                if (cg >= nk) break;
+#pragma unroll
+                for (int c = cg; c < cg + 8; ++c)
+                    if (c < nk) acc[c] = fma(x, arow[int64_t(c) * m], acc[c]);
             }
+        }
+        ss = warp_sum(ss);
+        if (lane == 0) red[wid][0] = ss;
+#pragma unroll
+        for (int c = 0; c < HH_B; ++c) {
+            if (c >= ((nk + 7) & ~7)) break;
+            const double v = warp_sum(acc[c]);
+            if (lane == 0) red[wid][1 + c] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x <= nk) {
+            double t = 0.0;
+            for (int w = 0; w < BT / 32; ++w) t += red[w][threadIdx.x];
+            parts[(int64_t(buf) * G + g) * W1 + threadIdx.x] = t;
+            if (j >= r0 && j < r1) pubs[buf * W1 + threadIdx.x] = col[j + int64_t(threadIdx.x) * m];
+        }
+        if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
+        // totals: every CTA sums the G partials in the same fixed order (lane-strided, then a
+        // warp tree), so the reflectors are identical everywhere
+        const volatile double* pall = parts + int64_t(buf) * G * W1;
+        const volatile double* pub = pubs + buf * W1;
+        for (int c = wid; c <= nk; c += BT / 32) {
+            double t = 0.0;
+            for (int b = lane; b < G; b += 32) t += pall[int64_t(b) * W1 + c];
+            t = warp_sum(t);
+            if (lane == 0) tot[c] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tau, scale, beta;
+            make_reflector(pub[0], tot[0], tau, scale, beta);
+            sc[0] = tau;
+            sc[1] = scale;
+            sc[2] = beta;
         }
         __syncthreads();
         const double tau = sc[0], scale = sc[1], beta = sc[2];
-        const int nk = pe - j - 1;
+        if (threadIdx.x < nk) wsh[threadIdx.x] = tau * (pub[1 + threadIdx.x] + scale * tot[1 + threadIdx.x]);
+        __syncthreads();
         const int64_t i0 = r0 > j ? r0 : j;
         if (nk > 0) {
-            // panel products v^T A[:, k]; groups of 8 columns past nk are skipped whole
-            double acc[HH_B];
-#pragma unroll
-            for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
-            for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
-                const double v = i == j ? 1.0 : col[i] * scale;
-                const double* arow = D.A + i + int64_t(j + 1) * m;
-#pragma unroll
-                for (int cg = 0; cg < HH_B; cg += 8) {
-                    if (cg >= nk) break;
-#pragma unroll
-                    for (int c = cg; c < cg + 8; ++c)
-                        if (c < nk) acc[c] = fma(v, arow[int64_t(c) * m], acc[c]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < HH_B; ++c) {
-                if (c >= ((nk + 7) & ~7)) break;
-                const double v = warp_sum(acc[c]);
-                if (lane == 0) red[wid][c] = v;
-            }
-            __syncthreads();
-            if (threadIdx.x < nk) {
-                double t = 0.0;
-                for (int w = 0; w < BT / 32; ++w) t += red[w][threadIdx.x];
-                part2[int64_t(g) * HH_B + threadIdx.x] = t;
-            }
-            if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
-            for (int c = wid; c < nk; c += BT / 32) {
-                double t = 0.0;
-                for (int b = lane; b < G; b += 32)
-                    t += reinterpret_cast<volatile double*>(part2)[int64_t(b) * HH_B + c];
-                t = warp_sum(t);
-                if (lane == 0) wsh[c] = tau * t;  // the partials include row j (v_j = 1)
-            }
-            __syncthreads();
             for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
                 const double v = i == j ? 1.0 : col[i] * scale;
                 for (int c = 0; c < nk; ++c) {
@@ -514,10 +520,6 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
                     *a = fma(-v, wsh[c], *a);
                 }
             }
-        } else {
-            // last column of the panel: every CTA must have read alpha (= A[j, j]) before
-            // its owner overwrites it with beta below
-            if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
         }
         for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) col[i] = i == j ? beta : col[i] * scale;
         if (g == 0 && threadIdx.x == 0) D.tau[j] = tau;
