@@ -484,7 +484,7 @@ def run_ours(args, world, rank, local, pg):
 # J1-J2 cylinder at chi = 2048: the bond problem of the 6 x 16 cylinder (Ly = 6, MPO bond
 # dimension 26 in the bulk) on a 6 x 4 cylinder, J2/J1 = 0.5, U(1), cutoff 1e-10
 J1J2_LX, J1J2_LY = 4, 6
-J1J2_RAMP = [256, 512, 1024, 2048]
+J1J2_RAMP = [256, 512, 1024, 2048, 2048, 2048]  # one sweep each; chi reaches 2048 in the last
 
 
 def run_j1j2(tn, local, args):

@@ -491,25 +491,33 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
         if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
         // totals: every CTA sums the G partials in the same fixed order (lane-strided, then a
         // warp tree), so the reflectors are identical everywhere
-        const volatile double* pall = parts + int64_t(buf) * G * W1;
-        const volatile double* pub = pubs + buf * W1;
+        // (L2 loads: the partials were written by other SMs before the barrier's fences)
+        const double* pall = parts + int64_t(buf) * G * W1;
+        const double* pub = pubs + buf * W1;
         for (int c = wid; c <= nk; c += BT / 32) {
-            double t = 0.0;
-            for (int b = lane; b < G; b += 32) t += pall[int64_t(b) * W1 + c];
-            t = warp_sum(t);
+            double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+            int b = lane;
+            for (; b + 96 < G; b += 128) {
+                t0 += __ldcg(pall + int64_t(b) * W1 + c);
+                t1 += __ldcg(pall + int64_t(b + 32) * W1 + c);
+                t2 += __ldcg(pall + int64_t(b + 64) * W1 + c);
+                t3 += __ldcg(pall + int64_t(b + 96) * W1 + c);
+            }
+            for (; b < G; b += 32) t0 += __ldcg(pall + int64_t(b) * W1 + c);
+            const double t = warp_sum((t0 + t1) + (t2 + t3));
             if (lane == 0) tot[c] = t;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             double tau, scale, beta;
-            make_reflector(pub[0], tot[0], tau, scale, beta);
+            make_reflector(__ldcg(pub), tot[0], tau, scale, beta);
             sc[0] = tau;
             sc[1] = scale;
             sc[2] = beta;
         }
         __syncthreads();
         const double tau = sc[0], scale = sc[1], beta = sc[2];
-        if (threadIdx.x < nk) wsh[threadIdx.x] = tau * (pub[1 + threadIdx.x] + scale * tot[1 + threadIdx.x]);
+        if (threadIdx.x < nk) wsh[threadIdx.x] = tau * (__ldcg(pub + 1 + threadIdx.x) + scale * tot[1 + threadIdx.x]);
         __syncthreads();
         const int64_t i0 = r0 > j ? r0 : j;
         if (nk > 0) {
