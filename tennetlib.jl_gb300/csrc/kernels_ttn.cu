@@ -22,44 +22,6 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// double-float (an unevaluated sum hi + lo of two FP32 numbers, about 48 significant bits;
-// Dekker 1971, Knuth's TwoSum, FMA-based TwoProd): the Householder panel runs its
-// arithmetic on the FP32 pipe, which on GB300 issues far more than the FP64 pipe
-struct dfl {
-    float hi, lo;
-};
-__device__ __forceinline__ dfl dfl_of(double x) {
-    const float h = __double2float_rn(x);
-    return dfl{h, __double2float_rn(x - double(h))};
-}
-__device__ __forceinline__ double dfl_val(dfl a) { return double(a.hi) + double(a.lo); }
-__device__ __forceinline__ dfl dfl_add(dfl a, dfl b) {
-    const float s = a.hi + b.hi;
-    const float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    const float h = s + e;
-    return dfl{h, e - (h - s)};
-}
-__device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    const float h = p + e;
-    return dfl{h, e - (h - p)};
-}
-__device__ __forceinline__ dfl dfl_fma(dfl a, dfl b, dfl c) { return dfl_add(dfl_mul(a, b), c); }
-__device__ __forceinline__ dfl dfl_neg(dfl a) { return dfl{-a.hi, -a.lo}; }
-__device__ __forceinline__ dfl dfl_warp_sum(dfl v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const dfl w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-        v = dfl_add(v, w);
-    }
-    return v;
-}
-
 // ------------------------------------------------------------------------------------
 // batched Krylov kernels
 // ------------------------------------------------------------------------------------
@@ -460,18 +422,16 @@ __device__ __forceinline__ bool inst_barrier(unsigned* bar, unsigned target, int
 // One grid barrier per column: every CTA reduces, over its own rows below j, sigma^2 = sum x_i^2
 // and s_c = sum x_i A[i, c] for the panel columns c right of j (x = column j), and the owner of
 // row j publishes A[j, j..pe).  After the barrier every CTA forms the same reflector
-// (beta, tau, scale = 1 / (alpha - beta), in FP64 from the double-float totals) and
-// w_c = tau (A[j, c] + scale s_c) = tau v^T A[:, c], then updates its rows.  Partials and the
-// published row are double-buffered by column parity: a CTA can only reuse a buffer after the
-// next barrier, which every CTA reaches only once it has read the totals of the previous
-// column.  The panel itself is held in double-float (P: hi/lo pairs, row i of panel column c
-// at P[i + c m]; hh_panel_to_df / hh_panel_from_df convert it once per panel).
+// (beta, tau, scale = 1 / (alpha - beta)) and w_c = tau (A[j, c] + scale s_c) = tau v^T A[:, c],
+// then updates its rows.  Partials and the published row are double-buffered by column parity:
+// a CTA can only reuse a buffer after the next barrier, which every CTA reaches only once it
+// has read the totals of the previous column.
 __global__ void __launch_bounds__(BT, 2)
 hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* err) {
     constexpr int W1 = HH_B + 1;
-    __shared__ dfl red[BT / 32][W1];
+    __shared__ double red[BT / 32][W1];
     __shared__ double tot[W1];
-    __shared__ dfl wsh[HH_B];
+    __shared__ double wsh[HH_B];
     __shared__ double sc[3];
     __shared__ int s_fail;
     int inst = -1;
@@ -488,139 +448,90 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
     const int64_t chunk = (m - p0 + G - 1) / G;
     const int64_t r0 = p0 + int64_t(g) * chunk;
     const int64_t r1 = (r0 + chunk) < m ? (r0 + chunk) : m;
-    dfl* P = reinterpret_cast<dfl*>(D.V + int64_t(p0) * m);
-    dfl* parts = reinterpret_cast<dfl*>(D.part);     // 2 x G x W1: [sigma^2, s_0, s_1, ...]
-    dfl* pubs = parts + 2 * int64_t(G) * W1;         // 2 x W1: A[j, j], A[j, j+1], ...
+    double* parts = D.part;                          // 2 x G x W1: [sigma^2, s_0, s_1, ...]
+    double* pubs = D.part + 2 * int64_t(G) * W1;     // 2 x W1: A[j, j], A[j, j+1], ...
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned nb = 0;
     for (int j = p0; j < pe; ++j) {
         const int buf = j & 1;
-        dfl* col = P + int64_t(j - p0) * m;
+        double* col = D.A + int64_t(j) * m;
         const int nk = pe - j - 1;
-        // the two halves of the CTA take panel columns [0, 16) and [16, 32) right of j over
-        // the same rows (half 0 also sums sigma^2); groups of 8 columns past nk are skipped
-        constexpr int HALF = HH_B / 2;
-        const int half = threadIdx.x / (BT / 2), c0 = half * HALF;
-        dfl ss{0.f, 0.f};
-        dfl acc[HALF];
+        double ss = 0.0;
+        double acc[HH_B];
 #pragma unroll
-        for (int c = 0; c < HALF; ++c) acc[c] = dfl{0.f, 0.f};
-        if (half == 0 || nk > HALF) {
-            for (int64_t i = (r0 > j + 1 ? r0 : j + 1) + threadIdx.x % (BT / 2); i < r1; i += BT / 2) {
-                const dfl x = col[i];
-                if (half == 0) ss = dfl_fma(x, x, ss);
-                const dfl* arow = col + i + int64_t(1 + c0) * m;
+        for (int c = 0; c < HH_B; ++c) acc[c] = 0.0;
+        for (int64_t i = (r0 > j + 1 ? r0 : j + 1) + threadIdx.x; i < r1; i += BT) {
+            const double x = col[i];
+            ss = fma(x, x, ss);
+            const double* arow = D.A + i + int64_t(j + 1) * m;
+            // groups of 8 columns past nk are skipped whole
 #pragma unroll
-                for (int cg = 0; cg < HALF; cg += 8) {
-                    if (c0 + cg >= nk) break;
+            for (int cg = 0; cg < HH_B; cg += 8) {
+                if (cg >= nk) break;
 #pragma unroll
-                    for (int c = cg; c < cg + 8; ++c)
-                        if (c0 + c < nk) acc[c] = dfl_fma(x, arow[int64_t(c) * m], acc[c]);
-                }
+                for (int c = cg; c < cg + 8; ++c)
+                    if (c < nk) acc[c] = fma(x, arow[int64_t(c) * m], acc[c]);
             }
         }
-        if (half == 0) {
-            ss = dfl_warp_sum(ss);
-            if (lane == 0) red[wid][0] = ss;
-        }
+        ss = warp_sum(ss);
+        if (lane == 0) red[wid][0] = ss;
 #pragma unroll
-        for (int c = 0; c < HALF; ++c) {
-            if (c0 + c >= ((nk + 7) & ~7)) break;
-            const dfl v = dfl_warp_sum(acc[c]);
-            if (lane == 0) red[wid][1 + c0 + c] = v;
+        for (int c = 0; c < HH_B; ++c) {
+            if (c >= ((nk + 7) & ~7)) break;
+            const double v = warp_sum(acc[c]);
+            if (lane == 0) red[wid][1 + c] = v;
         }
         __syncthreads();
         if (threadIdx.x <= nk) {
-            // index 0 (sigma^2) and columns [0, 16) come from the warps of half 0, the rest
-            // from half 1
-            const int w0 = threadIdx.x >= 1 + HALF ? BT / 64 : 0;
-            dfl t{0.f, 0.f};
-            for (int w = w0; w < w0 + BT / 64; ++w) t = dfl_add(t, red[w][threadIdx.x]);
+            double t = 0.0;
+            for (int w = 0; w < BT / 32; ++w) t += red[w][threadIdx.x];
             parts[(int64_t(buf) * G + g) * W1 + threadIdx.x] = t;
             if (j >= r0 && j < r1) pubs[buf * W1 + threadIdx.x] = col[j + int64_t(threadIdx.x) * m];
         }
         if (!inst_barrier(D.bar, (++nb) * unsigned(G), err, &s_fail)) return;
         // totals: every CTA sums the G partials in the same fixed order (lane-strided, then a
-        // warp tree), so the reflectors are identical everywhere; L2 loads, since the partials
-        // were written by other SMs before the barrier's fences
-        const float2* pall = reinterpret_cast<const float2*>(parts + int64_t(buf) * G * W1);
-        const float2* pub = reinterpret_cast<const float2*>(pubs + buf * W1);
+        // warp tree), so the reflectors are identical everywhere
+        // (L2 loads: the partials were written by other SMs before the barrier's fences)
+        const double* pall = parts + int64_t(buf) * G * W1;
+        const double* pub = pubs + buf * W1;
         for (int c = wid; c <= nk; c += BT / 32) {
-            dfl t0{0.f, 0.f}, t1{0.f, 0.f};
+            double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
             int b = lane;
-            for (; b + 32 < G; b += 64) {
-                const float2 u0 = __ldcg(pall + int64_t(b) * W1 + c);
-                const float2 u1 = __ldcg(pall + int64_t(b + 32) * W1 + c);
-                t0 = dfl_add(t0, dfl{u0.x, u0.y});
-                t1 = dfl_add(t1, dfl{u1.x, u1.y});
+            for (; b + 96 < G; b += 128) {
+                t0 += __ldcg(pall + int64_t(b) * W1 + c);
+                t1 += __ldcg(pall + int64_t(b + 32) * W1 + c);
+                t2 += __ldcg(pall + int64_t(b + 64) * W1 + c);
+                t3 += __ldcg(pall + int64_t(b + 96) * W1 + c);
             }
-            if (b < G) {
-                const float2 u0 = __ldcg(pall + int64_t(b) * W1 + c);
-                t0 = dfl_add(t0, dfl{u0.x, u0.y});
-            }
-            const dfl t = dfl_warp_sum(dfl_add(t0, t1));
-            if (lane == 0) tot[c] = dfl_val(t);
+            for (; b < G; b += 32) t0 += __ldcg(pall + int64_t(b) * W1 + c);
+            const double t = warp_sum((t0 + t1) + (t2 + t3));
+            if (lane == 0) tot[c] = t;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            const float2 a = __ldcg(pub);
             double tau, scale, beta;
-            make_reflector(double(a.x) + double(a.y), tot[0], tau, scale, beta);
+            make_reflector(__ldcg(pub), tot[0], tau, scale, beta);
             sc[0] = tau;
             sc[1] = scale;
             sc[2] = beta;
         }
         __syncthreads();
         const double tau = sc[0], scale = sc[1], beta = sc[2];
-        if (threadIdx.x < nk) {
-            const float2 a = __ldcg(pub + 1 + threadIdx.x);
-            wsh[threadIdx.x] = dfl_of(tau * ((double(a.x) + double(a.y)) + scale * tot[1 + threadIdx.x]));
-        }
+        if (threadIdx.x < nk) wsh[threadIdx.x] = tau * (__ldcg(pub + 1 + threadIdx.x) + scale * tot[1 + threadIdx.x]);
         __syncthreads();
-        const dfl scl = dfl_of(scale);
         const int64_t i0 = r0 > j ? r0 : j;
         if (nk > 0) {
             for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) {
-                const dfl v = i == j ? dfl{1.f, 0.f} : dfl_mul(col[i], scl);
-                const dfl nv = dfl_neg(v);
+                const double v = i == j ? 1.0 : col[i] * scale;
                 for (int c = 0; c < nk; ++c) {
-                    dfl* a = col + i + int64_t(1 + c) * m;
-                    *a = dfl_fma(nv, wsh[c], *a);
+                    double* a = D.A + i + int64_t(j + 1 + c) * m;
+                    *a = fma(-v, wsh[c], *a);
                 }
             }
         }
-        const dfl bet = dfl_of(beta);
-        for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) col[i] = i == j ? bet : dfl_mul(col[i], scl);
+        for (int64_t i = i0 + threadIdx.x; i < r1; i += BT) col[i] = i == j ? beta : col[i] * scale;
         if (g == 0 && threadIdx.x == 0) D.tau[j] = tau;
         __syncthreads();
-    }
-}
-
-// panel columns [p0, pe) of A, rows [p0, m), to double-float in the reflector buffer
-// (V's columns of this panel, free until hh_build_v) and back
-__global__ void __launch_bounds__(BT) hh_panel_to_df_kernel(const HhDesc* __restrict__ descs, int p0) {
-    const HhDesc& D = descs[blockIdx.y];
-    if (p0 >= D.kmin) return;
-    const int pb = (D.kmin - p0) < HH_B ? (D.kmin - p0) : HH_B;
-    const int64_t m = D.m, rows = m - p0, total = rows * pb;
-    dfl* P = reinterpret_cast<dfl*>(D.V + int64_t(p0) * m);
-    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t i = p0 + e % rows, c = e / rows;
-        P[i + c * m] = dfl_of(D.A[i + (p0 + c) * m]);
-    }
-}
-
-__global__ void __launch_bounds__(BT) hh_panel_from_df_kernel(const HhDesc* __restrict__ descs, int p0) {
-    const HhDesc& D = descs[blockIdx.y];
-    if (p0 >= D.kmin) return;
-    const int pb = (D.kmin - p0) < HH_B ? (D.kmin - p0) : HH_B;
-    const int64_t m = D.m, rows = m - p0, total = rows * pb;
-    const dfl* P = reinterpret_cast<const dfl*>(D.V + int64_t(p0) * m);
-    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t i = p0 + e % rows, c = e / rows;
-        D.A[i + (p0 + c) * m] = dfl_val(P[i + c * m]);
     }
 }
 
@@ -876,17 +787,12 @@ int hh_coop_capacity() {
     return cap;
 }
 
-void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int64_t mmax, int p0, int* err,
+void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int p0, int* err,
                           cudaStream_t s) {
-    const dim3 gc(grid_x(mmax * HH_B, 2 * TTN_PARTS), ninst);
-    hh_panel_to_df_kernel<<<gc, BT, 0, s>>>(d, p0);
-    TN_CUDA(cudaGetLastError());
     void* args[] = {(void*)&d, (void*)&ninst, (void*)&p0, (void*)&err};
     TN_CUDA(cudaLaunchCooperativeKernel((const void*)hh_panel_coop_kernel, dim3(nctas), dim3(BT),
                                         args, 0, s));
-    hh_panel_from_df_kernel<<<gc, BT, 0, s>>>(d, p0);
-    TN_CUDA(cudaGetLastError());
-    count_launch(3);
+    count_launch();
 }
 
 void launch_hh_panel_end(const HhDesc* d, int ninst, int64_t mmax, int p0, int pb,

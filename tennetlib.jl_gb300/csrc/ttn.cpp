@@ -1084,7 +1084,7 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
             const int q0 = ctx->timer.mark();
             if (coop) {
                 TN_CUDA(cudaMemsetAsync(G.bars.p, 0, size_t(nh) * sizeof(unsigned), st));
-                launch_hh_panel_coop(dh, nh, nctas, mmax, p0, ctx->err.as<int>(), st);
+                launch_hh_panel_coop(dh, nh, nctas, p0, ctx->err.as<int>(), st);
             } else {
                 for (int j = p0; j < std::min(pend, kmax); ++j)
                     launch_hh_column(dh, nh, mmax, j, p0, pend, st);

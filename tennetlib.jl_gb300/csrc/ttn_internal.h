@@ -112,7 +112,7 @@ void launch_hh_tall(const HhDesc* d, int ninst, cudaStream_t s);
 int hh_coop_capacity();
 // one panel [p0, p0 + HH_B) of every instance in one cooperative launch of nctas CTAs
 // (instance i owns CTAs [cta0, cta0 + ncta)); grid-wide waits are bounded and set *err
-void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int64_t mmax, int p0, int* err,
+void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int p0, int* err,
                           cudaStream_t s);
 
 }  // namespace tn
