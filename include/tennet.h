@@ -170,7 +170,7 @@ int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* re
 
 /* tdvpsweep!(engine, tau; nsite = 2, kwargs...) (TenNetLib src/mps/tdvp.jl:247-277): a full
  * sweep with exp_solver (src/base/solver.jl:66-88) at time step tau/2 and the reverse
- * one-site step (src/mps/update_site.jl:78-87).  tau is real in this build (imaginary-time
+ * one-site step (src/mps/update_site.jl:78-87).  tau is real in this library (imaginary-time
  * evolution exp(tau H)); p->krylovdim / maxiter / tol are the exp_solver settings
  * (reference defaults 30 / 100 / 1e-12).  Fields of res as for tn_env_fullsweep. */
 int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_sweep_result* res,

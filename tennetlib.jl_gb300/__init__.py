@@ -524,7 +524,7 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     """``tdvpsweep!`` (``src/mps/tdvp.jl:247-277``) with nsite = 2: one full sweep with
     ``exp_solver`` at time_step/2 and reverse one-site steps; ``abstime += |time_step|``.
 
-    This build evolves with real time steps (imaginary-time evolution exp(time_step H));
+    The engine evolves with real time steps (imaginary-time evolution exp(time_step H));
     complex steps and ``nsite = "dynamic"`` are not built.
     """
     if solver is not exp_solver:

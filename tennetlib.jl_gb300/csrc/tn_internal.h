@@ -95,7 +95,7 @@ SiteLayout make_site_layout(Layout lay, const Link& left, const Link& right,
 // block m has rows (s1, l) slabs (s1-major) and cols (s2, r) slabs (s2-major).  The rows of
 // block m are the LG rows of a left tensor with right sector m; the columns are the RG
 // columns of a right tensor with left sector m.  The same layout with one physical leg
-// (nsite = 1, the one-site tensor (l, s, r) grouped by m = q_r) is not used by this build.
+// (nsite = 1, the one-site tensor (l, s, r) grouped by m = q_r) is not used by the engine.
 struct PhiLayout {
     int d = 0;
     std::vector<int> m, rows, cols;

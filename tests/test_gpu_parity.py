@@ -1,7 +1,7 @@
 """Parity of the CUDA sweep path (through the C ABI) with the CPU oracle.
 
 Tolerances: FP64 path, relative 1e-12 for single products and block SVDs, 1e-10 relative
-for DMRG energies (the benchmark spec's bound); bond dimensions and charge sectors bit-exact.
+for DMRG energies (the accuracy bound of the sweep); bond dimensions and charge sectors bit-exact.
 """
 import json
 import os

@@ -2,7 +2,7 @@
 
 Tolerances: products and environments relative 5e-11 (Frobenius) at 5 slices (41 bits
 per operand element, two chained contractions); DMRG energies |dE/E| <= 1e-10 (the
-spec bound); bond dimensions and charge sectors bit-exact.
+accuracy bound of the sweep); bond dimensions and charge sectors bit-exact.
 """
 import json
 import os
