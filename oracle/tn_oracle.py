@@ -758,14 +758,15 @@ def expect_local(psi: MPS, op):
     return out
 
 
-def inner(a: MPS, b: MPS) -> float:
+def inner(a: MPS, b: MPS):
     """<a|b> of two MPS on the same sites by dense transfer matrices, left to right (the
     ITensorMPS ``inner(a, b)`` that users of TenNetLib call on its states; the library itself
-    calls no overlap on the sweep path)."""
+    calls no overlap on the sweep path).  A float for real states, else a complex."""
     E = np.ones((1, 1))
     for x, y in zip(a.A, b.A):
         E = np.einsum("ab,asc,bsd->cd", E, x.conj(), y)
-    return float(np.real(E[0, 0]))
+    v = E[0, 0]
+    return complex(v) if np.iscomplexobj(E) else float(v)
 
 
 def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,

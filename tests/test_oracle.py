@@ -13,7 +13,8 @@ import pytest
 from oracle import ed
 from oracle import tn_oracle as O
 
-GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
+GOLD_DIR = os.path.join(os.path.dirname(__file__), "golden")
+GOLD = json.load(open(os.path.join(GOLD_DIR, "ed_energies.json")))
 
 
 @pytest.mark.parametrize("N", [6, 8, 10, 12])
@@ -186,3 +187,25 @@ def test_inner_matches_dense():
 
     assert O.inner(a, b) == pytest.approx(dense(a) @ dense(b), rel=1e-12, abs=1e-12)
     assert O.inner(a, a) == pytest.approx(dense(a) @ dense(a), rel=1e-12)
+
+
+def test_real_time_tdvp_quench_matches_exact():
+    """Two-site TDVP with complex steps tau = -0.05i (the real-time workload's step) from the
+    Neel state of the N = 12 chain: <S^z_i(t)> against exact evolution (quench_sz.json) at
+    t = 0.5 and 1.0.  The difference is the TDVP projection error of the small bond
+    dimensions the sweep grows from a product state (7e-8 and 4e-7 here), bounded by 1e-6."""
+    with open(os.path.join(GOLD_DIR, "quench_sz.json")) as f:
+        q = json.load(f)
+    N = q["N"]
+    psi = O.product_mps([0 if i % 2 == 0 else 1 for i in range(N)], O.SPIN_HALF_Q)
+    psi.A = [a.astype(np.complex128) for a in psi.A]
+    env = O.StateEnvs(psi, O.heisenberg_mpo(N))
+    sw = O.SweepData()
+    t = 0.0
+    for tk, ref in zip(q["times"], q["sz"]):
+        while t < tk - 1e-12:
+            O.tdvp_sweep(env, sw, -0.05j, maxdim=64, cutoff=1e-12, krylovdim=30)
+            t += 0.05
+        sz = O.expect_local(env.psi, np.diag([0.5, -0.5]))
+        assert np.abs(sz - np.array(ref)).max() < 1e-6
+        assert abs(O.inner(env.psi, env.psi) - 1.0) < 1e-12
