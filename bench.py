@@ -479,6 +479,11 @@ def run_ours(args, world, rank, local, pg):
         res["cpu_baseline"] = cpu_baseline_from(tensors, links)
     if not args.no_ttn:
         res["ttn"] = run_ttn(tn, local, args, world)
+    if not args.no_j1j2:
+        try:
+            res["j1j2_chi2048"] = run_j1j2(tn, local, args)
+        except Exception as e:  # an extra leg: report it, keep the headline line
+            res["j1j2_chi2048"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(res), flush=True)
 
 
@@ -575,6 +580,8 @@ def main():
     ap.add_argument("--ttn-instances", type=int, default=TTN_INSTANCES)
     ap.add_argument("--j1j2-chi2048", action="store_true",
                     help="only the J1-J2 cylinder comparison at chi = 2048 (split vs FP64)")
+    ap.add_argument("--no-j1j2", action="store_true",
+                    help="skip the chi = 2048 J1-J2 comparison leg of the default run")
     ap.add_argument("--save-state", default="", help="save the prepared MPS (npz) and exit")
     ap.add_argument("--load-state", default="", help="start from a saved MPS (no ramp)")
     ap.add_argument("--partial-updates", type=int, default=0,
