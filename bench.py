@@ -176,22 +176,24 @@ def cores():
 
 
 def cpu_baseline_from(tensors, links):
-    """Time one full oracle sweep from the GPU-prepared state on the host cores."""
+    """Time one full oracle sweep from the GPU-prepared state on the host cores; also return
+    the oracle's energy and largest bond dimension after that sweep."""
     O, env = oracle_env_from(tensors, links)
     env.position(0, 2)  # right environments: setup, not timed
     t0 = time.perf_counter()
     oracle_halfsweep(O, env, "left")
-    oracle_halfsweep(O, env, "right")
+    e = oracle_halfsweep(O, env, "right")
     dt = time.perf_counter() - t0
-    return {"value": dt, "unit": "s/sweep", "cores": cores(), "kind": "port",
+    return {"value": dt, "unit": "s/sweep", "cores": cores(), "kind": "port", "dense": True,
+            "energy": e, "maxlinkdim": int(env.psi.maxlinkdim()),
             "sample": f"one full two-site sweep ({2 * (N_SITES - 1)} bond updates) of the numpy "
-                      "FP64 oracle (dense tensors with charge labels, OpenBLAS threads = all "
-                      "host cores) from the same converged chi~180 state"}
+                      "FP64 oracle (dense tensors with charge labels, not block-sparse; OpenBLAS "
+                      "threads = all host cores) from the same converged chi~180 state"}
 
 
 def run_reference(args, world, rank, pg):
     """--impl reference: the oracle port on the host cores (the reference is Julia and
-    cannot run here).  Each step is a bounded sample: one half sweep; value = 2 x its time."""
+    cannot run here).  Each step is one full two-site sweep at maxdim 1024."""
     if rank != 0:
         return
     import numpy as np
@@ -202,16 +204,15 @@ def run_reference(args, world, rank, pg):
     sw = O.SweepData()
     for md in RAMP:  # prepare (not timed)
         O.fullsweep(env, sw, md, CUTOFF, 1, KRYLOVDIM, MAXITER, 1e-14)
-    direction = "left"
     for _ in range(args.warmup):
-        oracle_halfsweep(O, env, direction)
-        direction = "right" if direction == "left" else "left"
+        oracle_halfsweep(O, env, "left")
+        oracle_halfsweep(O, env, "right")
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle_halfsweep(O, env, direction)
-        times.append(2.0 * (time.perf_counter() - t0))
-        direction = "right" if direction == "left" else "left"
+        oracle_halfsweep(O, env, "left")
+        oracle_halfsweep(O, env, "right")
+        times.append(time.perf_counter() - t0)
     value = statistics.mean(times)
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s/sweep",
@@ -219,8 +220,10 @@ def run_reference(args, world, rank, pg):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": config(args),
         "cpu_baseline": {"value": value, "unit": "s/sweep", "cores": cores(), "kind": "port",
-                         "sample": "per step one half sweep (99 bond updates) of the numpy FP64 "
-                                   "oracle from its own converged chi~180 state; value = 2 x time "
+                         "dense": True,
+                         "sample": "per step one full two-site sweep (198 bond updates) of the "
+                                   "numpy FP64 oracle (dense tensors with charge labels, not "
+                                   "block-sparse) from its own converged chi~180 state "
                                    "(TenNetLib.jl itself needs Julia + ITensors, absent here)"},
         "e2e": {"value": value, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -409,6 +412,7 @@ def run_ours(args, world, rank, local, pg):
         e2 = tn.StateEnvs(p2, H)
         s2 = tn.SweepData()
         tn.fullsweep_(e2, tn.eig_solver, 2, s2, **sweep_kwargs(MAXDIM))
+        e2e_energy, e2e_chi = s2.energy[-1], s2.maxchi[-1]
         out = download_state(e2.getpsi())
         e2e_times.append(time.perf_counter() - t1)
         d2h = sum(t.size * 8 for t in out[0])
@@ -476,7 +480,13 @@ def run_ours(args, world, rank, local, pg):
     if args.precision == "split" and not args.no_fp64_compare:
         res["fp64_compare"] = fp64_compare(tn, ctx, H, pq, tensors, links, local)
     if world == 1 and not args.no_cpu_baseline:
-        res["cpu_baseline"] = cpu_baseline_from(tensors, links)
+        cb = cpu_baseline_from(tensors, links)
+        res["cpu_baseline"] = cb
+        # the same sweep from the same state on the GPU (the e2e leg) and on the CPU oracle
+        res["vs_cpu"] = {"dE_rel_vs_cpu": abs(e2e_energy - cb["energy"]) / abs(cb["energy"]),
+                         "same_bond_dims_vs_cpu": int(e2e_chi) == int(cb["maxlinkdim"]),
+                         "gpu_energy": e2e_energy, "cpu_energy": cb["energy"],
+                         "gpu_maxlinkdim": int(e2e_chi), "cpu_maxlinkdim": cb["maxlinkdim"]}
     if not args.no_ttn:
         res["ttn"] = run_ttn(tn, local, args, world)
     if not args.no_j1j2:
@@ -487,17 +497,23 @@ def run_ours(args, world, rank, local, pg):
     print(json.dumps(res), flush=True)
 
 
-# J1-J2 cylinder at chi = 2048: the bond problem of the 6 x 16 cylinder (Ly = 6, MPO bond
-# dimension 26 in the bulk) on a 6 x 4 cylinder, J2/J1 = 0.5, U(1), cutoff 1e-10
-J1J2_LX, J1J2_LY = 4, 6
-J1J2_RAMP = [256, 512, 1024, 2048, 2048, 2048]  # one sweep each; chi reaches 2048 in the last
+# J1-J2 cylinder at chi = 2048: the 6 x 16 cylinder (Ly = 6 periodic, Lx = 16 open, 96 sites,
+# MPO bond dimension 26 in the bulk), J2/J1 = 0.5, U(1), cutoff 1e-10
+J1J2_LX, J1J2_LY = 16, 6
+J1J2_CHI = 2048
+# two-site DMRG from a Neel product state grows the bond dimension about fourfold per sweep
+# (4, 16, 64, 256, 1024, 2048): six ramp sweeps reach chi = 2048 in the bulk
+J1J2_RAMP = [256, 512, 1024, 2048, 2048, 2048]
 
 
 def run_j1j2(tn, local, args):
     """Ramp to chi = 2048 (untimed), then one sweep from the same state on the split path and
-    on the FP64 GPU path: sweep time, H_eff time and TFLOP/s, energy, state overlap."""
-    N = J1J2_LX * J1J2_LY
-    terms = tn.models.j1j2_cylinder_terms(J1J2_LX, J1J2_LY)
+    on the FP64 GPU path: sweep time, H_eff time and TFLOP/s, SVD time and flops, energies,
+    truncation errors and the state overlap.  States stay on the device (one context whose
+    precision is switched between the two sweeps)."""
+    Lx = args.j1j2_lx
+    N = Lx * J1J2_LY
+    terms = tn.models.j1j2_cylinder_terms(Lx, J1J2_LY)
     W, delta, pq = tn.models.mpo_from_terms(N, terms)
     neel = [((i // J1J2_LY) + (i % J1J2_LY)) % 2 for i in range(N)]
     ctx = tn.Context(local, precision="split", slices=args.slices)
@@ -508,32 +524,37 @@ def run_j1j2(tn, local, args):
     for md in J1J2_RAMP:
         tn.fullsweep_(env, tn.eig_solver, 2, sw, maxdim=md, cutoff=1e-10, outputlevel=0)
     prep = time.perf_counter() - t0
-    tensors, links = download_state(env.getpsi())
+    psi = env.getpsi()
     del env
-    out = {"workload": f"j1j2_cylinder_{J1J2_LY}x{J1J2_LX}_J2_0.5_u1_chi2048_cutoff1e-10",
+    out = {"workload": f"j1j2_cylinder_{J1J2_LY}x{Lx}_J2_0.5_u1_chi{J1J2_CHI}_cutoff1e-10",
            "sites": N, "mpo_bond_dim": int(max(w.shape[0] for w in W)), "ramp": J1J2_RAMP,
-           "prepare_s": prep, "chi_start": int(max(len(q) for q in links))}
+           "prepare_s": prep, "chi_start": int(psi.maxlinkdim()),
+           "note": "one sweep from the same ramped state on each path (2 (N - 1) bond updates)"}
     final = {}
     for prec in ("split", "fp64"):
-        c = ctx if prec == "split" else tn.Context(local, precision="fp64")
-        Hc = H if prec == "split" else tn.MPO(W, delta, pq, c)
-        e = tn.StateEnvs(tn.MPS(tensors, links, pq, 0, c), Hc)
+        ctx.set_precision(prec, args.slices)
+        e = tn.StateEnvs(psi, H)
         s = tn.SweepData()
-        tn.fullsweep_(e, tn.eig_solver, 2, s, maxdim=J1J2_RAMP[-1], cutoff=1e-10, outputlevel=0)
+        tn.fullsweep_(e, tn.eig_solver, 2, s, maxdim=J1J2_CHI, cutoff=1e-10, outputlevel=0)
         st = s.stats[-1]
         out[prec] = {"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
                      "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
-                     "svd_s": st["svd_ms"] / 1e3, "energy": s.energy[-1],
-                     "maxlinkdim": s.maxchi[-1], "maxtruncerr": s.maxtruncerr[-1]}
-        final[prec] = download_state(e.getpsi())
+                     "svd_s": st["svd_ms"] / 1e3, "env_s": st["env_ms"] / 1e3,
+                     "lanczos_s": st["lanczos_ms"] / 1e3,
+                     "svd_gemm_flops": st.get("svd_gemm_flops", 0.0),
+                     "svd_jacobi_flops": st.get("svd_jacobi_flops", 0.0),
+                     "energy": s.energy[-1], "maxlinkdim": s.maxchi[-1],
+                     "maxtruncerr": s.maxtruncerr[-1]}
+        final[prec] = e.getpsi()
         del e
-    ps = tn.MPS(final["split"][0], final["split"][1], pq, 0, ctx)
-    pd = tn.MPS(final["fp64"][0], final["fp64"][1], pq, 0, ctx)
+    ps, pd = final["split"], final["fp64"]
     out["overlap_split_fp64"] = abs(ps.inner(pd)) / math.sqrt(ps.inner(ps) * pd.inner(pd))
     out["dE_rel"] = abs(out["split"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])
     out["speedup_sweep_split_vs_fp64"] = out["fp64"]["sweep_s"] / out["split"]["sweep_s"]
     out["speedup_heff_split_vs_fp64"] = out["fp64"]["heff_s"] / out["split"]["heff_s"]
-    out["same_bond_dims"] = out["split"]["maxlinkdim"] == out["fp64"]["maxlinkdim"]
+    out["same_bond_dims"] = (out["split"]["maxlinkdim"] == out["fp64"]["maxlinkdim"] and
+                             ps.linkdims() == pd.linkdims())
+    ctx.set_precision("split", args.slices)
     return out
 
 
@@ -582,6 +603,8 @@ def main():
                     help="only the J1-J2 cylinder comparison at chi = 2048 (split vs FP64)")
     ap.add_argument("--no-j1j2", action="store_true",
                     help="skip the chi = 2048 J1-J2 comparison leg of the default run")
+    ap.add_argument("--j1j2-lx", type=int, default=J1J2_LX,
+                    help="cylinder length of the J1-J2 leg (16: the 6 x 16 cylinder)")
     ap.add_argument("--save-state", default="", help="save the prepared MPS (npz) and exit")
     ap.add_argument("--load-state", default="", help="start from a saved MPS (no ramp)")
     ap.add_argument("--partial-updates", type=int, default=0,

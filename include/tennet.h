@@ -92,6 +92,10 @@ typedef struct tn_sweep_result {
     double qr_panel_ms;        /* TTN: device time of the Householder column/panel kernels */
     double qr_gemm_ms;         /* TTN: device time of the QR's grouped GEMMs (with packing) */
     double krylov_bytes;       /* algorithmic HBM bytes of the Krylov vector kernels */
+    double svd_gemm_flops;     /* algorithmic flops of the multi-SM block SVD's grouped GEMMs */
+    double svd_jacobi_flops;   /* flops of its Jacobi rotations (dots and column updates) */
+    int32_t svd_sweeps32;      /* largest FP32 presolve sweep count of a block */
+    int32_t svd_sweeps_df;     /* largest double-float polish sweep count of a block */
 } tn_sweep_result;
 
 /* ---- context ------------------------------------------------------------------- */
@@ -100,6 +104,18 @@ int tn_ctx_create(int device, tn_ctx** out);
 int tn_ctx_destroy(tn_ctx* ctx);
 /* TN_PREC_FP64 or TN_PREC_SPLIT; slices = bf16 slices per FP64 operand (2..7). */
 int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices);
+/* Block SVD of replacebond!: charge blocks with more than ncols columns (of the m >= n
+ * orientation) are factored by the multi-SM pipeline (blocked QR + cooperative Jacobi), the
+ * others by one CTA each.  Default 96; 0 sends every block to the multi-SM pipeline. */
+int tn_ctx_set_svd_split(tn_ctx* ctx, int ncols);
+/* Test hook of the failure path (no counterpart in the reference, whose solver only raises
+ * on non-convergence, src/base/solver.jl:38-41): the next launch on this context of the
+ * named kernel makes one of its bounded device waits run out, without any fault:
+ * 1 = split-precision tensor-core GEMM (one CTA withholds one stage's bulk copies),
+ * 2 = cooperative Jacobi of the multi-SM block SVD, 3 = cooperative Householder panel of the
+ * TTN QR (one CTA leaves before its first barrier).  The call that ran the kernel returns
+ * TN_E_TIMEOUT after about a second; the context stays usable. */
+int tn_ctx_inject_wait_timeout(tn_ctx* ctx, int kernel);
 const char* tn_last_error(void);
 const char* tn_version(void);
 /* number of CUDA kernels this library has launched since it was loaded (diagnostics) */
@@ -163,6 +179,19 @@ int tn_env_product_flops(tn_env* env, double* flops);
  * eigs (optional, capacity eigs_cap) receives the kept S^2 sorted descending. */
 int tn_env_update_position(tn_env* env, int pos, int ortho, const tn_update_params* p,
                            tn_update_result* res, double* eigs, int eigs_cap);
+/* update_position!(sysenv, eig_solver, pos, nsite, ortho; kwargs...) for nsite 1 or 2:
+ * nsite = 1 is _update_one_site! (TenNetLib src/mps/update_site.jl:94-190, noise = 0): the
+ * one-site solve at pos (the orthogonality center), then unless the half sweep is done the
+ * block SVD with ITensors truncation of the link toward the next site, whose factor S V
+ * (ortho left) or U S (ortho right) is multiplied into that site. */
+int tn_env_update_position_nsite(tn_env* env, int pos, int nsite, int ortho,
+                                 const tn_update_params* p, tn_update_result* res, double* eigs,
+                                 int eigs_cap);
+/* fullsweep!(sysenv, eig_solver, nsite, swdata; kwargs...) (src/mps/sweep.jl:94-196) for
+ * nsite 1 (one-site DMRG, dmrg1 of src/mps/dmrg.jl:314-320) or 2. */
+int tn_env_fullsweep_nsite(tn_env* env, int nsite, const tn_update_params* p,
+                           tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                           int32_t* n_mid_eigs);
 /* fullsweep!(sysenv, eig_solver, 2, swdata; kwargs...) (TenNetLib src/mps/sweep.jl:94-196).
  * mid_eigs (optional) receives lasteigs[N/2] (1-based bond N/2), n_mid_eigs its length. */
 int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res,
@@ -262,14 +291,17 @@ int tn_ttn_envs_fullsweep(int count, tn_ttn_env* const* envs, int npath, const i
  * blocks that already live on the device (concatenated at `blocks`, dimensions in the
  * host arrays rows/cols), sorted descending per block into the device buffer `svals`
  * (sum of min(rows, cols) doubles), computed on `stream` (a cudaStream_t, NULL = legacy
- * default stream) with the same kernel as tn_svd_truncate.  Allocates nothing: its work
- * space is a file-scope device array of about 16.3 MiB that every GPU on which the
- * library is loaded holds until the process exits.  Limits: sum rows*cols <= 524288,
- * sum min(rows, cols) <= 65536, nblocks <= 1024, min(rows, cols) <= 3000 per block;
- * larger requests return TN_E_INVALID.  The first call on a device looks up the work
- * array's address with that device current, so make it before any stream capture.  All
- * calls share the work array: calls that overlap on the GPU race and must be serialised
- * by the caller.  The call is asynchronous; synchronise `stream` before reading svals. */
+ * default stream) with the same one-CTA-per-block kernel as the small blocks of
+ * tn_svd_truncate.  Allocates nothing: its work space is a file-scope device array of
+ * about 16.3 MiB that every GPU on which the library is loaded holds until the process
+ * exits.  Limits: sum rows*cols <= 524288, sum min(rows, cols) <= 65536, nblocks <= 1024,
+ * min(rows, cols) <= 3000 per block; larger requests return TN_E_INVALID.  Set-up: the
+ * first call on a device looks up the work array's address with that device current and
+ * keeps it, so make that first call before any stream capture; after a cudaDeviceReset of
+ * the device the kept address is stale and the entry point must not be used on it again.
+ * The caller's current device is unchanged on return.  All calls share the work array:
+ * calls that overlap on the GPU race and must be serialised by the caller.  The call is
+ * asynchronous; synchronise `stream` before reading svals. */
 int tn_block_svals_noalloc(int device, const double* blocks, int nblocks, const int32_t* rows,
                            const int32_t* cols, double* svals, void* stream);
 

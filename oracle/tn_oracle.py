@@ -798,6 +798,115 @@ def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylo
     return float("nan"), float("nan")
 
 
+def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdim, maxiter,
+                    tol, normalize=True):
+    """``_update_one_site!`` (``src/mps/update_site.jl:94-190``) for the eigensolver without
+    noise: solve the one-site problem at the orthogonality center; unless the half sweep is
+    done, SVD the tensor with the link toward the next site on the V side (ITensors
+    truncation), keep U at pos and multiply S V into the next site."""
+    psi = env.psi
+    N = psi.N
+    assert psi.center == pos
+    env.position(pos, 1)
+    phi = psi.A[pos]
+    shape = phi.shape
+
+    def apply(v):
+        return heff1_apply(env.L[pos], env.H.W[pos], env.R[pos], v.reshape(shape)).reshape(-1)
+
+    energy, vec, info = eigsolve_lowest(apply, phi.reshape(-1), krylovdim, maxiter, tol)
+    phi = vec.reshape(shape)
+    if normalize:
+        phi = phi / np.linalg.norm(phi)
+    if halfsweep_done(N, pos, 1, ortho):
+        psi.A[pos] = phi
+        env.lpos = min(env.lpos, pos)
+        env.rpos = max(env.rpos, pos)
+        return energy, Spectrum(eigs=np.zeros(0), truncerr=0.0), info
+    ql, qs, qr = psi.links[pos], psi.phys_q, psi.links[pos + 1]
+    Dl, d, Dr = shape
+    if ortho == "left":
+        # (l, s) | r blocked by the charge of r
+        M = phi.reshape(Dl * d, Dr)
+        qrow = (ql[:, None] + qs[None, :]).reshape(-1)
+        qcol = qr
+    else:
+        # l | (s, r) blocked by the charge of l
+        M = phi.reshape(Dl, d * Dr)
+        qrow = ql
+        qcol = (qr[None, :] - qs[:, None]).reshape(-1)
+    charges = sorted(set(qrow.tolist()) & set(qcol.tolist()))
+    rows = [np.nonzero(qrow == m)[0] for m in charges]
+    cols = [np.nonzero(qcol == m)[0] for m in charges]
+    blocks = [M[np.ix_(ri, ci)] for ri, ci in zip(rows, cols)]
+    res, spec, kept = svd_blocks_truncate(blocks, maxdim, mindim, cutoff)
+    chi = sum(kept)
+    norm = math.sqrt(sum(float(np.sum(S ** 2)) for _, S, _ in res)) if normalize else 1.0
+    Lm = np.zeros((M.shape[0], chi))
+    Rm = np.zeros((chi, M.shape[1]))
+    qnew = []
+    off = 0
+    for m, ri, ci, (U, S, Vh), k in zip(charges, rows, cols, res, kept):
+        if k == 0:
+            continue
+        Sn = S / norm
+        if ortho == "left":
+            Lm[np.ix_(ri, range(off, off + k))] = U
+            Rm[np.ix_(range(off, off + k), ci)] = Sn[:, None] * Vh
+        else:
+            Lm[np.ix_(ri, range(off, off + k))] = U * Sn[None, :]
+            Rm[np.ix_(range(off, off + k), ci)] = Vh
+        qnew.extend([m] * k)
+        off += k
+    qnew = np.array(qnew, dtype=np.int64)
+    if ortho == "left":
+        psi.A[pos] = Lm.reshape(Dl, d, chi)
+        psi.A[pos + 1] = np.tensordot(Rm, psi.A[pos + 1], axes=([1], [0]))
+        psi.links[pos + 1] = qnew
+        psi.center = pos + 1
+        nxt = pos + 1
+    else:
+        psi.A[pos] = Rm.reshape(chi, d, Dr)
+        psi.A[pos - 1] = np.tensordot(psi.A[pos - 1], Lm, axes=([2], [0]))
+        psi.links[pos] = qnew
+        psi.center = pos - 1
+        nxt = pos - 1
+    env.lpos = min(env.lpos, pos, nxt)
+    env.rpos = max(env.rpos, pos, nxt)
+    return energy, spec, info
+
+
+def fullsweep1(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,
+               maxiter=2, tol=1e-14, normalize=True):
+    """``fullsweep!`` with nsite = 1 (``src/mps/sweep.jl:94-196``): sites 1..N moving right,
+    then N..1 moving left; lasteigs[bond] from the left-moving update at site bond + 1."""
+    N = env.N
+    assert env.psi.center == 0
+    swdata.sweepcount += 1
+    energy = float("nan")
+    maxtruncerr = 0.0
+    lasteigs = [None] * (N - 1)
+    for q in range(N):
+        energy, spec, _ = update_one_site(env, q, "left", maxdim, mindim, cutoff, krylovdim,
+                                          maxiter, tol, normalize)
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+    for q in range(N - 1, -1, -1):
+        energy, spec, _ = update_one_site(env, q, "right", maxdim, mindim, cutoff, krylovdim,
+                                          maxiter, tol, normalize)
+        if q >= 1:
+            lasteigs[q - 1] = spec.eigs
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+    swdata.maxchi.append(env.psi.maxlinkdim())
+    swdata.energy.append(energy)
+    mid = lasteigs[N // 2 - 1]
+    swdata.entropy.append(entropy(mid / np.sum(mid)))
+    swdata.maxtruncerr.append(maxtruncerr)
+    swdata.lasteigs = lasteigs
+    if swdata.sweepcount > 1:
+        return swdata.energy[-1] - swdata.energy[-2], swdata.entropy[-1] - swdata.entropy[-2]
+    return float("nan"), float("nan")
+
+
 def dmrg(psi0: MPS, H: MPO, maxdim, nsweeps, cutoff, krylovdim=5, maxiter=2, tol=1e-14,
          mindim=1):
     """``dmrg!`` stage loop without noise (``src/mps/dmrg.jl:148-227``)."""

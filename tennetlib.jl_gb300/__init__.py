@@ -28,6 +28,7 @@ ABI.  It refuses to run without the library or without a GB300.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import math
 import time
 from dataclasses import dataclass, field
@@ -64,7 +65,8 @@ class Context:
 
     _default = None
 
-    def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 5):
+    def __init__(self, device: int = 0, precision: str = "fp64", slices: int = 5,
+                 svd_split: int | None = None):
         self.lib = L.load()
         self._users = 0
         self._closing = False
@@ -72,6 +74,8 @@ class Context:
         L.check(self.lib.tn_ctx_create(device, C.byref(h)))
         self.h = h
         self.set_precision(precision, slices)
+        if svd_split is not None:
+            self.set_svd_split(svd_split)
 
     # Objects that own device handles of this context hold it; the context is destroyed
     # only after the last of them, whatever order the garbage collector finalises them in.
@@ -93,6 +97,10 @@ class Context:
         L.check(self.lib.tn_ctx_set_precision(self.h, mode, slices))
         self.precision = precision
         self.slices = slices
+
+    def set_svd_split(self, ncols: int):
+        """Charge blocks with more than ``ncols`` columns take the multi-SM block SVD."""
+        L.check(self.lib.tn_ctx_set_svd_split(self.h, int(ncols)))
 
     @classmethod
     def default(cls) -> "Context":
@@ -386,18 +394,20 @@ def _params(kwargs, exp=False) -> L.UpdateParams:
 
 
 def update_position_(sysenv: StateEnvs, solver, pos: int, nsite: int, ortho: str, **kwargs):
-    """``update_position!`` for two-site DMRG.  Returns (energy, truncerr, eigs)."""
+    """``update_position!`` for one- or two-site DMRG (``src/mps/update_site.jl:231-277``).
+    Returns (energy, truncerr, eigs)."""
     if solver is not eig_solver:
         raise ValueError("only eig_solver is built")
-    if nsite != 2:
-        raise ValueError("only nsite = 2 is built")
+    if nsite not in (1, 2):
+        raise ValueError("nsite must be 1 or 2")
     p = _params(kwargs)
     res = L.UpdateResult()
     cap = max(int(p.maxdim if p.maxdim < 1 << 20 else 1 << 16), 1)
     eigs = np.zeros(cap)
     o = {"left": L.TN_ORTHO_LEFT, "right": L.TN_ORTHO_RIGHT}[ortho]
-    L.check(sysenv.ctx.lib.tn_env_update_position(sysenv.h, pos, o, C.byref(p), C.byref(res),
-                                                  eigs.ctypes.data_as(L.f64p), cap))
+    L.check(sysenv.ctx.lib.tn_env_update_position_nsite(sysenv.h, pos, nsite, o, C.byref(p),
+                                                        C.byref(res),
+                                                        eigs.ctypes.data_as(L.f64p), cap))
     return res.energy, res.truncerr, eigs[: res.neigs].copy()
 
 
@@ -425,12 +435,13 @@ def entropy(p) -> float:
 
 
 def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwargs):
-    """``fullsweep!``: left-to-right then right-to-left two-site updates.
+    """``fullsweep!``: left-to-right then right-to-left one- or two-site updates
+    (``src/mps/sweep.jl:94-196``).
 
     Returns (Delta E, Delta S) and appends to ``swdata``.
     """
-    if solver is not eig_solver or nsite != 2:
-        raise ValueError("only two-site eig_solver sweeps are built")
+    if solver is not eig_solver or nsite not in (1, 2):
+        raise ValueError("only one- and two-site eig_solver sweeps are built")
     p = _params(kwargs)
     outputlevel = kwargs.get("outputlevel", 1)
     res = L.SweepResult()
@@ -439,8 +450,9 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
     nmid = C.c_int32()
     swdata.sweepcount += 1
     t0 = time.perf_counter()
-    L.check(sysenv.ctx.lib.tn_env_fullsweep(sysenv.h, C.byref(p), C.byref(res),
-                                            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    L.check(sysenv.ctx.lib.tn_env_fullsweep_nsite(sysenv.h, nsite, C.byref(p), C.byref(res),
+                                                  mid.ctypes.data_as(L.f64p), cap,
+                                                  C.byref(nmid)))
     wall = time.perf_counter() - t0
     mid = mid[: nmid.value].copy()
     swdata.maxchi.append(int(res.maxlinkdim))
@@ -453,7 +465,9 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
         "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops, "pack_ms": res.pack_ms,
         "gemm_launches": res.gemm_launches, "kernel_launches": res.kernel_launches,
-        "krylov_bytes": res.krylov_bytes, "wall_s": wall})
+        "krylov_bytes": res.krylov_bytes, "svd_gemm_flops": res.svd_gemm_flops,
+        "svd_jacobi_flops": res.svd_jacobi_flops, "svd_sweeps32": res.svd_sweeps32,
+        "svd_sweeps_df": res.svd_sweeps_df, "wall_s": wall})
     if swdata.sweepcount > 1:
         enerr = swdata.energy[-1] - swdata.energy[-2]
         enterr = swdata.entropy[-1] - swdata.entropy[-2]
@@ -483,7 +497,8 @@ def _record_sweep(swdata, res, mid, wall, noise=0.0, outputlevel=0):
         "sweep_ms": res.sweep_ms, "gemm_ms": res.gemm_ms, "gemm_flops": res.gemm_flops,
         "pack_ms": res.pack_ms, "gemm_launches": res.gemm_launches,
         "kernel_launches": res.kernel_launches, "krylov_bytes": res.krylov_bytes,
-        "wall_s": wall})
+        "svd_gemm_flops": res.svd_gemm_flops, "svd_jacobi_flops": res.svd_jacobi_flops,
+        "svd_sweeps32": res.svd_sweeps32, "svd_sweeps_df": res.svd_sweeps_df, "wall_s": wall})
 
 
 class TDVPEngine:
@@ -624,6 +639,90 @@ def dmrg(psi0: MPS, H: MPO, params: DMRGParams, nsite: int, **kwargs):
 def dmrg2(psi0: MPS, H: MPO, params: DMRGParams, **kwargs):
     """``dmrg2`` (``src/mps/dmrg.jl:295-297``)."""
     return dmrg(psi0, H, params, 2, **kwargs)
+
+
+def dmrg1(psi0: MPS, H: MPO, params: DMRGParams, **kwargs):
+    """``dmrg1`` (``src/mps/dmrg.jl:314-320``): one-site DMRG (noise must be 0)."""
+    return dmrg(psi0, H, params, 1, **kwargs)
+
+
+# ------------------------------------------------------------------------------------
+# checkpoint / resume
+# ------------------------------------------------------------------------------------
+
+def _charge_mask(ql, pq, qr):
+    return (np.asarray(ql)[:, None, None] + np.asarray(pq)[None, :, None]) == \
+        np.asarray(qr)[None, None, :]
+
+
+def checkpoint_arrays(tensors, links, phys_q, center, swdata: SweepData | None = None) -> dict:
+    """Host arrays of a checkpoint: for every site only the entries its charges allow (the
+    charge blocks, concatenated), the link and site charges, the orthogonality centre and the
+    sweep history."""
+    out = {"phys_q": np.asarray(phys_q, dtype=np.int32), "center": np.int64(center),
+           "nsites": np.int64(len(tensors))}
+    for i, t in enumerate(tensors):
+        t = np.asarray(t, dtype=np.float64)
+        out[f"shape_{i}"] = np.array(t.shape, dtype=np.int64)
+        out[f"blocks_{i}"] = t[_charge_mask(links[i], phys_q, links[i + 1])]
+    for i, q in enumerate(links):
+        out[f"link_{i}"] = np.asarray(q, dtype=np.int32)
+    if swdata is not None:
+        out["sw_sweepcount"] = np.int64(swdata.sweepcount)
+        for k in ("maxchi", "energy", "entropy", "maxtruncerr"):
+            out[f"sw_{k}"] = np.asarray(getattr(swdata, k), dtype=np.float64)
+        lens = [len(e) for e in swdata.lasteigs]
+        out["sw_lasteigs_len"] = np.asarray(lens, dtype=np.int64)
+        out["sw_lasteigs"] = (np.concatenate([np.asarray(e, dtype=np.float64) for e in swdata.lasteigs])
+                              if lens else np.zeros(0))
+        out["sw_stats"] = np.array(json.dumps(swdata.stats))
+    return out
+
+
+def arrays_from_checkpoint(z) -> tuple:
+    """(tensors, links, phys_q, center, swdata or None) from checkpoint_arrays' dict."""
+    n = int(z["nsites"])
+    pq = np.asarray(z["phys_q"], dtype=np.int32)
+    links = [np.asarray(z[f"link_{i}"], dtype=np.int32) for i in range(n + 1)]
+    tensors = []
+    for i in range(n):
+        t = np.zeros(tuple(int(x) for x in z[f"shape_{i}"]))
+        t[_charge_mask(links[i], pq, links[i + 1])] = z[f"blocks_{i}"]
+        tensors.append(t)
+    sw = None
+    if "sw_sweepcount" in z:
+        sw = SweepData()
+        sw.sweepcount = int(z["sw_sweepcount"])
+        sw.maxchi = [int(x) for x in z["sw_maxchi"]]
+        for k in ("energy", "entropy", "maxtruncerr"):
+            setattr(sw, k, [float(x) for x in z[f"sw_{k}"]])
+        lens, flat, o = z["sw_lasteigs_len"], z["sw_lasteigs"], 0
+        sw.lasteigs = []
+        for ln in lens:
+            sw.lasteigs.append(np.asarray(flat[o:o + int(ln)]))
+            o += int(ln)
+        sw.stats = json.loads(str(z["sw_stats"]))
+    return tensors, links, pq, int(z["center"]), sw
+
+
+def save_checkpoint(path, psi, swdata: SweepData | None = None):
+    """Write a checkpoint of a DMRG run to ``path`` (numpy .npz): the state (an ``MPS`` or
+    the current state of a ``StateEnvs``) and the sweep history.  The reference restarts a
+    simulation from a serialised ``StateEnvs`` (docs/src/mps/example_dmrg.md:76-78); here the
+    environments are rebuilt from the state on resume."""
+    if isinstance(psi, StateEnvs):
+        psi = psi.getpsi()
+    tensors = [psi.site(i) for i in range(psi.N)]
+    links = [psi.link_charges(i) for i in range(psi.N + 1)]
+    np.savez(path, **checkpoint_arrays(tensors, links, psi.phys_q, psi.center, swdata))
+
+
+def load_checkpoint(path, ctx: Context | None = None):
+    """(MPS, SweepData or None) from a checkpoint; continue with ``StateEnvs(psi, H)`` and the
+    same ``SweepData``."""
+    with np.load(path, allow_pickle=False) as z:
+        tensors, links, pq, center, sw = arrays_from_checkpoint(z)
+    return MPS(tensors, links, pq, center, ctx), sw
 
 
 def svd_truncate(blocks, maxdim=INT32_MAX, mindim=1, cutoff=None, ctx: Context | None = None):

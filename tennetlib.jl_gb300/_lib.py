@@ -74,6 +74,10 @@ class SweepResult(C.Structure):
         ("qr_panel_ms", C.c_double),
         ("qr_gemm_ms", C.c_double),
         ("krylov_bytes", C.c_double),
+        ("svd_gemm_flops", C.c_double),
+        ("svd_jacobi_flops", C.c_double),
+        ("svd_sweeps32", C.c_int32),
+        ("svd_sweeps_df", C.c_int32),
     ]
 
 
@@ -82,6 +86,8 @@ PROTOS = {
     "tn_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
     "tn_ctx_destroy": (C.c_int, [vp]),
     "tn_ctx_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
+    "tn_ctx_set_svd_split": (C.c_int, [vp, C.c_int]),
+    "tn_ctx_inject_wait_timeout": (C.c_int, [vp, C.c_int]),
     "tn_last_error": (C.c_char_p, []),
     "tn_version": (C.c_char_p, []),
     "tn_kernel_launches": (C.c_int64, []),
@@ -106,6 +112,11 @@ PROTOS = {
                                          C.POINTER(UpdateResult), f64p, C.c_int]),
     "tn_env_fullsweep": (C.c_int, [vp, C.POINTER(UpdateParams), C.POINTER(SweepResult), f64p,
                                    C.c_int, i32p]),
+    "tn_env_update_position_nsite": (C.c_int, [vp, C.c_int, C.c_int, C.c_int,
+                                               C.POINTER(UpdateParams), C.POINTER(UpdateResult),
+                                               f64p, C.c_int]),
+    "tn_env_fullsweep_nsite": (C.c_int, [vp, C.c_int, C.POINTER(UpdateParams),
+                                         C.POINTER(SweepResult), f64p, C.c_int, i32p]),
     "tn_env_tdvpsweep": (C.c_int, [vp, C.c_double, C.POINTER(UpdateParams), C.POINTER(SweepResult),
                                    f64p, C.c_int, i32p]),
     "tn_svd_truncate": (C.c_int, [vp, C.c_int, i32p, i32p, f64p, C.c_int32, C.c_int32,

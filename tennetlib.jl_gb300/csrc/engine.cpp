@@ -345,7 +345,8 @@ void check_device_error(tn_ctx* ctx) {
     TN_CUDA(cudaStreamSynchronize(ctx->stream));
     if (e) {
         TN_CUDA(cudaMemsetAsync(ctx->err.p, 0, sizeof(int), ctx->stream));
-        throw Error(TN_E_TIMEOUT, "a bounded device wait gave up in the tensor-core GEMM");
+        throw Error(TN_E_TIMEOUT, "a bounded device wait gave up (tensor-core GEMM or "
+                                  "cooperative kernel barrier)");
     }
 }
 
@@ -978,11 +979,11 @@ struct EigOut {
     int matvecs, converged;
 };
 
-EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
+template <class MV>
+EigOut lanczos_lowest(tn_env* env, MV&& apply, int64_t n, double* x0, double* result,
                       const tn_update_params* prm) {
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
-    const int64_t n = P.ph.size;
     const int kd = prm->krylovdim;
     // vector pool: kd basis + kd restart + 1 residual
     const int nvec = 2 * kd + 1;
@@ -1039,7 +1040,7 @@ EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
     auto Hat = [&](int i, int j) -> double& { return Hm[size_t(i) * (kd + 1) + j]; };
     std::vector<double> h;
     double beta = 0.0;
-    heff_apply(env, P, V[0], w);
+    apply(V[0], w);
     out.matvecs++;
     gs2(1, h, beta);
     Hat(0, 0) = h[0];
@@ -1064,7 +1065,7 @@ EigOut lanczos_lowest(tn_env* env, Heff2Plan& P, double* x0, double* result,
             double* v = take();
             launch_scale_into(v, w, nullptr, 1.0 / beta, n, st);
             V.push_back(v);
-            heff_apply(env, P, v, w);
+            apply(v, w);
             out.matvecs++;
             gs2(K + 1, h, beta);
             for (int i = 0; i <= K; ++i) {
@@ -1288,39 +1289,65 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
     dP.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
     dS.alloc(size_t(std::max<int64_t>(so, 1)) * 8, st);
     dPerm.alloc(size_t(std::max<int64_t>(so, 1)) * 4, st);
-    ddesc.alloc(std::max<size_t>(size_t(nb) * sizeof(SvdBlockDesc), 16), st);
-    if (nb)
-        TN_CUDA(cudaMemcpyAsync(ddesc.p, R.desc.data(), nb * sizeof(SvdBlockDesc),
+    // blocks with more than ctx->svd_big_n columns (after orienting m >= n) go to the multi-SM
+    // pipeline, the others to the one-CTA-per-block kernel
+    std::vector<SvdBlockDesc> small, big;
+    int maxn_small = 1;
+    for (const auto& d : R.desc) {
+        if (d.n > ctx->svd_big_n && d.n <= bsvd_max_n() && bsvd_panel_width(d.m) > 0) {
+            big.push_back(d);
+        } else {
+            small.push_back(d);
+            maxn_small = std::max(maxn_small, d.n);
+        }
+    }
+    const int nsm_blocks = (int)small.size();
+    ddesc.alloc(std::max<size_t>(size_t(nsm_blocks) * sizeof(SvdBlockDesc), 16), st);
+    if (nsm_blocks)
+        TN_CUDA(cudaMemcpyAsync(ddesc.p, small.data(), nsm_blocks * sizeof(SvdBlockDesc),
                                 cudaMemcpyHostToDevice, st));
     static const bool dbg = std::getenv("TENNET_DEBUG_SVD") != nullptr;
     DevBuf dsw;
-    const size_t clk_off = size_t((nb + 1) & ~1) * 4;  // 8-byte aligned clock area
-    if (dbg) dsw.alloc(clk_off + size_t(std::max(nb, 1)) * 8 * 8, st);
+    const size_t clk_off = size_t((nsm_blocks + 1) & ~1) * 4;  // 8-byte aligned clock area
+    if (dbg) dsw.alloc(clk_off + size_t(std::max(nsm_blocks, 1)) * 8 * 8, st);
     const int e0 = ctx->timer.mark();
-    launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nb, maxn, src, dX.d(), dW.d(), dV.d(), dP.d(),
-                      dS.d(), dPerm.as<int>(), dbg ? dsw.as<int>() : nullptr, st);
+    launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nsm_blocks, maxn_small, src, dX.d(), dW.d(),
+                      dV.d(), dP.d(), dS.d(), dPerm.as<int>(), dbg ? dsw.as<int>() : nullptr, st);
+    BsvdStats bst;
+    big_block_svd(ctx, ctx->bsvd, big, src, dW.d(), dV.d(), dS.d(), dPerm.as<int>(), &bst);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
-    if (dbg && nb) {
-        std::vector<int> sw(nb);
-        std::vector<long long> ck(size_t(nb) * 8);
-        TN_CUDA(cudaMemcpyAsync(sw.data(), dsw.p, nb * 4, cudaMemcpyDeviceToHost, st));
+    ctx->svd_stats.gemm_flops += bst.gemm_flops;
+    ctx->svd_stats.jacobi_flops += bst.jacobi_flops;
+    ctx->svd_stats.sweeps32 = std::max(ctx->svd_stats.sweeps32, bst.sweeps32);
+    ctx->svd_stats.sweeps_df = std::max(ctx->svd_stats.sweeps_df, bst.sweeps_df);
+    if (dbg && nsm_blocks) {
+        std::vector<int> sw(nsm_blocks);
+        std::vector<long long> ck(size_t(nsm_blocks) * 8);
+        TN_CUDA(cudaMemcpyAsync(sw.data(), dsw.p, nsm_blocks * 4, cudaMemcpyDeviceToHost, st));
         TN_CUDA(cudaMemcpyAsync(ck.data(), static_cast<char*>(dsw.p) + clk_off, ck.size() * 8,
                                 cudaMemcpyDeviceToHost, st));
         TN_CUDA(cudaStreamSynchronize(st));
-        for (int b = 0; b < nb; ++b) {
+        for (int b = 0; b < nsm_blocks; ++b) {
             const long long* c = &ck[size_t(b) * 8];
             std::fprintf(stderr,
                          "svd block %d: %dx%d sweeps fp32=%d fp64=%d kcycles qr=%lld fp32=%lld "
                          "gs=%lld y=%lld polish=%lld norms=%lld qv=%lld\n",
-                         b, R.desc[b].m, R.desc[b].n, sw[b] >> 16, sw[b] & 0xffff, (c[1] - c[0]) / 1000,
+                         b, small[b].m, small[b].n, sw[b] >> 16, sw[b] & 0xffff, (c[1] - c[0]) / 1000,
                          (c[2] - c[1]) / 1000, (c[3] - c[2]) / 1000, (c[4] - c[3]) / 1000,
                          (c[5] - c[4]) / 1000, (c[6] - c[5]) / 1000, (c[7] - c[6]) / 1000);
         }
+    }
+    if (dbg && !big.empty()) {
+        int mx = 0;
+        for (const auto& d : big) mx = std::max(mx, d.n);
+        std::fprintf(stderr, "svd big blocks: %d (largest n %d) sweeps fp32=%d df=%d\n",
+                     (int)big.size(), mx, bst.sweeps32, bst.sweeps_df);
     }
     R.S.resize(size_t(so));
     if (so)
         TN_CUDA(cudaMemcpyAsync(R.S.data(), dS.p, size_t(so) * 8, cudaMemcpyDeviceToHost, st));
     sync(ctx);
+    if (!big.empty()) check_device_error(ctx);
 }
 
 struct TruncDecision {
@@ -1461,7 +1488,7 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     form_phi(env, p, P.ph, env->vecA.d());
     auto apply2 = [&](const double* x, double* y) { heff_apply(env, P, x, y); };
     if (!time_step) {
-        EigOut eo = lanczos_lowest(env, P, env->vecA.d(), env->vecB.d(), prm);
+        EigOut eo = lanczos_lowest(env, apply2, n, env->vecA.d(), env->vecB.d(), prm);
         if (prm->check_convergence && eo.converged < 1)
             throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
         res->energy = eo.energy;
@@ -1509,6 +1536,194 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         env->rpos = std::max(env->rpos, p1);
         env->hp_pos = -1;
     }
+    if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
+}
+
+// halfsweep_done (TenNetLib src/mps/update_site.jl:13-23), 0-based, nsite = 1
+bool halfsweep_done1(int N, int pos, int ortho) {
+    return (pos == 0 && ortho == TN_ORTHO_RIGHT) || (pos == N - 1 && ortho == TN_ORTHO_LEFT);
+}
+
+// _update_one_site! (TenNetLib src/mps/update_site.jl:94-190) with the eigensolver and no
+// noise: solve the one-site problem at pos; unless the half sweep is done, split the new
+// tensor by the block SVD with ITensors truncation, keep U at pos (a left isometry for
+// ortho "left", a right one for "right") and multiply S V (resp. U S) into the next site.
+void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
+                     tn_update_result* res, std::vector<double>& eigs) {
+    check_params(prm);
+    tn_mps* psi = env->psi.get();
+    const int N = psi->N;
+    TN_REQUIRE(p >= 0 && p < N, "site position out of range");
+    TN_REQUIRE(psi->center == p, "one-site update: the orthogonality center must be at pos");
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    position(env, p, 1);
+    Heff1Plan& P1 = heff1_plan(env);
+    const int64_t n1 = P1.lay.size;
+    env->vecC.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
+    env->vecD.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
+    tn_site& site = psi->sites[p];
+    const Link lk = psi->links[p];
+    const Link rk = psi->links[p + 1];
+    if (site.lay.layout == RG)
+        TN_CUDA(cudaMemcpyAsync(env->vecC.p, site.buf.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
+    else
+        regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk);
+    auto apply1 = [&](const double* x, double* y) { heff1_apply(env, P1, x, y); };
+    EigOut eo = lanczos_lowest(env, apply1, n1, env->vecC.d(), env->vecD.d(), prm);
+    if (prm->check_convergence && eo.converged < 1)
+        throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
+    res->energy = eo.energy;
+    res->matvecs = eo.matvecs;
+    res->converged = eo.converged;
+    res->truncerr = 0.0;
+    eigs.clear();
+    // the solver's vector is normalised (normalize!(phi) is then the identity)
+    if (halfsweep_done1(N, p, ortho)) {
+        if (site.lay.layout == RG)
+            TN_CUDA(cudaMemcpyAsync(site.buf.p, env->vecD.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
+        else
+            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk);
+        env->lpos = std::min(env->lpos, p);
+        env->rpos = std::max(env->rpos, p);
+        env->h1p_pos = -1;
+        env->hp_pos = -1;
+        res->newdim = (ortho == TN_ORTHO_LEFT ? rk : lk).total();
+        res->neigs = 0;
+        if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
+        return;
+    }
+    const bool left = ortho == TN_ORTHO_LEFT;
+    // SVD blocks: per right sector (LG grouping) for "left", per left sector (RG) for "right"
+    SiteLayout sv_lay = left ? make_site_layout(LG, lk, rk, psi->pq) : P1.lay;
+    const double* phi = env->vecD.d();
+    if (left) {
+        regroup(ctx, P1.lay, env->vecD.d(), sv_lay, env->vecC.d(), lk, rk);
+        phi = env->vecC.d();
+    }
+    SvdResult R;
+    block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm, env->desc,
+              sv_lay.rows, sv_lay.cols, sv_lay.off, phi, R);
+    TruncDecision D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
+    const Link& olink = left ? rk : lk;  // the link that is truncated
+    Link nl;
+    std::vector<int> osec;  // sector of the old link of each kept block
+    for (int b = 0; b < sv_lay.nblk(); ++b)
+        if (D.kept[b] > 0) {
+            const int sec = b;  // LG blocks follow the right link's sectors, RG the left's
+            nl.q.push_back(olink.q[sec]);
+            nl.dim.push_back(D.kept[b]);
+            osec.push_back(sec);
+        }
+    tn_site here;
+    here.lay = left ? make_site_layout(LG, lk, nl, psi->pq) : make_site_layout(RG, nl, rk, psi->pq);
+    here.buf.alloc(size_t(std::max<int64_t>(here.lay.size, 1)) * 8, st);
+    // bond matrix per kept sector: S V^T (k x D) for "left", U S (D x k) for "right"
+    std::vector<int64_t> moff;
+    int64_t msize = 0;
+    for (size_t j = 0; j < osec.size(); ++j) {
+        moff.push_back(msize);
+        msize += int64_t(nl.dim[j]) * olink.dim[osec[j]];
+    }
+    env->t1.alloc(size_t(std::max<int64_t>(msize, 1)) * 8, st);
+    std::vector<ExtractDesc> ed;
+    for (int b = 0, j = 0; b < sv_lay.nblk(); ++b) {
+        if (D.kept[b] == 0) continue;
+        ExtractDesc e{};
+        e.x_off = R.desc[b].x_off;
+        e.v_off = R.desc[b].v_off;
+        e.s_off = R.desc[b].s_off;
+        e.rows = sv_lay.rows[b];
+        e.cols = sv_lay.cols[b];
+        e.n = R.desc[b].n;
+        e.trans = R.desc[b].trans;
+        e.k = D.kept[b];
+        if (left) {
+            TN_REQUIRE(here.lay.rows[j] == sv_lay.rows[b], "internal: one-site SVD layout mismatch");
+            e.left_off = here.lay.off[j];
+            e.right_off = moff[j];
+        } else {
+            TN_REQUIRE(here.lay.cols[j] == sv_lay.cols[b], "internal: one-site SVD layout mismatch");
+            e.left_off = moff[j];
+            e.right_off = here.lay.off[j];
+        }
+        ed.push_back(e);
+        ++j;
+    }
+    env->desc2.alloc(std::max<size_t>(ed.size() * sizeof(ExtractDesc), 16), st);
+    TN_CUDA(cudaMemcpyAsync(env->desc2.p, ed.data(), ed.size() * sizeof(ExtractDesc),
+                            cudaMemcpyHostToDevice, st));
+    const double inv = (prm->normalize && D.norm > 0) ? 1.0 / D.norm : 1.0;
+    const int e0 = ctx->timer.mark();
+    // "left": U stays (ortho 0), S V^T to the bond matrix; "right": V^T stays (ortho 1)
+    if (left)
+        launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(), env->svdV.d(),
+                           env->svdS.d(), env->svdPerm.as<int>(), here.buf.d(), env->t1.d(),
+                           TN_ORTHO_LEFT, inv, st);
+    else
+        launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(), env->svdV.d(),
+                           env->svdS.d(), env->svdPerm.as<int>(), env->t1.d(), here.buf.d(),
+                           TN_ORTHO_RIGHT, inv, st);
+    ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    // next site: RG (blocks per left sector) for "left", LG (per right sector) for "right"
+    const int q = left ? p + 1 : p - 1;
+    tn_site& nxt = psi->sites[q];
+    const Link& qa = psi->links[q];
+    const Link& qb = psi->links[q + 1];
+    SiteLayout nlay_old = make_site_layout(left ? RG : LG, qa, qb, psi->pq);
+    DevBuf oldbuf;
+    const double* oldp = nxt.buf.d();
+    if (nxt.lay.layout != nlay_old.layout) {
+        oldbuf.alloc(size_t(std::max<int64_t>(nlay_old.size, 1)) * 8, st);
+        regroup(ctx, nxt.lay, nxt.buf.d(), nlay_old, oldbuf.d(), qa, qb);
+        oldp = oldbuf.d();
+    }
+    tn_site nnew;
+    nnew.lay = left ? make_site_layout(RG, nl, qb, psi->pq) : make_site_layout(LG, qa, nl, psi->pq);
+    nnew.buf.alloc(size_t(std::max<int64_t>(nnew.lay.size, 1)) * 8, st);
+    GemmPlan g;
+    for (size_t j = 0; j < osec.size(); ++j) {
+        const int sec = osec[j], k = nl.dim[j], D0 = olink.dim[sec];
+        if (left) {
+            // new (k x cols) = M (k x D0) * old (D0 x cols)
+            const int cols = nlay_old.cols[sec];
+            if (cols == 0) continue;
+            g.add_task(S_Y, nnew.lay.off[j], k, cols, k);
+            g.add_seg(S_X, moff[j], k, 0, S_A, nlay_old.off[sec], D0, 0, D0);
+        } else {
+            // new (rows x k) = old (rows x D0) * M (D0 x k)
+            const int rows = nlay_old.rows[sec];
+            if (rows == 0) continue;
+            g.add_task(S_Y, nnew.lay.off[j], rows, k, rows);
+            g.add_seg(S_A, nlay_old.off[sec], rows, 0, S_X, moff[j], D0, 0, D0);
+        }
+    }
+    if (!g.tasks.empty()) {
+        g.finalize(st);
+        Bases bs{};
+        bs.p[S_X] = env->t1.d();
+        bs.p[S_A] = const_cast<double*>(oldp);
+        bs.p[S_Y] = nnew.buf.d();
+        const int e1 = ctx->timer.mark();
+        launch_gemm_f64(g, bs, st);  // the small bond matrix is multiplied in FP64
+        ctx->timer.add(T_SVD, e1, ctx->timer.mark());
+    }
+    psi->sites[p] = std::move(here);
+    psi->sites[q] = std::move(nnew);
+    if (left)
+        psi->links[p + 1] = nl;
+    else
+        psi->links[p] = nl;
+    psi->center = q;
+    env->lpos = std::min(env->lpos, std::min(p, q));
+    env->rpos = std::max(env->rpos, std::max(p, q));
+    env->hp_pos = -1;
+    env->h1p_pos = -1;
+    sync(ctx);  // oldbuf and the plan's buffers are released after the launches
+    res->truncerr = D.truncerr;
+    res->newdim = nl.total();
+    eigs = D.eigs;
+    res->neigs = (int)eigs.size();
     if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
 }
 
@@ -1710,8 +1925,8 @@ int tn_ctx_create(int device, tn_ctx** out) {
         TN_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         c->timer.s = c->stream;
         c->nsm = pr.multiProcessorCount;
-        c->err.alloc(sizeof(int), c->stream);
-        TN_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+        c->err.alloc(4 * sizeof(int), c->stream);  // [0] error flag, [1] injected wait timeout
+        TN_CUDA(cudaMemsetAsync(c->err.p, 0, 4 * sizeof(int), c->stream));
         TN_CUDA(cudaStreamSynchronize(c->stream));
         cudaMemPool_t mp;
         TN_CUDA(cudaDeviceGetDefaultMemPool(&mp, device));
@@ -1740,6 +1955,25 @@ int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices) {
                    "split precision needs 4..7 slices");
         ctx->prec = mode;
         ctx->slices = slices;
+    });
+}
+
+int tn_ctx_inject_wait_timeout(tn_ctx* ctx, int kernel) {
+    return guarded([&] {
+        TN_REQUIRE(ctx, "null context");
+        TN_REQUIRE(kernel >= 1 && kernel <= 3, "kernel must be 1, 2 or 3");
+        const int code = kernel;
+        TN_CUDA(cudaMemcpyAsync(ctx->err.as<int>() + 1, &code, sizeof(int), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        TN_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int tn_ctx_set_svd_split(tn_ctx* ctx, int ncols) {
+    return guarded([&] {
+        TN_REQUIRE(ctx, "null context");
+        TN_REQUIRE(ncols >= 0, "the column threshold must be >= 0");
+        ctx->svd_big_n = ncols;
     });
 }
 
@@ -1998,12 +2232,22 @@ int tn_env_product(tn_env* env, const double* v, double* out, int64_t n) {
 
 int tn_env_update_position(tn_env* env, int pos, int ortho, const tn_update_params* p,
                            tn_update_result* res, double* eigs, int eigs_cap) {
+    return tn_env_update_position_nsite(env, pos, 2, ortho, p, res, eigs, eigs_cap);
+}
+
+int tn_env_update_position_nsite(tn_env* env, int pos, int nsite, int ortho,
+                                 const tn_update_params* p, tn_update_result* res, double* eigs,
+                                 int eigs_cap) {
     return guarded([&] {
         TN_REQUIRE(env && res, "null argument");
         TN_REQUIRE(ortho == TN_ORTHO_LEFT || ortho == TN_ORTHO_RIGHT, "ortho must be left or right");
+        TN_REQUIRE(nsite == 1 || nsite == 2, "nsite must be 1 or 2");
         std::vector<double> ev;
         *res = tn_update_result{};
-        update_two_site(env, pos, ortho, p, res, ev);
+        if (nsite == 2)
+            update_two_site(env, pos, ortho, p, res, ev);
+        else
+            update_one_site(env, pos, ortho, p, res, ev);
         if (eigs) {
             const int k = std::min<int>(eigs_cap, (int)ev.size());
             std::copy(ev.begin(), ev.begin() + k, eigs);
@@ -2019,7 +2263,7 @@ namespace {
 // fullsweep! (TenNetLib src/mps/sweep.jl:94-196) with the eigensolver (time_step null) or
 // the exponential solver at time_step with reverse steps (tdvpsweep!, src/mps/tdvp.jl:268)
 void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
-                int mid_cap, int32_t* n_mid_eigs, const double* time_step) {
+                int mid_cap, int32_t* n_mid_eigs, const double* time_step, int nsite = 2) {
     TN_REQUIRE(env && res, "null argument");
     check_params(p);
     tn_mps* psi = env->psi.get();
@@ -2036,21 +2280,41 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     const int64_t kl0 = launch_count();
     const int64_t kb0 = krylov_bytes();
     *res = tn_sweep_result{};
+    ctx->svd_stats = BsvdStats{};
     const int es = ctx->timer.mark();
     double maxerr = 0.0, energy = NAN;
     std::vector<double> ev, mid;
-    for (int b = 0; b < N - 1; ++b) {
-        tn_update_result r{};
-        update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step);
-        energy = r.energy;
-        maxerr = std::max(maxerr, r.truncerr);
-    }
-    for (int b = N - 2; b >= 0; --b) {
-        tn_update_result r{};
-        update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step);
-        energy = r.energy;
-        maxerr = std::max(maxerr, r.truncerr);
-        if (b == N / 2 - 1) mid = ev;
+    if (nsite == 2) {
+        for (int b = 0; b < N - 1; ++b) {
+            tn_update_result r{};
+            update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+        }
+        for (int b = N - 2; b >= 0; --b) {
+            tn_update_result r{};
+            update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+            if (b == N / 2 - 1) mid = ev;
+        }
+    } else {
+        // one-site sweep (src/mps/sweep.jl:118-152 with nsite = 1): sites 1..N left, then
+        // N..1 right; lasteigs[bond] comes from the right-moving update at site bond + 1
+        TN_REQUIRE(!time_step, "one-site TDVP is not built");
+        for (int q = 0; q < N; ++q) {
+            tn_update_result r{};
+            update_one_site(env, q, TN_ORTHO_LEFT, p, &r, ev);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+        }
+        for (int q = N - 1; q >= 0; --q) {
+            tn_update_result r{};
+            update_one_site(env, q, TN_ORTHO_RIGHT, p, &r, ev);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+            if (q == N / 2) mid = ev;
+        }
     }
     ctx->timer.add(T_SWEEP, es, ctx->timer.mark());
     sync(ctx);
@@ -2073,6 +2337,10 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     res->gemm_launches = env->gemm_launches - gl0;
     res->kernel_launches = launch_count() - kl0;
     res->krylov_bytes = double(krylov_bytes() - kb0);
+    res->svd_gemm_flops = ctx->svd_stats.gemm_flops;
+    res->svd_jacobi_flops = ctx->svd_stats.jacobi_flops;
+    res->svd_sweeps32 = ctx->svd_stats.sweeps32;
+    res->svd_sweeps_df = ctx->svd_stats.sweeps_df;
     if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
     if (mid_eigs) {
         const int k = std::min<int>(mid_cap, (int)mid.size());
@@ -2086,6 +2354,15 @@ extern "C" {
 int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res,
                      double* mid_eigs, int mid_cap, int32_t* n_mid_eigs) {
     return guarded([&] { full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, nullptr); });
+}
+
+int tn_env_fullsweep_nsite(tn_env* env, int nsite, const tn_update_params* p,
+                           tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                           int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(nsite == 1 || nsite == 2, "nsite must be 1 or 2");
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, nullptr, nsite);
+    });
 }
 
 int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_sweep_result* res,

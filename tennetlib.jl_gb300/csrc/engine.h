@@ -30,6 +30,17 @@ struct EventTimer {
 
 struct Scratch;  // fixed-capacity device scratch used by the allocation-free entry points
 
+// work buffers of the multi-SM block SVD (bsvd.cpp), kept by the context between bonds
+struct BsvdWork {
+    DevBuf arena, blks, flags, bars, sweeps;
+    DevBuf bjd[2];
+};
+struct BsvdStats {
+    double gemm_flops = 0;    // algorithmic flops of the SVD's grouped GEMMs
+    double jacobi_flops = 0;  // flops of the Jacobi rotations (dots and column updates)
+    int sweeps32 = 0, sweeps_df = 0;
+};
+
 }  // namespace tn
 
 struct tn_ctx;
@@ -43,6 +54,10 @@ void run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs);
 void check_device_error_public(tn_ctx* ctx);
 int svd_truncate_dense(tn_ctx* ctx, const double* A, int m, int n, int maxdim, int mindim,
                        double cutoff, double* U, double* SVt, double* truncerr);
+// SVD of large charge blocks on the whole GPU (bsvd.cpp): outputs as svd_qrj_kernel's
+void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& blocks,
+                   const double* src, double* QV, double* PY, double* S, int* perm,
+                   BsvdStats* stats);
 }  // namespace tn
 
 struct tn_ctx {
@@ -53,6 +68,9 @@ struct tn_ctx {
     int slices = 5;
     tn::EventTimer timer;
     tn::DevBuf err;  // device error word of bounded waits (0 = ok)
+    int svd_big_n = 96;  // charge blocks with more columns take the multi-SM SVD
+    tn::BsvdWork bsvd;
+    tn::BsvdStats svd_stats;  // accumulated by the block SVDs (read and reset by the sweeps)
 };
 
 struct tn_mpo {

@@ -420,6 +420,9 @@ split_gemm_kernel(const SplitItem* __restrict__ items, int nitems,
     if (warp == 0) {
         // ---------------- producer ----------------
         if (lane == 0) {
+            // test hook (tn_ctx_inject_wait_timeout, code 1): CTA 0 withholds the copies of its
+            // first stage, so that the MMA warp's wait on it runs out and every role drains
+            const bool withhold = blockIdx.x == 0 && atomicCAS(err + 1, 1, 0) == 1;
             uint32_t g = 0;  // global stage counter
             for (int it = blockIdx.x; it < nitems && !*serr; it += gridDim.x) {
                 const SplitItem item = items[it];
@@ -429,6 +432,7 @@ split_gemm_kernel(const SplitItem* __restrict__ items, int nitems,
                         const int st = g % NST;
                         const uint32_t ph = (g / NST) & 1;
                         if (!mbar_wait(&sh->empty[st], ph ^ 1, err, serr)) break;
+                        if (withhold && g == 0) continue;
                         uint8_t* dst = ring + st * STAGE;
                         mbar_expect_tx(&sh->full[st], STAGE);
                         const int64_t ao = tk.a_off + (int64_t(item.mt) * tk.nkt + kt) * slices * A_TILE +

@@ -440,9 +440,12 @@ hh_panel_coop_kernel(const HhDesc* __restrict__ descs, int ninst, int p0, int* e
     if (inst < 0) return;
     const HhDesc& D = descs[inst];
     if (p0 >= D.kmin) return;  // uniform over the instance's CTAs
-    if (threadIdx.x == 0) s_fail = 0;
-    __syncthreads();
     const int G = D.ncta, g = int(blockIdx.x) - D.cta0;
+    // test hook (tn_ctx_inject_wait_timeout, code 3): the first CTA of the first instance leaves
+    // before its first barrier, so that the other CTAs' barrier waits run out
+    if (threadIdx.x == 0) s_fail = (inst == 0 && g == 0 && atomicCAS(err + 1, 3, 0) == 3) ? 1 : 0;
+    __syncthreads();
+    if (s_fail) return;
     const int pe = (p0 + HH_B) < D.kmin ? (p0 + HH_B) : D.kmin;
     const int64_t m = D.m;
     const int64_t chunk = (m - p0 + G - 1) / G;
@@ -775,16 +778,20 @@ void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, i
     count_launch(2);
 }
 
+// co-resident CTAs of the cooperative panel kernel on the current device (cached per device)
 int hh_coop_capacity() {
-    static int cap = -1;
-    if (cap < 0) {
-        int dev = 0, nsm = 0, per = 0;
-        TN_CUDA(cudaGetDevice(&dev));
+    constexpr int MAXDEV = 64;
+    static int cap[MAXDEV] = {};
+    int dev = 0;
+    TN_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= MAXDEV) throw Error(-1, "device index out of range");
+    if (cap[dev] <= 0) {
+        int nsm = 0, per = 0;
         TN_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         TN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, hh_panel_coop_kernel, BT, 0));
-        cap = nsm * per;
+        cap[dev] = nsm * per;
     }
-    return cap;
+    return cap[dev];
 }
 
 void launch_hh_panel_coop(const HhDesc* d, int ninst, int nctas, int p0, int* err,

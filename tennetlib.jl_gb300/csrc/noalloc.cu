@@ -14,11 +14,15 @@
 // Footprint: 4 x 4 MiB work matrices + 256 KiB permutation + descriptors, about 16.3 MiB.
 //
 // All calls share the one array and it keeps the previous call's contents; nothing in it
-// has to start at zero (every word the kernel reads it has written earlier in the same
+// has to start at zero (every word the kernels read they have written earlier in the same
 // call).  Two calls whose work overlaps on the GPU (different streams, or different host
 // threads without ordering) race on the array: the caller must serialise them.
-// The first call on a device looks up the array's device address (cudaGetSymbolAddress)
-// with that device current and caches it; make that first call before any stream capture.
+// Set-up: the first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current and keeps it for the process; make that
+// first call before any stream capture.  A cudaDeviceReset of the device discards the
+// module and with it the address: the entry point must not be called on that device again.
+// The block dimensions reach the device as kernel arguments (no host staging buffer is
+// read after the call returns), and the caller's current device is restored on return.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -46,10 +50,42 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_scratch;
 
+// Block dimensions passed by value (8 KiB of kernel arguments).
+struct BlockDims {
+    int32_t rows[MAX_BLOCKS];
+    int32_t cols[MAX_BLOCKS];
+    int32_t nblocks;
+};
+
+// Writes the SVD descriptors of the blocks into the scratch array: inputs packed back to
+// back, work matrices packed like the inputs, n x n matrices packed back to back.
+__global__ void noalloc_desc_kernel(const BlockDims dims, NoAllocScratch* sc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t elems = 0, vo = 0, so = 0;
+    for (int b = 0; b < dims.nblocks; ++b) {
+        const int r = dims.rows[b], c = dims.cols[b];
+        SvdBlockDesc d{};
+        d.src_off = elems;
+        d.x_off = elems;
+        d.v_off = vo;
+        d.s_off = so;
+        d.rows = r;
+        d.cols = c;
+        d.trans = r < c ? 1 : 0;
+        d.m = r > c ? r : c;
+        d.n = r < c ? r : c;
+        sc->desc[b] = d;
+        elems += int64_t(r) * c;
+        vo += int64_t(d.n) * d.n;
+        so += d.n;
+    }
+}
+
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
 NoAllocScratch* g_addr[MAX_DEVICES] = {nullptr};
 
+// set-up, once per device, with that device current
 NoAllocScratch* scratch_for(int device) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_addr[device]) {
@@ -60,7 +96,19 @@ NoAllocScratch* scratch_for(int device) {
     return g_addr[device];
 }
 
-thread_local SvdBlockDesc t_desc[MAX_BLOCKS];
+// makes `device` current for the lifetime of the guard and restores the caller's device
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int device) {
+        TN_CUDA(cudaGetDevice(&prev));
+        if (prev != device) TN_CUDA(cudaSetDevice(device));
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 thread_local std::string t_err;
 
 }  // namespace
@@ -75,42 +123,35 @@ extern "C" int tn_block_svals_noalloc(int device, const double* blocks, int nblo
         if (nblocks < 1 || nblocks > MAX_BLOCKS)
             throw Error(TN_E_INVALID, "tn_block_svals_noalloc: number of blocks must be in [1, 1024]");
         if (device < 0 || device >= MAX_DEVICES) throw Error(TN_E_INVALID, "device out of range");
+        int ndev = 0;
+        TN_CUDA(cudaGetDeviceCount(&ndev));
+        if (device >= ndev) throw Error(TN_E_INVALID, "device out of range");
+        BlockDims dims;
+        dims.nblocks = nblocks;
         int64_t elems = 0, nsv = 0;
         int maxn = 1;
         for (int b = 0; b < nblocks; ++b) {
             if (rows[b] < 1 || cols[b] < 1) throw Error(TN_E_INVALID, "block dimensions must be >= 1");
-            SvdBlockDesc& d = t_desc[b];
-            d = SvdBlockDesc{};
-            d.src_off = elems;
-            d.rows = rows[b];
-            d.cols = cols[b];
-            d.trans = rows[b] < cols[b] ? 1 : 0;
-            d.m = rows[b] > cols[b] ? rows[b] : cols[b];
-            d.n = rows[b] < cols[b] ? rows[b] : cols[b];
-            if (d.n > MAX_N)
+            const int n = rows[b] < cols[b] ? rows[b] : cols[b];
+            if (n > MAX_N)
                 throw Error(TN_E_INVALID, "tn_block_svals_noalloc: min(rows, cols) above 3000");
-            d.x_off = elems;   // m n per block, packed like the input
-            d.v_off = 0;       // set below
-            d.s_off = nsv;
+            dims.rows[b] = rows[b];
+            dims.cols[b] = cols[b];
             elems += int64_t(rows[b]) * cols[b];
-            nsv += d.n;
-            if (d.n > maxn) maxn = d.n;
+            nsv += n;
+            if (n > maxn) maxn = n;
         }
         if (elems > MAX_ELEMS)
             throw Error(TN_E_INVALID, "tn_block_svals_noalloc: sum of rows*cols above 524288");
         if (nsv > MAX_SVALS)
             throw Error(TN_E_INVALID, "tn_block_svals_noalloc: sum of min(rows, cols) above 65536");
-        int64_t vo = 0;
-        for (int b = 0; b < nblocks; ++b) {
-            t_desc[b].v_off = vo;
-            vo += int64_t(t_desc[b].n) * t_desc[b].n;  // <= sum m n
-        }
-        TN_CUDA(cudaSetDevice(device));
+        DeviceGuard guard(device);
         NoAllocScratch* sc = scratch_for(device);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        TN_CUDA(cudaMemcpyAsync(sc->desc, t_desc, size_t(nblocks) * sizeof(SvdBlockDesc),
-                                cudaMemcpyHostToDevice, st));
-        // the kernel writes the sorted singular values straight into the caller's buffer
+        noalloc_desc_kernel<<<1, 32, 0, st>>>(dims, sc);
+        TN_CUDA(cudaGetLastError());
+        count_launch();
+        // the SVD kernel writes the sorted singular values straight into the caller's buffer
         launch_svd_jacobi(sc->desc, nblocks, maxn, blocks, sc->X, sc->W, sc->V, sc->P, svals,
                           sc->perm, nullptr, st);
         return TN_OK;

@@ -285,6 +285,54 @@ void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, const double* s
                        double* W, double* V, double* P, double* S, int* perm, int* sweeps_out,
                        cudaStream_t s);
 
+// ------------------------------------------------------------------------------------
+// multi-SM SVD of large charge blocks (kernels_bsvd.cu, host driver bsvd.cpp):
+// blocked Householder QR (one-CTA panels, grouped-GEMM trailing updates), one-sided Jacobi
+// on R^T by rounds of column-block pairs spread over many CTAs (FP32 presolve, Newton-Schulz
+// re-orthonormalisation, double-float polish), Q applied by grouped GEMMs.  All offsets are
+// in doubles from the start of one work arena.
+// ------------------------------------------------------------------------------------
+struct BsvdBlk {
+    int64_t src_off;          // block in the source buffer
+    int64_t xq;               // QR work matrix, m x n (ld m)
+    int64_t vp;               // explicit reflectors of panel p at vp + p * m * pw, (m - p0) x w
+    int64_t tm;               // panel p: -T^T at tm + p * 2 pw^2, -T after it (w x w, ld w)
+    int64_t rt64, v64, g64, v64b, y64;  // n x n FP64
+    int64_t r32, v32;         // n x n FP32 (float arrays)
+    int64_t ydf, vdf;         // n x n double-float
+    int64_t x_off, v_off, s_off;  // outputs: QV (m x n) in the QV buffer, PY (n x n), S / perm
+    int32_t rows, cols, trans, m, n, pad;
+};
+struct BjDesc {               // one matrix of the cooperative one-sided Jacobi
+    void* X;                  // n x n, column-major (float or double-float)
+    void* V;                  // n x n rotations
+    int32_t n, nb, cta0, ncta;
+    unsigned* bar;            // barrier counter of the CTA group
+    int* flags;               // [0..3) rotated flags, [3..6) largest rotated cosine (float bits)
+    int* sweeps;              // sweeps run
+};
+// panel width for a largest row count m (the panel lives in shared memory)
+int bsvd_panel_width(int mmax);
+// largest n the Jacobi kernels accept
+int bsvd_max_n();
+void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* src, double* ar,
+                        cudaStream_t s);
+void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int mmax, double* ar,
+                       cudaStream_t s);
+// op 0: R^T (FP32 and FP64) and V32 = I; 1: V64 = V32; 2: G <- 1.5 I - 0.5 G (g64);
+// 3: Ydf, Vdf from y64, v64
+void launch_bsvd_elem(const BsvdBlk* d, int nb, int64_t nnmax, int op, double* ar, cudaStream_t s);
+// cooperative Jacobi sweeps (precision 0: FP32 presolve, 1: double-float polish); returns
+// the CTAs used per matrix in descs (cta0 / ncta filled by the caller)
+void launch_bsvd_jacobi(const BjDesc* d, int nd, int nctas, int maxn, int precision, int* err,
+                        cudaStream_t s);
+int bsvd_jacobi_capacity(int maxn, int precision);
+// columns per block of the Jacobi kernel for the largest n (precision 0 FP32, 1 double-float)
+int bsvd_jacobi_block(int maxn, int precision);
+// singular values (sorted, with the permutation), PY = Y and QV = [V; 0]
+void launch_bsvd_finish(const BsvdBlk* d, int nb, double* ar, double* qv, double* py, double* S,
+                        int* perm, cudaStream_t s);
+
 // extraction of truncated factors into site tensors
 struct ExtractDesc {
     int64_t x_off, v_off, s_off;

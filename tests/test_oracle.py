@@ -209,3 +209,59 @@ def test_real_time_tdvp_quench_matches_exact():
         sz = O.expect_local(env.psi, np.diag([0.5, -0.5]))
         assert np.abs(sz - np.array(ref)).max() < 1e-6
         assert abs(O.inner(env.psi, env.psi) - 1.0) < 1e-12
+
+
+def test_oracle_one_site_sweeps_reach_ed():
+    """fullsweep! with nsite = 1 (src/mps/sweep.jl:94-196, _update_one_site! of
+    src/mps/update_site.jl:94-190): after a two-site warm-up the one-site sweeps keep the
+    bond dimensions, lower the energy monotonically, keep every site but the centre an
+    isometry, and at full bond dimension (N = 8, chi = 16) reach the exact ground energy."""
+    N = 8
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+    env = O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H)
+    sw = O.SweepData()
+    for md in (4, 16):
+        O.fullsweep(env, sw, md, 1e-14, 1, 4, 2, 1e-14)
+    chi = env.psi.maxlinkdim()
+    for _ in range(3):
+        O.fullsweep1(env, sw, 16, 1e-14, 1, 4, 2, 1e-14)
+        assert sw.energy[-1] <= sw.energy[-2] + 1e-12
+        assert env.psi.maxlinkdim() == chi
+    for i in range(1, N):
+        A = env.psi.A[i].reshape(env.psi.A[i].shape[0], -1)
+        assert np.allclose(A @ A.T, np.eye(A.shape[0]), atol=1e-12)
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
+    assert abs(sw.energy[-1] - gold["heisenberg_chain"][str(N)]) < 1e-10
+
+
+def test_checkpoint_arrays_round_trip():
+    """save_checkpoint / load_checkpoint host format: charge blocks, links, centre and the
+    sweep history come back unchanged (CPU only: the arrays, not the device MPS)."""
+    import __graft_entry__ as g
+    tn = g.load_package()
+    rng = np.random.default_rng(3)
+    N = 6
+    links = [np.array([0])] + [np.repeat(np.array([q for q in range(-i, i + 1, 2)
+                                                   if abs(q) <= N - i]),
+                                         rng.integers(1, 4, size=len([q for q in range(-i, i + 1, 2)
+                                                                      if abs(q) <= N - i])))
+                               for i in range(1, N)] + [np.array([0])]
+    pq = O.SPIN_HALF_Q
+    tensors = [rng.standard_normal((len(links[i]), 2, len(links[i + 1])))
+               * O.qn_mask3(links[i], pq, links[i + 1]) for i in range(N)]
+    sw = tn.SweepData(sweepcount=2, maxchi=[4, 8], energy=[-1.0, -1.5], entropy=[0.1, 0.2],
+                      maxtruncerr=[1e-9, 1e-10], lasteigs=[np.array([0.7, 0.3]), np.array([1.0])],
+                      stats=[{"sweep_ms": 1.0}])
+    z = tn.checkpoint_arrays(tensors, links, pq, 0, sw)
+    t2, l2, pq2, c2, sw2 = tn.arrays_from_checkpoint(z)
+    assert c2 == 0 and np.array_equal(pq2, pq)
+    for a, b in zip(tensors, t2):
+        assert np.array_equal(a, b)
+    for a, b in zip(links, l2):
+        assert np.array_equal(a, b)
+    assert sw2.sweepcount == 2 and sw2.maxchi == [4, 8] and sw2.energy == [-1.0, -1.5]
+    assert all(np.array_equal(a, b) for a, b in zip(sw.lasteigs, sw2.lasteigs))
+    assert sw2.stats == [{"sweep_ms": 1.0}]
+    # only the allowed entries are stored
+    assert sum(v.size for k, v in z.items() if k.startswith("blocks_")) < sum(t.size for t in tensors)

@@ -3,8 +3,10 @@
 It is meant for callers that cannot let the library allocate device memory: their
 inputs and outputs already live on the device, and the library works in a fixed
 file-scope device array.  The test calls it through the C ABI on device buffers and
-compares with tn_svd_truncate (which copies host data and allocates its own work space),
-on two consecutive calls with different blocks, so that a stale work array would show.
+compares with tn_svd_truncate (which copies host data and allocates its own work space)
+and with LAPACK, on two consecutive calls with different blocks, so that a stale work
+array would show.  The second list holds a 300 x 200 block behind a small one: its
+Jacobi matrices do not fit shared memory and live at a nonzero offset of the array.
 """
 import ctypes as C
 
@@ -34,11 +36,13 @@ def _noalloc(tn, torch, blocks):
     nsv = int(np.minimum(rows, cols).sum())
     d_out = torch.full((nsv,), float("nan"), dtype=torch.float64, device="cuda:0")
     stream = torch.cuda.current_stream(0)
+    dev_before = torch.cuda.current_device()
     rc = lib.tn_block_svals_noalloc(0, C.c_void_p(d_in.data_ptr()), len(blocks),
                                     rows.ctypes.data_as(tn._lib.i32p),
                                     cols.ctypes.data_as(tn._lib.i32p),
                                     C.c_void_p(d_out.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert rc == 0, lib.tn_last_error()
+    assert torch.cuda.current_device() == dev_before
     stream.synchronize()
     sv = d_out.cpu().numpy()
     out, o = [], 0
@@ -56,13 +60,15 @@ def test_noalloc_matches_allocating_entry_point(tn):
     ctx = tn.Context(0)
     rng = np.random.default_rng(2024)
     for shapes in ([(40, 40), (12, 70), (90, 30), (1, 1), (7, 3)],
-                   [(64, 64), (33, 50), (5, 9)]):
+                   [(64, 64), (33, 50), (300, 200), (5, 9)]):
         blocks = _blocks(rng, shapes)
         got = _noalloc(tn, torch, blocks)
         _, ref, _ = tn.svd_truncate(blocks, maxdim=10**6, cutoff=0.0, ctx=ctx)
-        for g, r in zip(got, ref):
+        for b, g, r in zip(blocks, got, ref):
             # same tolerance as the block SVD parity tests: 1e-13 of the largest value
             assert np.allclose(g, r, rtol=0, atol=1e-13 * r[0])
+            lap = np.linalg.svd(b, compute_uv=False)
+            assert np.allclose(g, lap, rtol=0, atol=1e-13 * lap[0])
 
 
 def test_noalloc_rejects_oversize(tn):
