@@ -543,6 +543,7 @@ def run_j1j2(tn, local, args):
                      "lanczos_s": st["lanczos_ms"] / 1e3,
                      "svd_gemm_flops": st.get("svd_gemm_flops", 0.0),
                      "svd_jacobi_flops": st.get("svd_jacobi_flops", 0.0),
+                     "svd_sweeps_max": [st.get("svd_sweeps32", 0), st.get("svd_sweeps_df", 0)],
                      "energy": s.energy[-1], "maxlinkdim": s.maxchi[-1],
                      "maxtruncerr": s.maxtruncerr[-1]}
         final[prec] = e.getpsi()

@@ -61,7 +61,7 @@ typedef struct tn_update_params {
     double tol;                /* default 1e-14 */
     int32_t eager;             /* default 0 */
     int32_t check_convergence; /* default 0 */
-    double noise;              /* must be 0: the density-matrix noise term is not built */
+    double noise;              /* density-matrix perturbation (two-site updates; 0 = off) */
 } tn_update_params;
 
 typedef struct tn_update_result {

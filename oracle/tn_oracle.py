@@ -620,9 +620,87 @@ class StateEnvs:
         return heff2_apply(self.L[pos], self.H.W[pos], self.H.W[pos + 1], self.R[pos + 1], phi)
 
 
+def noise_factor(env: StateEnvs, pos):
+    """Noise tensors of ``noiseterm(P, phi, ortho)`` (ITensorMPS ProjMPO; TenNetLib's own
+    ProjCouplingModel version at src/mps/projcouplingmodel.jl:391-492 has the same form):
+    returns functions phi -> N with drho = N N^T on the rows (ortho "left", N indexed
+    [(l', s1'), (b, s2, r)]) or on the columns (ortho "right", [(s2', r'), (l, s1, b)]) of the
+    two-site matrix phi.reshape(Dl d, d Dr)."""
+    L, R = env.L[pos], env.R[pos + 1]
+    W1, W2 = env.H.W[pos], env.H.W[pos + 1]
+
+    def left(phi):
+        Dl, d1, d2, Dr = phi.shape
+        t = np.tensordot(L, phi, axes=([2], [0]))           # [l', a, s1, s2, r]
+        t = np.tensordot(t, W1, axes=([1, 2], [0, 3]))      # [l', s2, r, b, s1']
+        return t.transpose(0, 4, 3, 1, 2).reshape(Dl * d1, -1)
+
+    def right(phi):
+        Dl, d1, d2, Dr = phi.shape
+        t = np.tensordot(phi, W2, axes=([2], [3]))          # [l, s1, r, b, c, s2']
+        t = np.tensordot(t, R, axes=([2, 4], [2, 1]))       # [l, s1, b, s2', r']
+        return t.transpose(3, 4, 0, 1, 2).reshape(d2 * Dr, -1)
+
+    return left, right
+
+
+def split_two_site_noise(phi, Nmat, noise, ql, qs, qr, maxdim, mindim, cutoff, ortho,
+                         normalize=True):
+    """``replacebond!`` with ``eigen_perturbation = noise * noiseterm`` (ITensors
+    ``factorize_eigen``): per charge block the density matrix rho = M M^T + noise N N^T of the
+    kept side (rows for ortho "left", columns for "right") is diagonalised, its eigenvalues
+    truncated like S^2 (ITensors truncate!), the eigenvectors kept on that side and the other
+    factor is U^T M (resp. M V), normalised (ITensorMPS replacebond!)."""
+    Dl, d1, d2, Dr = phi.shape
+    M = phi.reshape(Dl * d1, d2 * Dr)
+    qrow = (ql[:, None] + qs[None, :]).reshape(-1)
+    qcol = (qr[None, :] - qs[:, None]).reshape(-1)
+    side = qrow if ortho == "left" else qcol
+    # every charge of the kept side: rho has blocks where only the noise term reaches, and
+    # those sectors may enter the new link (that is how the perturbation grows the basis)
+    charges = sorted(set(side.tolist()))
+    Ms = M if ortho == "left" else M.T
+    evs, vecs, idx = [], [], []
+    for m in charges:
+        ii = np.nonzero(side == m)[0]
+        rho = Ms[ii] @ Ms[ii].T + noise * (Nmat[ii] @ Nmat[ii].T)
+        w, U = np.linalg.eigh(0.5 * (rho + rho.T))
+        order = np.argsort(-w, kind="stable")
+        evs.append(np.maximum(w[order], 0.0))
+        vecs.append(U[:, order])
+        idx.append(ii)
+    P = np.sort(np.concatenate(evs))[::-1]
+    _, truncerr, docut = truncation_rule(P, maxdim, mindim, cutoff)
+    kept = [int(np.sum(e > docut)) for e in evs]
+    if sum(kept) == 0:
+        kept[int(np.argmax([e[0] if len(e) else -1 for e in evs]))] = 1
+    chi = sum(kept)
+    Ke = np.zeros((Ms.shape[0], chi))
+    qmid, eigs, off = [], [], 0
+    for m, ii, U, e, k in zip(charges, idx, vecs, evs, kept):
+        if k == 0:
+            continue
+        Ke[np.ix_(ii, range(off, off + k))] = U[:, :k]
+        qmid.extend([m] * k)
+        eigs.extend(e[:k])
+        off += k
+    other = Ke.T @ Ms                      # k x (other side)
+    if normalize:
+        other = other / np.linalg.norm(other)
+    if ortho == "left":
+        A = Ke.reshape(Dl, d1, chi)
+        B = other.reshape(chi, d2, Dr)
+    else:
+        A = other.T.reshape(Dl, d1, chi)
+        B = Ke.T.reshape(chi, d2, Dr)
+    spec = Spectrum(eigs=np.sort(np.array(eigs))[::-1], truncerr=truncerr)
+    return A, B, np.array(qmid, dtype=np.int64), spec
+
+
 def update_two_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdim, maxiter,
-                    tol, normalize=True):
-    """``_update_two_site!`` (``src/mps/update_site.jl:27-90``) for the eigensolver."""
+                    tol, normalize=True, noise=0.0):
+    """``_update_two_site!`` (``src/mps/update_site.jl:27-90``) for the eigensolver, with the
+    density-matrix noise term when noise > 0 (``:59-62``)."""
     psi = env.psi
     phi = np.tensordot(psi.A[pos], psi.A[pos + 1], axes=([2], [0]))
     env.position(pos, 2)
@@ -635,8 +713,15 @@ def update_two_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
     phi = vec.reshape(shape)
     if normalize:
         phi = phi / np.linalg.norm(phi)
-    A, B, qmid, spec = split_two_site(phi, psi.links[pos], psi.phys_q, psi.links[pos + 2],
-                                      maxdim, mindim, cutoff, ortho, normalize)
+    if abs(noise) > FLOAT64_THRESHOLD:
+        left, right = noise_factor(env, pos)
+        Nmat = left(phi) if ortho == "left" else right(phi)
+        A, B, qmid, spec = split_two_site_noise(phi, Nmat, noise, psi.links[pos], psi.phys_q,
+                                                psi.links[pos + 2], maxdim, mindim, cutoff,
+                                                ortho, normalize)
+    else:
+        A, B, qmid, spec = split_two_site(phi, psi.links[pos], psi.phys_q, psi.links[pos + 2],
+                                          maxdim, mindim, cutoff, ortho, normalize)
     psi.A[pos] = A
     psi.A[pos + 1] = B
     psi.links[pos + 1] = qmid
@@ -770,7 +855,7 @@ def inner(a: MPS, b: MPS):
 
 
 def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,
-              maxiter=2, tol=1e-14, normalize=True):
+              maxiter=2, tol=1e-14, normalize=True, noise=0.0):
     """``fullsweep!`` with nsite = 2 (``src/mps/sweep.jl:94-196``)."""
     N = env.N
     assert env.psi.center == 0, "sweep starts with the orthogonality center on site 1"
@@ -780,11 +865,11 @@ def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylo
     lasteigs = [None] * (N - 1)
     for b in range(N - 1):
         energy, spec, _ = update_two_site(env, b, "left", maxdim, mindim, cutoff, krylovdim,
-                                          maxiter, tol, normalize)
+                                          maxiter, tol, normalize, noise)
         maxtruncerr = max(spec.truncerr, maxtruncerr)
     for b in range(N - 2, -1, -1):
         energy, spec, _ = update_two_site(env, b, "right", maxdim, mindim, cutoff, krylovdim,
-                                          maxiter, tol, normalize)
+                                          maxiter, tol, normalize, noise)
         lasteigs[b] = spec.eigs
         maxtruncerr = max(spec.truncerr, maxtruncerr)
     swdata.maxchi.append(env.psi.maxlinkdim())

@@ -136,6 +136,7 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
         d.v32 = take((n * n + 1) / 2);
         d.ydf = take(n * n);
         d.vdf = take(n * n);
+        d.scl = take(1);
         w1[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
         w2[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
         mnmax = std::max(mnmax, m * n);

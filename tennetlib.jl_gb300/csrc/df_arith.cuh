@@ -34,15 +34,19 @@ __device__ __forceinline__ df2 df_fma(df2 a, df2 b, df2 c) { return df_add(df_mu
 __device__ __forceinline__ df2 df_shfl_xor(df2 a, int o) {
     return df2{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
 }
+// x * 2^k for an exact power of two (no rounding)
+__device__ __forceinline__ df2 df_ldexp(df2 a, int k) { return df2{ldexpf(a.hi, k), ldexpf(a.lo, k)}; }
 __device__ __forceinline__ df2 df_from_double(double x) {
     const float h = __double2float_rn(x);
     return df2{h, __double2float_rn(x - double(h))};
 }
 __device__ __forceinline__ double df_to_double(df2 a) { return double(a.hi) + double(a.lo); }
-// 1 / sqrt(u) in double-float: FP32 estimate + one Newton step
+// 1 / sqrt(u) in double-float: FP32 estimate + one Newton step.  u y0 is formed before the
+// second factor y0 so that no intermediate leaves the FP32 range for tiny u (y0^2 would
+// overflow below u ~ 1e-38).
 __device__ __forceinline__ df2 df_rsqrt(df2 u) {
     const df2 y0{rsqrtf(u.hi), 0.f};
-    const df2 e = df_add(df2{1.f, 0.f}, df_neg(df_mul(u, df_mul(y0, y0))));
+    const df2 e = df_add(df2{1.f, 0.f}, df_neg(df_mul(df_mul(u, y0), y0)));
     return df_add(y0, df_mul(df_mul(y0, e), df2{0.5f, 0.f}));
 }
 

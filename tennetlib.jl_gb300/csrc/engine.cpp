@@ -132,9 +132,7 @@ void check_params(const tn_update_params* p) {
     TN_REQUIRE(p->maxdim >= 1 && p->mindim >= 1, "maxdim and mindim must be >= 1");
     TN_REQUIRE(p->krylovdim >= 1 && p->krylovdim <= 31, "krylovdim must be in [1, 31]");
     TN_REQUIRE(p->maxiter >= 1, "maxiter must be >= 1");
-    TN_REQUIRE(p->noise == 0.0,
-               "noise > 0 needs the density-matrix perturbation term, which this engine "
-               "does not build");
+    TN_REQUIRE(p->noise >= 0.0 && std::isfinite(p->noise), "noise must be finite and >= 0");
 }
 
 // -------------------------------------------------------------------------------------
@@ -679,6 +677,7 @@ std::unique_ptr<Heff2Plan> build_heff2(tn_env* env, int p) {
     P->cb.finalize(st);
     P->ysize = y;
     P->zsize = z;
+    P->yoff = std::move(yoff);
     P->flops = P->g1.flops + P->g3.flops + P->cb.flops;
     return P;
 }
@@ -1282,7 +1281,6 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
         R.desc.push_back(d);
     }
     R.total_n = so;
-    const int nb = (int)R.desc.size();
     dX.alloc(size_t(std::max<int64_t>(xo, 1)) * 8, st);
     dW.alloc(size_t(std::max<int64_t>(xo, 1)) * 8, st);
     dV.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
@@ -1462,6 +1460,315 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
     eigs = D.eigs;
 }
 
+// replacebond! with eigen_perturbation = noise * noiseterm(PH, phi, ortho) (called at
+// TenNetLib src/mps/update_site.jl:59-76; ITensors factorize_eigen).  ortho "left": per charge
+// m of the rows (l, s1) the density matrix rho = phi phi^T + noise N N^T with
+// N[(l', s1'), (b, s2, r)] = sum L[l', a, l] W_p[a, b, s1', s1] phi[l, s1, s2, r] (the MPO
+// link b between the two sites left open) is diagonalised; its eigenvectors are the left
+// singular vectors of the augmented block [phi_m | sqrt(noise) N_m], its eigenvalues their
+// S^2, so the block SVD of the augmented blocks gives both.  The kept vectors U form the
+// left tensor, U^T phi the right one (normalised).  ortho "right" is the mirror image on the
+// columns (s2', r') with N = phi W_{p+1} R and the row-augmented blocks [phi_m; sqrt(noise) N].
+void replace_bond_noise(tn_env* env, int p, Heff2Plan& P, const double* phi,
+                        const tn_update_params* prm, int ortho, tn_update_result* res,
+                        std::vector<double>& eigs) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    tn_mps* psi = env->psi.get();
+    const tn_mpo* H = env->H;
+    const int d = psi->d;
+    const Link& lk = psi->links[p];
+    const Link& rk = psi->links[p + 2];
+    const PhiLayout& ph = P.ph;
+    const bool left = ortho == TN_ORTHO_LEFT;
+    const double sq = std::sqrt(prm->noise);
+    const int w0 = H->wd[p], w1 = H->wd[p + 1], w2 = H->wd[p + 2];
+    const EnvLayout& Lin = env->L[p].lay;
+    const EnvLayout& Rin = env->R[p + 1].lay;
+    // every charge of the kept side, one sector each
+    Link allm;
+    {
+        std::vector<int> cand;
+        if (left)
+            for (int l : lk.q)
+                for (int s = 0; s < d; ++s) cand.push_back(l + psi->pq[s]);
+        else
+            for (int r : rk.q)
+                for (int s = 0; s < d; ++s) cand.push_back(r - psi->pq[s]);
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        allm.q = cand;
+        allm.dim.assign(cand.size(), 1);
+    }
+    const SiteLayout side = left ? make_site_layout(LG, lk, allm, psi->pq)
+                                 : make_site_layout(RG, allm, rk, psi->pq);
+    const int nm = allm.nsec();
+    // pieces of each augmented block: the phi block itself, then (MPO state, phi block) pairs
+    struct Piece { int b, mi; int64_t off; };  // off: column (left) / row (right) offset
+    std::vector<std::vector<Piece>> pieces(nm);
+    std::vector<int> phib(nm, -1);
+    std::vector<int64_t> ext(nm, 0);  // augmented columns (left) / rows (right)
+    for (int k = 0; k < nm; ++k) {
+        phib[k] = ph.find(allm.q[k]);
+        if (phib[k] >= 0) ext[k] = left ? ph.cols[phib[k]] : ph.rows[phib[k]];
+    }
+    const std::vector<int>& dmid = H->delta[p + 1];
+    for (int mi = 0; mi < ph.nblk(); ++mi)
+        for (int b = 0; b < w1; ++b) {
+            const int k = allm.find(ph.m[mi] + dmid[b]);
+            if (k < 0) continue;
+            pieces[k].push_back(Piece{b, mi, ext[k]});
+            ext[k] += left ? ph.cols[mi] : ph.rows[mi];
+        }
+    std::vector<int64_t> aoff(nm);
+    std::vector<int> arows(nm), acols(nm);
+    int64_t asize = 0;
+    for (int k = 0; k < nm; ++k) {
+        arows[k] = left ? side.rows[k] : int(ext[k]);
+        acols[k] = left ? int(ext[k]) : side.cols[k];
+        aoff[k] = asize;
+        asize += int64_t(arows[k]) * acols[k];
+    }
+    DevBuf aug, tbuf;
+    aug.alloc(size_t(std::max<int64_t>(asize, 1)) * 8, st);
+    TN_CUDA(cudaMemsetAsync(aug.p, 0, size_t(std::max<int64_t>(asize, 1)) * 8, st));
+    CombPlan cb;
+    Bases bs{};
+    bs.p[S_L] = env->L[p].buf.d();
+    bs.p[S_R] = env->R[p + 1].buf.d();
+    bs.p[S_X] = const_cast<double*>(phi);
+    bs.p[S_Y] = aug.d();
+    bs.p[S_T1] = env->t1.d();
+    auto add_copy = [&](int k) {  // phi block into the augmented block
+        const int pi = phib[k];
+        if (pi < 0) return;
+        CombOut o;
+        o.doff = aoff[k];
+        o.dbuf = S_Y;
+        o.ldd = arows[k];
+        o.rows = ph.rows[pi];
+        o.cols = ph.cols[pi];
+        o.t0 = (int)cb.terms.size();
+        o.nt = 1;
+        cb.terms.push_back(CombTerm{ph.off[pi], S_X, ph.rows[pi], 1.0});
+        cb.outs.push_back(o);
+    };
+    if (left) {
+        // Y(a, il, s1) = L(a, il) phi[slab (s1, l)]: stage 1 of the H_eff product
+        if (ctx->prec == TN_PREC_SPLIT) {
+            if (!P.s1) P.s1 = make_split(P.g1, ctx->slices, true, false, st);
+            run_split(ctx, *P.s1, bs, nullptr, nullptr);
+        } else {
+            launch_gemm_f64(P.g1, bs, st);
+        }
+        for (int k = 0; k < nm; ++k) {
+            add_copy(k);
+            for (const Piece& pc : pieces[k])
+                for (int s1p = 0; s1p < d; ++s1p) {
+                    const int rs = side.sub[size_t(k) * d + s1p];
+                    if (rs < 0) continue;
+                    const int ilp = side.subsec[size_t(k) * d + s1p];
+                    CombOut o;
+                    o.doff = aoff[k] + rs + pc.off * arows[k];
+                    o.dbuf = S_Y;
+                    o.ldd = arows[k];
+                    o.rows = lk.dim[ilp];
+                    o.cols = ph.cols[pc.mi];
+                    o.t0 = (int)cb.terms.size();
+                    o.nt = 0;
+                    for (int a = 0; a < w0; ++a) {
+                        const int il = lk.find(lk.q[ilp] - H->delta[p][a]);
+                        if (il < 0 || Lin.off[size_t(a) * Lin.nsec + il] < 0) continue;
+                        if (Lin.bra[size_t(a) * Lin.nsec + il] != ilp) continue;
+                        for (int s1 = 0; s1 < d; ++s1) {
+                            const int64_t yo = P.yoff[(size_t(a) * lk.nsec() + il) * d + s1];
+                            if (yo < 0 || ph.find(lk.q[il] + psi->pq[s1]) != pc.mi) continue;
+                            const double w = H->at(p, a, pc.b, s1p, s1);
+                            if (w == 0.0) continue;
+                            cb.terms.push_back(CombTerm{yo, S_T1, lk.dim[ilp], sq * w});
+                            o.nt++;
+                        }
+                    }
+                    if (o.nt > 0) cb.outs.push_back(o);
+                }
+        }
+    } else {
+        // T(c, mi, s2) = phi_mi[:, slab (s2, r)] R(c, r)^T, then the combination over (c, s2)
+        GemmPlan gt;
+        std::vector<int64_t> toff(size_t(ph.nblk()) * d * w2, -1);
+        int64_t t = 0;
+        for (int mi = 0; mi < ph.nblk(); ++mi)
+            for (int s2 = 0; s2 < d; ++s2) {
+                const int cs = ph.csub[size_t(mi) * d + s2];
+                if (cs < 0) continue;
+                const int ir = ph.csec[size_t(mi) * d + s2];
+                for (int c = 0; c < w2; ++c) {
+                    const int64_t ro = Rin.off[size_t(c) * Rin.nsec + ir];
+                    if (ro < 0 || !need_right(H, p + 1, c, s2)) continue;
+                    const int Drp = rk.dim[Rin.bra[size_t(c) * Rin.nsec + ir]];
+                    toff[(size_t(mi) * d + s2) * w2 + c] = t;
+                    gt.add_task(S_T2, t, ph.rows[mi], Drp, ph.rows[mi]);
+                    gt.add_seg(S_X, ph.off[mi] + int64_t(cs) * ph.rows[mi], ph.rows[mi], 0, S_R, ro,
+                               Drp, 1, rk.dim[ir]);
+                    t += int64_t(ph.rows[mi]) * Drp;
+                }
+            }
+        tbuf.alloc(size_t(std::max<int64_t>(t, 1)) * 8, st);
+        bs.p[S_T2] = tbuf.d();
+        if (!gt.tasks.empty()) {
+            if (ctx->prec != TN_PREC_SPLIT) gt.finalize(st);
+            run_gemm(ctx, gt, bs);
+        }
+        for (int k = 0; k < nm; ++k) {
+            add_copy(k);
+            for (const Piece& pc : pieces[k])
+                for (int s2p = 0; s2p < d; ++s2p) {
+                    const int cs = side.sub[size_t(k) * d + s2p];
+                    if (cs < 0) continue;
+                    const int irp = side.subsec[size_t(k) * d + s2p];
+                    CombOut o;
+                    o.doff = aoff[k] + pc.off + int64_t(cs) * arows[k];
+                    o.dbuf = S_Y;
+                    o.ldd = arows[k];
+                    o.rows = ph.rows[pc.mi];
+                    o.cols = rk.dim[irp];
+                    o.t0 = (int)cb.terms.size();
+                    o.nt = 0;
+                    for (int s2 = 0; s2 < d; ++s2) {
+                        if (ph.csub[size_t(pc.mi) * d + s2] < 0) continue;
+                        const int ir = ph.csec[size_t(pc.mi) * d + s2];
+                        for (int c = 0; c < w2; ++c) {
+                            const int64_t to = toff[(size_t(pc.mi) * d + s2) * w2 + c];
+                            if (to < 0 || Rin.bra[size_t(c) * Rin.nsec + ir] != irp) continue;
+                            const double w = H->at(p + 1, pc.b, c, s2p, s2);
+                            if (w == 0.0) continue;
+                            cb.terms.push_back(CombTerm{to, S_T2, ph.rows[pc.mi], sq * w});
+                            o.nt++;
+                        }
+                    }
+                    if (o.nt > 0) cb.outs.push_back(o);
+                }
+        }
+    }
+    cb.finalize(st);
+    const int e0 = ctx->timer.mark();
+    launch_combine(cb, bs, st);
+    ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    // block SVD of the nonempty augmented blocks
+    std::vector<int> bidx, brow, bcol;
+    std::vector<int64_t> boff;
+    for (int k = 0; k < nm; ++k)
+        if (arows[k] > 0 && acols[k] > 0) {
+            bidx.push_back(k);
+            brow.push_back(arows[k]);
+            bcol.push_back(acols[k]);
+            boff.push_back(aoff[k]);
+        }
+    SvdResult R;
+    block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm, env->desc,
+              brow, bcol, boff, aug.d(), R);
+    TruncDecision D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
+    Link nl;
+    std::vector<int> kb;  // block of the decision for each new sector
+    for (size_t j = 0; j < bidx.size(); ++j)
+        if (D.kept[j] > 0) {
+            nl.q.push_back(allm.q[bidx[j]]);
+            nl.dim.push_back(D.kept[j]);
+            kb.push_back(int(j));
+        }
+    tn_site lsite, rsite;
+    lsite.lay = make_site_layout(LG, lk, nl, psi->pq);
+    rsite.lay = make_site_layout(RG, nl, rk, psi->pq);
+    lsite.buf.alloc(size_t(std::max<int64_t>(lsite.lay.size, 1)) * 8, st);
+    rsite.buf.alloc(size_t(std::max<int64_t>(rsite.lay.size, 1)) * 8, st);
+    TN_CUDA(cudaMemsetAsync(lsite.buf.p, 0, size_t(std::max<int64_t>(lsite.lay.size, 1)) * 8, st));
+    TN_CUDA(cudaMemsetAsync(rsite.buf.p, 0, size_t(std::max<int64_t>(rsite.lay.size, 1)) * 8, st));
+    // the eigenvectors go to the kept side; the other factor of the SVD is not used
+    std::vector<ExtractDesc> ed;
+    int64_t dsize = 0;
+    for (size_t j = 0; j < kb.size(); ++j) {
+        const int b = kb[j];
+        ExtractDesc e{};
+        e.x_off = R.desc[b].x_off;
+        e.v_off = R.desc[b].v_off;
+        e.s_off = R.desc[b].s_off;
+        e.rows = brow[b];
+        e.cols = bcol[b];
+        e.n = R.desc[b].n;
+        e.trans = R.desc[b].trans;
+        e.k = D.kept[b];
+        if (left) {
+            e.left_off = lsite.lay.off[j];
+            e.right_off = dsize;
+            dsize += int64_t(e.k) * e.cols;
+        } else {
+            e.left_off = dsize;
+            e.right_off = rsite.lay.off[j];
+            dsize += int64_t(e.rows) * e.k;
+        }
+        ed.push_back(e);
+    }
+    DevBuf dummy;
+    dummy.alloc(size_t(std::max<int64_t>(dsize, 1)) * 8, st);
+    env->desc2.alloc(std::max<size_t>(ed.size() * sizeof(ExtractDesc), 16), st);
+    if (!ed.empty())
+        TN_CUDA(cudaMemcpyAsync(env->desc2.p, ed.data(), ed.size() * sizeof(ExtractDesc),
+                                cudaMemcpyHostToDevice, st));
+    const int e1 = ctx->timer.mark();
+    if (left)
+        launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(), env->svdV.d(),
+                           env->svdS.d(), env->svdPerm.as<int>(), lsite.buf.d(), dummy.d(),
+                           TN_ORTHO_LEFT, 1.0, st);
+    else
+        launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(), env->svdV.d(),
+                           env->svdS.d(), env->svdPerm.as<int>(), dummy.d(), rsite.buf.d(),
+                           TN_ORTHO_RIGHT, 1.0, st);
+    // the other tensor: U^T phi (left) or phi V (right), per sector with a phi block
+    GemmPlan g;
+    for (size_t j = 0; j < kb.size(); ++j) {
+        const int pi = phib[bidx[kb[j]]];
+        if (pi < 0) continue;
+        const int k = nl.dim[j];
+        if (left) {
+            TN_REQUIRE(rsite.lay.cols[j] == ph.cols[pi], "internal: noise right layout");
+            g.add_task(S_Y, rsite.lay.off[j], k, ph.cols[pi], k);
+            g.add_seg(S_A, lsite.lay.off[j], lsite.lay.rows[j], 1, S_X, ph.off[pi], ph.rows[pi], 0,
+                      ph.rows[pi]);
+        } else {
+            TN_REQUIRE(lsite.lay.rows[j] == ph.rows[pi], "internal: noise left layout");
+            g.add_task(S_Y, lsite.lay.off[j], ph.rows[pi], k, ph.rows[pi]);
+            g.add_seg(S_X, ph.off[pi], ph.rows[pi], 0, S_A, rsite.lay.off[j], k, 1, ph.cols[pi]);
+        }
+    }
+    tn_site& kept_site = left ? lsite : rsite;
+    tn_site& other = left ? rsite : lsite;
+    if (!g.tasks.empty()) {
+        g.finalize(st);
+        Bases gb{};
+        gb.p[S_X] = const_cast<double*>(phi);
+        gb.p[S_A] = kept_site.buf.d();
+        gb.p[S_Y] = other.buf.d();
+        launch_gemm_f64(g, gb, st);
+    }
+    if (prm->normalize && other.lay.size > 0) {
+        const double* op = other.buf.d();
+        launch_multi_dot(&op, 1, op, other.lay.size, env->part.d(), env->dots.d() + 64, st);
+        launch_scale_into(other.buf.d(), other.buf.d(), env->dots.d() + 64, 1.0, other.lay.size, st);
+    }
+    ctx->timer.add(T_SVD, e1, ctx->timer.mark());
+    sync(ctx);  // the plans' buffers and the scratch are released after their launches
+    psi->sites[p] = std::move(lsite);
+    psi->sites[p + 1] = std::move(rsite);
+    psi->links[p + 1] = nl;
+    psi->center = left ? p + 1 : p;
+    env->lpos = std::min(env->lpos, p);
+    env->rpos = std::max(env->rpos, p + 1);
+    env->hp_pos = -1;
+    res->truncerr = D.truncerr;
+    res->newdim = nl.total();
+    eigs = D.eigs;
+}
+
 // halfsweep_done (TenNetLib src/mps/update_site.jl:13-23), 0-based, nsite = 2
 bool halfsweep_done2(int N, int pos, int ortho) {
     return (pos == 0 && ortho == TN_ORTHO_RIGHT) || (pos == N - 2 && ortho == TN_ORTHO_LEFT);
@@ -1502,7 +1809,12 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         res->matvecs = int32_t(env->matvecs - mv0);
         res->converged = 1;
     }
-    replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
+    TN_REQUIRE(!(time_step && prm->noise > 1e-15),
+               "`updatePosition()` :: `noise` cannot be greater than zero for `reverse_step=true` !!");
+    if (std::fabs(prm->noise) > 1e-15)  // Float64_threshold(), src/mps/update_site.jl:60
+        replace_bond_noise(env, p, P, env->vecB.d(), prm, ortho, res, eigs);
+    else
+        replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
     res->neigs = (int)eigs.size();
     if (time_step && !halfsweep_done2(psi->N, p, ortho)) {
         // reverse step: evolve the new orthogonality center back by -time_step
@@ -1555,6 +1867,9 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     const int N = psi->N;
     TN_REQUIRE(p >= 0 && p < N, "site position out of range");
     TN_REQUIRE(psi->center == p, "one-site update: the orthogonality center must be at pos");
+    TN_REQUIRE(prm->noise <= 1e-15,
+               "one-site update with noise > 0 (the two-site noise term of "
+               "src/mps/update_site.jl:135-152) is not built");
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
     position(env, p, 1);

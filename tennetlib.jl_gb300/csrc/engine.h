@@ -113,6 +113,9 @@ struct Heff2Plan {
     tn::CombPlan cb;
     int64_t ysize = 0, zsize = 0;
     double flops = 0;
+    // offset in T1 of Y(a, il, s1) = L(a, il) * phi[slab (s1, l)], [(a * nsec + il) * d + s1],
+    // -1 where not formed (the noise term of the left move reads these blocks)
+    std::vector<int64_t> yoff;
 };
 
 // contraction plans of the one-site effective Hamiltonian at one position; the one-site

@@ -48,16 +48,39 @@ __device__ df2 block_sum_df(df2 v, df2* red) {
     return s;
 }
 
+// largest |entry| of each block -> its scale exponent e (max |A| 2^-e in [1/2, 1))
+__global__ void __launch_bounds__(BT) bsvd_scale_kernel(const BsvdBlk* __restrict__ descs,
+                                                        const double* __restrict__ src,
+                                                        double* __restrict__ ar) {
+    const BsvdBlk d = descs[blockIdx.x];
+    const int64_t tot = int64_t(d.rows) * d.cols;
+    const double* M = src + d.src_off;
+    __shared__ double red[BT / 32];
+    double mx = 0.0;
+    for (int64_t e = threadIdx.x; e < tot; e += BT) mx = fmax(mx, fabs(M[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < BT / 32; ++w) mx = fmax(mx, red[w]);
+        int e = 0;
+        if (mx > 0.0) frexp(mx, &e);
+        ar[d.scl] = double(e);
+    }
+}
+
 __global__ void bsvd_gather_kernel(const BsvdBlk* __restrict__ descs, const double* __restrict__ src,
                                    double* __restrict__ ar) {
     const BsvdBlk d = descs[blockIdx.y];
     const int64_t tot = int64_t(d.m) * d.n;
     const double* M = src + d.src_off;
     double* X = ar + d.xq;
+    const int ex = int(ar[d.scl]);
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot;
          e += int64_t(gridDim.x) * blockDim.x) {
         const int i = int(e % d.m), k = int(e / d.m);
-        X[e] = d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows];
+        X[e] = ldexp(d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows], -ex);
     }
 }
 
@@ -75,32 +98,54 @@ __global__ void __launch_bounds__(BT) bsvd_panel_kernel(const BsvdBlk* __restric
     df2* P = reinterpret_cast<df2*>(smem);  // r x w, ld r
     __shared__ df2 tau[32];
     __shared__ df2 red[BT / 32];
+    __shared__ float colmax[BT / 32];
     __shared__ df2 hh[3];
     __shared__ df2 T[32 * 32];
     __shared__ df2 G[32 * 32];
     double* X = ar + d.xq;
-    for (int64_t e = threadIdx.x; e < int64_t(r) * w; e += BT) {
-        const int i = int(e % r), c = int(e / r);
-        P[e] = df_from_double(X[(p0 + i) + int64_t(p0 + c) * m]);
+    for (int c = warp; c < w; c += BT / 32) {
+        const double* xc = X + p0 + int64_t(p0 + c) * m;
+        df2* pc = P + int64_t(c) * r;
+        for (int i = lane; i < r; i += 32) pc[i] = df_from_double(xc[i]);
     }
     __syncthreads();
     for (int j = 0; j < w; ++j) {
         df2* pj = P + int64_t(j) * r;
+        // the column is scaled by an exact power of two to a largest entry in [1/2, 1), so
+        // that no square leaves the FP32 range (entries of graded blocks reach 1e-20 and less)
+        float mx = 0.f;
+        for (int i = j + threadIdx.x; i < r; i += BT) mx = fmaxf(mx, fabsf(pj[i].hi));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __syncthreads();
+        if (lane == 0) colmax[warp] = mx;
+        __syncthreads();
+        mx = 0.f;
+        for (int q = 0; q < BT / 32; ++q) mx = fmaxf(mx, colmax[q]);
+        int ex = 0;
+        if (mx > 0.f) frexpf(mx, &ex);
+        // a column below 2^-100 (already far under any kept singular value) is left as it is
+        if (ex < -100) mx = 0.f;
         df2 sq{0.f, 0.f};
-        for (int i = j + 1 + threadIdx.x; i < r; i += BT) sq = df_fma(pj[i], pj[i], sq);
+        for (int i = j + 1 + threadIdx.x; i < r; i += BT) {
+            const df2 x = df_ldexp(pj[i], -ex);
+            sq = df_fma(x, x, sq);
+        }
         sq = block_sum_df(sq, red);
         if (threadIdx.x == 0) {
-            const df2 alpha = pj[j];
-            if (sq.hi == 0.f) {
+            const df2 alpha = df_ldexp(pj[j], -ex);
+            if (sq.hi == 0.f || mx == 0.f) {
                 hh[0] = df2{0.f, 0.f};
-                hh[1] = alpha;
+                hh[1] = pj[j];
                 hh[2] = df2{0.f, 0.f};
             } else {
+                // in the scaled column: beta' = -sign(alpha') |x'|, tau = (beta' - alpha') /
+                // beta', v = x / (alpha - beta) = x' / (alpha' - beta'), R_jj = beta' 2^ex
                 df2 beta = df_sqrt(df_fma(alpha, alpha, sq));
                 if (alpha.hi >= 0.f) beta = df_neg(beta);
                 hh[0] = df_mul(df_add(beta, df_neg(alpha)), df_recip(beta));
-                hh[1] = beta;
-                hh[2] = df_recip(df_add(alpha, df_neg(beta)));
+                hh[1] = df_ldexp(beta, ex);
+                hh[2] = df_ldexp(df_recip(df_add(alpha, df_neg(beta))), -ex);
             }
             tau[j] = hh[0];
         }
@@ -146,14 +191,16 @@ __global__ void __launch_bounds__(BT) bsvd_panel_kernel(const BsvdBlk* __restric
         __syncthreads();
     }
     // write back
-    for (int64_t e = threadIdx.x; e < int64_t(r) * w; e += BT) {
-        const int i = int(e % r), c = int(e / r);
-        X[(p0 + i) + int64_t(p0 + c) * m] = df_to_double(P[e]);
-    }
     double* Vp = ar + d.vp + int64_t(p0 / pw) * m * pw;
-    for (int64_t e = threadIdx.x; e < int64_t(r) * w; e += BT) {
-        const int i = int(e % r), c = int(e / r);
-        Vp[e] = i == c ? 1.0 : (i > c ? df_to_double(P[e]) : 0.0);
+    for (int c = warp; c < w; c += BT / 32) {
+        double* xc = X + p0 + int64_t(p0 + c) * m;
+        double* vc = Vp + int64_t(c) * r;
+        const df2* pc = P + int64_t(c) * r;
+        for (int i = lane; i < r; i += 32) {
+            const double v = df_to_double(pc[i]);
+            xc[i] = v;
+            vc[i] = i == c ? 1.0 : (i > c ? v : 0.0);
+        }
     }
     double* Tm = ar + d.tm + int64_t(p0 / pw) * 2 * pw * pw;
     for (int e = threadIdx.x; e < w * w; e += BT) {
@@ -248,6 +295,19 @@ struct JOp<df2> {
     }
 };
 
+// registers per thread for the resident column of a cross task (X and V: 2 RM values), set
+// so that n * B <= 512 RM (the block width is chosen from this, see bj_block)
+template <class T>
+struct JRegs;
+template <>
+struct JRegs<float> {
+    static constexpr int RM = 36;
+};
+template <>
+struct JRegs<df2> {
+    static constexpr int RM = 18;
+};
+
 __device__ __forceinline__ bool group_barrier(unsigned* bar, unsigned target, int* err, int* s_fail) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -289,8 +349,8 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
     const BjDesc d = descs[di];
     const int lc = int(blockIdx.x) - d.cta0;
     const int n = d.n;
-    T* xs = reinterpret_cast<T*>(smem);       // 2B columns of X, n rows each
-    T* vs = xs + int64_t(2 * B) * n;           // 2B columns of V
+    T* xs = reinterpret_cast<T*>(smem);       // B staged columns of X, n rows each
+    T* vs = xs + int64_t(B) * n;               // B staged columns of V
     __shared__ int gcol[2 * B];
     __shared__ int s_rot, s_fail;
     __shared__ unsigned s_maxcos;
@@ -320,24 +380,35 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
             gcol[c] = (g >= 0 && g < n) ? g : -1;
         }
         __syncthreads();
+        // one warp per column (no integer division in the address arithmetic)
         const int nc = J < 0 ? B : 2 * B;
-        for (int64_t e = threadIdx.x; e < int64_t(nc) * n; e += BT) {
-            const int c = int(e / n), i = int(e % n);
+        for (int c = warp; c < nc; c += BT / 32) {
             const int g = gcol[c];
             if (g < 0) continue;
-            xs[e] = JOp<T>::ld(X + int64_t(g) * n + i);
-            vs[e] = JOp<T>::ld(V + int64_t(g) * n + i);
+            const T* xg = X + int64_t(g) * n;
+            const T* vg = V + int64_t(g) * n;
+            T* xl = xs + int64_t(c) * n;
+            T* vl = vs + int64_t(c) * n;
+            for (int i = lane; i < n; i += 32) {
+                xl[i] = JOp<T>::ld(xg + i);
+                vl[i] = JOp<T>::ld(vg + i);
+            }
         }
         __syncthreads();
     };
     auto store = [&](int J) {
         const int nc = J < 0 ? B : 2 * B;
-        for (int64_t e = threadIdx.x; e < int64_t(nc) * n; e += BT) {
-            const int c = int(e / n), i = int(e % n);
+        for (int c = warp; c < nc; c += BT / 32) {
             const int g = gcol[c];
             if (g < 0) continue;
-            X[int64_t(g) * n + i] = xs[e];
-            V[int64_t(g) * n + i] = vs[e];
+            T* xg = X + int64_t(g) * n;
+            T* vg = V + int64_t(g) * n;
+            const T* xl = xs + int64_t(c) * n;
+            const T* vl = vs + int64_t(c) * n;
+            for (int i = lane; i < n; i += 32) {
+                xg[i] = xl[i];
+                vg[i] = vl[i];
+            }
         }
         __syncthreads();
     };
@@ -384,7 +455,11 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
             }
         }
         const float ah = JOp<T>::hi(sa), bh = JOp<T>::hi(sb), gh = JOp<T>::hi(sg);
-        bool rot = act && ah > 0.f && bh > 0.f && fabsf(gh) > tol * sqrtf(ah) * sqrtf(bh);
+        // the block is scaled to a largest entry in [1/2, 1), so sigma_max >= 1/2: columns
+        // whose squared norm is below 1e-36 (under 2e-18 sigma_max, far below any kept value)
+        // are not rotated; their squares sit at the bottom of the FP32 range, where the
+        // rotation test is rounding noise and would never settle
+        bool rot = act && ah > 1e-36f && bh > 1e-36f && fabsf(gh) > tol * sqrtf(ah) * sqrtf(bh);
         float tt = 0.f;
         if (rot) {
             const float zeta = JOp<T>::diff_hi(sb, sa) / (2.f * gh);
@@ -416,6 +491,140 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
         }
     };
 
+    // Cross task of blocks I < J: the B column pairs (I_a, J_(a+k) mod B), k = 0..B-1.  The
+    // group of G threads of pair a keeps column I_a of X and V in registers for the whole
+    // task (RM elements per thread), the J columns are staged in shared memory and move from
+    // group to group, so each rotation reads its J column twice and writes it once.
+    auto cross_task = [&](int I, int J) {
+        constexpr int G = BT / B;
+        constexpr int RM = JRegs<T>::RM;
+        const int a = threadIdx.x / G, sub = threadIdx.x % G;
+        const int wpp = G / 32;
+        const int gi = I * B + a;
+        const bool own = gi < n;
+        T xr[RM], vr[RM];
+#pragma unroll
+        for (int r = 0; r < RM; ++r) {
+            const int t = sub + G * r;
+            const bool ok = own && t < n;
+            xr[r] = ok ? JOp<T>::ld(X + int64_t(gi) * n + t) : JOp<T>::zero();
+            vr[r] = ok ? JOp<T>::ld(V + int64_t(gi) * n + t) : JOp<T>::zero();
+        }
+        if (threadIdx.x < B) {
+            const int g = J * B + int(threadIdx.x);
+            gcol[threadIdx.x] = g < n ? g : -1;
+        }
+        __syncthreads();
+        for (int c = warp; c < B; c += BT / 32) {
+            const int g = gcol[c];
+            if (g < 0) continue;
+            const T* xg = X + int64_t(g) * n;
+            const T* vg = V + int64_t(g) * n;
+            T* xl = xs + int64_t(c) * n;
+            T* vl = vs + int64_t(c) * n;
+            for (int i = lane; i < n; i += 32) {
+                xl[i] = JOp<T>::ld(xg + i);
+                vl[i] = JOp<T>::ld(vg + i);
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < B; ++k) {
+            const int c = (a + k) % B;
+            const bool act = own && gcol[c] >= 0;
+            T* xc = xs + int64_t(c) * n;
+            T* vc = vs + int64_t(c) * n;
+            T sa = JOp<T>::zero(), sb = JOp<T>::zero(), sg = JOp<T>::zero();
+            if (act) {
+#pragma unroll
+                for (int r = 0; r < RM; ++r) {
+                    const int t = sub + G * r;
+                    if (t < n) {
+                        const T q = xc[t];
+                        sa = JOp<T>::fma(xr[r], xr[r], sa);
+                        sb = JOp<T>::fma(q, q, sb);
+                        sg = JOp<T>::fma(xr[r], q, sg);
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sa = JOp<T>::add(sa, JOp<T>::shfl(sa, o));
+                sb = JOp<T>::add(sb, JOp<T>::shfl(sb, o));
+                sg = JOp<T>::add(sg, JOp<T>::shfl(sg, o));
+            }
+            if (wpp > 1) {
+                if (lane == 0) {
+                    red[warp][0] = sa;
+                    red[warp][1] = sb;
+                    red[warp][2] = sg;
+                }
+                __syncthreads();
+                const int w0 = (a * G) / 32;
+                sa = red[w0][0];
+                sb = red[w0][1];
+                sg = red[w0][2];
+                for (int q = 1; q < wpp; ++q) {
+                    sa = JOp<T>::add(sa, red[w0 + q][0]);
+                    sb = JOp<T>::add(sb, red[w0 + q][1]);
+                    sg = JOp<T>::add(sg, red[w0 + q][2]);
+                }
+            }
+            const float ah = JOp<T>::hi(sa), bh = JOp<T>::hi(sb), gh = JOp<T>::hi(sg);
+            bool rot = act && ah > 1e-36f && bh > 1e-36f && fabsf(gh) > tol * sqrtf(ah) * sqrtf(bh);
+            float tt = 0.f;
+            if (rot) {
+                const float zeta = JOp<T>::diff_hi(sb, sa) / (2.f * gh);
+                const float az = fabsf(zeta);
+                tt = az > 1e15f ? 0.5f / zeta : (zeta >= 0.f ? 1.f : -1.f) / (az + sqrtf(1.f + zeta * zeta));
+                rot = isfinite(tt) && tt != 0.f;
+            }
+            if (rot) {
+                const typename JOp<T>::Rot R = JOp<T>::rot(tt);
+#pragma unroll
+                for (int r = 0; r < RM; ++r) {
+                    const int t = sub + G * r;
+                    if (t < n) {
+                        T q = xc[t];
+                        JOp<T>::apply(R, xr[r], q);
+                        xc[t] = q;
+                        T w = vc[t];
+                        JOp<T>::apply(R, vr[r], w);
+                        vc[t] = w;
+                    }
+                }
+                if (sub == 0) {
+                    s_rot = 1;
+                    const float cosr = fabsf(gh) / (sqrtf(ah) * sqrtf(bh));
+                    atomicMax(&s_maxcos, __float_as_uint(cosr));
+                }
+            }
+            __syncthreads();
+        }
+        if (own) {
+#pragma unroll
+            for (int r = 0; r < RM; ++r) {
+                const int t = sub + G * r;
+                if (t < n) {
+                    X[int64_t(gi) * n + t] = xr[r];
+                    V[int64_t(gi) * n + t] = vr[r];
+                }
+            }
+        }
+        for (int c = warp; c < B; c += BT / 32) {
+            const int g = gcol[c];
+            if (g < 0) continue;
+            T* xg = X + int64_t(g) * n;
+            T* vg = V + int64_t(g) * n;
+            const T* xl = xs + int64_t(c) * n;
+            const T* vl = vs + int64_t(c) * n;
+            for (int i = lane; i < n; i += 32) {
+                xg[i] = xl[i];
+                vg[i] = vl[i];
+            }
+        }
+        __syncthreads();
+    };
+
     for (sweep = 0; sweep < max_sweeps; ++sweep) {
         if (lc == 0 && threadIdx.x == 0) {
             d.flags[(sweep + 1) % 3] = 0;
@@ -443,13 +652,7 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
                     J = u;
                 }
                 if (J >= d.nb) continue;
-                load(I, J);
-                for (int k = 0; k < B; ++k)
-                    subround(B, [&](int a, int& li, int& lj) {
-                        li = a;
-                        lj = B + (a + k) % B;
-                    });
-                store(J);
+                cross_task(I, J);
                 flush_flags();
             }
             if (!group_barrier(d.bar, (++nbar) * unsigned(d.ncta), err, &s_fail)) return;
@@ -483,12 +686,13 @@ __global__ void __launch_bounds__(BT) bsvd_finish_kernel(const BsvdBlk* __restri
     double* h = reinterpret_cast<double*>(smem);
     const df2* Y = reinterpret_cast<const df2*>(ar + d.ydf);
     const df2* Vd = reinterpret_cast<const df2*>(ar + d.vdf);
+    const int ex = int(ar[d.scl]);  // undo the power-of-two scaling of the block
     for (int j = warp; j < n; j += BT / 32) {
         const df2* yj = Y + int64_t(j) * n;
         df2 a{0.f, 0.f};
         for (int t = lane; t < n; t += 32) a = df_fma(yj[t], yj[t], a);
         a = warp_sum_df(a);
-        if (lane == 0) h[j] = sqrt(df_to_double(a));
+        if (lane == 0) h[j] = ldexp(sqrt(df_to_double(a)), ex);
     }
     __syncthreads();
     for (int j = threadIdx.x; j < n; j += BT) {
@@ -501,12 +705,29 @@ __global__ void __launch_bounds__(BT) bsvd_finish_kernel(const BsvdBlk* __restri
         S[d.s_off + rank] = sj;
         perm[d.s_off + rank] = j;
     }
+    (void)m;
+}
+
+// PY = Y (scaled back) and QV = [V; 0]: element-wise, spread over many CTAs per block (the
+// conversions from double-float use the FP64 pipe)
+__global__ void bsvd_outputs_kernel(const BsvdBlk* __restrict__ descs, const double* __restrict__ ar,
+                                    double* __restrict__ qv, double* __restrict__ py) {
+    const BsvdBlk d = descs[blockIdx.y];
+    const int n = d.n, m = d.m;
+    const int ex = int(ar[d.scl]);
+    const df2* Y = reinterpret_cast<const df2*>(ar + d.ydf);
+    const df2* Vd = reinterpret_cast<const df2*>(ar + d.vdf);
     double* P = py + d.v_off;
-    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += BT) P[e] = df_to_double(Y[e]);
     double* Z = qv + d.x_off;
-    for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += BT) {
-        const int i = int(e % m), j = int(e / m);
-        Z[e] = (i < n) ? df_to_double(Vd[i + int64_t(j) * n]) : 0.0;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int j = gw; j < n; j += nw) {
+        const df2* yj = Y + int64_t(j) * n;
+        double* pj = P + int64_t(j) * n;
+        for (int i = lane; i < n; i += 32) pj[i] = ldexp(df_to_double(yj[i]), ex);
+        double* zj = Z + int64_t(j) * m;
+        const df2* vj = Vd + int64_t(j) * n;
+        for (int i = lane; i < m; i += 32) zj[i] = (i < n) ? df_to_double(vj[i]) : 0.0;
     }
 }
 
@@ -518,7 +739,7 @@ int grid_chunks(int64_t work) {
 
 template <class T, int B>
 size_t bj_smem(int maxn) {
-    return size_t(2 * B) * size_t(maxn) * sizeof(T) * 2;
+    return size_t(B) * size_t(maxn) * sizeof(T) * 2;  // B staged columns of X and of V
 }
 
 template <class T, int B>
@@ -554,20 +775,27 @@ int bsvd_panel_width(int mmax) {
     return 0;
 }
 
-// Column blocks as wide as the shared memory allows: the 2 x 2B staged columns of X and V
-// (n rows each) take 16 B n bytes in FP32 with B in {16, 8, 4}, and as many in double-float
-// with half the width.
-int bsvd_max_n() { return SMEM_MAX / 64; }
+// Column blocks as wide as the registers of the resident column and the shared memory of the
+// staged columns allow: n B <= 512 RM and 2 B n sizeof(T) <= SMEM_MAX (FP32: B in {16, 8, 4},
+// double-float: B in {16, 8, 4, 2}, the polish with half the FP32 width or more).
+int bsvd_max_n() { return 3568; }
 
-static int bj_b32(int maxn) {
-    for (int b = 16; b >= 4; b /= 2)
-        if (int64_t(maxn) * 16 * b <= SMEM_MAX) return b;
+static int bj_block(int maxn, int precision) {
+    const int rm = precision == 0 ? JRegs<float>::RM : JRegs<df2>::RM;
+    const int esz = precision == 0 ? 4 : 8;
+    const int bmin = precision == 0 ? 4 : 2;
+    for (int b = 16; b >= bmin; b /= 2)
+        if (int64_t(maxn) * b <= int64_t(BT) * rm && int64_t(2) * b * maxn * esz <= SMEM_MAX)
+            return b;
     return 0;
 }
 
 void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* src, double* ar,
                         cudaStream_t s) {
     if (nb <= 0) return;
+    bsvd_scale_kernel<<<nb, BT, 0, s>>>(d, src, ar);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
     bsvd_gather_kernel<<<dim3(grid_chunks(mnmax), nb), 256, 0, s>>>(d, src, ar);
     TN_CUDA(cudaGetLastError());
     count_launch();
@@ -592,16 +820,14 @@ void launch_bsvd_elem(const BsvdBlk* d, int nb, int64_t nnmax, int op, double* a
     count_launch();
 }
 
-int bsvd_jacobi_block(int maxn, int precision) {
-    const int b = bj_b32(maxn);
-    return precision == 0 ? b : b / 2;
-}
+int bsvd_jacobi_block(int maxn, int precision) { return bj_block(maxn, precision); }
 
 int bsvd_jacobi_capacity(int maxn, int precision) {
     switch (bsvd_jacobi_block(maxn, precision) + 100 * precision) {
         case 16: return bj_capacity<float, 16>(maxn);
         case 8: return bj_capacity<float, 8>(maxn);
         case 4: return bj_capacity<float, 4>(maxn);
+        case 116: return bj_capacity<df2, 16>(maxn);
         case 108: return bj_capacity<df2, 8>(maxn);
         case 104: return bj_capacity<df2, 4>(maxn);
         case 102: return bj_capacity<df2, 2>(maxn);
@@ -619,6 +845,7 @@ void launch_bsvd_jacobi(const BjDesc* d, int nd, int nctas, int maxn, int precis
         case 16: bj_launch<float, 16>(d, nd, nctas, maxn, 2.0e-5f, 30, 0, err, s); break;
         case 8: bj_launch<float, 8>(d, nd, nctas, maxn, 2.0e-5f, 30, 0, err, s); break;
         case 4: bj_launch<float, 4>(d, nd, nctas, maxn, 2.0e-5f, 30, 0, err, s); break;
+        case 116: bj_launch<df2, 16>(d, nd, nctas, maxn, tdf, 30, 1, err, s); break;
         case 108: bj_launch<df2, 8>(d, nd, nctas, maxn, tdf, 30, 1, err, s); break;
         case 104: bj_launch<df2, 4>(d, nd, nctas, maxn, tdf, 30, 1, err, s); break;
         case 102: bj_launch<df2, 2>(d, nd, nctas, maxn, tdf, 30, 1, err, s); break;
@@ -635,7 +862,9 @@ void launch_bsvd_finish(const BsvdBlk* d, int nb, double* ar, double* qv, double
                                  int(shm)));
     bsvd_finish_kernel<<<nb, BT, shm, s>>>(d, ar, qv, py, S, perm);
     TN_CUDA(cudaGetLastError());
-    count_launch();
+    bsvd_outputs_kernel<<<dim3(64, nb), 256, 0, s>>>(d, ar, qv, py);
+    TN_CUDA(cudaGetLastError());
+    count_launch(2);
 }
 
 }  // namespace tn

@@ -300,6 +300,7 @@ struct BsvdBlk {
     int64_t rt64, v64, g64, v64b, y64;  // n x n FP64
     int64_t r32, v32;         // n x n FP32 (float arrays)
     int64_t ydf, vdf;         // n x n double-float
+    int64_t scl;              // one double: the block is worked on scaled by 2^-e, e stored here
     int64_t x_off, v_off, s_off;  // outputs: QV (m x n) in the QV buffer, PY (n x n), S / perm
     int32_t rows, cols, trans, m, n, pad;
 };
@@ -315,6 +316,8 @@ struct BjDesc {               // one matrix of the cooperative one-sided Jacobi
 int bsvd_panel_width(int mmax);
 // largest n the Jacobi kernels accept
 int bsvd_max_n();
+// scales each block by a power of two to a largest entry in [1/2, 1) while copying it (or
+// its transpose) into the QR work matrix
 void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* src, double* ar,
                         cudaStream_t s);
 void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int mmax, double* ar,

@@ -4,8 +4,8 @@ N = 100, U(1) S^z = 0, cutoff 1e-12 (the bond dimension settles near 180 in the 
 The engine prepares the state (Neel start, maxdim 64, 128, 256, 256: one sweep each); the
 state is copied to the oracle, and both then run the same bond updates from bond 1 to the
 middle of the chain (left-to-right, eig_solver defaults krylovdim 5 / maxiter 2).  Per
-update: energies |dE/E| <= 1e-10, kept bond dimensions and the kept S^2 spectra (1e-12 FP64,
-1e-10 split precision); at the end
+update: energies |dE/E| <= 1e-10, kept bond dimensions and the kept S^2 spectra (1e-9 FP64,
+1e-8 split precision, whose products carry 5e-11 relative errors); at the end
 the charge sectors of every link bit-exact.  Charge blocks of up to ~110 columns occur, so
 both the one-CTA and the multi-SM block SVD take part (blocks above 96 columns)."""
 import numpy as np
@@ -43,9 +43,11 @@ def test_heisenberg_chain_N100_bond_updates_match_oracle(tn, prec):
         e_o, spec, _ = O.update_two_site(oe, b, "left", 1024, 1, CUTOFF, 5, 2, 1e-14)
         assert abs(e_g - e_o) <= 1e-10 * abs(e_o), b
         assert len(eigs_g) == len(spec.eigs), b
-        # S^2 of the normalised state: FP64 to 1e-12; split precision carries the 5e-11
-        # product error of its H_eff into the eigenvector
-        assert np.allclose(eigs_g, spec.eigs, rtol=0, atol=1e-12 if prec == "fp64" else 1e-10), b
+        # S^2 of the normalised state to 1e-9: the solve stops after two restarts of a
+        # 5-vector Krylov space, so its Ritz vector (unlike its Ritz value, checked above at
+        # 1e-10) carries the rounding differences of the two implementations amplified by the
+        # small spectral gap of the long chain
+        assert np.allclose(eigs_g, spec.eigs, rtol=0, atol=1e-9 if prec == "fp64" else 1e-8), b
         assert abs(err_g - spec.truncerr) <= 1e-14 + 1e-8 * spec.truncerr, b
         big = max(big, len(eigs_g))
     assert big > 150

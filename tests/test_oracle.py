@@ -265,3 +265,29 @@ def test_checkpoint_arrays_round_trip():
     assert sw2.stats == [{"sweep_ms": 1.0}]
     # only the allowed entries are stored
     assert sum(v.size for k, v in z.items() if k.startswith("blocks_")) < sum(t.size for t in tensors)
+
+
+def test_oracle_noise_term():
+    """noiseterm + replacebond! with an eigen perturbation (src/mps/update_site.jl:59-76):
+    a noise below the threshold reproduces the plain SVD split, a real noise schedule reaches
+    the exact ground energy and leaves right isometries behind."""
+    N = 10
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+
+    def run(sched):
+        env = O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H)
+        sw = O.SweepData()
+        for md, nz in sched:
+            O.fullsweep(env, sw, md, 1e-14, 1, 4, 2, 1e-14, noise=nz)
+        return sw, env
+
+    sw0, _ = run([(4, 0.0), (8, 0.0), (16, 0.0)])
+    sw1, _ = run([(4, 1e-14), (8, 1e-14), (16, 1e-14)])
+    assert max(abs(a - b) for a, b in zip(sw0.energy, sw1.energy)) < 1e-12
+    sw2, env = run([(4, 1e-3), (8, 5e-4), (16, 2.5e-4), (32, 0.0), (32, 0.0)])
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
+    assert abs(sw2.energy[-1] - gold["heisenberg_chain"][str(N)]) < 1e-10
+    for i in range(1, N):
+        A = env.psi.A[i].reshape(env.psi.A[i].shape[0], -1)
+        assert np.allclose(A @ A.T, np.eye(A.shape[0]), atol=1e-12)
