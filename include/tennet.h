@@ -159,6 +159,13 @@ int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out);
  * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO
  * environments lazily. */
 int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out);
+/* StateEnvs(psi, H, Ms; weight) (src/mps/state_envs.jl:88-105): excited-state projectors.
+ * The effective Hamiltonian of every later update and product becomes ProjMPO_MPS2's
+ * (src/mps/projmpo_mps2.jl:94-101), H_eff + weight sum_k |m_k><m_k| with m_k the projection
+ * of Ms[k] onto the sites being optimised (ProjMPS2, src/mps/projmps2.jl:26-224).  The
+ * states are copied; count 0 removes the projectors.  weight <= 0 with count > 0 is
+ * TN_E_INVALID with the reference's message; at most 32 states. */
+int tn_env_set_projectors(tn_env* env, const tn_mps* const* Ms, int count, double weight);
 int tn_env_destroy(tn_env* env);
 /* getpsi(sysenv) (state_envs.jl:36): a copy of the current state */
 int tn_env_getpsi(tn_env* env, tn_mps** out);

@@ -581,10 +581,29 @@ class SweepData:
     lasteigs: list = field(default_factory=list)
 
 
-class StateEnvs:
-    """MPS + MPO environments.  ``L[i]`` contracts sites < i, ``R[i]`` sites > i."""
+def overlap_left_update(E, A, M):
+    """ProjMPS2 ``_makeL!`` step (``src/mps/projmps2.jl:76-91``): E_new[r, r_M] =
+    sum A[l, s, r] E[l, l_M] conj(M[l_M, s, r_M]) (psi on the first index, M on the second)."""
+    t = np.tensordot(E, M.conj(), axes=([1], [0]))         # [l, s, r_M]
+    return np.tensordot(A, t, axes=([0, 1], [0, 1]))       # [r, r_M]
 
-    def __init__(self, psi: MPS, H: MPO):
+
+def overlap_right_update(E, A, M):
+    """ProjMPS2 ``_makeR!`` step (``src/mps/projmps2.jl:106-122``): E_new[l, l_M] =
+    sum A[l, s, r] E[r, r_M] conj(M[l_M, s, r_M])."""
+    t = np.tensordot(A, E, axes=([2], [0]))                # [l, s, r_M]
+    return np.tensordot(t, M.conj(), axes=([1, 2], [1, 2]))  # [l, l_M]
+
+
+class StateEnvs:
+    """MPS + MPO environments.  ``L[i]`` contracts sites < i, ``R[i]`` sites > i.
+
+    With ``Ms`` (``StateEnvs(psi, H, Ms; weight)``, ``src/mps/state_envs.jl:88-105``) the
+    effective Hamiltonian is ProjMPO_MPS2's (``src/mps/projmpo_mps2.jl:94-101``):
+    H_eff v + weight sum_k m_k <m_k|v>, with m_k the projection of M_k onto the sites being
+    optimised through the overlap environments ``LM[k][i]`` / ``RM[k][i]`` (sites < i / > i)."""
+
+    def __init__(self, psi: MPS, H: MPO, Ms=None, weight=None):
         assert psi.N == H.N
         self.psi = MPS([a.copy() for a in psi.A], [q.copy() for q in psi.links],
                        psi.phys_q.copy(), psi.center)
@@ -597,27 +616,68 @@ class StateEnvs:
         self.lpos = 0       # L[0..lpos] valid
         self.rpos = N - 1   # R[rpos..N-1] valid
         self.matvec_flops = 0
+        self.Ms = []
+        self.weight = 0.0
+        if Ms:
+            if weight is None or weight <= 0.0:
+                raise ValueError("`weight` parameter should be > 0.0 (value passed was "
+                                 f"`weight={weight}`)")
+            self.Ms = [[a.copy() for a in M.A] for M in Ms]
+            self.weight = float(weight)
+            self.LM = [[None] * (N + 1) for _ in Ms]
+            self.RM = [[None] * (N + 1) for _ in Ms]
+            for k, M in enumerate(Ms):
+                same_l = M.links[0][0] == psi.links[0][0]
+                same_r = M.links[N][0] == psi.links[N][0]
+                self.LM[k][0] = np.ones((1, 1)) * float(same_l)
+                self.RM[k][N - 1] = np.ones((1, 1)) * float(same_r)
 
     @property
     def N(self):
         return self.psi.N
 
     def position(self, pos, nsite):
-        """Make L[pos] and R[pos+nsite-1] valid (ProjMPO ``position!`` restated)."""
+        """Make L[pos] and R[pos+nsite-1] valid (ProjMPO ``position!`` restated; the
+        projector environments follow the same positions)."""
         while self.lpos < pos:
             i = self.lpos
             self.L[i + 1] = left_env_update(self.L[i], self.psi.A[i], self.H.W[i])
+            for k, M in enumerate(self.Ms):
+                self.LM[k][i + 1] = overlap_left_update(self.LM[k][i], self.psi.A[i], M[i])
             self.lpos += 1
         self.lpos = pos
         last = pos + nsite - 1
         while self.rpos > last:
             i = self.rpos
             self.R[i - 1] = right_env_update(self.R[i], self.psi.A[i], self.H.W[i])
+            for k, M in enumerate(self.Ms):
+                self.RM[k][i - 1] = overlap_right_update(self.RM[k][i], self.psi.A[i], M[i])
             self.rpos -= 1
         self.rpos = last
 
+    def proj_vectors(self, pos, nsite):
+        """``proj_mps`` (``src/mps/projmps2.jl:168-184``) of every M_k at the sites
+        pos..pos+nsite-1: LM M_pos (M_pos+1) RM^T, in the shape of the local tensor."""
+        out = []
+        for k, M in enumerate(self.Ms):
+            t = np.tensordot(self.LM[k][pos], M[pos].conj(), axes=([1], [0]))
+            if nsite == 2:
+                t = np.tensordot(t, M[pos + 1].conj(), axes=([-1], [0]))
+            out.append(np.tensordot(t, self.RM[k][pos + nsite - 1], axes=([-1], [1])))
+        return out
+
+    def _add_proj(self, pos, nsite, phi, out):
+        for m in self.proj_vectors(pos, nsite):
+            out = out + self.weight * m * float(np.vdot(m, phi))
+        return out
+
     def product2(self, pos, phi):
-        return heff2_apply(self.L[pos], self.H.W[pos], self.H.W[pos + 1], self.R[pos + 1], phi)
+        out = heff2_apply(self.L[pos], self.H.W[pos], self.H.W[pos + 1], self.R[pos + 1], phi)
+        return self._add_proj(pos, 2, phi, out) if self.Ms else out
+
+    def product1(self, pos, phi):
+        out = heff1_apply(self.L[pos], self.H.W[pos], self.R[pos], phi)
+        return self._add_proj(pos, 1, phi, out) if self.Ms else out
 
 
 def noise_factor(env: StateEnvs, pos):
@@ -884,11 +944,13 @@ def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylo
 
 
 def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdim, maxiter,
-                    tol, normalize=True):
-    """``_update_one_site!`` (``src/mps/update_site.jl:94-190``) for the eigensolver without
-    noise: solve the one-site problem at the orthogonality center; unless the half sweep is
-    done, SVD the tensor with the link toward the next site on the V side (ITensors
-    truncation), keep U at pos and multiply S V into the next site."""
+                    tol, normalize=True, noise=0.0):
+    """``_update_one_site!`` (``src/mps/update_site.jl:94-190``) for the eigensolver: solve
+    the one-site problem at the orthogonality center; unless the half sweep is done, SVD the
+    tensor with the link toward the next site on the V side (ITensors truncation), keep U at
+    pos and multiply S V into the next site.  With noise > 0 (``:135-152``) the solved tensor
+    times the next site is split as a two-site tensor at pos0 (pos for "left", pos - 1 for
+    "right") with the density-matrix perturbation of that bond."""
     psi = env.psi
     N = psi.N
     assert psi.center == pos
@@ -897,7 +959,7 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
     shape = phi.shape
 
     def apply(v):
-        return heff1_apply(env.L[pos], env.H.W[pos], env.R[pos], v.reshape(shape)).reshape(-1)
+        return env.product1(pos, v.reshape(shape)).reshape(-1)
 
     energy, vec, info = eigsolve_lowest(apply, phi.reshape(-1), krylovdim, maxiter, tol)
     phi = vec.reshape(shape)
@@ -908,6 +970,26 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
         env.lpos = min(env.lpos, pos)
         env.rpos = max(env.rpos, pos)
         return energy, Spectrum(eigs=np.zeros(0), truncerr=0.0), info
+    if abs(noise) > FLOAT64_THRESHOLD:
+        if ortho == "left":
+            pos0 = pos
+            phi2 = np.tensordot(phi, psi.A[pos + 1], axes=([2], [0]))
+        else:
+            pos0 = pos - 1
+            phi2 = np.tensordot(psi.A[pos - 1], phi, axes=([2], [0]))
+        env.position(pos0, 2)
+        left, right = noise_factor(env, pos0)
+        Nmat = left(phi2) if ortho == "left" else right(phi2)
+        A, B, qmid, spec = split_two_site_noise(phi2, Nmat, noise, psi.links[pos0], psi.phys_q,
+                                                psi.links[pos0 + 2], maxdim, mindim, cutoff,
+                                                ortho, normalize)
+        psi.A[pos0] = A
+        psi.A[pos0 + 1] = B
+        psi.links[pos0 + 1] = qmid
+        psi.center = pos0 + 1 if ortho == "left" else pos0
+        env.lpos = min(env.lpos, pos0)
+        env.rpos = max(env.rpos, pos0 + 1)
+        return energy, spec, info
     ql, qs, qr = psi.links[pos], psi.phys_q, psi.links[pos + 1]
     Dl, d, Dr = shape
     if ortho == "left":
@@ -962,7 +1044,7 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
 
 
 def fullsweep1(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylovdim=5,
-               maxiter=2, tol=1e-14, normalize=True):
+               maxiter=2, tol=1e-14, normalize=True, noise=0.0):
     """``fullsweep!`` with nsite = 1 (``src/mps/sweep.jl:94-196``): sites 1..N moving right,
     then N..1 moving left; lasteigs[bond] from the left-moving update at site bond + 1."""
     N = env.N
@@ -973,11 +1055,11 @@ def fullsweep1(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, kryl
     lasteigs = [None] * (N - 1)
     for q in range(N):
         energy, spec, _ = update_one_site(env, q, "left", maxdim, mindim, cutoff, krylovdim,
-                                          maxiter, tol, normalize)
+                                          maxiter, tol, normalize, noise)
         maxtruncerr = max(spec.truncerr, maxtruncerr)
     for q in range(N - 1, -1, -1):
         energy, spec, _ = update_one_site(env, q, "right", maxdim, mindim, cutoff, krylovdim,
-                                          maxiter, tol, normalize)
+                                          maxiter, tol, normalize, noise)
         if q >= 1:
             lasteigs[q - 1] = spec.eigs
         maxtruncerr = max(spec.truncerr, maxtruncerr)

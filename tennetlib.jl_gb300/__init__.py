@@ -272,9 +272,13 @@ class MPS:
 
 
 class StateEnvs:
-    """``StateEnvs(psi, H::MPO)``: a copy of psi plus lazily built ProjMPO environments."""
+    """``StateEnvs(psi, H::MPO)``: a copy of psi plus lazily built ProjMPO environments.
 
-    def __init__(self, psi: MPS, H: MPO):
+    ``StateEnvs(psi, H, Ms, weight=w)`` (``src/mps/state_envs.jl:88-105``) adds the
+    excited-state projectors of the states Ms: the effective Hamiltonian becomes
+    ProjMPO_MPS2's, H_eff + w sum_k |m_k><m_k| (``src/mps/projmpo_mps2.jl:94-101``)."""
+
+    def __init__(self, psi: MPS, H: MPO, Ms=None, *, weight=None):
         self.ctx = psi.ctx
         self.H = H
         self.phys_q = psi.phys_q
@@ -283,6 +287,16 @@ class StateEnvs:
         h = L.vp()
         L.check(self.ctx.lib.tn_env_create(psi.h, H.h, C.byref(h)))
         _own(self, h)
+        if Ms is not None:
+            self.set_projectors(Ms, weight)
+
+    def set_projectors(self, Ms, weight):
+        """Excited-state projectors (copies of the states in Ms) with the given weight."""
+        Ms = list(Ms)
+        arr = (L.vp * max(len(Ms), 1))(*[m.h for m in Ms])
+        w = -1.0 if weight is None else float(weight)
+        L.check(self.ctx.lib.tn_env_set_projectors(self.h, arr, len(Ms), w))
+        return self
 
     def __len__(self):
         return self.N
@@ -629,21 +643,30 @@ def dmrg_(sysenv: StateEnvs, params: DMRGParams, nsite: int, **kwargs) -> SweepD
     return sw
 
 
-def dmrg(psi0: MPS, H: MPO, params: DMRGParams, nsite: int, **kwargs):
-    """``dmrg(psi0, H, params, nsite)`` -> (energy, psi) (``src/mps/dmrg.jl:231-236``)."""
-    env = StateEnvs(psi0, H)
+def dmrg(psi0: MPS, H: MPO, *args, **kwargs):
+    """``dmrg(psi0, H, params, nsite)`` -> (energy, psi) (``src/mps/dmrg.jl:231-236``), or
+    ``dmrg(psi0, H, Ms, params, nsite; weight)`` for the lowest state with the states Ms
+    projected out (``src/mps/dmrg.jl:238-249``; weight must be > 0)."""
+    if args and isinstance(args[0], (list, tuple)):
+        Ms, params, nsite = args
+        env = StateEnvs(psi0, H, Ms, weight=kwargs.pop("weight", -1.0))
+    else:
+        params, nsite = args
+        env = StateEnvs(psi0, H)
     sw = dmrg_(env, params, nsite, **kwargs)
     return sw.energy[-1], env.getpsi()
 
 
-def dmrg2(psi0: MPS, H: MPO, params: DMRGParams, **kwargs):
-    """``dmrg2`` (``src/mps/dmrg.jl:295-297``)."""
-    return dmrg(psi0, H, params, 2, **kwargs)
+def dmrg2(psi0: MPS, H: MPO, *args, **kwargs):
+    """``dmrg2(psi0, H, [Ms,] params)`` (``src/mps/dmrg.jl:295-301``)."""
+    return dmrg(psi0, H, *args, 2, **kwargs)
 
 
-def dmrg1(psi0: MPS, H: MPO, params: DMRGParams, **kwargs):
-    """``dmrg1`` (``src/mps/dmrg.jl:314-320``): one-site DMRG (noise must be 0)."""
-    return dmrg(psi0, H, params, 1, **kwargs)
+def dmrg1(psi0: MPS, H: MPO, *args, **kwargs):
+    """``dmrg1(psi0, H, [Ms,] params)`` (``src/mps/dmrg.jl:314-320``): one-site DMRG (with
+    noise > 0 each site's solution is split with its neighbour through the two-site
+    density-matrix perturbation)."""
+    return dmrg(psi0, H, *args, 1, **kwargs)
 
 
 # ------------------------------------------------------------------------------------

@@ -102,6 +102,7 @@ PROTOS = {
     "tn_mps_expect_local": (C.c_int, [vp, f64p, f64p]),
     "tn_mps_overlap": (C.c_int, [vp, vp, f64p]),
     "tn_env_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
+    "tn_env_set_projectors": (C.c_int, [vp, C.POINTER(vp), C.c_int, C.c_double]),
     "tn_env_destroy": (C.c_int, [vp]),
     "tn_env_getpsi": (C.c_int, [vp, C.POINTER(vp)]),
     "tn_env_position": (C.c_int, [vp, C.c_int, C.c_int]),

@@ -1,13 +1,15 @@
 // Host driver of the multi-SM SVD of large charge blocks (kernels in kernels_bsvd.cu).
 //
-// For the blocks of one bond it lays out a work arena, runs the blocked Householder QR
+// For the blocks of one bond it lays out a work arena, orders each block's columns by
+// decreasing norm (a static column pivoting), runs the blocked Householder QR
 // (panel kernel + three grouped GEMMs per 32-column panel), the cooperative FP32 Jacobi
 // presolve on R^T, two Newton-Schulz steps V <- V (3 I - V^T V) / 2 and Y = R^T V by grouped
 // GEMMs, the cooperative double-float polish, and Q [V; 0] by grouped GEMMs.  The GEMMs run in
 // the context's precision: FP64 on CUDA cores, or bf16 slices on the tensor cores with seven
 // slices per operand (56 bits, FP64-equivalent products); the two w x w T products always run
 // in FP64.  Results land where the one-CTA kernel puts them: QV (m x n) at x_off of the QV
-// buffer, PY (n x n) at v_off, singular values and permutation at s_off.
+// buffer, PY (n x n, rows in the source column order) at v_off, singular values and
+// permutation at s_off.
 #include <algorithm>
 #include <cstdlib>
 #include <vector>
@@ -137,6 +139,8 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
         d.ydf = take(n * n);
         d.vdf = take(n * n);
         d.scl = take(1);
+        d.cn = take(n);
+        d.piv = take(n);
         w1[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
         w2[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
         mnmax = std::max(mnmax, m * n);

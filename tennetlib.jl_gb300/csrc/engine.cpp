@@ -441,6 +441,7 @@ void env_left_step(tn_env* env, int i) {
     run_gemm(ctx, g1, bs);
     launch_combine(cb, bs, st);
     run_gemm(ctx, g3, bs);
+    if (!env->proj.empty()) proj_left_step(env, i);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
 
@@ -535,6 +536,7 @@ void env_right_step(tn_env* env, int i) {
     run_gemm(ctx, g1, bs);
     launch_combine(cb, bs, st);
     run_gemm(ctx, g3, bs);
+    if (!env->proj.empty()) proj_right_step(env, i);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
 
@@ -1793,7 +1795,14 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     env->vecA.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     env->vecB.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     form_phi(env, p, P.ph, env->vecA.d());
-    auto apply2 = [&](const double* x, double* y) { heff_apply(env, P, x, y); };
+    if (!env->proj.empty()) {
+        TN_REQUIRE(!time_step, "excited-state projectors are built for the eigensolver only");
+        proj_vectors2(env, p, P.ph);
+    }
+    auto apply2 = [&](const double* x, double* y) {
+        heff_apply(env, P, x, y);
+        proj_apply(env, x, y, n);
+    };
     if (!time_step) {
         EigOut eo = lanczos_lowest(env, apply2, n, env->vecA.d(), env->vecB.d(), prm);
         if (prm->check_convergence && eo.converged < 1)
@@ -1856,10 +1865,11 @@ bool halfsweep_done1(int N, int pos, int ortho) {
     return (pos == 0 && ortho == TN_ORTHO_RIGHT) || (pos == N - 1 && ortho == TN_ORTHO_LEFT);
 }
 
-// _update_one_site! (TenNetLib src/mps/update_site.jl:94-190) with the eigensolver and no
-// noise: solve the one-site problem at pos; unless the half sweep is done, split the new
-// tensor by the block SVD with ITensors truncation, keep U at pos (a left isometry for
-// ortho "left", a right one for "right") and multiply S V (resp. U S) into the next site.
+// _update_one_site! (TenNetLib src/mps/update_site.jl:94-190) with the eigensolver: solve
+// the one-site problem at pos; unless the half sweep is done, split the new tensor by the
+// block SVD with ITensors truncation, keep U at pos (a left isometry for ortho "left", a
+// right one for "right") and multiply S V (resp. U S) into the next site.  With noise > 0
+// the new tensor times the next site goes through the two-site noise split instead.
 void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
                      tn_update_result* res, std::vector<double>& eigs) {
     check_params(prm);
@@ -1867,9 +1877,6 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     const int N = psi->N;
     TN_REQUIRE(p >= 0 && p < N, "site position out of range");
     TN_REQUIRE(psi->center == p, "one-site update: the orthogonality center must be at pos");
-    TN_REQUIRE(prm->noise <= 1e-15,
-               "one-site update with noise > 0 (the two-site noise term of "
-               "src/mps/update_site.jl:135-152) is not built");
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
     position(env, p, 1);
@@ -1884,7 +1891,11 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         TN_CUDA(cudaMemcpyAsync(env->vecC.p, site.buf.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
     else
         regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk);
-    auto apply1 = [&](const double* x, double* y) { heff1_apply(env, P1, x, y); };
+    if (!env->proj.empty()) proj_vectors1(env, p, P1.lay);
+    auto apply1 = [&](const double* x, double* y) {
+        heff1_apply(env, P1, x, y);
+        proj_apply(env, x, y, n1);
+    };
     EigOut eo = lanczos_lowest(env, apply1, n1, env->vecC.d(), env->vecD.d(), prm);
     if (prm->check_convergence && eo.converged < 1)
         throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
@@ -1909,6 +1920,34 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         return;
     }
     const bool left = ortho == TN_ORTHO_LEFT;
+    if (prm->noise > 1e-15) {
+        // src/mps/update_site.jl:135-152: the solved site times the next one is split as a
+        // two-site tensor at pos0 with the density-matrix perturbation of that bond.  The
+        // solved site is stored in a grouping the two-site former accepts next to its
+        // neighbour (every pair but right-grouped left of left-grouped).
+        const int p0 = left ? p : p - 1;
+        const Layout nbr = psi->sites[left ? p + 1 : p - 1].lay.layout;
+        const Layout want = left ? (nbr == LG ? LG : site.lay.layout)
+                                 : (nbr == RG ? RG : site.lay.layout);
+        if (want != site.lay.layout) {
+            site.lay = make_site_layout(want, lk, rk, psi->pq);
+            site.buf.alloc(size_t(std::max<int64_t>(site.lay.size, 1)) * 8, st);
+        }
+        if (site.lay.layout == RG)
+            TN_CUDA(cudaMemcpyAsync(site.buf.p, env->vecD.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
+        else
+            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk);
+        env->h1p_pos = -1;
+        position(env, p0, 2);
+        Heff2Plan& P = heff_plan(env);
+        const int64_t n2 = P.ph.size;
+        env->vecA.alloc(size_t(std::max<int64_t>(n2, 1)) * 8, st);
+        form_phi(env, p0, P.ph, env->vecA.d());
+        replace_bond_noise(env, p0, P, env->vecA.d(), prm, ortho, res, eigs);
+        res->neigs = int(eigs.size());
+        if (ctx->prec == TN_PREC_SPLIT) check_device_error(ctx);
+        return;
+    }
     // SVD blocks: per right sector (LG grouping) for "left", per left sector (RG) for "right"
     SiteLayout sv_lay = left ? make_site_layout(LG, lk, rk, psi->pq) : P1.lay;
     const double* phi = env->vecD.d();
@@ -2442,6 +2481,40 @@ int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out) {
     });
 }
 
+int tn_env_set_projectors(tn_env* env, const tn_mps* const* Ms, int count, double weight) {
+    return guarded([&] {
+        TN_REQUIRE(env, "null argument");
+        TN_REQUIRE(count >= 0 && count <= 32, "between 0 and 32 projector states");
+        const tn_mps* psi = env->psi.get();
+        if (count > 0) {
+            TN_REQUIRE(Ms, "null argument");
+            if (!(weight > 0.0)) {
+                char msg[160];
+                std::snprintf(msg, sizeof msg,
+                              "`weight` parameter should be > 0.0 (value passed was `weight=%g`)",
+                              weight);
+                throw Error(TN_E_INVALID, msg);
+            }
+            for (int k = 0; k < count; ++k)
+                TN_REQUIRE(Ms[k] && Ms[k]->ctx == env->ctx && Ms[k]->N == psi->N &&
+                               Ms[k]->d == psi->d && Ms[k]->pq == psi->pq,
+                           "projector states must share the context and the site indices of psi");
+        }
+        sync(env->ctx);
+        env->proj.clear();
+        for (int k = 0; k < count; ++k) {
+            ProjState P;
+            P.M = copy_mps(Ms[k]);
+            env->proj.push_back(std::move(P));
+        }
+        env->proj_weight = count > 0 ? weight : 0.0;
+        proj_init(env);
+        sync(env->ctx);
+        check_device_error(env->ctx);
+        env->ctx->timer.collect(env->acc_ms);
+    });
+}
+
 int tn_env_destroy(tn_env* env) {
     if (env) cudaStreamSynchronize(env->ctx->stream);
     delete env;
@@ -2535,6 +2608,11 @@ int tn_env_product(tn_env* env, const double* v, double* out, int64_t n) {
         if (!hb.empty())
             TN_CUDA(cudaMemcpyAsync(env->vecA.p, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
         heff_apply(env, P, env->vecA.d(), env->vecB.d());
+        if (!env->proj.empty()) {  // ProjMPO_MPS2 product (src/mps/projmpo_mps2.jl:94-101)
+            env->part.alloc(size_t(32) * blas_nparts() * 8, st);
+            proj_vectors2(env, p, P.ph);
+            proj_apply(env, env->vecA.d(), env->vecB.d(), P.ph.size);
+        }
         if (!hb.empty())
             TN_CUDA(cudaMemcpyAsync(hb.data(), env->vecB.p, hb.size() * 8, cudaMemcpyDeviceToHost, st));
         sync(env->ctx);

@@ -41,6 +41,16 @@ struct BsvdStats {
     int sweeps32 = 0, sweeps_df = 0;
 };
 
+// overlap environment of psi against a projector state on one link: one D_psi(q) x D_M(q)
+// block (column-major) per charge q that both links carry
+struct OvEnv {
+    std::vector<int> q, da, db;
+    std::vector<int64_t> off;
+    int64_t size = 0;
+    DevBuf buf;
+    int find(int charge) const;
+};
+
 }  // namespace tn
 
 struct tn_ctx;
@@ -129,6 +139,24 @@ struct Heff1Plan {
     double flops = 0;
 };
 
+// one excited-state projector (ProjMPS2): a copy of M and its overlap environments with psi,
+// L[i] over sites < i (link i), R[i] over sites > i (link i + 1)
+struct ProjState {
+    std::unique_ptr<tn_mps> M;
+    std::vector<tn::OvEnv> L, R;
+};
+
+struct tn_env;
+namespace tn {
+// excited-state projectors (proj.cpp)
+void proj_init(tn_env* env);             // edge blocks and the environments up to lpos / rpos
+void proj_left_step(tn_env* env, int i);   // LM[i+1] of every projector
+void proj_right_step(tn_env* env, int i);  // RM[i-1]
+void proj_vectors2(tn_env* env, int p, const PhiLayout& ph);    // m_k at bond p -> projm
+void proj_vectors1(tn_env* env, int p, const SiteLayout& lay);  // m_k at site p (RG) -> projm
+void proj_apply(tn_env* env, const double* x, double* y, int64_t n);  // y += w sum m (m . x)
+}  // namespace tn
+
 struct tn_env {
     tn_ctx* ctx = nullptr;
     std::unique_ptr<tn_mps> psi;
@@ -149,4 +177,9 @@ struct tn_env {
     int64_t gemm_launches = 0;
     int64_t matvecs = 0;
     double heff_flops = 0;
+    // excited-state projectors (ProjMPO_MPS2): states, weight, the projected vectors of the
+    // current position (K x n) and work buffers
+    std::vector<ProjState> proj;
+    double proj_weight = 0.0;
+    tn::DevBuf projm, projc, projt1, projt2;
 };

@@ -3,6 +3,9 @@
 // A charge block of a two-site tensor at chi ~ 2048 has several hundred columns; one CTA per
 // block (svd_qrj_kernel) then works out of L2 and uses a handful of SMs.  Here the O(n^3)
 // work is spread over the whole GPU:
+//  * the columns are ordered by decreasing norm before the QR: a static column pivoting that
+//    leaves the rows of R graded as the pivoted QR of the Jacobi preconditioner does, so
+//    that the sweeps on R^T converge several times faster on the graded blocks of DMRG;
 //  * blocked Householder QR A = Q R: each 32-column panel is factored by one CTA in shared
 //    memory (double-float), the trailing matrix is updated by grouped GEMMs with the compact
 //    WY form Q_p = I - V T V^T (Schreiber & Van Loan 1989);
@@ -77,10 +80,84 @@ __global__ void bsvd_gather_kernel(const BsvdBlk* __restrict__ descs, const doub
     const double* M = src + d.src_off;
     double* X = ar + d.xq;
     const int ex = int(ar[d.scl]);
+    const int* pv = reinterpret_cast<const int*>(ar + d.piv);
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot;
          e += int64_t(gridDim.x) * blockDim.x) {
-        const int i = int(e % d.m), k = int(e / d.m);
+        const int i = int(e % d.m), k = pv[int(e / d.m)];
         X[e] = ldexp(d.trans ? M[k + int64_t(i) * d.rows] : M[i + int64_t(k) * d.rows], -ex);
+    }
+}
+
+// norms of the work matrix's columns (columns of the block, or its rows when it is worked on
+// transposed): a warp per column, or a thread per row of the source when transposed, so the
+// loads stay coalesced
+__global__ void bsvd_colnorm_kernel(const BsvdBlk* __restrict__ descs,
+                                    const double* __restrict__ src, double* __restrict__ ar) {
+    const BsvdBlk d = descs[blockIdx.y];
+    const double* M = src + d.src_off;
+    double* cn = ar + d.cn;
+    if (d.trans) {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.n; k += gridDim.x * blockDim.x) {
+            double s = 0.0;
+            for (int i = 0; i < d.m; ++i) {
+                const double x = M[k + int64_t(i) * d.rows];
+                s = fma(x, x, s);
+            }
+            cn[k] = sqrt(s);
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < d.n; k += nw) {
+        const double* mk = M + int64_t(k) * d.rows;
+        double s = 0.0;
+        for (int i = lane; i < d.m; i += 32) s = fma(mk[i], mk[i], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) cn[k] = sqrt(s);
+    }
+}
+
+// column order by decreasing norm, ties by index (bitonic sort of the padded key list in
+// shared memory, one CTA per block): piv[k] = source column of work column k, piv[n + c] =
+// work column of source column c
+constexpr int SORT_MAX = 4096;  // >= bsvd_max_n()
+__global__ void __launch_bounds__(BT) bsvd_presort_kernel(const BsvdBlk* __restrict__ descs,
+                                                          double* __restrict__ ar) {
+    __shared__ float key[SORT_MAX];
+    __shared__ int idx[SORT_MAX];
+    const BsvdBlk d = descs[blockIdx.x];
+    const int n = d.n;
+    int np = 1;
+    while (np < n) np <<= 1;
+    const double* cn = ar + d.cn;
+    for (int k = threadIdx.x; k < np; k += BT) {
+        key[k] = k < n ? float(cn[k]) : -1.f;
+        idx[k] = k;
+    }
+    __syncthreads();
+    for (int size = 2; size <= np; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < (np >> 1); t += BT) {
+                const int lo = 2 * t - (t & (stride - 1)), hi = lo + stride;
+                const float kl = key[lo], kh = key[hi];
+                const int il = idx[lo], ih = idx[hi];
+                const bool lo_first = kl > kh || (kl == kh && il < ih);
+                if (lo_first != ((lo & size) == 0)) {
+                    key[lo] = kh;
+                    key[hi] = kl;
+                    idx[lo] = ih;
+                    idx[hi] = il;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    int* pv = reinterpret_cast<int*>(ar + d.piv);
+    for (int k = threadIdx.x; k < n; k += BT) {
+        pv[k] = idx[k];
+        pv[n + idx[k]] = k;
     }
 }
 
@@ -672,7 +749,7 @@ bj_kernel(const BjDesc* __restrict__ descs, int nd, float tol, int max_sweeps, i
 }
 
 // singular values = column norms of Y (double-float), sorted descending with the
-// permutation; PY = Y (no pivoting), QV = [V; 0] (m x n) for the application of Q
+// permutation (PY = P Y and QV = [V; 0] are written by bsvd_outputs_kernel)
 __global__ void __launch_bounds__(BT) bsvd_finish_kernel(const BsvdBlk* __restrict__ descs,
                                                          double* __restrict__ ar,
                                                          double* __restrict__ qv,
@@ -685,7 +762,6 @@ __global__ void __launch_bounds__(BT) bsvd_finish_kernel(const BsvdBlk* __restri
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double* h = reinterpret_cast<double*>(smem);
     const df2* Y = reinterpret_cast<const df2*>(ar + d.ydf);
-    const df2* Vd = reinterpret_cast<const df2*>(ar + d.vdf);
     const int ex = int(ar[d.scl]);  // undo the power-of-two scaling of the block
     for (int j = warp; j < n; j += BT / 32) {
         const df2* yj = Y + int64_t(j) * n;
@@ -708,7 +784,7 @@ __global__ void __launch_bounds__(BT) bsvd_finish_kernel(const BsvdBlk* __restri
     (void)m;
 }
 
-// PY = Y (scaled back) and QV = [V; 0]: element-wise, spread over many CTAs per block (the
+// PY = P Y (scaled back, rows in the source column order) and QV = [V; 0]: element-wise, spread over many CTAs per block (the
 // conversions from double-float use the FP64 pipe)
 __global__ void bsvd_outputs_kernel(const BsvdBlk* __restrict__ descs, const double* __restrict__ ar,
                                     double* __restrict__ qv, double* __restrict__ py) {
@@ -719,12 +795,13 @@ __global__ void bsvd_outputs_kernel(const BsvdBlk* __restrict__ descs, const dou
     const df2* Vd = reinterpret_cast<const df2*>(ar + d.vdf);
     double* P = py + d.v_off;
     double* Z = qv + d.x_off;
+    const int* ip = reinterpret_cast<const int*>(ar + d.piv) + n;  // work column of source c
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int j = gw; j < n; j += nw) {
         const df2* yj = Y + int64_t(j) * n;
         double* pj = P + int64_t(j) * n;
-        for (int i = lane; i < n; i += 32) pj[i] = ldexp(df_to_double(yj[i]), ex);
+        for (int c = lane; c < n; c += 32) pj[c] = ldexp(df_to_double(yj[ip[c]]), ex);
         double* zj = Z + int64_t(j) * m;
         const df2* vj = Vd + int64_t(j) * n;
         for (int i = lane; i < m; i += 32) zj[i] = (i < n) ? df_to_double(vj[i]) : 0.0;
@@ -794,6 +871,12 @@ void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* s
                         cudaStream_t s) {
     if (nb <= 0) return;
     bsvd_scale_kernel<<<nb, BT, 0, s>>>(d, src, ar);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+    bsvd_colnorm_kernel<<<dim3(16, nb), 256, 0, s>>>(d, src, ar);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+    bsvd_presort_kernel<<<nb, BT, 0, s>>>(d, ar);
     TN_CUDA(cudaGetLastError());
     count_launch();
     bsvd_gather_kernel<<<dim3(grid_chunks(mnmax), nb), 256, 0, s>>>(d, src, ar);

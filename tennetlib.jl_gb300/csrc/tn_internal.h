@@ -301,6 +301,9 @@ struct BsvdBlk {
     int64_t r32, v32;         // n x n FP32 (float arrays)
     int64_t ydf, vdf;         // n x n double-float
     int64_t scl;              // one double: the block is worked on scaled by 2^-e, e stored here
+    int64_t cn;               // n doubles: norms of the work matrix's columns
+    int64_t piv;              // n doubles holding 2 n ints: the column order (work column k is
+                              // source column piv[k]) and its inverse at piv + n
     int64_t x_off, v_off, s_off;  // outputs: QV (m x n) in the QV buffer, PY (n x n), S / perm
     int32_t rows, cols, trans, m, n, pad;
 };
@@ -317,7 +320,7 @@ int bsvd_panel_width(int mmax);
 // largest n the Jacobi kernels accept
 int bsvd_max_n();
 // scales each block by a power of two to a largest entry in [1/2, 1) while copying it (or
-// its transpose) into the QR work matrix
+// its transpose) into the QR work matrix, its columns ordered by decreasing norm
 void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* src, double* ar,
                         cudaStream_t s);
 void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int mmax, double* ar,
@@ -332,7 +335,8 @@ void launch_bsvd_jacobi(const BjDesc* d, int nd, int nctas, int maxn, int precis
 int bsvd_jacobi_capacity(int maxn, int precision);
 // columns per block of the Jacobi kernel for the largest n (precision 0 FP32, 1 double-float)
 int bsvd_jacobi_block(int maxn, int precision);
-// singular values (sorted, with the permutation), PY = Y and QV = [V; 0]
+// singular values (sorted, with the permutation), PY = P Y (rows back in the source column
+// order) and QV = [V; 0]
 void launch_bsvd_finish(const BsvdBlk* d, int nb, double* ar, double* qv, double* py, double* S,
                         int* perm, cudaStream_t s);
 

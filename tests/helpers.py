@@ -47,3 +47,13 @@ def oracle_envs(mps, H, p):
     env = O.StateEnvs(mps, H)
     env.position(p, 2)
     return env.L[p], env.R[p + 1]
+
+
+def dense_mpo(H):
+    """Contract an MPO to a dense matrix (small N only)."""
+    acc = H.W[0][0]  # (b, s', s)
+    for W in H.W[1:]:
+        b, Sp, S = acc.shape
+        d = W.shape[2]
+        acc = np.einsum("bxy,bcuv->cxuyv", acc, W).reshape(W.shape[1], Sp * d, S * d)
+    return acc[0]

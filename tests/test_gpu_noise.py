@@ -1,6 +1,7 @@
 """Density-matrix noise term of the two-site update (noiseterm + replacebond! with an
-eigen perturbation, TenNetLib src/mps/update_site.jl:59-76) against the oracle's
-restatement, through dmrg!'s noise schedule (src/mps/dmrg.jl:212-223).
+eigen perturbation, TenNetLib src/mps/update_site.jl:59-76) and of the one-site update
+(:135-152) against the oracle's restatement, through dmrg!'s noise schedule
+(src/mps/dmrg.jl:212-223).
 
 Per sweep: |dE/E| <= 1e-10 and identical largest bond dimension; at the end the charge
 sectors of every link bit-exact and the energy at the exact ground energy (1e-8)."""
@@ -71,3 +72,29 @@ def test_noise_update_matches_oracle_both_directions(tn):
         # the updates chain 17 noisy bond splits: 1e-10 on the density-matrix eigenvalues
         assert np.allclose(eigs_g, spec.eigs, rtol=0, atol=1e-10), (b, ortho)
         assert abs(err_g - spec.truncerr) <= 1e-14 + 1e-8 * spec.truncerr, (b, ortho)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_one_site_noise_sweeps_match_oracle(tn, prec):
+    # one-site DMRG from a product state: only the noise term can grow the bonds (the
+    # reference's own test runs dmrg1 this way, test/test_MPS_DMRG.jl:50-65)
+    N = 12
+    ctx = tn.Context(0, precision=prec, slices=5)
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+    eo = O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H)
+    so = O.SweepData()
+    pq = H.phys_q.astype(np.int32)
+    eg = tn.StateEnvs(tn.MPS.product(start, pq, ctx), upload_mpo(tn, ctx, H))
+    sg = tn.SweepData()
+    sched = [(8, 1e-3), (16, 5e-4), (32, 2.5e-4), (64, 1.25e-4), (64, 0.0), (64, 0.0)]
+    for md, nz in sched:
+        O.fullsweep1(eo, so, md, 1e-14, 1, 4, 2, 1e-14, noise=nz)
+        tn.fullsweep_(eg, tn.eig_solver, 1, sg, maxdim=md, cutoff=1e-14, solver_krylovdim=4,
+                      noise=nz, outputlevel=0)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1]), (md, nz)
+        assert sg.maxchi[-1] == so.maxchi[-1], (md, nz)
+    assert so.maxchi[-1] > 8
+    psi = eg.getpsi()
+    for i in range(N + 1):
+        assert np.array_equal(psi.link_charges(i), eo.psi.links[i]), i

@@ -163,8 +163,8 @@ def test_update_position_errors(tn, ctx):
     env = tn.StateEnvs(tn.MPS.product(tn.models.neel_states(N), pq, ctx), tn.MPO(W, delta, pq, ctx))
     with pytest.raises(tn.TenNetError):
         tn.update_position_(env, tn.eig_solver, 2, 2, "left")  # center is at site 0
-    with pytest.raises(tn.TenNetError):  # one-site update with noise: not built
-        tn.update_position_(env, tn.eig_solver, 0, 1, "left", noise=1e-3)
+    with pytest.raises(tn.TenNetError):  # negative noise
+        tn.update_position_(env, tn.eig_solver, 0, 1, "left", noise=-1e-3)
     e, err, eigs = tn.update_position_(env, tn.eig_solver, 0, 2, "left", maxdim=4)
     assert np.isfinite(e) and len(eigs) >= 1
 

@@ -231,6 +231,24 @@ def test_oracle_one_site_sweeps_reach_ed():
     for i in range(1, N):
         A = env.psi.A[i].reshape(env.psi.A[i].shape[0], -1)
         assert np.allclose(A @ A.T, np.eye(A.shape[0]), atol=1e-12)
+
+
+def test_oracle_one_site_noise():
+    """One-site DMRG with noise (src/mps/update_site.jl:135-152) grows the bonds of a product
+    state and reaches the exact ground energy; without noise the bonds stay at 1."""
+    N = 10
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+    env = O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H)
+    sw = O.SweepData()
+    O.fullsweep1(env, sw, 8, 1e-14, 1, 4, 2, 1e-14)
+    assert sw.maxchi[-1] == 1
+    for md, nz in [(8, 1e-3), (16, 5e-4), (32, 2.5e-4), (32, 0.0), (32, 0.0)]:
+        O.fullsweep1(env, sw, md, 1e-14, 1, 4, 2, 1e-14, noise=nz)
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
+    assert sw.maxchi[-1] > 8
+    assert abs(sw.energy[-1] - gold["heisenberg_chain"][str(N)]) < 1e-10
+
     gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ed_energies.json")))
     assert abs(sw.energy[-1] - gold["heisenberg_chain"][str(N)]) < 1e-10
 
@@ -291,3 +309,33 @@ def test_oracle_noise_term():
     for i in range(1, N):
         A = env.psi.A[i].reshape(env.psi.A[i].shape[0], -1)
         assert np.allclose(A @ A.T, np.eye(A.shape[0]), atol=1e-12)
+
+
+@pytest.mark.parametrize("nsite", [1, 2])
+def test_oracle_excited_state_projector(nsite):
+    """ProjMPO_MPS2 (src/mps/projmpo_mps2.jl:94-101) with the ground state as M and weight 10
+    (the reference's own excited-state test, test/test_MPS_DMRG.jl:71-96): DMRG reaches the
+    second-lowest energy of the S^z = 0 sector, and the result is orthogonal to M."""
+    N = 8
+    H = O.heisenberg_mpo(N)
+    D = _dense_h(H)
+    sz = np.array([sum(0.5 - ((k >> (N - 1 - i)) & 1) for i in range(N)) for k in range(2 ** N)])
+    sec = np.nonzero(sz == 0)[0]
+    ev = np.linalg.eigvalsh(D[np.ix_(sec, sec)])
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+    sw, env = O.dmrg(O.product_mps(start, O.SPIN_HALF_Q), H, maxdim=[16, 32], nsweeps=[3, 4],
+                     cutoff=1e-14)
+    assert abs(sw.energy[-1] - ev[0]) < 1e-10
+    gr = env.psi
+    with pytest.raises(ValueError):
+        O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H, [gr], weight=0.0)
+    ex = O.StateEnvs(O.product_mps(start, O.SPIN_HALF_Q), H, [gr], weight=10.0)
+    sx = O.SweepData()
+    # two-site sweeps grow the bonds; one-site ones then run from the grown state
+    for md in (16, 32, 32, 32, 32, 32):
+        O.fullsweep(ex, sx, md, 1e-14, 1, 5, 2, 1e-14)
+    if nsite == 1:
+        for _ in range(3):
+            O.fullsweep1(ex, sx, 32, 1e-14, 1, 5, 2, 1e-14)
+    assert abs(sx.energy[-1] - ev[1]) < 1e-8
+    assert abs(O.inner(ex.psi, gr)) < 1e-6
