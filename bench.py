@@ -358,6 +358,10 @@ def run_ours(args, world, rank, local, pg):
         if rank == 0:
             print(json.dumps({"j1j2_chi2048": run_j1j2(tn, local, args)}), flush=True)
         return
+    if args.svd_bond:
+        if rank == 0:
+            print(json.dumps({"svd_bond": run_svd_bond(tn, local, args)}), flush=True)
+        return
     ctx = tn.Context(local)
     if args.precision == "split":
         ctx.set_precision("split", args.slices)
@@ -559,6 +563,34 @@ def run_j1j2(tn, local, args):
     return out
 
 
+# one bond's charge blocks at chi ~ 2048 (the sizes of the largest bond of the 6 x 16 J1-J2
+# cylinder): rows x cols of the seven largest blocks
+SVD_BOND_SHAPES = [(1200, 1100), (1150, 1050), (1100, 1000), (900, 850), (600, 450), (300, 250),
+                   (150, 126)]
+
+
+def run_svd_bond(tn, local, args):
+    """The block SVD of one chi ~ 2048 bond (seeded synthetic blocks graded over 8 decades on
+    both sides, as a two-site tensor between Schmidt bases) through tn_svd_truncate, in the
+    context's precision: wall time per call and the SVD's work counters."""
+    import numpy as np
+    rng = np.random.default_rng(7)
+    blocks = []
+    for r, c in SVD_BOND_SHAPES:
+        dl = 10.0 ** (-8.0 * (np.arange(r) / r) ** 0.8) * rng.uniform(0.7, 1.3, r)
+        dr = 10.0 ** (-8.0 * (np.arange(c) / c) ** 0.8) * rng.uniform(0.7, 1.3, c)
+        blocks.append(dl[:, None] * rng.standard_normal((r, c)) * dr[None, :])
+    ctx = tn.Context(local, precision=args.precision, slices=args.slices)
+    walls = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        kept, _, err = tn.svd_truncate(blocks, cutoff=1e-12, ctx=ctx)
+        walls.append(time.perf_counter() - t0)
+    return {"workload": "block SVD of one chi~2048 bond (7 charge blocks, largest 1200 x 1100)",
+            "precision": args.precision, "calls": len(walls), "wall_s": walls,
+            "kept": [int(k) for k in kept], "truncerr": float(err)}
+
+
 def fp64_compare(tn, ctx, H, pq, tensors, links, local):
     """One sweep from the same state on the split path and on the FP64 GPU path."""
     out = {}
@@ -602,6 +634,8 @@ def main():
     ap.add_argument("--ttn-instances", type=int, default=TTN_INSTANCES)
     ap.add_argument("--j1j2-chi2048", action="store_true",
                     help="only the J1-J2 cylinder comparison at chi = 2048 (split vs FP64)")
+    ap.add_argument("--svd-bond", action="store_true",
+                    help="only the block SVD of one chi ~ 2048 bond (--steps calls)")
     ap.add_argument("--no-j1j2", action="store_true",
                     help="skip the chi = 2048 J1-J2 comparison leg of the default run")
     ap.add_argument("--j1j2-lx", type=int, default=J1J2_LX,
