@@ -449,10 +449,12 @@ def run_ours(args, world, rank, local, pg):
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
              for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
     dominant = max(("svd_ms", "heff_ms", "lanczos_ms", "env_ms"), key=lambda k: share[k])
-    dom = {"svd_ms": {"kernel": "svd_qrj_kernel (block SVD: double-float QR with pivoting, FP32 "
-                                "Jacobi presolve, double-float polish)",
-                      "bound": "FP32 and FP64 pipes of one SM per charge block (latency-bound at "
-                               "chi~180: 7-9 blocks of <= ~103 columns per bond)"},
+    dom = {"svd_ms": {"kernel": "block SVD per bond: svd_qrj_kernel (one CTA per charge block: "
+                                "double-float QR with pivoting, FP32 Jacobi presolve, double-float "
+                                "polish) or the multi-SM pipeline (blocked QR + cooperative "
+                                "block-pair Jacobi), split tuned per block-size histogram",
+                      "bound": "FP32 pipe of one SM per charge block (latency-bound at chi~180: "
+                               "7-9 blocks of <= ~110 columns per bond)"},
            "heff_ms": {"kernel": "split_pack_kernel + split_gemm_kernel + combine_kernel",
                        "bound": "tensor (see roofline)"},
            "lanczos_ms": {"kernel": "gs_pass_kernel", "bound": "hbm"},
@@ -481,6 +483,7 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": d2h,
                 "what": "upload MPS from host + build environments + one sweep + download MPS"},
     }
+    res["svd_schedule"] = ctx.svd_schedule()
     if args.precision == "split" and not args.no_fp64_compare:
         res["fp64_compare"] = fp64_compare(tn, ctx, H, pq, tensors, links, local)
     if world == 1 and not args.no_cpu_baseline:
@@ -548,10 +551,16 @@ def run_j1j2(tn, local, args):
                      "svd_gemm_flops": st.get("svd_gemm_flops", 0.0),
                      "svd_jacobi_flops": st.get("svd_jacobi_flops", 0.0),
                      "svd_sweeps_max": [st.get("svd_sweeps32", 0), st.get("svd_sweeps_df", 0)],
+                     # algorithmic SVD flops (GEMMs + Jacobi rotations, FP64-equivalent) over
+                     # the whole SVD time (QR panels and small-block kernels included)
+                     "svd_algorithmic_tflops": (st.get("svd_gemm_flops", 0.0) +
+                                                st.get("svd_jacobi_flops", 0.0))
+                                               / max(st["svd_ms"], 1e-9) / 1e9,
                      "energy": s.energy[-1], "maxlinkdim": s.maxchi[-1],
                      "maxtruncerr": s.maxtruncerr[-1]}
         final[prec] = e.getpsi()
         del e
+    out["svd_schedule"] = ctx.svd_schedule()
     ps, pd = final["split"], final["fp64"]
     out["overlap_split_fp64"] = abs(ps.inner(pd)) / math.sqrt(ps.inner(ps) * pd.inner(pd))
     out["dE_rel"] = abs(out["split"]["energy"] - out["fp64"]["energy"]) / abs(out["fp64"]["energy"])

@@ -106,8 +106,16 @@ int tn_ctx_destroy(tn_ctx* ctx);
 int tn_ctx_set_precision(tn_ctx* ctx, int mode, int slices);
 /* Block SVD of replacebond!: charge blocks with more than ncols columns (of the m >= n
  * orientation) are factored by the multi-SM pipeline (blocked QR + cooperative Jacobi), the
- * others by one CTA each.  Default 96; 0 sends every block to the multi-SM pipeline. */
+ * others by one CTA each; 0 sends every block to the multi-SM pipeline.  Default -1: the
+ * threshold is tuned per block-size histogram (keyed on the bond's largest block in
+ * 32-column buckets; each candidate threshold is timed once on the first bonds of a key,
+ * then the fastest is kept). */
 int tn_ctx_set_svd_split(tn_ctx* ctx, int ncols);
+/* The tuned SVD schedule so far: *count keys; for the first cap of them entries[9 i ..] =
+ * (bucket, candidates, chosen threshold or -1 while still timing, candidates timed,
+ * threshold of candidate 0..4 (2147483647: every block on one CTA)) and ms[5 i ..] = the
+ * measured milliseconds of each candidate (-1: not yet timed). */
+int tn_ctx_svd_schedule(tn_ctx* ctx, int32_t* entries, float* ms, int cap, int* count);
 /* Test hook of the failure path (no counterpart in the reference, whose solver only raises
  * on non-convergence, src/base/solver.jl:38-41): the next launch on this context of the
  * named kernel makes one of its bounded device waits run out, without any fault:

@@ -99,8 +99,32 @@ class Context:
         self.slices = slices
 
     def set_svd_split(self, ncols: int):
-        """Charge blocks with more than ``ncols`` columns take the multi-SM block SVD."""
+        """Charge blocks with more than ``ncols`` columns take the multi-SM block SVD (-1:
+        the threshold is tuned per block-size histogram, the default)."""
         L.check(self.lib.tn_ctx_set_svd_split(self.h, int(ncols)))
+
+    def svd_schedule(self) -> list:
+        """The tuned block-SVD schedule: per 32-column bucket of a bond's largest block, the
+        candidate thresholds (None: every block on one CTA), their measured milliseconds,
+        whether the choice is settled, and the chosen threshold (None: one CTA each)."""
+        n = C.c_int(0)
+        L.check(self.lib.tn_ctx_svd_schedule(self.h, None, None, 0, C.byref(n)))
+        cap = max(n.value, 1)
+        ent = (C.c_int32 * (9 * cap))()
+        ms = (C.c_float * (5 * cap))()
+        L.check(self.lib.tn_ctx_svd_schedule(self.h, ent, ms, cap, C.byref(n)))
+        big = 2147483647
+        out = []
+        for i in range(n.value):
+            e = ent[9 * i: 9 * i + 9]
+            k = e[1]
+            th = [None if t == big else int(t) for t in e[4:4 + k]]
+            out.append({"bucket": int(e[0]), "candidates": th,
+                        "ms": [float(x) for x in ms[5 * i: 5 * i + k]],
+                        "settled": e[2] != -1,
+                        "chosen": None if e[2] in (-1, big) else int(e[2]),
+                        "timed": int(e[3])})
+        return out
 
     @classmethod
     def default(cls) -> "Context":

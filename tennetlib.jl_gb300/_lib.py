@@ -87,6 +87,8 @@ PROTOS = {
     "tn_ctx_destroy": (C.c_int, [vp]),
     "tn_ctx_set_precision": (C.c_int, [vp, C.c_int, C.c_int]),
     "tn_ctx_set_svd_split": (C.c_int, [vp, C.c_int]),
+    "tn_ctx_svd_schedule": (C.c_int, [vp, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_int,
+                                      C.POINTER(C.c_int)]),
     "tn_ctx_inject_wait_timeout": (C.c_int, [vp, C.c_int]),
     "tn_last_error": (C.c_char_p, []),
     "tn_version": (C.c_char_p, []),

@@ -1257,6 +1257,21 @@ struct SvdResult {
 };
 
 // SVD of the listed blocks of src (device); results stay in the env work buffers.
+// Thresholds the SVD tuner tries for a bond whose largest pipeline-eligible block falls in
+// bucket k (32 (k - 1) < n <= 32 k, k <= 32): every block on the one-CTA kernel while n <= 256
+// (beyond that its work matrices leave shared memory and it is known to lose), and the
+// thresholds 64, 96, 128 and 176 below the bucket (the mid-size blocks ride along with the
+// large ones in the cooperative launch).
+std::vector<int> svd_candidates(int k) {
+    const int lo = 32 * (k - 1) + 1, hi = 32 * k;
+    std::vector<int> c;
+    if (hi <= 256) c.push_back(INT_MAX);
+    for (int t : {64, 96, 128, 176})
+        if (t < lo) c.push_back(t);
+    if (c.empty()) c.push_back(INT_MAX);
+    return c;
+}
+
 void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevBuf& dS,
                DevBuf& dPerm, DevBuf& ddesc, const std::vector<int>& rows,
                const std::vector<int>& cols, const std::vector<int64_t>& offs, const double* src,
@@ -1289,17 +1304,45 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
     dP.alloc(size_t(std::max<int64_t>(vo, 1)) * 8, st);
     dS.alloc(size_t(std::max<int64_t>(so, 1)) * 8, st);
     dPerm.alloc(size_t(std::max<int64_t>(so, 1)) * 4, st);
-    // blocks with more than ctx->svd_big_n columns (after orienting m >= n) go to the multi-SM
-    // pipeline, the others to the one-CTA-per-block kernel
+    // blocks with more than `thr` columns (after orienting m >= n) go to the multi-SM
+    // pipeline, the others to the one-CTA-per-block kernel; thr is the context's fixed
+    // threshold, or the tuned one of this bond's block-size histogram
+    auto eligible = [](const SvdBlockDesc& d) {
+        return d.n <= bsvd_max_n() && bsvd_panel_width(d.m) > 0;
+    };
+    int thr = ctx->svd_big_n;
+    SvdTuner::Entry* te = nullptr;
+    int ci = -1;
+    if (thr < 0) {
+        int nmax_e = 0;
+        for (const auto& d : R.desc)
+            if (eligible(d)) nmax_e = std::max(nmax_e, d.n);
+        SvdTuner::Entry& e = ctx->svd_tune.table[std::min((nmax_e + 31) / 32, 32)];
+        if (e.cand.empty()) {
+            e.cand = svd_candidates(std::min((nmax_e + 31) / 32, 32));
+            e.ms.assign(e.cand.size(), -1.f);
+            if (e.cand.size() == 1) e.best = 0;
+        }
+        ci = e.best >= 0 ? e.best : e.next;
+        thr = e.cand[size_t(ci)];
+        if (e.best < 0) te = &e;
+    }
     std::vector<SvdBlockDesc> small, big;
     int maxn_small = 1;
     for (const auto& d : R.desc) {
-        if (d.n > ctx->svd_big_n && d.n <= bsvd_max_n() && bsvd_panel_width(d.m) > 0) {
+        if (d.n > thr && eligible(d)) {
             big.push_back(d);
         } else {
             small.push_back(d);
             maxn_small = std::max(maxn_small, d.n);
         }
+    }
+    if (te) {
+        if (!ctx->svd_tune.a) {
+            TN_CUDA(cudaEventCreate(&ctx->svd_tune.a));
+            TN_CUDA(cudaEventCreate(&ctx->svd_tune.b));
+        }
+        TN_CUDA(cudaEventRecord(ctx->svd_tune.a, st));
     }
     const int nsm_blocks = (int)small.size();
     ddesc.alloc(std::max<size_t>(size_t(nsm_blocks) * sizeof(SvdBlockDesc), 16), st);
@@ -1343,11 +1386,19 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
         std::fprintf(stderr, "svd big blocks: %d (largest n %d) sweeps fp32=%d df=%d\n",
                      (int)big.size(), mx, bst.sweeps32, bst.sweeps_df);
     }
+    if (te) TN_CUDA(cudaEventRecord(ctx->svd_tune.b, st));
     R.S.resize(size_t(so));
     if (so)
         TN_CUDA(cudaMemcpyAsync(R.S.data(), dS.p, size_t(so) * 8, cudaMemcpyDeviceToHost, st));
     sync(ctx);
     if (!big.empty()) check_device_error(ctx);
+    if (te) {
+        float ms = 0.f;
+        TN_CUDA(cudaEventElapsedTime(&ms, ctx->svd_tune.a, ctx->svd_tune.b));
+        te->ms[size_t(ci)] = ms;
+        if (++te->next == int(te->cand.size()))
+            te->best = int(std::min_element(te->ms.begin(), te->ms.end()) - te->ms.begin());
+    }
 }
 
 struct TruncDecision {
@@ -2197,6 +2248,10 @@ void tn::run_split_plan(tn_ctx* ctx, SplitPlan& sp, const Bases& bs) {
     run_split(ctx, sp, bs, nullptr, nullptr);
 }
 void tn::check_device_error_public(tn_ctx* ctx) { check_device_error(ctx); }
+tn::SvdTuner::~SvdTuner() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+}
 
 // SVD with ITensors truncation of one dense m x n matrix A on the device (the block SVD of
 // replacebond! on a single block): U (m x k, ld m) and S V^T (k x n, ld k); returns k.
@@ -2326,8 +2381,30 @@ int tn_ctx_inject_wait_timeout(tn_ctx* ctx, int kernel) {
 int tn_ctx_set_svd_split(tn_ctx* ctx, int ncols) {
     return guarded([&] {
         TN_REQUIRE(ctx, "null context");
-        TN_REQUIRE(ncols >= 0, "the column threshold must be >= 0");
+        TN_REQUIRE(ncols >= -1, "the column threshold must be >= 0, or -1 (tuned)");
         ctx->svd_big_n = ncols;
+    });
+}
+
+int tn_ctx_svd_schedule(tn_ctx* ctx, int32_t* entries, float* ms, int cap, int* count) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && count && (cap == 0 || (entries && ms)), "null argument");
+        *count = int(ctx->svd_tune.table.size());
+        int i = 0;
+        for (const auto& kv : ctx->svd_tune.table) {
+            if (i >= cap) break;
+            const SvdTuner::Entry& e = kv.second;
+            int32_t* o = entries + size_t(i) * 9;
+            o[0] = kv.first;
+            o[1] = int(e.cand.size());
+            o[2] = e.best >= 0 ? e.cand[size_t(e.best)] : -1;
+            o[3] = e.next;
+            for (int j = 0; j < 5; ++j) {
+                o[4 + j] = j < int(e.cand.size()) ? e.cand[size_t(j)] : 0;
+                ms[size_t(i) * 5 + j] = j < int(e.ms.size()) ? e.ms[size_t(j)] : -1.f;
+            }
+            ++i;
+        }
     });
 }
 

@@ -1,6 +1,7 @@
 // Host-side objects of the sweep engine (behind the opaque handles of tennet.h).
 #pragma once
 
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -41,6 +42,25 @@ struct BsvdStats {
     int sweeps32 = 0, sweeps_df = 0;
 };
 
+// Autotuned schedule of a bond's block SVD: which charge blocks take the one-CTA kernel and
+// which the multi-SM pipeline.  Keyed on the bond's block-size histogram through its largest
+// block that the pipeline accepts (32-column buckets); the candidate thresholds of a key are
+// timed once each (CUDA events around the whole SVD) on the first bonds with that key, then
+// the fastest is used for every later bond with it.
+struct SvdTuner {
+    struct Entry {
+        std::vector<int> cand;  // column thresholds (INT_MAX: every block on one CTA)
+        std::vector<float> ms;  // measured milliseconds, -1 until tried
+        int next = 0, best = -1;
+    };
+    std::map<int, Entry> table;
+    cudaEvent_t a = nullptr, b = nullptr;
+    SvdTuner() = default;
+    SvdTuner(const SvdTuner&) = delete;
+    SvdTuner& operator=(const SvdTuner&) = delete;
+    ~SvdTuner();
+};
+
 // overlap environment of psi against a projector state on one link: one D_psi(q) x D_M(q)
 // block (column-major) per charge q that both links carry
 struct OvEnv {
@@ -78,7 +98,8 @@ struct tn_ctx {
     int slices = 5;
     tn::EventTimer timer;
     tn::DevBuf err;  // device error word of bounded waits (0 = ok)
-    int svd_big_n = 96;  // charge blocks with more columns take the multi-SM SVD
+    int svd_big_n = -1;  // charge blocks with more columns take the multi-SM SVD (-1: tuned)
+    tn::SvdTuner svd_tune;
     tn::BsvdWork bsvd;
     tn::BsvdStats svd_stats;  // accumulated by the block SVDs (read and reset by the sweeps)
 };

@@ -6,8 +6,10 @@ state is copied to the oracle, and both then run the same bond updates from bond
 middle of the chain (left-to-right, eig_solver defaults krylovdim 5 / maxiter 2).  Per
 update: energies |dE/E| <= 1e-10, kept bond dimensions and the kept S^2 spectra (1e-9 FP64,
 1e-8 split precision, whose products carry 5e-11 relative errors); at the end
-the charge sectors of every link bit-exact.  Charge blocks of up to ~110 columns occur, so
-both the one-CTA and the multi-SM block SVD take part (blocks above 96 columns)."""
+the charge sectors of every link bit-exact.  Charge blocks of up to ~110 columns occur: the
+FP64 case fixes the SVD threshold at 96 columns, so both the one-CTA and the multi-SM block
+SVD take part; the split case runs the tuned schedule (every candidate is timed on the first
+bonds, so both paths take part there too)."""
 import numpy as np
 import pytest
 
@@ -19,9 +21,9 @@ N = 100
 CUTOFF = 1e-12
 
 
-@pytest.mark.parametrize("prec", ["fp64", "split"])
-def test_heisenberg_chain_N100_bond_updates_match_oracle(tn, prec):
-    ctx = tn.Context(0, precision=prec, slices=5)
+@pytest.mark.parametrize("prec,svd_split", [("fp64", 96), ("split", -1)])
+def test_heisenberg_chain_N100_bond_updates_match_oracle(tn, prec, svd_split):
+    ctx = tn.Context(0, precision=prec, slices=5, svd_split=svd_split)
     W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
     H = tn.MPO(W, delta, pq, ctx)
     env = tn.StateEnvs(tn.MPS.product(tn.models.neel_states(N), pq, ctx), H)
