@@ -163,9 +163,12 @@ __device__ __forceinline__ double pow2(int e) {
 }
 
 // ------------------------------------------------------------------------------------
-// pack kernel: one CTA per row tile (128 rows for A, 64 for B)
+// pack kernel: a row tile (128 rows for A, 64 for B) is shared by tile_rows / PACK_ROWS CTAs
+// (gridDim.y), each packing all k tiles of its PACK_ROWS rows: the row maxima stay within a
+// CTA, and small operands still spread over many SMs
 // ------------------------------------------------------------------------------------
 constexpr int PACK_THREADS = 256;
+constexpr int PACK_ROWS = 32;
 
 // Work item of the pack kernel: row r of the tile and one 8-wide chunk (16 bytes of bf16)
 // of one k tile; consecutive threads take consecutive rows so that the loads of a column-
@@ -173,17 +176,20 @@ constexpr int PACK_THREADS = 256;
 __global__ void __launch_bounds__(PACK_THREADS)
 split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__ ksrc, Bases b,
                   uint8_t* __restrict__ out, int* __restrict__ expo, int slices, int tile_rows) {
-    __shared__ unsigned long long rowmax[BM];
+    __shared__ unsigned long long rowmax[PACK_ROWS];
     const PackJob jb = jobs[blockIdx.x];
+    const int r0 = blockIdx.y * PACK_ROWS;
+    const int nr = (tile_rows - r0) < PACK_ROWS ? (tile_rows - r0) : PACK_ROWS;
+    if (nr <= 0) return;
     const int tile_bytes = tile_rows * BKT * 2;
-    const int per_tile = tile_rows * 8;             // (row, chunk) items per k tile
+    const int per_tile = nr * 8;                    // (row, chunk) items per k tile
     const int nitems = per_tile * jb.nkt;
-    for (int r = threadIdx.x; r < tile_rows; r += blockDim.x) rowmax[r] = 0ull;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) rowmax[r] = 0ull;
     __syncthreads();
     // pass 1: row maxima of |x| as IEEE bit patterns (integer compare, no FP64 pipe)
     for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
         const int t = it / per_tile, rem = it % per_tile;
-        const int r = rem % tile_rows, ch = rem / tile_rows;
+        const int rl = rem % nr, ch = rem / nr, r = r0 + rl;
         if (r >= jb.rows) continue;
         const KTileSrc ks = ksrc[jb.kt0 + t];
         const long long* x = reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
@@ -197,22 +203,22 @@ split_pack_kernel(const PackJob* __restrict__ jobs, const KTileSrc* __restrict__
                 mx = v > mx ? v : mx;
             }
         }
-        if (mx) atomicMax(&rowmax[r], mx);
+        if (mx) atomicMax(&rowmax[rl], mx);
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < jb.rows; r += blockDim.x) {
-        const unsigned long long m = rowmax[r];
-        expo[jb.eoff + r] = m ? int((m >> 52) & 0x7ff) - 1022 : 0;
+    for (int rl = threadIdx.x; rl < nr && r0 + rl < jb.rows; rl += blockDim.x) {
+        const unsigned long long m = rowmax[rl];
+        expo[jb.eoff + r0 + rl] = m ? int((m >> 52) & 0x7ff) - 1022 : 0;
     }
     // pass 2: balanced base-256 digits.  x * 2^(8s - E) = sig * 2^(ex - 1075 + 8s - E), sig
     // the 53-bit significand: the rounded integer is sig shifted right by
     // sh = 1075 + E - 8s - ex (round half away from zero), integer pipe only.
     for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
         const int t = it / per_tile, rem = it % per_tile;
-        const int r = rem % tile_rows, ch = rem / tile_rows;
+        const int rl = rem % nr, ch = rem / nr, r = r0 + rl;
         const KTileSrc ks = ksrc[jb.kt0 + t];
         const bool live = r < jb.rows && ks.kvalid > 0;
-        const unsigned long long mxb = live ? rowmax[r] : 0ull;
+        const unsigned long long mxb = live ? rowmax[rl] : 0ull;
         const int E = mxb ? int((mxb >> 52) & 0x7ff) - 1022 : 0;
         const int base_sh = 1075 + E - 8 * slices;
         const long long* x = live ? reinterpret_cast<const long long*>(b.p[ks.buf] + ks.off) +
@@ -584,7 +590,8 @@ void launch_split_pack(const PackJob* jobs, int njobs, const KTileSrc* ksrc, con
     TN_REQUIRE(tile_rows <= BM, "pack tile taller than the A tile");
     constexpr int KPER = 2;  // k tiles per CTA of the k-split pack
     if (max_nkt <= 2 * KPER || !gmax) {
-        split_pack_kernel<<<njobs, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
+        const dim3 g(njobs, (tile_rows + PACK_ROWS - 1) / PACK_ROWS);
+        split_pack_kernel<<<g, PACK_THREADS, 0, s>>>(jobs, ksrc, b, out, expo, slices, tile_rows);
         TN_CUDA(cudaGetLastError());
         count_launch();
         return;
