@@ -213,8 +213,9 @@ __device__ df2 df_block_sum(df2 v, df2* red) {
 
 // Preconditioned mixed-precision one-sided Jacobi SVD, one CTA per block (work matrix
 // A = M or M^T, m x n with m >= n):
-//  1. QR with column pivoting A P = Q R (double-float Householder; A and the reflectors
-//     stay in the global work buffer X);
+//  1. QR with column pivoting A P = Q R (double-float Householder; A is factored in shared
+//     memory when m n double-floats fit the region of the Jacobi matrices, which is free
+//     until step 2, and the reflectors are then kept in the global work buffer X);
 //  2. FP32 one-sided Jacobi on R^T, accumulating V in float: graded R^T makes cyclic Jacobi
 //     converge in a few sweeps (Drmac & Veselic, SIMAX 29, 2008);
 //  3. V re-orthonormalised in double-float (one classical Gram-Schmidt pass);
@@ -222,7 +223,8 @@ __device__ df2 df_block_sum(df2 v, df2* red) {
 //     (quadratic convergence from the FP32 start: Higham, Tisseur, Webb & Zhou, SIMAX 42,
 //     2021); double-float (FP32 pairs, ~48 bits) runs on the FP32 pipe, which issues 64
 //     times the FP64 rate of GB300;
-//  5. QV = Q [V; 0] (reflectors applied in reverse order) and PY = P Y.
+//  5. PY = P Y, then QV = Q [V; 0] (reflectors applied in reverse order; QV in shared
+//     memory when it fits there, Y being dead by then).
 // Then A = QV * diag(s) * (PY / s)^T: QV is the orthonormal factor on the A-row side,
 // PY = (A-column side) * diag(s).  Outputs: QV in W (m x n), PY in V (n x n), singular
 // values sorted descending in S with the sorting permutation in perm.  The n x n Jacobi
@@ -257,7 +259,10 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
     df2* taud = reinterpret_cast<df2*>(tau);        // Householder tau in double-float
     __shared__ df2 hhd[3];                          // tau, beta, scale of the current reflector
     const bool in_smem = int64_t(2) * n * n * 8 <= smem_region;
-    df2* A = reinterpret_cast<df2*>(X + d.x_off);    // work matrix and reflectors (double-float)
+    // the m x n work matrix (double-float) in shared memory while the Jacobi region is free
+    const bool a_smem = int64_t(m) * n * 8 <= smem_region;
+    df2* const Ag = reinterpret_cast<df2*>(X + d.x_off);  // reflectors after step 1
+    df2* A = a_smem ? reinterpret_cast<df2*>(smem) : Ag;
     double* Pm = in_smem ? reinterpret_cast<double*>(smem) : P + d.v_off;
     double* Qm = in_smem ? reinterpret_cast<double*>(smem) + int64_t(n) * n : V + d.v_off;
     const double* M = src + d.src_off;
@@ -352,6 +357,11 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         }
         __syncthreads();
     }
+    if (a_smem) {  // R and the reflectors to the global work buffer; the region is reused
+        for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) Ag[e] = A[e];
+        __syncthreads();
+        A = Ag;
+    }
     stamp(1);
     // 2. R^T as double-float into the W scratch (unused until step 5); FP32 Jacobi on
     //    R^T (n x n lower triangular) in the P region
@@ -441,11 +451,47 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         perm[d.s_off + rank] = j;
     }
     stamp(6);
-    // 5a. QV = Q [V; 0] in W (double-float; R^T stored there is dead), then FP64 in place
+    // 5b. PY = P Y into the V output (row cp[r] of P Y is row r of Y).  Y lives in shared
+    // memory or in the P scratch, never in V; V (the double-float rotations) is read
+    // below, so PY goes through the P scratch when V is not in shared memory.
+    double* py = V + d.v_off;
+    const bool v_in_V = !in_smem;  // v (Qm) is the V output region itself
+    double* pyw = v_in_V ? P + d.v_off : py;
+    if (v_in_V) {  // y is in P (Pm): stage PY in the W scratch instead (R^T there is dead)
+        double* wt = W + d.x_off;
+        for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
+            const int r = int(e % n), j = int(e / n);
+            wt[cp[r] + int64_t(j) * n] = df_to_double(y[e]);
+        }
+        __syncthreads();
+        for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) pyw[e] = wt[e];
+    } else {
+        for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
+            const int r = int(e % n), j = int(e / n);
+            pyw[cp[r] + int64_t(j) * n] = df_to_double(y[e]);
+        }
+    }
+    __syncthreads();
+    // 5a. QV = Q [V; 0] (double-float; in shared memory when it fits, Y being dead), then
+    // FP64 into W
+    const bool qv_smem = in_smem && int64_t(m) * n * 8 <= smem_region;
     df2* qv = reinterpret_cast<df2*>(W + d.x_off);
-    for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
-        const int i = int(e % m), j = int(e / m);
-        qv[e] = (i < n) ? v[i + int64_t(j) * n] : df2{0.f, 0.f};
+    if (qv_smem) {
+        // v sits in the upper half of the region that qv will cover: stage it in W first
+        df2* vt = qv;
+        for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) vt[e] = v[e];
+        __syncthreads();
+        df2* qs = reinterpret_cast<df2*>(smem);
+        for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
+            const int i = int(e % m), j = int(e / m);
+            qs[e] = (i < n) ? vt[i + int64_t(j) * n] : df2{0.f, 0.f};
+        }
+        qv = qs;
+    } else {
+        for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
+            const int i = int(e % m), j = int(e / m);
+            qv[e] = (i < n) ? v[i + int64_t(j) * n] : df2{0.f, 0.f};
+        }
     }
     __syncthreads();
     for (int k = n - 1; k >= 0; --k) {
@@ -466,19 +512,15 @@ svd_qrj_kernel(const SvdBlockDesc* __restrict__ desc, const double* __restrict__
         __syncthreads();
     }
     {
-        double* qvd = W + d.x_off;  // same bytes, element by element
+        double* qvd = W + d.x_off;  // same bytes element by element, or from shared memory
         for (int64_t e = threadIdx.x; e < int64_t(m) * n; e += blockDim.x) {
             const df2 t = qv[e];
             qvd[e] = df_to_double(t);
         }
     }
-    // 5b. PY = P Y into the V output (row cp[r] of P Y is row r of Y).  Y lives in shared
-    // memory or in the P scratch, never in V, and V (the FP64 rotations) is dead after 5a.
-    __syncthreads();
-    double* py = V + d.v_off;
-    for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
-        const int r = int(e % n), j = int(e / n);
-        py[cp[r] + int64_t(j) * n] = df_to_double(y[e]);
+    if (v_in_V) {  // PY from the P scratch into the V output (v is dead now)
+        __syncthreads();
+        for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) py[e] = pyw[e];
     }
     stamp(7);
     if (threadIdx.x == 0 && sweeps_out) sweeps_out[blockIdx.x] = (sw32 << 16) | sw64;
