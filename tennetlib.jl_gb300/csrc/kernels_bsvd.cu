@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(BT) bsvd_panel_kernel(const BsvdBlk* __restric
         __syncthreads();
     }
     // write back
-    double* Vp = ar + d.vp + int64_t(p0 / pw) * m * pw;
+    double* Vp = ar + d.vp + int64_t(p0) * m;
     for (int c = warp; c < w; c += BT / 32) {
         double* xc = X + p0 + int64_t(p0 + c) * m;
         double* vc = Vp + int64_t(c) * r;
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(BT) bsvd_panel_kernel(const BsvdBlk* __restric
             vc[i] = i == c ? 1.0 : (i > c ? v : 0.0);
         }
     }
-    double* Tm = ar + d.tm + int64_t(p0 / pw) * 2 * pw * pw;
+    double* Tm = ar + d.tm + int64_t(p0) * 64;
     for (int e = threadIdx.x; e < w * w; e += BT) {
         const int i = e % w, j = e / w;
         Tm[e] = -df_to_double(T[j + i * 32]);         // -T^T
@@ -884,10 +884,10 @@ void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* s
     count_launch();
 }
 
-void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int mmax, double* ar,
+void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int rmax, double* ar,
                        cudaStream_t s) {
     if (nb <= 0) return;
-    const size_t shm = size_t(mmax) * pw * 8;
+    const size_t shm = size_t(rmax) * pw * 8;  // the panel rows of the tallest block
     TN_REQUIRE(pw >= 1 && pw <= 32 && shm <= size_t(PANEL_SMEM), "block SVD: panel too large");
     TN_CUDA(cudaFuncSetAttribute(bsvd_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(shm)));

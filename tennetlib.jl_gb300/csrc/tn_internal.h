@@ -323,7 +323,7 @@ int bsvd_max_n();
 // its transpose) into the QR work matrix, its columns ordered by decreasing norm
 void launch_bsvd_gather(const BsvdBlk* d, int nb, int64_t mnmax, const double* src, double* ar,
                         cudaStream_t s);
-void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int mmax, double* ar,
+void launch_bsvd_panel(const BsvdBlk* d, int nb, int p0, int pw, int rmax, double* ar,
                        cudaStream_t s);
 // op 0: R^T (FP32 and FP64) and V32 = I; 1: V64 = V32; 2: G <- 1.5 I - 0.5 G (g64);
 // 3: Ydf, Vdf from y64, v64
