@@ -1,9 +1,9 @@
 // Host driver of the multi-SM SVD of large charge blocks (kernels in kernels_bsvd.cu).
 //
 // For the blocks of one bond it lays out a work arena, orders each block's columns by
-// decreasing norm (a static column pivoting), runs the blocked Householder QR
-// (panel kernel + three grouped GEMMs per 32-column panel), the cooperative FP32 Jacobi
-// presolve on R^T, two Newton-Schulz steps V <- V (3 I - V^T V) / 2 and Y = R^T V by grouped
+// decreasing norm (a static column pivoting), runs the blocked Householder QR (panel kernel
+// + three grouped GEMMs per panel of up to 32 columns), the cooperative FP32 Jacobi presolve
+// on R^T, two Newton-Schulz steps V <- V (3 I - V^T V) / 2 and Y = R^T V by grouped
 // GEMMs, the cooperative double-float polish, and Q [V; 0] by grouped GEMMs.  The GEMMs run in
 // the context's precision: FP64 on CUDA cores, or bf16 slices on the tensor cores with seven
 // slices per operand (56 bits, FP64-equivalent products); the two w x w T products always run
@@ -23,6 +23,8 @@ constexpr int SVD_SLICES = 7;  // bf16 slices per operand of the SVD GEMMs on th
 
 int64_t align32(int64_t x) { return (x + 31) & ~int64_t(31); }
 
+constexpr int KC = 256;  // rows per k chunk of the W1 = V^T C products (split k)
+
 struct Mm {  // one GEMM task of a grouped plan: C (+)= op(A) op(B), offsets in doubles
     int cbuf;
     int64_t coff;
@@ -33,6 +35,7 @@ struct Mm {  // one GEMM task of a grouped plan: C (+)= op(A) op(B), offsets in 
     int bbuf;
     int64_t boff;
     int ldb, tb, k;
+    int cont = 0;  // 1: one more segment of the previous task (its C fields are ignored)
 };
 
 struct GemmRun {
@@ -44,7 +47,7 @@ struct GemmRun {
         if (mm.empty()) return;
         GemmPlan g;
         for (const Mm& t : mm) {
-            g.add_task(t.cbuf, t.coff, t.m, t.n, t.ldc, t.accum);
+            if (!t.cont) g.add_task(t.cbuf, t.coff, t.m, t.n, t.ldc, t.accum);
             g.add_seg(t.abuf, t.aoff, t.lda, t.ta, t.bbuf, t.boff, t.ldb, t.tb, t.k);
         }
         flops += g.flops;
@@ -97,13 +100,20 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
         mmax = std::max(mmax, b.m);
         nmax = std::max(nmax, b.n);
     }
-    const int pw = bsvd_panel_width(mmax);
-    TN_REQUIRE(pw > 0, "block SVD: block too tall for the panel kernel");
+    // panel schedule shared by all blocks: at column p0 the widest panel (32, 16, 8 or 4
+    // columns) whose rows (those of the tallest block below p0) fit the panel kernel's
+    // shared memory; panels widen as the QR proceeds down the tall blocks
+    std::vector<std::pair<int, int>> panels;
+    for (int p0 = 0; p0 < nmax;) {
+        const int w = bsvd_panel_width(mmax - p0);
+        TN_REQUIRE(w > 0, "block SVD: block too tall for the panel kernel");
+        panels.emplace_back(p0, w);
+        p0 += w;
+    }
     TN_REQUIRE(nmax <= bsvd_max_n(), "block SVD: block too wide for the Jacobi kernel");
     // arena layout
     std::vector<BsvdBlk> bd(nb);
     std::vector<int64_t> w1(nb), w2(nb);
-    std::vector<int> npan(nb);
     int64_t off = 0;
     auto take = [&](int64_t n) {
         const int64_t o = off;
@@ -125,10 +135,9 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
         d.v_off = s.v_off;
         d.s_off = s.s_off;
         const int64_t m = s.m, n = s.n;
-        npan[j] = int((n + pw - 1) / pw);
         d.xq = take(m * n);
-        d.vp = take(int64_t(npan[j]) * m * pw);
-        d.tm = take(int64_t(npan[j]) * 2 * pw * pw);
+        d.vp = take(m * n);    // reflectors of the panel at column p0: at p0 m, (m - p0) x w
+        d.tm = take(64 * n);   // its -T^T and -T (2 w^2 <= 64 w): at 64 p0
         d.rt64 = take(n * n);
         d.v64 = take(n * n);
         d.g64 = take(n * n);
@@ -141,8 +150,8 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
         d.scl = take(1);
         d.cn = take(n);
         d.piv = take(n);
-        w1[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
-        w2[j] = take(int64_t(pw) * std::max(n, int64_t(1)));
+        w1[j] = take(32 * std::max(n, int64_t(1)) * ((m + KC - 1) / KC));  // one per k chunk
+        w2[j] = take(32 * std::max(n, int64_t(1)));
         mnmax = std::max(mnmax, m * n);
         nnmax = std::max(nnmax, n * n);
     }
@@ -159,22 +168,30 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
 
     // ---- blocked Householder QR -------------------------------------------------------
     launch_bsvd_gather(dblk, nb, mnmax, src, ar, st);
-    const int maxnp = *std::max_element(npan.begin(), npan.end());
-    for (int p = 0; p < maxnp; ++p) {
-        const int p0 = p * pw;
-        launch_bsvd_panel(dblk, nb, p0, pw, mmax, ar, st);
+    for (const auto& pp : panels) {
+        const int p0 = pp.first, pw = pp.second;
+        launch_bsvd_panel(dblk, nb, p0, pw, mmax - p0, ar, st);
         std::vector<Mm> g1, g2, g3;
         for (int j = 0; j < nb; ++j) {
             const BsvdBlk& d = bd[j];
             if (p0 >= d.n) continue;
             const int w = std::min(pw, d.n - p0), r = d.m - p0, nt = d.n - p0 - w;
             if (nt <= 0) continue;
-            const int64_t vpo = d.vp + int64_t(p) * d.m * pw;
+            const int64_t vpo = d.vp + int64_t(p0) * d.m;
             const int64_t co = d.xq + p0 + int64_t(p0 + w) * d.m;
-            const int64_t tmo = d.tm + int64_t(p) * 2 * pw * pw;
-            // W1 = V^T C, W2 = (-T^T) W1, C += V W2
-            g1.push_back(Mm{AR, w1[j], w, nt, w, 0, AR, vpo, r, 1, AR, co, d.m, 0, r});
-            g2.push_back(Mm{AR, w2[j], w, nt, w, 0, AR, tmo, w, 0, AR, w1[j], w, 0, w});
+            const int64_t tmo = d.tm + int64_t(p0) * 64;
+            // W1_c = V_c^T C_c over row chunks c of KC rows (split k: the output has only w
+            // rows, so one long-k product would occupy few CTAs), W2 = (-T^T) sum_c W1_c
+            // (one task, a segment per chunk), C += V W2
+            const int nch = (r + KC - 1) / KC;
+            for (int c = 0; c < nch; ++c) {
+                const int r0 = c * KC, rc = std::min(KC, r - r0);
+                const int64_t wc = w1[j] + int64_t(c) * w * nt;
+                g1.push_back(Mm{AR, wc, w, nt, w, 0, AR, vpo + r0, r, 1, AR, co + r0, d.m, 0, rc});
+                Mm t2{AR, w2[j], w, nt, w, 0, AR, tmo, w, 0, AR, wc, w, 0, w};
+                t2.cont = c > 0;
+                g2.push_back(t2);
+            }
             g3.push_back(Mm{AR, co, r, nt, d.m, 1, AR, vpo, r, 0, AR, w2[j], w, 0, w});
         }
         G.run(g1);
@@ -247,19 +264,26 @@ void big_block_svd(tn_ctx* ctx, BsvdWork& W, const std::vector<SvdBlockDesc>& bl
     jacobi(1);
     launch_bsvd_finish(dblk, nb, ar, QV, PY, S, perm, st);
     // ---- QV = Q [V; 0], panels in reverse ------------------------------------------------
-    for (int p = maxnp - 1; p >= 0; --p) {
-        const int p0 = p * pw;
+    for (auto it = panels.rbegin(); it != panels.rend(); ++it) {
+        const int p0 = it->first, pw = it->second;
         std::vector<Mm> g1, g2, g3;
         for (int j = 0; j < nb; ++j) {
             const BsvdBlk& d = bd[j];
             if (p0 >= d.n) continue;
             const int w = std::min(pw, d.n - p0), r = d.m - p0;
-            const int64_t vpo = d.vp + int64_t(p) * d.m * pw;
+            const int64_t vpo = d.vp + int64_t(p0) * d.m;
             const int64_t zo = d.x_off + p0;
-            const int64_t tmo = d.tm + int64_t(p) * 2 * pw * pw + int64_t(w) * w;
-            // W1 = V^T Z, W2 = (-T) W1, Z += V W2
-            g1.push_back(Mm{AR, w1[j], w, d.n, w, 0, AR, vpo, r, 1, QB, zo, d.m, 0, r});
-            g2.push_back(Mm{AR, w2[j], w, d.n, w, 0, AR, tmo, w, 0, AR, w1[j], w, 0, w});
+            const int64_t tmo = d.tm + int64_t(p0) * 64 + int64_t(w) * w;
+            // W1_c = V_c^T Z_c over row chunks (split k), W2 = (-T) sum_c W1_c, Z += V W2
+            const int nch = (r + KC - 1) / KC;
+            for (int c = 0; c < nch; ++c) {
+                const int r0 = c * KC, rc = std::min(KC, r - r0);
+                const int64_t wc = w1[j] + int64_t(c) * w * d.n;
+                g1.push_back(Mm{AR, wc, w, d.n, w, 0, AR, vpo + r0, r, 1, QB, zo + r0, d.m, 0, rc});
+                Mm t2{AR, w2[j], w, d.n, w, 0, AR, tmo, w, 0, AR, wc, w, 0, w};
+                t2.cont = c > 0;
+                g2.push_back(t2);
+            }
             g3.push_back(Mm{QB, zo, r, d.n, d.m, 1, AR, vpo, r, 0, AR, w2[j], w, 0, w});
         }
         G.run(g1);
