@@ -96,6 +96,8 @@ typedef struct tn_sweep_result {
     double svd_jacobi_flops;   /* flops of its Jacobi rotations (dots and column updates) */
     int32_t svd_sweeps32;      /* largest FP32 presolve sweep count of a block */
     int32_t svd_sweeps_df;     /* largest double-float polish sweep count of a block */
+    double svd_small_flops;    /* algorithmic flops of the one-CTA block SVDs (QR, Jacobi
+                                * sweeps as run, Gram-Schmidt, R^T V, Q V) */
 } tn_sweep_result;
 
 /* ---- context ------------------------------------------------------------------- */

@@ -505,7 +505,8 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
         "gemm_launches": res.gemm_launches, "kernel_launches": res.kernel_launches,
         "krylov_bytes": res.krylov_bytes, "svd_gemm_flops": res.svd_gemm_flops,
         "svd_jacobi_flops": res.svd_jacobi_flops, "svd_sweeps32": res.svd_sweeps32,
-        "svd_sweeps_df": res.svd_sweeps_df, "wall_s": wall})
+        "svd_sweeps_df": res.svd_sweeps_df, "svd_small_flops": res.svd_small_flops,
+        "wall_s": wall})
     if swdata.sweepcount > 1:
         enerr = swdata.energy[-1] - swdata.energy[-2]
         enterr = swdata.entropy[-1] - swdata.entropy[-2]
@@ -536,7 +537,8 @@ def _record_sweep(swdata, res, mid, wall, noise=0.0, outputlevel=0):
         "pack_ms": res.pack_ms, "gemm_launches": res.gemm_launches,
         "kernel_launches": res.kernel_launches, "krylov_bytes": res.krylov_bytes,
         "svd_gemm_flops": res.svd_gemm_flops, "svd_jacobi_flops": res.svd_jacobi_flops,
-        "svd_sweeps32": res.svd_sweeps32, "svd_sweeps_df": res.svd_sweeps_df, "wall_s": wall})
+        "svd_sweeps32": res.svd_sweeps32, "svd_sweeps_df": res.svd_sweeps_df,
+        "svd_small_flops": res.svd_small_flops, "wall_s": wall})
 
 
 class TDVPEngine:

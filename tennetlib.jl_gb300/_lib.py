@@ -78,6 +78,7 @@ class SweepResult(C.Structure):
         ("svd_jacobi_flops", C.c_double),
         ("svd_sweeps32", C.c_int32),
         ("svd_sweeps_df", C.c_int32),
+        ("svd_small_flops", C.c_double),
     ]
 
 

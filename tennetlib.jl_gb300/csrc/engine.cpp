@@ -1350,12 +1350,13 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
         TN_CUDA(cudaMemcpyAsync(ddesc.p, small.data(), nsm_blocks * sizeof(SvdBlockDesc),
                                 cudaMemcpyHostToDevice, st));
     static const bool dbg = std::getenv("TENNET_DEBUG_SVD") != nullptr;
-    DevBuf dsw;
+    // sweep counts of the one-CTA blocks (work accounting) and their phase clocks
+    DevBuf& dsw = ctx->svd_counts;
     const size_t clk_off = size_t((nsm_blocks + 1) & ~1) * 4;  // 8-byte aligned clock area
-    if (dbg) dsw.alloc(clk_off + size_t(std::max(nsm_blocks, 1)) * 8 * 8, st);
+    dsw.alloc(clk_off + size_t(std::max(nsm_blocks, 1)) * 8 * 8, st);
     const int e0 = ctx->timer.mark();
     launch_svd_jacobi(ddesc.as<SvdBlockDesc>(), nsm_blocks, maxn_small, src, dX.d(), dW.d(),
-                      dV.d(), dP.d(), dS.d(), dPerm.as<int>(), dbg ? dsw.as<int>() : nullptr, st);
+                      dV.d(), dP.d(), dS.d(), dPerm.as<int>(), dsw.as<int>(), st);
     BsvdStats bst;
     big_block_svd(ctx, ctx->bsvd, big, src, dW.d(), dV.d(), dS.d(), dPerm.as<int>(), &bst);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
@@ -1363,10 +1364,11 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
     ctx->svd_stats.jacobi_flops += bst.jacobi_flops;
     ctx->svd_stats.sweeps32 = std::max(ctx->svd_stats.sweeps32, bst.sweeps32);
     ctx->svd_stats.sweeps_df = std::max(ctx->svd_stats.sweeps_df, bst.sweeps_df);
-    if (dbg && nsm_blocks) {
-        std::vector<int> sw(nsm_blocks);
-        std::vector<long long> ck(size_t(nsm_blocks) * 8);
+    std::vector<int> sw(size_t(std::max(nsm_blocks, 1)));
+    if (nsm_blocks)
         TN_CUDA(cudaMemcpyAsync(sw.data(), dsw.p, nsm_blocks * 4, cudaMemcpyDeviceToHost, st));
+    if (dbg && nsm_blocks) {
+        std::vector<long long> ck(size_t(nsm_blocks) * 8);
         TN_CUDA(cudaMemcpyAsync(ck.data(), static_cast<char*>(dsw.p) + clk_off, ck.size() * 8,
                                 cudaMemcpyDeviceToHost, st));
         TN_CUDA(cudaStreamSynchronize(st));
@@ -1391,6 +1393,15 @@ void block_svd(tn_ctx* ctx, DevBuf& dX, DevBuf& dW, DevBuf& dV, DevBuf& dP, DevB
     if (so)
         TN_CUDA(cudaMemcpyAsync(R.S.data(), dS.p, size_t(so) * 8, cudaMemcpyDeviceToHost, st));
     sync(ctx);
+    // algorithmic flops of the one-CTA blocks: Householder QR 2mn^2 - 2n^3/3, per Jacobi
+    // sweep 9 n^2 (n - 1) (18 n per rotated pair), Gram-Schmidt 2n^3, R^T V n^3, Q V
+    // 4mn^2 - 2n^3
+    for (int b = 0; b < nsm_blocks; ++b) {
+        const double m = small[size_t(b)].m, n = small[size_t(b)].n;
+        const double sweeps = double(sw[size_t(b)] >> 16) + double(sw[size_t(b)] & 0xffff);
+        ctx->svd_stats.small_flops += 2 * m * n * n - 2 * n * n * n / 3 + sweeps * 9 * n * n * (n - 1) +
+                                      3 * n * n * n + 4 * m * n * n - 2 * n * n * n;
+    }
     if (!big.empty()) check_device_error(ctx);
     if (te) {
         float ms = 0.f;
@@ -2811,6 +2822,7 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     res->svd_jacobi_flops = ctx->svd_stats.jacobi_flops;
     res->svd_sweeps32 = ctx->svd_stats.sweeps32;
     res->svd_sweeps_df = ctx->svd_stats.sweeps_df;
+    res->svd_small_flops = ctx->svd_stats.small_flops;
     if (n_mid_eigs) *n_mid_eigs = (int32_t)mid.size();
     if (mid_eigs) {
         const int k = std::min<int>(mid_cap, (int)mid.size());

@@ -40,6 +40,7 @@ struct BsvdStats {
     double gemm_flops = 0;    // algorithmic flops of the SVD's grouped GEMMs
     double jacobi_flops = 0;  // flops of the Jacobi rotations (dots and column updates)
     int sweeps32 = 0, sweeps_df = 0;
+    double small_flops = 0;   // algorithmic flops of the one-CTA block SVDs
 };
 
 // Autotuned schedule of a bond's block SVD: which charge blocks take the one-CTA kernel and
@@ -101,6 +102,7 @@ struct tn_ctx {
     int svd_big_n = -1;  // charge blocks with more columns take the multi-SM SVD (-1: tuned)
     tn::SvdTuner svd_tune;
     tn::BsvdWork bsvd;
+    tn::DevBuf svd_counts;  // sweep counts (and debug clocks) of the one-CTA block SVDs
     tn::BsvdStats svd_stats;  // accumulated by the block SVDs (read and reset by the sweeps)
 };
 
