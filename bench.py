@@ -566,6 +566,8 @@ def run_j1j2(tn, local, args):
         st = s.stats[-1]
         out[prec] = {"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
                      "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
+                     "gemm_s": st["gemm_ms"] / 1e3, "pack_s": st["pack_ms"] / 1e3,
+                     "gemm_tflops": st["gemm_flops"] / max(st["gemm_ms"], 1e-9) / 1e9,
                      "svd_s": st["svd_ms"] / 1e3, "env_s": st["env_ms"] / 1e3,
                      "lanczos_s": st["lanczos_ms"] / 1e3,
                      "svd_gemm_flops": st.get("svd_gemm_flops", 0.0),
