@@ -147,6 +147,14 @@ def download_state(psi):
     return tensors, links
 
 
+def download_blocks(psi):
+    """Block-sparse host copy of an engine MPS (the charge blocks only, as an ITensors QN MPS
+    stores them): (per-site block arrays, link charge arrays)."""
+    blocks = [psi.site_blocks(i) for i in range(psi.N)]
+    links = [psi.link_charges(i) for i in range(psi.N + 1)]
+    return blocks, links
+
+
 # ------------------------------------------------------------------------------------
 # CPU oracle legs (the checker, timed as the CPU baseline / reference arm)
 # ------------------------------------------------------------------------------------
@@ -407,21 +415,24 @@ def run_ours(args, world, rank, local, pg):
     energy = sw.energy[-1]
     chi = sw.maxchi[-1]
 
-    # end to end through the C ABI with host buffers: upload the MPS, build the
-    # environments, sweep, download the MPS
-    tensors, links = download_state(env.getpsi())
-    h2d = sum(t.size * 8 for t in tensors)
+    # end to end through the C ABI with host buffers: upload the MPS (charge blocks, as an
+    # ITensors QN MPS holds them), build the environments, sweep, download the MPS blocks
+    psi_t = env.getpsi()
+    tensors, links = download_state(psi_t)
+    blocks, _ = download_blocks(psi_t)
+    del psi_t
+    h2d = sum(b.size * 8 for b in blocks)
     e2e_times = []
     for _ in range(max(1, min(args.steps, 2))):
         t1 = time.perf_counter()
-        p2 = tn.MPS(tensors, links, pq, 0, ctx)
+        p2 = tn.MPS.from_blocks(blocks, links, pq, 0, ctx)
         e2 = tn.StateEnvs(p2, H)
         s2 = tn.SweepData()
         tn.fullsweep_(e2, tn.eig_solver, 2, s2, **sweep_kwargs(MAXDIM))
         e2e_energy, e2e_chi = s2.energy[-1], s2.maxchi[-1]
-        out = download_state(e2.getpsi())
+        out = download_blocks(e2.getpsi())
         e2e_times.append(time.perf_counter() - t1)
-        d2h = sum(t.size * 8 for t in out[0])
+        d2h = sum(b.size * 8 for b in out[0])
         del e2, p2
     e2e = allmax(pg, statistics.mean(e2e_times))
 
@@ -443,11 +454,12 @@ def run_ours(args, world, rank, local, pg):
                       "FP64 grouped block-sparse GEMM of H_eff (two launches per matvec)")
     roof["flops_per_launch"] = gemm_fl / max(gemm_n, 1)
     roof["ms_per_launch"] = gemm_ms / max(gemm_n, 1)
-    # DRAM bytes (read + write) of one captured launch of this kernel at this workload
-    # (ncu, dram__bytes_read.sum + dram__bytes_write.sum: split_gemm_kernel 4.57 MB, one
-    # H_eff stage at chi ~ 182); per launch like `achieved`
-    roof["traffic"] = 4.574208e6 if args.precision == "split" else None
-    roof["traffic_unit"] = "bytes per launch (one ncu capture)"
+    # DRAM bytes (read + write) per launch of this kernel at this workload: the mean over
+    # 20 consecutive launches of one ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum, profiles/split_gemm_traffic_heisenberg_N100.md); per launch
+    # like `achieved`
+    roof["traffic"] = 2.808704e6 if args.precision == "split" else None
+    roof["traffic_unit"] = "bytes per launch (mean of 20 launches, one ncu capture)"
     share = {k: sum(s[k] for s in st) / max(sum(s["sweep_ms"] for s in st), 1e-9)
              for k in ("heff_ms", "svd_ms", "env_ms", "lanczos_ms", "pack_ms", "gemm_ms")}
     dominant = max(("svd_ms", "heff_ms", "lanczos_ms", "env_ms"), key=lambda k: share[k])
@@ -501,7 +513,8 @@ def run_ours(args, world, rank, local, pg):
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": "s/sweep", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "what": "upload MPS from host + build environments + one sweep + download MPS"},
+                "what": "upload the MPS charge blocks from host + build environments + one sweep "
+                        "+ download the MPS charge blocks"},
     }
     res["svd_schedule"] = ctx.svd_schedule()
     if args.precision == "split" and not args.no_fp64_compare:

@@ -148,11 +148,23 @@ int tn_mpo_destroy(tn_mpo* mpo);
 int tn_mps_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
                   const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
                   const double* site_data, int center, tn_mps** out);
+/* The same from charge blocks only (the block-sparse storage of an ITensors QN MPS, no
+ * zeros crossing the boundary).  Site i's data is the concatenation, over its left sectors a
+ * (ascending charge) and physical states s (ascending), of the Dl(a) x Dr(b) block with
+ * q_b = q_a + phys_q[s] (column-major), for every such b present in link i + 1;
+ * site_len[i] is its length and block_data holds all sites back to back. */
+int tn_mps_create_blocks(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                         const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
+                         const double* block_data, const int64_t* site_len, int center,
+                         tn_mps** out);
 int tn_mps_destroy(tn_mps* mps);
 /* number of sectors of link i, and (when q/dim are non-null) their charges and dims */
 int tn_mps_link(const tn_mps* mps, int link, int32_t* nsec, int32_t* q, int32_t* dim, int cap);
 /* dense site tensor (Dl, d, Dr) column-major */
 int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap);
+/* site tensor as charge blocks in the order of tn_mps_create_blocks; *len receives the
+ * length (out == NULL: only the length) */
+int tn_mps_site_blocks(const tn_mps* mps, int site, double* out, int64_t cap, int64_t* len);
 int tn_mps_center(const tn_mps* mps);
 /* measure(T, psi, opstr) for every site (TenNetLib src/mps/measure.jl:150-219): out[i] =
  * <psi|O_i|psi> / <psi|psi> with the single-site operator op (d x d column-major [s', s]),

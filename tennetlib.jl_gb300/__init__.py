@@ -228,6 +228,35 @@ class MPS:
         _own(self, h)
 
     @classmethod
+    def from_blocks(cls, blocks, links, phys_q, center: int = 0, ctx: Context | None = None):
+        """MPS from charge blocks only (``tn_mps_create_blocks``): ``blocks[i]`` is site i's
+        data in the block order of the C ABI (left sectors by ascending charge, then physical
+        states, each Dl x Dr block column-major, see ``dense_to_blocks``); ``links`` are the
+        per-basis-state charge arrays of links 0..N."""
+        ctx = ctx or Context.default()
+        phys_q = np.asarray(phys_q, dtype=np.int32)
+        N = len(blocks)
+        nsec, q, dim = _links_to_sectors(links)
+        flat = np.concatenate([np.asarray(b, dtype=np.float64).ravel() for b in blocks])
+        lens = np.ascontiguousarray([np.asarray(b).size for b in blocks], dtype=np.int64)
+        bufs = [L.as_i32(phys_q), L.as_i32(nsec), L.as_i32(q), L.as_i32(dim), L.as_f64(flat)]
+        h = L.vp()
+        L.check(ctx.lib.tn_mps_create_blocks(ctx.h, N, len(phys_q), bufs[0][1], bufs[1][1],
+                                             bufs[2][1], bufs[3][1], bufs[4][1],
+                                             lens.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             center, C.byref(h)))
+        return cls(ctx=ctx, _handle=h, _N=N, _d=len(phys_q), phys_q=phys_q)
+
+    def site_blocks(self, i):
+        """Site i as charge blocks in the order of ``from_blocks`` (1-D array)."""
+        n = C.c_int64()
+        L.check(self.ctx.lib.tn_mps_site_blocks(self.h, i, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        L.check(self.ctx.lib.tn_mps_site_blocks(self.h, i, out.ctypes.data_as(L.f64p), out.size,
+                                                C.byref(n)))
+        return out
+
+    @classmethod
     def product(cls, states, phys_q, ctx=None):
         t, lk = models.product_state(states, phys_q)
         return cls(t, lk, phys_q, 0, ctx)
@@ -384,6 +413,39 @@ SPIN_HALF_OPS = {
     "Ndn": np.diag([0.0, 1.0]),
 }
 
+
+def dense_to_blocks(t, ql, phys_q, qr):
+    """Charge blocks of a dense site tensor t[l, s, r] in the order of the C ABI's
+    ``tn_mps_create_blocks``: left sectors by ascending charge, then physical states, each
+    Dl x Dr block column-major."""
+    t = np.asarray(t, dtype=np.float64)
+    ql, qr = np.asarray(ql), np.asarray(qr)
+    out = []
+    for a in np.unique(ql):
+        rows = np.nonzero(ql == a)[0]
+        for s, qs in enumerate(np.asarray(phys_q)):
+            cols = np.nonzero(qr == a + qs)[0]
+            if len(cols):
+                out.append(t[np.ix_(rows, [s], cols)][:, 0, :].ravel(order="F"))
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+def blocks_to_dense(b, ql, phys_q, qr):
+    """Inverse of ``dense_to_blocks``: the dense site tensor (Dl, d, Dr)."""
+    ql, qr = np.asarray(ql), np.asarray(qr)
+    pq = np.asarray(phys_q)
+    t = np.zeros((len(ql), len(pq), len(qr)))
+    off = 0
+    for a in np.unique(ql):
+        rows = np.nonzero(ql == a)[0]
+        for s, qs in enumerate(pq):
+            cols = np.nonzero(qr == a + qs)[0]
+            if len(cols):
+                n = len(rows) * len(cols)
+                t[np.ix_(rows, [s], cols)] = np.asarray(b[off:off + n]).reshape(
+                    (len(rows), len(cols)), order="F")[:, None, :]
+                off += n
+    return t
 
 def measure(psi: MPS, op, pos: int | None = None, sites=None):
     """``measure(Float64, psi, opstr[, pos]; sites)`` (``src/mps/measure.jl:150-219``):

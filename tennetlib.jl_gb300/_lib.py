@@ -98,6 +98,9 @@ PROTOS = {
     "tn_mpo_destroy": (C.c_int, [vp]),
     "tn_mps_create": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p, C.c_int,
                                 C.POINTER(vp)]),
+    "tn_mps_create_blocks": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p,
+                                       C.POINTER(C.c_int64), C.c_int, C.POINTER(vp)]),
+    "tn_mps_site_blocks": (C.c_int, [vp, C.c_int, f64p, C.c_int64, C.POINTER(C.c_int64)]),
     "tn_mps_destroy": (C.c_int, [vp]),
     "tn_mps_link": (C.c_int, [vp, C.c_int, i32p, i32p, i32p, C.c_int]),
     "tn_mps_site": (C.c_int, [vp, C.c_int, f64p, C.c_int64]),

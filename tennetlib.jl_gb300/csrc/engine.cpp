@@ -2506,6 +2506,91 @@ int tn_mps_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q, const i
     });
 }
 
+int tn_mps_create_blocks(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                         const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
+                         const double* block_data, const int64_t* site_len, int center,
+                         tn_mps** out) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && out && phys_q && nsec && sec_q && sec_dim && block_data && site_len,
+                   "null argument");
+        TN_REQUIRE(nsites >= 2, "need at least two sites");
+        TN_REQUIRE(center >= 0 && center < nsites, "center out of range");
+        auto m = std::make_unique<tn_mps>();
+        m->ctx = ctx;
+        m->N = nsites;
+        m->d = d;
+        m->pq.assign(phys_q, phys_q + d);
+        m->center = center;
+        size_t so = 0;
+        for (int i = 0; i <= nsites; ++i) {
+            Link L;
+            for (int k = 0; k < nsec[i]; ++k) {
+                L.q.push_back(sec_q[so + k]);
+                L.dim.push_back(sec_dim[so + k]);
+                TN_REQUIRE(sec_dim[so + k] >= 1, "sector dimension must be >= 1");
+                if (k) TN_REQUIRE(sec_q[so + k] > sec_q[so + k - 1], "sectors must be sorted by charge");
+            }
+            so += nsec[i];
+            TN_REQUIRE(L.nsec() >= 1, "every link needs a sector");
+            m->links.push_back(L);
+        }
+        TN_REQUIRE(m->links[0].total() == 1 && m->links[nsites].total() == 1,
+                   "boundary links must have dimension 1");
+        m->sites.resize(nsites);
+        cudaStream_t st = ctx->stream;
+        DevBuf tmp;
+        int64_t off = 0;
+        for (int i = 0; i < nsites; ++i) {
+            const Link& lk = m->links[i];
+            const Link& rk = m->links[i + 1];
+            // the block order of the ABI is the right-grouped layout's memory order
+            const SiteLayout rg = make_site_layout(RG, lk, rk, m->pq);
+            TN_REQUIRE(site_len[i] == rg.size, "site block data has the wrong length");
+            tn_site& S = m->sites[i];
+            S.lay = i < center ? make_site_layout(LG, lk, rk, m->pq) : rg;
+            S.buf.alloc(size_t(std::max<int64_t>(rg.size, 1)) * 8, st);
+            if (rg.size == 0) continue;
+            if (S.lay.layout == RG) {
+                TN_CUDA(cudaMemcpyAsync(S.buf.p, block_data + off, size_t(rg.size) * 8,
+                                        cudaMemcpyHostToDevice, st));
+            } else {
+                tmp.alloc(size_t(rg.size) * 8, st);
+                TN_CUDA(cudaMemcpyAsync(tmp.p, block_data + off, size_t(rg.size) * 8,
+                                        cudaMemcpyHostToDevice, st));
+                regroup(ctx, rg, tmp.d(), S.lay, S.buf.d(), lk, rk);
+            }
+            off += rg.size;
+        }
+        sync(ctx);
+        *out = m.release();
+    });
+}
+
+int tn_mps_site_blocks(const tn_mps* mps, int site, double* out, int64_t cap, int64_t* len) {
+    return guarded([&] {
+        TN_REQUIRE(mps && len, "null argument");
+        TN_REQUIRE(site >= 0 && site < mps->N, "site out of range");
+        const tn_site& S = mps->sites[site];
+        *len = S.lay.size;
+        if (!out) return;
+        TN_REQUIRE(cap >= S.lay.size, "capacity too small");
+        if (S.lay.size == 0) return;
+        cudaStream_t st = mps->ctx->stream;
+        if (S.lay.layout == RG) {
+            TN_CUDA(cudaMemcpyAsync(out, S.buf.p, size_t(S.lay.size) * 8, cudaMemcpyDeviceToHost, st));
+        } else {
+            const Link& lk = mps->links[site];
+            const Link& rk = mps->links[site + 1];
+            const SiteLayout rg = make_site_layout(RG, lk, rk, mps->pq);
+            DevBuf tmp;
+            tmp.alloc(size_t(rg.size) * 8, st);
+            regroup(mps->ctx, S.lay, S.buf.d(), rg, tmp.d(), lk, rk);
+            TN_CUDA(cudaMemcpyAsync(out, tmp.p, size_t(rg.size) * 8, cudaMemcpyDeviceToHost, st));
+        }
+        TN_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 int tn_mps_destroy(tn_mps* mps) {
     if (mps) cudaStreamSynchronize(mps->ctx->stream);
     delete mps;
