@@ -479,6 +479,37 @@ class LinkEnv:
         return out
 
 
+class LinkProj:
+    """``LinkProjTTN`` (src/ttn/linkproj.jl:15-224) without charges: ``E[(v, u)]`` is the
+    overlap of psi and M on v's side of the link (v, u), indexed [a_psi, a_M]
+    (``move_linkproj_to_next!``, linkproj.jl:56-78); the projected vector at the centre
+    contracts M's centre tensor with the overlaps of all its links (``contract``,
+    linkproj.jl:143-157)."""
+
+    def __init__(self, psi: TTN, M: TTN):
+        self.M = M.copy()
+        self.E = {}
+        oc = psi.center
+        for v in nodes_from_bfs_reverse(psi.adj, oc)[:-1]:
+            self.move_to_next(psi, v, shortest_path(psi.adj, v, oc)[1])
+
+    def _mapped(self, psi: TTN, v, skip):
+        y = self.M.tensors[v].conj()
+        for li, leg in enumerate(psi.legs(v)):
+            if leg[0] == "n" and leg[1] != skip and (leg[1], v) in self.E:
+                y = _apply_leg(y, self.E[(leg[1], v)], li)
+        return y
+
+    def move_to_next(self, psi: TTN, v, u):
+        y = self._mapped(psi, v, u)
+        lu = psi.leg_index(v, u)
+        rest = [i for i in range(y.ndim) if i != lu]
+        self.E[(v, u)] = np.tensordot(psi.tensors[v], y, axes=(rest, rest))  # [a_psi, a_M]
+
+    def vector(self, psi: TTN, v):
+        return self._mapped(psi, v, None)
+
+
 # --------------------------------------------------------------------------------------
 # StateEnvsTTN, update, sweeps
 # --------------------------------------------------------------------------------------
@@ -492,11 +523,21 @@ class SweepDataTTN:
 
 
 class StateEnvsTTN:
-    """``StateEnvsTTN(psi, M)`` (state_envs_ttn.jl:27-31)."""
+    """``StateEnvsTTN(psi, M)`` (state_envs_ttn.jl:27-31); with ``Ms`` and ``weight`` the
+    projected environment ``EnvCouplingModelProjTTN`` (src/ttn/environment.jl:44-110):
+    H_eff x + weight sum_k m_k (m_k . x)."""
 
-    def __init__(self, psi: TTN, terms):
+    def __init__(self, psi: TTN, terms, Ms=None, weight=None):
         self.psi = psi.copy()
         self.env = LinkEnv(self.psi, terms)
+        self.proj = []
+        self.weight = 0.0
+        if Ms:
+            if weight is None or weight <= 0.0:
+                raise ValueError("`weight` parameter should be > 0.0 (value passed was "
+                                 f"`weight={weight}`)")
+            self.proj = [LinkProj(self.psi, M) for M in Ms]
+            self.weight = float(weight)
 
     def position(self, node, normalize=True, maxdim=2**62, mindim=1, cutoff=1e-15):
         """``position!`` (state_envs_ttn.jl:120-141)."""
@@ -506,9 +547,15 @@ class StateEnvsTTN:
         path = shortest_path(self.psi.adj, oc, node)
         for a, b in zip(path[:-1], path[1:]):
             self.env.move_to_next(self.psi, a, b)
+            for P in self.proj:
+                P.move_to_next(self.psi, a, b)
 
     def product(self, x):
-        return self.env.product(self.psi, self.psi.center, x)
+        out = self.env.product(self.psi, self.psi.center, x)
+        for P in self.proj:
+            m = P.vector(self.psi, self.psi.center)
+            out = out + self.weight * m * float(np.vdot(m, x))
+        return out
 
 
 def update_position(se: StateEnvsTTN, node, maxdim=2**62, mindim=1, cutoff=-1.0,

@@ -89,3 +89,26 @@ def test_oracle_sweeps_reach_exact_energies():
     sw = T.optimize(se, [16], [4], T.default_sweeppath(N, g.keys()))
     e0 = np.linalg.eigvalsh(T.dense_hamiltonian(N, T.heisenberg_terms(N)))[0]
     assert abs(sw.energy[-1] - e0) < 1e-10
+
+
+def test_ttn_oracle_excited_state_projector():
+    """EnvCouplingModelProjTTN / LinkProjTTN (src/ttn/environment.jl:44-110,
+    src/ttn/linkproj.jl): with the ground state projected out (weight 10, as in the
+    reference's test/test_TTN.jl:36-48) the sweep reaches the second eigenvalue of the dense
+    Hamiltonian and a state orthogonal to the ground state."""
+    N = 8
+    J, h = T.tfim_instance(N, 3)
+    terms = T.tfim_terms(J, h)
+    ev = np.linalg.eigvalsh(T.dense_hamiltonian(N, terms))
+    path = T.default_sweeppath(N, T.default_graph_sitenodes(N)[0].keys())
+    se = T.StateEnvsTTN(T.random_ttn(N, 16, 1), terms)
+    sw = T.optimize(se, [16], [6], path)
+    assert abs(sw.energy[-1] - ev[0]) < 1e-10
+    gs = se.psi
+    with pytest.raises(ValueError):
+        T.StateEnvsTTN(T.random_ttn(N, 16, 2), terms, [gs], weight=0.0)
+    ex = T.StateEnvsTTN(T.random_ttn(N, 16, 2), terms, [gs], weight=10.0)
+    sx = T.optimize(ex, [16], [8], path)
+    assert abs(sx.energy[-1] - ev[1]) < 1e-8
+    ov = float(np.vdot(T.ttn_to_dense(ex.psi), T.ttn_to_dense(gs)))
+    assert abs(ov) < 1e-6
