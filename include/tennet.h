@@ -300,9 +300,18 @@ int tn_ttn_env_position(tn_ttn_env* env, int node);
 int tn_ttn_env_product(tn_ttn_env* env, const double* v, double* out, int64_t n);
 /* algorithmic flops of one product at the centre */
 int tn_ttn_env_product_flops(tn_ttn_env* env, double* flops);
+/* StateEnvsTTN(psi, H, Ms; weight) (src/ttn/state_envs_ttn.jl:36-52): excited-state
+ * projectors.  Every later product and update uses EnvCouplingModelProjTTN's effective
+ * Hamiltonian (src/ttn/environment.jl:104-110), H_eff + weight sum_k |m_k><m_k|, with m_k
+ * the centre tensor of Ms[k] contracted with its overlaps with psi on every link of the
+ * centre (LinkProjTTN, src/ttn/linkproj.jl:56-78, 143-224).  The states are copied and need
+ * psi's tree and sites; count 0 removes the projectors; weight <= 0 with count > 0 is
+ * TN_E_INVALID with the reference's message; at most 32 states. */
+int tn_ttn_env_set_projectors(tn_ttn_env* env, const tn_ttn* const* Ms, int count,
+                              double weight);
 /* update_position!(sysenv, eig_solver, node; kwargs...) (src/ttn/update_site_ttn.jl:42-63);
- * p->maxdim bounds the links moved through (a larger link would need the truncating SVD
- * move, which is not built: TN_E_INVALID); p->noise must be 0 */
+ * a link larger than p->maxdim on the path is truncated by an SVD move
+ * (moveisometry_to_next!, src/ttn/ttn.jl:292-300); p->noise must be 0 */
 int tn_ttn_env_update_position(tn_ttn_env* env, int node, const tn_update_params* p,
                                tn_update_result* res);
 /* fullsweep!(sysenv, sweeppath, eig_solver, swdata; kwargs...), noise = 0 branch

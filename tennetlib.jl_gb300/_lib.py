@@ -147,6 +147,7 @@ PROTOS = {
     "tn_ttn_env_position": (C.c_int, [vp, C.c_int]),
     "tn_ttn_env_product": (C.c_int, [vp, f64p, f64p, C.c_int64]),
     "tn_ttn_env_product_flops": (C.c_int, [vp, f64p]),
+    "tn_ttn_env_set_projectors": (C.c_int, [vp, C.POINTER(vp), C.c_int, C.c_double]),
     "tn_ttn_env_update_position": (C.c_int, [vp, C.c_int, C.POINTER(UpdateParams),
                                              C.POINTER(UpdateResult)]),
     "tn_ttn_envs_fullsweep": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, i32p,

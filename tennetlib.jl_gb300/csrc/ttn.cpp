@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -243,6 +244,19 @@ struct QrPlan {         // isometry move v -> u: blocked-QR GEMMs and the R mode
 
 }  // namespace
 
+// One state M of an excited-state projector (LinkProjTTN, TenNetLib src/ttn/linkproj.jl:15-224):
+// M's node tensors and, per tree link, the overlap matrix of psi and M on one side of it
+// (psi's link index first, leading dimension psi's link dimension), oriented toward the
+// orthogonality centre like the link tensors.
+struct TtnProj {
+    std::vector<std::vector<int>> mdims;  // M's node dimensions (legs ordered as psi's)
+    std::vector<int64_t> moff;            // node offsets in mbuf
+    DevBuf mbuf;
+    std::vector<int64_t> eoff;            // per edge: overlap matrix offset in ebuf
+    std::vector<int> efrom;               // node whose side the overlap describes (-1: none yet)
+    DevBuf ebuf;
+};
+
 struct TtnGroup;
 
 struct tn_ttn_env {
@@ -281,6 +295,11 @@ struct tn_ttn_env {
     int kry_vecs = 0;
     int nchunk_t = 1;                 // k chunks of the link-tensor contractions
     int nchunk_q = 1;                 // k chunks of the QR panel products
+    // excited-state projectors (none when empty): H_eff x + proj_weight sum_k m_k (m_k . x)
+    std::vector<TtnProj> proj;
+    double proj_weight = 0;
+    DevBuf proj_t1, proj_t2, proj_m, proj_c, proj_part;
+    int64_t proj_tn = 0;              // elements of one temporary
     // statistics of the last solve
     double energy = 0;
     int matvecs = 0, converged = 0;
@@ -840,6 +859,136 @@ void run_link_move(TtnGroup& G, int v, int u) {
     for (auto* e : members(G)) e->estore[eid].from = v;
 }
 
+// ---- excited-state projectors (LinkProjTTN) -----------------------------------------------
+// Buffers: S_L the group arena (psi), S_X M's node tensors, S_A M's overlap matrices,
+// S_T1 / S_T2 temporaries, S_Y the projected vector being formed.
+Bases proj_bases(TtnGroup& G, tn_ttn_env* e, TtnProj& P, double* out) {
+    Bases bs{};
+    bs.p[S_L] = G.arena.d();
+    bs.p[S_X] = P.mbuf.d();
+    bs.p[S_A] = P.ebuf.d();
+    bs.p[S_T1] = e->proj_t1.d();
+    bs.p[S_T2] = e->proj_t2.d();
+    bs.p[S_Y] = out;
+    return bs;
+}
+
+struct ProjSrc {
+    int buf;
+    int64_t off;
+};
+
+// M[v] with the overlap matrix of every link of v but the one toward `skip` applied to its
+// leg (the M side of move_linkproj_to_next! and contract, linkproj.jl:56-78 and 143-157):
+// one FP64 GEMM launch per mapped leg.  The last product goes to S_Y when `out` is given.
+ProjSrc proj_mapped(tn_ttn_env* e, TtnProj& P, int v, int skip, const Bases& bs, double* out) {
+    const TtnTree& t = e->tree;
+    cudaStream_t st = e->ctx->stream;
+    std::vector<int> dims = P.mdims[v];
+    const int ns = int(t.sites[v].size());
+    std::vector<int> legs;
+    for (size_t j = 0; j < t.nbr[v].size(); ++j)
+        if (t.nbr[v][j] != skip) legs.push_back(int(j));
+    ProjSrc cur{S_X, P.moff[v]};
+    int tmp = 0;
+    for (size_t a = 0; a < legs.size(); ++a) {
+        const int j = legs[a], w = t.nbr[v][j], li = ns + j;
+        const int eid = t.edge(w, v);
+        TN_REQUIRE(P.efrom[eid] == w, "TTN internal: projector overlap not oriented toward the node");
+        const int dout = e->dims[v][li];
+        const ProjSrc dst = (a + 1 == legs.size() && out) ? ProjSrc{S_Y, 0}
+                                                          : ProjSrc{tmp ? S_T2 : S_T1, 0};
+        GemmPlan g;
+        add_mode_tasks(g, dims, li, dout, dst.buf, dst.off,
+                       {ModeIn{cur.buf, cur.off, S_A, P.eoff[eid]}}, 0);
+        g.finalize(st);
+        launch_gemm_f64(g, bs, st);
+        dims[li] = dout;
+        cur = dst;
+        if (dst.buf != S_Y) tmp ^= 1;
+    }
+    if (out && cur.buf != S_Y) {  // no link mapped (a single-node tree): M[v] itself
+        TN_CUDA(cudaMemcpyAsync(out, P.mbuf.d() + P.moff[v], size_t(vol(dims)) * 8,
+                                cudaMemcpyDeviceToDevice, st));
+        cur = ProjSrc{S_Y, 0};
+    }
+    return cur;
+}
+
+// overlap of link (v, u) on v's side: psi[v] contracted with the mapped M[v] over every leg
+// but the one toward u (move_linkproj_to_next!, linkproj.jl:56-78)
+void proj_move(TtnGroup& G, tn_ttn_env* e, TtnProj& P, int v, int u) {
+    const TtnTree& t = e->tree;
+    cudaStream_t st = e->ctx->stream;
+    const Bases bs = proj_bases(G, e, P, nullptr);
+    const ProjSrc y = proj_mapped(e, P, v, u, bs, nullptr);
+    const auto& dp = e->dims[v];
+    const int lu = t.leg_nbr(v, u);
+    const int Dp = dp[lu], Dm = P.mdims[v][lu];
+    const int64_t Pr = prod(dp, 0, lu), Q = prod(dp, lu + 1, int(dp.size()));
+    const int eid = t.edge(v, u);
+    const int64_t phi = e->node_off[v];
+    GemmPlan g;
+    g.add_task(S_A, P.eoff[eid], Dp, Dm, Dp, 0);
+    if (Q == 1) {         // E = Phi^T Y over the rows
+        g.add_seg(S_L, phi, int(Pr), 1, y.buf, y.off, int(Pr), 0, int(Pr));
+    } else if (Pr == 1) { // E = Phi Y^T over the columns
+        g.add_seg(S_L, phi, Dp, 0, y.buf, y.off, Dm, 1, int(Q));
+    } else {              // E = sum_q Phi_q^T Y_q
+        for (int64_t q = 0; q < Q; ++q)
+            g.add_seg(S_L, phi + q * Pr * Dp, int(Pr), 1, y.buf, y.off + q * Pr * Dm, int(Pr), 0,
+                      int(Pr));
+    }
+    g.finalize(st);
+    launch_gemm_f64(g, bs, st);
+    P.efrom[eid] = v;
+}
+
+void proj_move_all(TtnGroup& G, int v, int u) {
+    const int e0 = G.ctx->timer.mark();
+    bool any = false;
+    for (auto* e : members(G))
+        for (auto& P : e->proj) {
+            proj_move(G, e, P, v, u);
+            any = true;
+        }
+    if (any) G.ctx->timer.add(T_ENV, e0, G.ctx->timer.mark());
+}
+
+// m_k at `node` for every member with projectors (ProjTTN's contract, linkproj.jl:143-157)
+void proj_vectors(TtnGroup& G, int node) {
+    for (auto* e : members(G)) {
+        const int64_t S = (e->S + 31) / 32 * 32;
+        for (size_t k = 0; k < e->proj.size(); ++k) {
+            double* out = e->proj_m.d() + int64_t(k) * S;
+            proj_mapped(e, e->proj[k], node, -1, proj_bases(G, e, e->proj[k], out), out);
+        }
+    }
+}
+
+// y += w sum_k m_k (m_k . x) on the matvec buffers (EnvCouplingModelProjTTN's product,
+// src/ttn/environment.jl:104-110)
+void proj_apply(TtnGroup& G, int node) {
+    for (auto* e : members(G)) {
+        const int K = int(e->proj.size());
+        if (K == 0) continue;
+        const int64_t n = vol(e->dims[node]), S = (e->S + 31) / 32 * 32;
+        std::vector<const double*> m(K);
+        for (int k = 0; k < K; ++k) m[k] = e->proj_m.d() + int64_t(k) * S;
+        launch_multi_dot(m.data(), K, wptr(G, e, e->w_x), n, e->proj_part.d(), e->proj_c.d(),
+                         G.ctx->stream);
+        launch_multi_axpy(wptr(G, e, e->w_y), m.data(), K, e->proj_c.d(), e->proj_weight, n,
+                          G.ctx->stream);
+    }
+}
+
+void run_product_proj(TtnGroup& G, int v) {
+    run_product(G, v);
+    const int e0 = G.ctx->timer.mark();
+    proj_apply(G, v);
+    G.ctx->timer.add(T_HEFF, e0, G.ctx->timer.mark());
+}
+
 // ---- isometry move v -> u (QR; all members) ------------------------------------------------
 std::unique_ptr<QrPlan> build_qr_plan(TtnGroup& G, int v, int u, const std::vector<char>& blocked,
                                       const std::vector<int>& kmins) {
@@ -1157,7 +1306,10 @@ void position_group(TtnGroup& G, int node, bool normalize, int maxdim) {
         }
         normalize_batch(G, E, x, n);
     }
-    for (size_t k = 0; k + 1 < path.size(); ++k) run_link_move(G, path[k], path[k + 1]);
+    for (size_t k = 0; k + 1 < path.size(); ++k) {
+        run_link_move(G, path[k], path[k + 1]);
+        proj_move_all(G, path[k], path[k + 1]);
+    }
 }
 
 // Lowest eigenpair of H_eff at `node` for every member, thick-restart Lanczos in lockstep
@@ -1251,7 +1403,8 @@ void lanczos_group(TtnGroup& G, int node, const tn_update_params* prm) {
         gs_launch(G, d, 1, 0.0, false, true);
         scale_launch(G, s);
     }
-    run_product(G, node);
+    proj_vectors(G, node);
+    run_product_proj(G, node);
     for (auto& s : S) s.matvecs++;
     {
         std::vector<size_t> all(ni);
@@ -1351,7 +1504,7 @@ void lanczos_group(TtnGroup& G, int node, const tn_update_params* prm) {
             scale_launch(G, d);
             ctx->timer.add(T_LANCZOS, e0, ctx->timer.mark());
         }
-        run_product(G, node);
+        run_product_proj(G, node);
         for (size_t i : act) S[i].matvecs++;
         gs2(act);
         for (size_t i : act) {
@@ -1566,6 +1719,65 @@ void fill_sweep_result(TtnGroup& G, tn_ttn_env* e, tn_sweep_result* r, int64_t l
     r->qr_panel_ms = G.acc_ms[T_QRPANEL];
     r->qr_gemm_ms = G.acc_ms[T_QRGEMM];
     r->krylov_bytes = G.krylov_bytes;
+}
+
+// StateEnvsTTN(psi, H, Ms; weight) (src/ttn/state_envs_ttn.jl:36-52): copies of the Ms and
+// their overlaps built from the leaves toward the centre (LinkProjTTN, linkproj.jl:188-224)
+void proj_setup(TtnGroup& G, tn_ttn_env* e, const tn_ttn* const* Ms, int count, double weight) {
+    cudaStream_t st = e->ctx->stream;
+    const TtnTree& t = e->tree;
+    TN_CUDA(cudaStreamSynchronize(st));
+    e->proj.clear();
+    e->proj_weight = count > 0 ? weight : 0.0;
+    if (count == 0) return;
+    auto r32 = [](int64_t n) { return (n + 31) / 32 * 32; };
+    int64_t tn = 32;
+    for (int k = 0; k < count; ++k) {
+        const tn_ttn* M = Ms[k];
+        TtnProj P;
+        P.mdims = M->dims;
+        P.moff.assign(t.nn, 0);
+        int64_t c = 0;
+        for (int v = 0; v < t.nn; ++v) {
+            P.moff[v] = c;
+            c += r32(vol(M->dims[v]));
+            // a temporary holds M[v] with any subset of its links mapped to psi's dimensions
+            int64_t big = 1;
+            for (size_t l = 0; l < M->dims[v].size(); ++l)
+                big *= std::max(M->dims[v][l], e->dims[v][l]);
+            tn = std::max(tn, big);
+        }
+        P.mbuf.alloc(size_t(std::max<int64_t>(c, 32)) * 8, st);
+        for (int v = 0; v < t.nn; ++v)
+            TN_CUDA(cudaMemcpyAsync(P.mbuf.d() + P.moff[v], M->node[v].p,
+                                    size_t(vol(M->dims[v])) * 8, cudaMemcpyDeviceToDevice, st));
+        // psi's link dimensions only shrink while the environment lives: slots sized now fit
+        c = 0;
+        P.eoff.assign(t.edges.size(), 0);
+        for (size_t ei = 0; ei < t.edges.size(); ++ei) {
+            const int a = t.edges[ei].first, b = t.edges[ei].second;
+            const int la = t.leg_nbr(a, b);
+            P.eoff[ei] = c;
+            c += r32(int64_t(e->dims[a][la]) * M->dims[a][la]);
+        }
+        P.ebuf.alloc(size_t(std::max<int64_t>(c, 32)) * 8, st);
+        TN_CUDA(cudaMemsetAsync(P.ebuf.p, 0, P.ebuf.bytes, st));
+        P.efrom.assign(t.edges.size(), -1);
+        e->proj.push_back(std::move(P));
+    }
+    e->proj_tn = tn;
+    e->proj_t1.alloc(size_t(tn) * 8, st);
+    e->proj_t2.alloc(size_t(tn) * 8, st);
+    e->proj_m.alloc(size_t(count) * r32(e->S) * 8, st);
+    e->proj_c.alloc(64 * 8, st);
+    e->proj_part.alloc(size_t(count) * blas_nparts() * 8, st);
+    const int oc = e->center;
+    for (int v : bfs_reverse(t, oc)) {
+        if (v == oc) continue;
+        const int next = t.path(v, oc)[1];
+        for (auto& P : e->proj) proj_move(G, e, P, v, next);
+    }
+    TN_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace
@@ -1796,7 +2008,8 @@ int tn_ttn_env_product(tn_ttn_env* env, const double* v, double* out, int64_t n)
         TN_REQUIRE(n == vol(env->dims[c]), "vector size does not match the centre tensor");
         cudaStream_t st = env->ctx->stream;
         TN_CUDA(cudaMemcpyAsync(wptr(G, env, env->w_x), v, size_t(n) * 8, cudaMemcpyHostToDevice, st));
-        run_product(G, c);
+        proj_vectors(G, c);
+        run_product_proj(G, c);
         TN_CUDA(cudaMemcpyAsync(out, wptr(G, env, env->w_y), size_t(n) * 8, cudaMemcpyDeviceToHost, st));
         collect_stats(G);
         check_device_error_public(env->ctx);
@@ -1808,6 +2021,34 @@ int tn_ttn_env_product_flops(tn_ttn_env* env, double* flops) {
         TtnGroup& G = solo(env);
         TN_REQUIRE(flops, "null argument");
         *flops = product_plan(G, env->center).flops;
+    });
+}
+
+int tn_ttn_env_set_projectors(tn_ttn_env* env, const tn_ttn* const* Ms, int count, double weight) {
+    return guarded([&] {
+        TN_REQUIRE(env && env->grp, "null argument");
+        TN_REQUIRE(count >= 0 && count <= 32, "between 0 and 32 projector states");
+        if (count > 0) {
+            TN_REQUIRE(Ms, "null argument");
+            if (!(weight > 0.0)) {
+                char msg[160];
+                std::snprintf(msg, sizeof msg,
+                              "`weight` parameter should be > 0.0 (value passed was `weight=%g`)",
+                              weight);
+                throw Error(TN_E_INVALID, msg);
+            }
+            const TtnTree& t = env->tree;
+            for (int k = 0; k < count; ++k) {
+                const tn_ttn* M = Ms[k];
+                TN_REQUIRE(M && M->ctx == env->ctx, "projector states must share the context");
+                TN_REQUIRE(M->tree.N == t.N && M->tree.nn == t.nn && M->tree.d == t.d &&
+                               M->tree.edges == t.edges && M->tree.site_node == t.site_node,
+                           "projector states must have the tree and the sites of psi "
+                           "(linkproj.jl:190-191)");
+            }
+        }
+        proj_setup(*env->grp, env, Ms, count, weight);
+        check_device_error_public(env->ctx);
     });
 }
 

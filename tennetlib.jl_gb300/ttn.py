@@ -348,9 +348,13 @@ def heisenberg_terms(N: int):
 # --------------------------------------------------------------------------------------
 
 class StateEnvsTTN:
-    """``StateEnvsTTN(psi, H)``: a copy of psi and its link tensors on the device."""
+    """``StateEnvsTTN(psi, H)``: a copy of psi and its link tensors on the device.
 
-    def __init__(self, psi: TTN, H: CouplingModel, _handle=None):
+    ``StateEnvsTTN(psi, H, Ms, weight=w)`` (src/ttn/state_envs_ttn.jl:36-52) adds the
+    excited-state projectors of the states ``Ms``: products and updates then use
+    H_eff + w sum_k |m_k><m_k| (EnvCouplingModelProjTTN, src/ttn/environment.jl:104-110)."""
+
+    def __init__(self, psi: TTN, H: CouplingModel, Ms=None, *, weight=None, _handle=None):
         self.ctx = psi.ctx
         self.template = psi
         self.H = H
@@ -360,6 +364,16 @@ class StateEnvsTTN:
         hs = (L.vp * 1)()
         L.check(self.ctx.lib.tn_ttn_envs_create(1, (L.vp * 1)(psi.h), (L.vp * 1)(H.h), hs))
         _own(self, L.vp(hs[0]))
+        if Ms is not None:
+            self.set_projectors(Ms, -1.0 if weight is None else weight)
+
+    def set_projectors(self, Ms, weight: float):
+        """Projectors onto the states ``Ms`` (copied) with weight > 0; ``[]`` removes them."""
+        Ms = list(Ms)
+        self._Ms = Ms
+        arr = (L.vp * max(len(Ms), 1))(*[m.h for m in Ms])
+        L.check(self.ctx.lib.tn_ttn_env_set_projectors(self.h, arr, len(Ms), float(weight)))
+        return self
 
     @classmethod
     def batch(cls, psis, models):
@@ -522,8 +536,18 @@ def optimize_(sysenv, params: OptimizeParamsTTN, sweeppath, **kwargs) -> SweepDa
     return sw
 
 
-def optimize(psi0: TTN, H: CouplingModel, params: OptimizeParamsTTN, sweeppath, **kwargs):
-    """``optimize(psi0, H, params, sweeppath)``: returns (energy, psi)."""
-    se = StateEnvsTTN(psi0, H)
+def optimize(psi0: TTN, H: CouplingModel, *args, **kwargs):
+    """``optimize(psi0, H, params, sweeppath)`` or, for an excited state,
+    ``optimize(psi0, H, Ms, params, sweeppath; weight)`` (src/ttn/optimize_ttn.jl:274-301):
+    returns (energy, psi)."""
+    if len(args) == 3:
+        Ms, params, sweeppath = args
+        weight = kwargs.pop("weight", -1.0)
+        se = StateEnvsTTN(psi0, H, Ms, weight=weight)
+    elif len(args) == 2:
+        params, sweeppath = args
+        se = StateEnvsTTN(psi0, H)
+    else:
+        raise TypeError("optimize(psi0, H, [Ms,] params, sweeppath)")
     sw = optimize_(se, params, sweeppath, **kwargs)
     return sw.energy[-1], se.getpsi()
