@@ -166,6 +166,20 @@ int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap);
  * length (out == NULL: only the length) */
 int tn_mps_site_blocks(const tn_mps* mps, int site, double* out, int64_t cap, int64_t* len);
 int tn_mps_center(const tn_mps* mps);
+/* Complex states (the ComplexF64 MPS of a real-time evolution).  A complex MPS keeps real
+ * and imaginary parts of every charge block on the device; tn_mps_make_complex turns a real
+ * state into one (imaginary parts zero), tn_mps_is_complex answers 1 or 0, and
+ * tn_mps_site_complex writes the dense site tensor (Dl, d, Dr) column-major as interleaved
+ * (re, im) pairs, Julia's ComplexF64 memory layout (cap in doubles, >= 2 Dl d Dr; a real
+ * state reads with zero imaginary parts).  tn_mps_site and tn_mps_site_blocks take real
+ * states only. */
+int tn_mps_make_complex(tn_mps* mps);
+/* tn_mps_create for a complex state: site_data interleaved (re, im) pairs (ComplexF64) */
+int tn_mps_create_complex(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                          const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
+                          const double* site_data, int center, tn_mps** out);
+int tn_mps_is_complex(const tn_mps* mps);
+int tn_mps_site_complex(const tn_mps* mps, int site, double* out, int64_t cap);
 /* measure(T, psi, opstr) for every site (TenNetLib src/mps/measure.jl:150-219): out[i] =
  * <psi|O_i|psi> / <psi|psi> with the single-site operator op (d x d column-major [s', s]),
  * from GPU transfer matrices instead of moving the orthogonality centre (equal for the
@@ -176,6 +190,9 @@ int tn_mps_expect_local(tn_mps* mps, const double* op, double* out);
  * TenNetLib call on the states it returns; TenNetLib's own sweep calls no overlap), from GPU
  * transfer matrices over the charge sectors both states carry. */
 int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out);
+/* inner(a, b) when either state is complex: out[0] + i out[1] = <a|b> (a conjugated).
+ * tn_mps_expect_local also takes complex states (the real part of <O_i>, O Hermitian). */
+int tn_mps_overlap_complex(const tn_mps* a, const tn_mps* b, double* out);
 
 /* ---- StateEnvs --------------------------------------------------------------------
  * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO
@@ -196,6 +213,10 @@ int tn_env_position(tn_env* env, int pos, int nsite);
 /* product(sysenv, v) = H_eff * v at the current position (state_envs.jl:376-378).
  * v/out dense (Dl, d, Dr) for nsite = 1 or (Dl, d, d, Dr) for nsite = 2. */
 int tn_env_product(tn_env* env, const double* v, double* out, int64_t n);
+/* the same for a complex state: v and out interleaved (re, im), n complex entries */
+int tn_env_product_complex(tn_env* env, const double* v, double* out, int64_t n);
+/* the state of env and its environments made complex (imaginary parts zero) */
+int tn_env_make_complex(tn_env* env);
 /* dense copy of environment L[i] (side 0: contracts sites < i) or R[i] (side 1: contracts
  * sites > i) as (D, w, D) [bra, MPO state, ket] column-major; dims[3] receives (D, w, D).
  * With out == NULL only dims are written.  The environment must have been built by a
@@ -233,6 +254,13 @@ int tn_env_fullsweep(tn_env* env, const tn_update_params* p, tn_sweep_result* re
  * (reference defaults 30 / 100 / 1e-12).  Fields of res as for tn_env_fullsweep. */
 int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_sweep_result* res,
                      double* mid_eigs, int mid_cap, int32_t* n_mid_eigs);
+/* tdvpsweep! with a complex time step tau = tau_re + i tau_im (real-time evolution
+ * exp(-i dt H) is tau = -i dt).  A real state is made complex first (ITensors promotes the
+ * MPS to ComplexF64 the same way); the Krylov exponential, the contractions and the block
+ * SVD then run on complex tensors (FP64 on the GPU whatever the context's precision). */
+int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn_update_params* p,
+                             tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                             int32_t* n_mid_eigs);
 
 /* ---- block SVD + truncation -------------------------------------------------------
  * The SVD/truncation of replacebond! (called at TenNetLib src/mps/update_site.jl:64-76)

@@ -219,12 +219,18 @@ class MPS:
         self.d = len(phys_q)
         self.phys_q = np.asarray(phys_q, dtype=np.int32)
         nsec, q, dim = _links_to_sectors(links)
-        flat = np.concatenate([np.asarray(t, dtype=np.float64).ravel(order="F") for t in tensors])
+        cplx = any(np.iscomplexobj(t) for t in tensors)
+        if cplx:  # interleaved (re, im): ComplexF64 memory
+            flat = np.concatenate([np.asarray(t, dtype=np.complex128).ravel(order="F")
+                                   for t in tensors]).view(np.float64)
+        else:
+            flat = np.concatenate([np.asarray(t, dtype=np.float64).ravel(order="F")
+                                   for t in tensors])
         bufs = [L.as_i32(self.phys_q), L.as_i32(nsec), L.as_i32(q), L.as_i32(dim), L.as_f64(flat)]
         h = L.vp()
-        L.check(self.ctx.lib.tn_mps_create(self.ctx.h, self.N, self.d, bufs[0][1], bufs[1][1],
-                                           bufs[2][1], bufs[3][1], bufs[4][1], center,
-                                           C.byref(h)))
+        create = self.ctx.lib.tn_mps_create_complex if cplx else self.ctx.lib.tn_mps_create
+        L.check(create(self.ctx.h, self.N, self.d, bufs[0][1], bufs[1][1], bufs[2][1], bufs[3][1],
+                       bufs[4][1], center, C.byref(h)))
         _own(self, h)
 
     @classmethod
@@ -286,9 +292,24 @@ class MPS:
     def maxlinkdim(self):
         return max(self.linkdims())
 
+    @property
+    def is_complex(self) -> bool:
+        return self.ctx.lib.tn_mps_is_complex(self.h) == 1
+
+    def to_complex_(self):
+        """Make the state complex in place (imaginary parts zero)."""
+        L.check(self.ctx.lib.tn_mps_make_complex(self.h))
+        return self
+
     def site(self, i):
+        """Dense site tensor (Dl, d, Dr): float64, or complex128 for a complex state."""
         Dl = int(self.link(i)[1].sum())
         Dr = int(self.link(i + 1)[1].sum())
+        if self.is_complex:
+            out = np.zeros(2 * Dl * self.d * Dr)
+            L.check(self.ctx.lib.tn_mps_site_complex(self.h, i, out.ctypes.data_as(L.f64p),
+                                                     out.size))
+            return out.view(np.complex128).reshape((Dl, self.d, Dr), order="F")
         out = np.zeros(Dl * self.d * Dr)
         L.check(self.ctx.lib.tn_mps_site(self.h, i, out.ctypes.data_as(L.f64p), out.size))
         return out.reshape((Dl, self.d, Dr), order="F")
@@ -297,8 +318,13 @@ class MPS:
     def center(self):
         return self.ctx.lib.tn_mps_center(self.h)
 
-    def inner(self, other: "MPS") -> float:
-        """<self|other> (both states on this context, same sites)."""
+    def inner(self, other: "MPS"):
+        """<self|other> (both states on this context, same sites); complex when either is."""
+        if self.is_complex or other.is_complex:
+            v = np.zeros(2)
+            L.check(self.ctx.lib.tn_mps_overlap_complex(self.h, other.h,
+                                                        v.ctypes.data_as(L.f64p)))
+            return complex(v[0], v[1])
         v = C.c_double()
         L.check(self.ctx.lib.tn_mps_overlap(self.h, other.h, C.byref(v)))
         return v.value
@@ -370,13 +396,36 @@ class StateEnvs:
         return self
 
     def product(self, v):
-        """H_eff * v at the current position, v dense (Dl, d, d, Dr)."""
+        """H_eff * v at the current position, v dense (Dl, d, d, Dr); complex for a complex
+        state."""
+        if np.iscomplexobj(v) or self.is_complex:
+            v = np.asarray(v, dtype=np.complex128)
+            flat = np.ascontiguousarray(v.ravel(order="F"))
+            out = np.zeros_like(flat)
+            L.check(self.ctx.lib.tn_env_product_complex(
+                self.h, flat.view(np.float64).ctypes.data_as(L.f64p),
+                out.view(np.float64).ctypes.data_as(L.f64p), flat.size))
+            return out.reshape(v.shape, order="F")
         v = np.asarray(v, dtype=np.float64)
         flat = np.ascontiguousarray(v.ravel(order="F"))
         out = np.zeros_like(flat)
         L.check(self.ctx.lib.tn_env_product(self.h, flat.ctypes.data_as(L.f64p),
                                             out.ctypes.data_as(L.f64p), flat.size))
         return out.reshape(v.shape, order="F")
+
+    @property
+    def is_complex(self) -> bool:
+        h = L.vp()
+        L.check(self.ctx.lib.tn_env_getpsi(self.h, C.byref(h)))
+        try:
+            return self.ctx.lib.tn_mps_is_complex(h) == 1
+        finally:
+            self.ctx.lib.tn_mps_destroy(h)
+
+    def to_complex_(self):
+        """Make the state and its environments complex (imaginary parts zero)."""
+        L.check(self.ctx.lib.tn_env_make_complex(self.h))
+        return self
 
     __call__ = product
 
@@ -641,15 +690,14 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     """``tdvpsweep!`` (``src/mps/tdvp.jl:247-277``) with nsite = 2: one full sweep with
     ``exp_solver`` at time_step/2 and reverse one-site steps; ``abstime += |time_step|``.
 
-    The engine evolves with real time steps (imaginary-time evolution exp(time_step H));
-    complex steps and ``nsite = "dynamic"`` are not built.
+    A real time step is imaginary-time evolution exp(time_step H); a complex one (real-time
+    evolution exp(-i dt H) is ``time_step = -1j * dt``) makes the state complex first, as
+    ITensors promotes the MPS to ComplexF64.  ``nsite = "dynamic"`` is not built.
     """
     if solver is not exp_solver:
         raise ValueError("`tdvpsweep!()`: `solver` must be `exp_solver` !!")
     if nsite != 2:
         raise ValueError("only nsite = 2 TDVP sweeps are built")
-    if isinstance(time_step, complex) or np.iscomplexobj(time_step):
-        raise NotImplementedError("complex time steps are not built in this engine")
     if kwargs.get("noise", 0.0):
         raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
                          "`reverse_step=true` !!")
@@ -660,8 +708,14 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     nmid = C.c_int32()
     sysenv = engine.sysenv
     t0 = time.perf_counter()
-    L.check(sysenv.ctx.lib.tn_env_tdvpsweep(sysenv.h, float(time_step), C.byref(p), C.byref(res),
-                                            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    tau = complex(time_step)
+    if tau.imag != 0.0:
+        L.check(sysenv.ctx.lib.tn_env_tdvpsweep_complex(
+            sysenv.h, tau.real, tau.imag, C.byref(p), C.byref(res), mid.ctypes.data_as(L.f64p),
+            cap, C.byref(nmid)))
+    else:
+        L.check(sysenv.ctx.lib.tn_env_tdvpsweep(sysenv.h, tau.real, C.byref(p), C.byref(res),
+                                                mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
     _record_sweep(engine.swdata, res, mid[: nmid.value], time.perf_counter() - t0)
     engine.abstime += abs(time_step)
     return None

@@ -98,6 +98,8 @@ PROTOS = {
     "tn_mpo_destroy": (C.c_int, [vp]),
     "tn_mps_create": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p, C.c_int,
                                 C.POINTER(vp)]),
+    "tn_mps_create_complex": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p,
+                                        C.c_int, C.POINTER(vp)]),
     "tn_mps_create_blocks": (C.c_int, [vp, C.c_int, C.c_int, i32p, i32p, i32p, i32p, f64p,
                                        C.POINTER(C.c_int64), C.c_int, C.POINTER(vp)]),
     "tn_mps_site_blocks": (C.c_int, [vp, C.c_int, f64p, C.c_int64, C.POINTER(C.c_int64)]),
@@ -105,6 +107,10 @@ PROTOS = {
     "tn_mps_link": (C.c_int, [vp, C.c_int, i32p, i32p, i32p, C.c_int]),
     "tn_mps_site": (C.c_int, [vp, C.c_int, f64p, C.c_int64]),
     "tn_mps_center": (C.c_int, [vp]),
+    "tn_mps_make_complex": (C.c_int, [vp]),
+    "tn_mps_is_complex": (C.c_int, [vp]),
+    "tn_mps_site_complex": (C.c_int, [vp, C.c_int, f64p, C.c_int64]),
+    "tn_mps_overlap_complex": (C.c_int, [vp, vp, f64p]),
     "tn_mps_expect_local": (C.c_int, [vp, f64p, f64p]),
     "tn_mps_overlap": (C.c_int, [vp, vp, f64p]),
     "tn_env_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
@@ -113,6 +119,8 @@ PROTOS = {
     "tn_env_getpsi": (C.c_int, [vp, C.POINTER(vp)]),
     "tn_env_position": (C.c_int, [vp, C.c_int, C.c_int]),
     "tn_env_product": (C.c_int, [vp, f64p, f64p, C.c_int64]),
+    "tn_env_product_complex": (C.c_int, [vp, f64p, f64p, C.c_int64]),
+    "tn_env_make_complex": (C.c_int, [vp]),
     "tn_env_environment": (C.c_int, [vp, C.c_int, C.c_int, f64p, C.c_int64, i32p]),
     "tn_env_product_flops": (C.c_int, [vp, f64p]),
     "tn_env_update_position": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(UpdateParams),
@@ -126,6 +134,8 @@ PROTOS = {
                                          C.POINTER(SweepResult), f64p, C.c_int, i32p]),
     "tn_env_tdvpsweep": (C.c_int, [vp, C.c_double, C.POINTER(UpdateParams), C.POINTER(SweepResult),
                                    f64p, C.c_int, i32p]),
+    "tn_env_tdvpsweep_complex": (C.c_int, [vp, C.c_double, C.c_double, C.POINTER(UpdateParams),
+                                           C.POINTER(SweepResult), f64p, C.c_int, i32p]),
     "tn_svd_truncate": (C.c_int, [vp, C.c_int, i32p, i32p, f64p, C.c_int32, C.c_int32,
                                   C.c_double, i32p, f64p, f64p]),
     "tn_block_svals_noalloc": (C.c_int, [C.c_int, vp, C.c_int, i32p, i32p, vp, vp]),

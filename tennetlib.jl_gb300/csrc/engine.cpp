@@ -140,14 +140,19 @@ void check_params(const tn_update_params* p) {
 // -------------------------------------------------------------------------------------
 void sync(tn_ctx* c) { TN_CUDA(cudaStreamSynchronize(c->stream)); }
 
-void make_trivial_env(tn_ctx* ctx, tn_envt& E, const Link& link, const std::vector<int>& delta) {
+void make_trivial_env(tn_ctx* ctx, tn_envt& E, const Link& link, const std::vector<int>& delta,
+                      int planes = 1) {
     E.lay = make_env_layout(link, delta);
     TN_REQUIRE(E.lay.size == 1, "boundary link and boundary MPO link must have dimension 1");
-    E.buf.alloc(sizeof(double), ctx->stream);
-    const double one = 1.0;
-    TN_CUDA(cudaMemcpyAsync(E.buf.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    E.buf.alloc(sizeof(double) * planes, ctx->stream);
+    const double one[2] = {1.0, 0.0};
+    TN_CUDA(cudaMemcpyAsync(E.buf.p, one, sizeof(double) * planes, cudaMemcpyHostToDevice,
+                            ctx->stream));
     TN_CUDA(cudaStreamSynchronize(ctx->stream));
 }
+
+// the imaginary plane of a complex buffer of `plane` values per plane into slot s + S_IM
+void set_im(Bases& bs, int slot, int64_t plane) { bs.p[slot + S_IM] = bs.p[slot] + plane; }
 
 bool need_left(const tn_mpo* H, int site, int a, int s) {
     for (int b = 0; b < H->wd[site + 1]; ++b)
@@ -174,6 +179,8 @@ void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 
 std::unique_ptr<SplitPlan> make_split(const GemmPlan& g, int slices, bool a_static,
                                       bool b_static, cudaStream_t st, bool own_packs = true) {
+    for (const Seg& sg : g.segs)
+        TN_REQUIRE(sg.sgn == 1, "internal: the split-precision GEMM takes unsigned segments");
     auto sp = std::make_unique<SplitPlan>();
     sp->slices = slices;
     sp->a_static = a_static;
@@ -425,12 +432,10 @@ void env_left_step(tn_env* env, int i) {
             t2 += int64_t(rowsA) * rk.dim[ir];
         }
     cudaStream_t st = ctx->stream;
-    g1.finalize(st);
-    g3.finalize(st);
-    cb.finalize(st);
-    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8, st);
-    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8, st);
-    Lout.buf.alloc(size_t(std::max<int64_t>(Lout.lay.size, 1)) * 8, st);
+    const int np = env->psi->planes();
+    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8 * np, st);
+    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8 * np, st);
+    Lout.buf.alloc(size_t(std::max<int64_t>(Lout.lay.size, 1)) * 8 * np, st);
     Bases bs{};
     bs.p[S_L] = env->L[i].buf.d();
     bs.p[S_X] = A.buf.d();
@@ -438,9 +443,28 @@ void env_left_step(tn_env* env, int i) {
     bs.p[S_T2] = env->t2.d();
     bs.p[S_Y] = Lout.buf.d();
     const int e0 = ctx->timer.mark();
-    run_gemm(ctx, g1, bs);
-    launch_combine(cb, bs, st);
-    run_gemm(ctx, g3, bs);
+    if (np == 2) {  // L' = A^H (L W A): the bra (the transposed site tensor of g3) conjugated
+        set_im(bs, S_L, Lin.size);
+        set_im(bs, S_X, A.lay.size);
+        set_im(bs, S_T1, t1);
+        set_im(bs, S_T2, t2);
+        set_im(bs, S_Y, Lout.lay.size);
+        GemmPlan c1 = complex_plan(g1, 0), c3 = complex_plan(g3, 1u << S_X);
+        CombPlan cc = complex_comb(cb);
+        c1.finalize(st);
+        c3.finalize(st);
+        cc.finalize(st);
+        launch_gemm_f64(c1, bs, st);
+        launch_combine(cc, bs, st);
+        launch_gemm_f64(c3, bs, st);
+    } else {
+        g1.finalize(st);
+        g3.finalize(st);
+        cb.finalize(st);
+        run_gemm(ctx, g1, bs);
+        launch_combine(cb, bs, st);
+        run_gemm(ctx, g3, bs);
+    }
     if (!env->proj.empty()) proj_left_step(env, i);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
@@ -520,12 +544,10 @@ void env_right_step(tn_env* env, int i) {
             t2 += int64_t(colsB) * lk.dim[il];
         }
     cudaStream_t st = ctx->stream;
-    g1.finalize(st);
-    g3.finalize(st);
-    cb.finalize(st);
-    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8, st);
-    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8, st);
-    Rout.buf.alloc(size_t(std::max<int64_t>(Rout.lay.size, 1)) * 8, st);
+    const int np = env->psi->planes();
+    env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8 * np, st);
+    env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8 * np, st);
+    Rout.buf.alloc(size_t(std::max<int64_t>(Rout.lay.size, 1)) * 8 * np, st);
     Bases bs{};
     bs.p[S_R] = env->R[i].buf.d();
     bs.p[S_X] = B.buf.d();
@@ -533,9 +555,28 @@ void env_right_step(tn_env* env, int i) {
     bs.p[S_T2] = env->t2.d();
     bs.p[S_Y] = Rout.buf.d();
     const int e0 = ctx->timer.mark();
-    run_gemm(ctx, g1, bs);
-    launch_combine(cb, bs, st);
-    run_gemm(ctx, g3, bs);
+    if (np == 2) {  // R' = (B W R) B^H: the bra (the untransposed site tensor of g3) conjugated
+        set_im(bs, S_R, Rin.size);
+        set_im(bs, S_X, B.lay.size);
+        set_im(bs, S_T1, t1);
+        set_im(bs, S_T2, t2);
+        set_im(bs, S_Y, Rout.lay.size);
+        GemmPlan c1 = complex_plan(g1, 0), c3 = complex_plan(g3, 1u << S_X);
+        CombPlan cc = complex_comb(cb);
+        c1.finalize(st);
+        c3.finalize(st);
+        cc.finalize(st);
+        launch_gemm_f64(c1, bs, st);
+        launch_combine(cc, bs, st);
+        launch_gemm_f64(c3, bs, st);
+    } else {
+        g1.finalize(st);
+        g3.finalize(st);
+        cb.finalize(st);
+        run_gemm(ctx, g1, bs);
+        launch_combine(cb, bs, st);
+        run_gemm(ctx, g3, bs);
+    }
     if (!env->proj.empty()) proj_right_step(env, i);
     ctx->timer.add(T_ENV, e0, ctx->timer.mark());
 }
@@ -681,6 +722,15 @@ std::unique_ptr<Heff2Plan> build_heff2(tn_env* env, int p) {
     P->zsize = z;
     P->yoff = std::move(yoff);
     P->flops = P->g1.flops + P->g3.flops + P->cb.flops;
+    if (psi->cplx) {
+        P->g1c = complex_plan(P->g1, 0);
+        P->g3c = complex_plan(P->g3, 0);
+        P->cbc = complex_comb(P->cb);
+        P->g1c.finalize(st);
+        P->g3c.finalize(st);
+        P->cbc.finalize(st);
+        P->flops = P->g1c.flops + P->g3c.flops + P->cbc.flops;
+    }
     return P;
 }
 
@@ -689,8 +739,9 @@ Heff2Plan& heff_plan(tn_env* env) {
         env->hp = build_heff2(env, env->pos);
         env->hp_pos = env->pos;
         cudaStream_t st = env->ctx->stream;
-        env->t1.alloc(size_t(std::max<int64_t>(env->hp->ysize, 1)) * 8, st);
-        env->t2.alloc(size_t(std::max<int64_t>(env->hp->zsize, 1)) * 8, st);
+        const int np = env->psi->planes();
+        env->t1.alloc(size_t(std::max<int64_t>(env->hp->ysize, 1)) * 8 * np, st);
+        env->t2.alloc(size_t(std::max<int64_t>(env->hp->zsize, 1)) * 8 * np, st);
     }
     return *env->hp;
 }
@@ -705,6 +756,23 @@ void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
     bs.p[S_T1] = env->t1.d();
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
+    if (env->psi->cplx) {
+        set_im(bs, S_L, env->L[env->pos].lay.size);
+        set_im(bs, S_R, env->R[env->pos + 1].lay.size);
+        set_im(bs, S_X, P.ph.size);
+        set_im(bs, S_Y, P.ph.size);
+        set_im(bs, S_T1, P.ysize);
+        set_im(bs, S_T2, P.zsize);
+        launch_gemm_f64(P.g1c, bs, ctx->stream);
+        launch_combine(P.cbc, bs, ctx->stream);
+        launch_gemm_f64(P.g3c, bs, ctx->stream);
+        ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+        env->matvecs++;
+        env->heff_flops += P.flops;
+        env->gemm_flops += P.g1c.flops + P.g3c.flops;
+        env->gemm_launches += (P.g1c.tiles.empty() ? 0 : 1) + (P.g3c.tiles.empty() ? 0 : 1);
+        return;
+    }
     if (ctx->prec == TN_PREC_SPLIT) {
         if (!P.s1) P.s1 = make_split(P.g1, ctx->slices, true, false, ctx->stream);   // A = L
         if (!P.s3) P.s3 = make_split(P.g3, ctx->slices, false, true, ctx->stream);   // B = R
@@ -823,6 +891,15 @@ std::unique_ptr<Heff1Plan> build_heff1(tn_env* env, int p) {
     P->ysize = y;
     P->zsize = z;
     P->flops = P->g1.flops + P->g3.flops + P->cb.flops;
+    if (psi->cplx) {
+        P->g1c = complex_plan(P->g1, 0);
+        P->g3c = complex_plan(P->g3, 0);
+        P->cbc = complex_comb(P->cb);
+        P->g1c.finalize(st);
+        P->g3c.finalize(st);
+        P->cbc.finalize(st);
+        P->flops = P->g1c.flops + P->g3c.flops + P->cbc.flops;
+    }
     return P;
 }
 
@@ -831,8 +908,9 @@ Heff1Plan& heff1_plan(tn_env* env) {
         env->h1p = build_heff1(env, env->pos);
         env->h1p_pos = env->pos;
         cudaStream_t st = env->ctx->stream;
-        env->t1.alloc(size_t(std::max<int64_t>(env->h1p->ysize, 1)) * 8, st);
-        env->t2.alloc(size_t(std::max<int64_t>(env->h1p->zsize, 1)) * 8, st);
+        const int np = env->psi->planes();
+        env->t1.alloc(size_t(std::max<int64_t>(env->h1p->ysize, 1)) * 8 * np, st);
+        env->t2.alloc(size_t(std::max<int64_t>(env->h1p->zsize, 1)) * 8 * np, st);
     }
     return *env->h1p;
 }
@@ -847,6 +925,23 @@ void heff1_apply(tn_env* env, Heff1Plan& P, const double* x, double* y) {
     bs.p[S_T1] = env->t1.d();
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
+    if (env->psi->cplx) {
+        set_im(bs, S_L, env->L[env->pos].lay.size);
+        set_im(bs, S_R, env->R[env->pos].lay.size);
+        set_im(bs, S_X, P.lay.size);
+        set_im(bs, S_Y, P.lay.size);
+        set_im(bs, S_T1, P.ysize);
+        set_im(bs, S_T2, P.zsize);
+        launch_gemm_f64(P.g1c, bs, ctx->stream);
+        launch_combine(P.cbc, bs, ctx->stream);
+        launch_gemm_f64(P.g3c, bs, ctx->stream);
+        ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
+        env->matvecs++;
+        env->heff_flops += P.flops;
+        env->gemm_flops += P.g1c.flops + P.g3c.flops;
+        env->gemm_launches += (P.g1c.tiles.empty() ? 0 : 1) + (P.g3c.tiles.empty() ? 0 : 1);
+        return;
+    }
     if (ctx->prec == TN_PREC_SPLIT) {
         if (!P.s1) P.s1 = make_split(P.g1, ctx->slices, true, false, ctx->stream);
         if (!P.s3) P.s3 = make_split(P.g3, ctx->slices, false, true, ctx->stream);
@@ -870,7 +965,7 @@ void heff1_apply(tn_env* env, Heff1Plan& P, const double* x, double* y) {
 
 // copy a site tensor between the left-grouped and right-grouped layouts (block copies)
 void regroup(tn_ctx* ctx, const SiteLayout& src, const double* sp, const SiteLayout& dst,
-             double* dp, const Link& lk, const Link& rk) {
+             double* dp, const Link& lk, const Link& rk, int planes = 1) {
     CombPlan cb;
     const int d = src.d;
     for (int b = 0; b < src.nblk(); ++b)
@@ -910,10 +1005,12 @@ void regroup(tn_ctx* ctx, const SiteLayout& src, const double* sp, const SiteLay
             cb.outs.push_back(o);
         }
     cb.finalize(ctx->stream);
-    Bases bs{};
-    bs.p[S_X] = const_cast<double*>(sp);
-    bs.p[S_Y] = dp;
-    launch_combine(cb, bs, ctx->stream);
+    for (int pl = 0; pl < planes; ++pl) {  // the same block copies on each plane
+        Bases bs{};
+        bs.p[S_X] = const_cast<double*>(sp) + pl * src.size;
+        bs.p[S_Y] = dp + pl * dst.size;
+        launch_combine(cb, bs, ctx->stream);
+    }
 }
 
 // phi = site p * site p+1 in the phi layout
@@ -964,11 +1061,20 @@ void form_phi(tn_env* env, int p, const PhiLayout& ph, double* out) {
             throw Error(TN_E_INVALID, "two-site tensor needs the orthogonality center on the bond");
         }
     }
-    g.finalize(env->ctx->stream);
     Bases bs{};
     bs.p[S_A] = X.buf.d();
     bs.p[S_B] = Y.buf.d();
     bs.p[S_Y] = out;
+    if (psi->cplx) {
+        set_im(bs, S_A, X.lay.size);
+        set_im(bs, S_B, Y.lay.size);
+        set_im(bs, S_Y, ph.size);
+        GemmPlan c = complex_plan(g, 0);
+        c.finalize(env->ctx->stream);
+        launch_gemm_f64(c, bs, env->ctx->stream);
+        return;
+    }
+    g.finalize(env->ctx->stream);
     launch_gemm_f64(g, bs, env->ctx->stream);
 }
 
@@ -1109,22 +1215,30 @@ EigOut lanczos_lowest(tn_env* env, MV&& apply, int64_t n, double* x0, double* re
 }
 
 // -------------------------------------------------------------------------------------
-// Krylov exponentiation exp(t H_eff) x (KrylovKit exponentiate semantics restated): eager
-// Lanczos with full re-orthogonalisation; after each expansion y = exp(dt T) e1 and the
-// step is accepted when |dt| * beta * |y[K-1]| <= tol (or beta <= tol, or the space is
-// exhausted); a full Krylov space that misses the tolerance takes the largest dt / 2^j
-// that meets it and restarts from the evolved vector for the remaining time.
+// Krylov exponentiation exp(tau H_eff) x, tau = t + i ti (KrylovKit exponentiate semantics
+// restated): eager Lanczos with full re-orthogonalisation; after each expansion
+// y = exp(dt T) e1 and the step is accepted when |dt| * beta * |y[K-1]| <= tol (or
+// beta <= tol, or the space is exhausted); a full Krylov space that misses the tolerance
+// takes the largest dt = tau f / 2^j that meets it and restarts from the evolved vector for
+// the remaining time.
+//
+// Complex vectors are planar (n = 2 nc reals: real parts, then imaginary parts).  For a
+// Hermitian H_eff the Lanczos coefficients of the complex iteration are real and its basis
+// vectors are those of the real iteration on the planar vectors (whose inner product is the
+// real part of the complex one), so the same real kernels build T; only the final
+// combination takes the complex y: x = sum_j Re(y_j) v_j + i sum_j Im(y_j) v_j.
 // -------------------------------------------------------------------------------------
 template <class MV>
 int krylov_exp(tn_env* env, MV&& apply, int64_t n, double t, const double* x0, double* out,
-               const tn_update_params* prm) {
+               const tn_update_params* prm, double ti = 0.0, int64_t nc = 0) {
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
+    TN_REQUIRE(ti == 0.0 || 2 * nc == n, "internal: a complex time step needs complex vectors");
     const int kd = prm->krylovdim;
     const int nvec = kd + 2;  // basis + residual + current vector
     env->kry.alloc(size_t(nvec) * size_t(std::max<int64_t>(n, 1)) * 8, st);
     env->part.alloc(size_t(32) * blas_nparts() * 8, st);
-    env->dots.alloc(128 * 8, st);
+    env->dots.alloc(256 * 8, st);
     if (!env->ticket.p) {
         env->ticket.alloc(sizeof(unsigned), st);
         TN_CUDA(cudaMemsetAsync(env->ticket.p, 0, sizeof(unsigned), st));
@@ -1140,7 +1254,12 @@ int krylov_exp(tn_env* env, MV&& apply, int64_t n, double t, const double* x0, d
     TN_CUDA(cudaMemcpyAsync(cur, x0, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
     std::vector<double> hostd(65);
     int matvecs = 0;
-    double remaining = t;
+    double rem = 1.0;  // fraction of tau still to go
+    const double tabs = std::hypot(t, ti);
+    if (ti != 0.0) {
+        const double one = 1.0;
+        TN_CUDA(cudaMemcpyAsync(dv + 224, &one, 8, cudaMemcpyHostToDevice, st));
+    }
     auto norm2 = [&](double* v) {
         const double* vp = v;
         launch_gs_pass(&vp, 0, v, nullptr, 0.0, n, false, true, env->part.d(), dv + 64, tk, st);
@@ -1149,7 +1268,7 @@ int krylov_exp(tn_env* env, MV&& apply, int64_t n, double t, const double* x0, d
         sync(ctx);
         return r;
     };
-    for (int it = 0; it < prm->maxiter && remaining != 0.0; ++it) {
+    for (int it = 0; it < prm->maxiter && rem != 0.0; ++it) {
         const double nrm = std::sqrt(std::max(norm2(cur), 0.0));
         if (nrm == 0.0) break;
         std::vector<double*> V;
@@ -1175,39 +1294,57 @@ int krylov_exp(tn_env* env, MV&& apply, int64_t n, double t, const double* x0, d
         matvecs++;
         gs(1, h, beta);
         Hat(0, 0) = h[0];
-        double dt = remaining;
+        double f = rem;  // this step: tau f
         while (true) {
             const int K = (int)V.size();
             std::vector<double> A(size_t(K) * K);
             for (int i = 0; i < K; ++i)
                 for (int j = 0; j < K; ++j) A[size_t(i) * K + j] = 0.5 * (Hat(i, j) + Hat(j, i));
             sym_eig(K, A, D, U);
-            auto expv = [&](double tau, std::vector<double>& y) {
-                y.assign(K, 0.0);
+            // y = exp(tau f T) e1 = U exp(tau f D) U^T e1, real and imaginary parts
+            auto expv = [&](double fr, std::vector<double>& yr, std::vector<double>& yi) {
+                yr.assign(K, 0.0);
+                yi.assign(K, 0.0);
                 for (int j = 0; j < K; ++j) {
-                    const double c = std::exp(tau * D[j]) * U[size_t(0) * K + j];
-                    for (int i = 0; i < K; ++i) y[i] += U[size_t(i) * K + j] * c;
+                    const double m = std::exp(fr * t * D[j]) * U[size_t(0) * K + j];
+                    const double ph = fr * ti * D[j];
+                    const double cr = ph == 0.0 ? m : m * std::cos(ph);
+                    const double ci = ph == 0.0 ? 0.0 : m * std::sin(ph);
+                    for (int i = 0; i < K; ++i) {
+                        yr[i] += U[size_t(i) * K + j] * cr;
+                        yi[i] += U[size_t(i) * K + j] * ci;
+                    }
                 }
             };
-            std::vector<double> y;
-            expv(dt, y);
-            double err = std::fabs(dt) * beta * std::fabs(y[K - 1]);
-            const bool exhausted = int64_t(K) >= n;
+            std::vector<double> yr, yi;
+            expv(f, yr, yi);
+            double err = f * tabs * beta * std::hypot(yr[K - 1], yi[K - 1]);
+            const bool exhausted = int64_t(K) >= (nc > 0 ? nc : n);  // the complex dimension
             bool accept = err <= prm->tol || beta <= prm->tol || exhausted;
             if (!accept && K == kd) {
-                while (err > prm->tol && std::fabs(dt) > 1e-300) {
-                    dt *= 0.5;
-                    expv(dt, y);
-                    err = std::fabs(dt) * beta * std::fabs(y[K - 1]);
+                while (err > prm->tol && f * tabs > 1e-300) {
+                    f *= 0.5;
+                    expv(f, yr, yi);
+                    err = f * tabs * beta * std::hypot(yr[K - 1], yi[K - 1]);
                 }
                 accept = true;
             }
             if (accept) {
-                for (double& c : y) c *= nrm;
-                TN_CUDA(cudaMemcpyAsync(dv + 96, y.data(), K * 8, cudaMemcpyHostToDevice, st));
+                for (double& c : yr) c *= nrm;
+                TN_CUDA(cudaMemcpyAsync(dv + 96, yr.data(), K * 8, cudaMemcpyHostToDevice, st));
                 launch_lincomb(cur, V.data(), K, dv + 96, n, st);
+                if (ti != 0.0) {
+                    // cur += i (sum_j Im(y_j) v_j), through the residual buffer
+                    for (double& c : yi) c *= nrm;
+                    TN_CUDA(cudaMemcpyAsync(dv + 160, yi.data(), K * 8, cudaMemcpyHostToDevice, st));
+                    launch_lincomb(w, V.data(), K, dv + 160, n, st);
+                    const double* wim = w + nc;
+                    const double* wre = w;
+                    launch_multi_axpy(cur, &wim, 1, dv + 224, -1.0, nc, st);
+                    launch_multi_axpy(cur + nc, &wre, 1, dv + 224, 1.0, nc, st);
+                }
                 sync(ctx);
-                remaining -= dt;
+                rem -= f;
                 break;
             }
             double* v = pool[K];
@@ -1511,6 +1648,199 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
     launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(),
                        env->svdV.d(), env->svdS.d(), env->svdPerm.as<int>(), left.buf.d(),
                        right.buf.d(), ortho, inv, st);
+    ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    psi->sites[p] = std::move(left);
+    psi->sites[p + 1] = std::move(right);
+    psi->links[p + 1] = nl;
+    psi->center = (ortho == TN_ORTHO_LEFT) ? p + 1 : p;
+    env->lpos = std::min(env->lpos, p);
+    env->rpos = std::max(env->rpos, p + 1);
+    env->hp_pos = -1;
+    res->truncerr = D.truncerr;
+    res->newdim = nl.total();
+    eigs = D.eigs;
+}
+
+// replacebond! of a complex two-site tensor (planar phi, ITensors' complex svd +
+// truncate!): each complex block A = Ar + i Ai is factorised through the real SVD of
+// [[Ar, -Ai], [Ai, Ar]] (2 rows x 2 cols), whose singular values are those of A, each twice;
+// the columns of one pair span a complex singular vector [re; im] and i times it, so the
+// first column of each pair is taken.  Within a cluster of (nearly) equal complex values the
+// taken columns are made complex-orthonormal on the host (the same combinations applied to
+// the partner factor), which keeps A v = s u.
+void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double* phi,
+                          const tn_update_params* prm, int ortho, tn_update_result* res,
+                          std::vector<double>& eigs) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    tn_mps* psi = env->psi.get();
+    const int nb = ph.nblk();
+    std::vector<int> rows2(nb), cols2(nb);
+    std::vector<int64_t> off2(nb);
+    int64_t tot = 0;
+    CombPlan rb;
+    auto quad = [&](int64_t doff, int ldd, int r, int c, int sbuf, int64_t soff, double coef) {
+        CombOut o{};
+        o.doff = doff;
+        o.dbuf = S_Y;
+        o.ldd = ldd;
+        o.rows = r;
+        o.cols = c;
+        o.t0 = int(rb.terms.size());
+        o.nt = 1;
+        rb.terms.push_back(CombTerm{soff, sbuf, r, coef});
+        rb.outs.push_back(o);
+    };
+    for (int b = 0; b < nb; ++b) {
+        const int r = ph.rows[b], c = ph.cols[b];
+        rows2[b] = 2 * r;
+        cols2[b] = 2 * c;
+        off2[b] = tot;
+        quad(tot, 2 * r, r, c, S_X, ph.off[b], 1.0);
+        quad(tot + r, 2 * r, r, c, S_X + S_IM, ph.off[b], 1.0);
+        quad(tot + int64_t(c) * 2 * r, 2 * r, r, c, S_X + S_IM, ph.off[b], -1.0);
+        quad(tot + r + int64_t(c) * 2 * r, 2 * r, r, c, S_X, ph.off[b], 1.0);
+        tot += int64_t(4) * r * c;
+    }
+    env->cx.alloc(size_t(std::max<int64_t>(tot, 1)) * 8, st);
+    rb.finalize(st);
+    {
+        Bases bs{};
+        bs.p[S_X] = const_cast<double*>(phi);
+        set_im(bs, S_X, ph.size);
+        bs.p[S_Y] = env->cx.d();
+        launch_combine(rb, bs, st);
+    }
+    SvdResult R;
+    block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm,
+              env->desc, rows2, cols2, off2, env->cx.d(), R);
+    // the complex values: the first of each realified pair
+    SvdResult C;
+    C.desc = R.desc;
+    for (int b = 0; b < nb; ++b) {
+        C.desc[b].n = R.desc[b].n / 2;
+        C.desc[b].s_off = int64_t(C.S.size());
+        for (int j = 0; j < C.desc[b].n; ++j) C.S.push_back(R.S[size_t(R.desc[b].s_off + 2 * j)]);
+    }
+    C.total_n = int64_t(C.S.size());
+    TruncDecision D = decide(C, prm->maxdim, prm->mindim, prm->cutoff);
+    // clusters of kept values closer than 1e-8 of the block's largest: complex Gram-Schmidt
+    std::vector<int> perm;
+    for (int b = 0; b < nb; ++b) {
+        const int k = D.kept[b];
+        if (k < 2) continue;
+        const double* sb = &C.S[size_t(C.desc[b].s_off)];
+        for (int j0 = 0; j0 < k;) {
+            int j1 = j0;
+            while (j1 + 1 < k && sb[j1] - sb[j1 + 1] <= 1e-8 * sb[0]) ++j1;
+            if (j1 > j0) {
+                if (perm.empty()) {
+                    perm.resize(size_t(R.total_n));
+                    TN_CUDA(cudaMemcpyAsync(perm.data(), env->svdPerm.p, perm.size() * 4,
+                                            cudaMemcpyDeviceToHost, st));
+                    sync(ctx);
+                }
+                const SvdBlockDesc& d = R.desc[b];
+                const int mq = d.m, np = d.n;  // lengths of the QV and PY columns
+                const int hq = mq / 2, hp = np / 2;
+                const int cnt = j1 - j0 + 1;
+                std::vector<std::vector<double>> q, y;  // candidate columns
+                for (int c = 2 * j0; c <= 2 * j1 + 1; ++c) {
+                    const int pc = perm[size_t(d.s_off + c)];
+                    std::vector<double> a(static_cast<size_t>(mq)), bcol(static_cast<size_t>(np));
+                    TN_CUDA(cudaMemcpyAsync(a.data(), env->svdW.d() + d.x_off + int64_t(pc) * mq,
+                                            size_t(mq) * 8, cudaMemcpyDeviceToHost, st));
+                    TN_CUDA(cudaMemcpyAsync(bcol.data(), env->svdV.d() + d.v_off + int64_t(pc) * np,
+                                            size_t(np) * 8, cudaMemcpyDeviceToHost, st));
+                    q.push_back(std::move(a));
+                    y.push_back(std::move(bcol));
+                }
+                sync(ctx);
+                std::vector<std::vector<double>> qa, ya;  // accepted (complex-orthonormal)
+                for (size_t c = 0; c < q.size() && int(qa.size()) < cnt; ++c) {
+                    std::vector<double> x = q[c], z = y[c];
+                    for (int pass = 0; pass < 2; ++pass)
+                        for (size_t a = 0; a < qa.size(); ++a) {
+                            // h = <qa, x> (complex), x -= h qa, z -= h ya
+                            double hr = 0, hi = 0;
+                            for (int i = 0; i < hq; ++i) {
+                                hr += qa[a][i] * x[i] + qa[a][hq + i] * x[hq + i];
+                                hi += qa[a][i] * x[hq + i] - qa[a][hq + i] * x[i];
+                            }
+                            for (int i = 0; i < hq; ++i) {
+                                const double ar = qa[a][i], ai = qa[a][hq + i];
+                                x[i] -= hr * ar - hi * ai;
+                                x[hq + i] -= hr * ai + hi * ar;
+                            }
+                            for (int i = 0; i < hp; ++i) {
+                                const double ar = ya[a][i], ai = ya[a][hp + i];
+                                z[i] -= hr * ar - hi * ai;
+                                z[hp + i] -= hr * ai + hi * ar;
+                            }
+                        }
+                    double nx = 0;
+                    for (double v : x) nx += v * v;
+                    nx = std::sqrt(nx);
+                    if (nx < 0.5) continue;  // (nearly) i times an accepted vector
+                    for (double& v : x) v /= nx;
+                    for (double& v : z) v /= nx;
+                    qa.push_back(std::move(x));
+                    ya.push_back(std::move(z));
+                }
+                TN_REQUIRE(int(qa.size()) == cnt, "complex SVD: degenerate cluster not resolved");
+                for (int a = 0; a < cnt; ++a) {
+                    const int pc = perm[size_t(d.s_off + 2 * (j0 + a))];
+                    TN_CUDA(cudaMemcpyAsync(env->svdW.d() + d.x_off + int64_t(pc) * mq, qa[a].data(),
+                                            size_t(mq) * 8, cudaMemcpyHostToDevice, st));
+                    TN_CUDA(cudaMemcpyAsync(env->svdV.d() + d.v_off + int64_t(pc) * np, ya[a].data(),
+                                            size_t(np) * 8, cudaMemcpyHostToDevice, st));
+                }
+                sync(ctx);  // host columns go out of scope
+            }
+            j0 = j1 + 1;
+        }
+    }
+    Link nl;
+    for (int b = 0; b < nb; ++b)
+        if (D.kept[b] > 0) {
+            nl.q.push_back(ph.m[b]);
+            nl.dim.push_back(D.kept[b]);
+        }
+    const Link& lk = psi->links[p];
+    const Link& rk = psi->links[p + 2];
+    tn_site left, right;
+    left.lay = make_site_layout(LG, lk, nl, psi->pq);
+    right.lay = make_site_layout(RG, nl, rk, psi->pq);
+    left.buf.alloc(size_t(std::max<int64_t>(left.lay.size, 1)) * 16, st);
+    right.buf.alloc(size_t(std::max<int64_t>(right.lay.size, 1)) * 16, st);
+    std::vector<ExtractDesc> ed;
+    for (int b = 0, j = 0; b < nb; ++b) {
+        if (D.kept[b] == 0) continue;
+        TN_REQUIRE(left.lay.rows[j] == ph.rows[b] && right.lay.cols[j] == ph.cols[b],
+                   "internal: SVD block layout mismatch");
+        ExtractDesc e{};
+        e.x_off = R.desc[b].x_off;
+        e.v_off = R.desc[b].v_off;
+        e.s_off = R.desc[b].s_off;
+        e.left_off = left.lay.off[j];
+        e.right_off = right.lay.off[j];
+        e.rows = ph.rows[b];
+        e.cols = ph.cols[b];
+        e.n = R.desc[b].n;
+        e.trans = R.desc[b].trans;
+        e.k = D.kept[b];
+        ed.push_back(e);
+        ++j;
+    }
+    env->desc2.alloc(std::max<size_t>(ed.size() * sizeof(ExtractDesc), 16), st);
+    if (!ed.empty())
+        TN_CUDA(cudaMemcpyAsync(env->desc2.p, ed.data(), ed.size() * sizeof(ExtractDesc),
+                                cudaMemcpyHostToDevice, st));
+    const double inv = (prm->normalize && D.norm > 0) ? 1.0 / D.norm : 1.0;
+    const int e0 = ctx->timer.mark();
+    launch_svd_extract_complex(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(),
+                               env->svdV.d(), env->svdS.d(), env->svdPerm.as<int>(), left.buf.d(),
+                               left.lay.size, right.buf.d(), right.lay.size, ortho, inv, st);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
     psi->sites[p] = std::move(left);
     psi->sites[p + 1] = std::move(right);
@@ -1842,9 +2172,12 @@ bool halfsweep_done2(int N, int pos, int ortho) {
 // eigensolver; otherwise the exponential solver with the reverse one-site step.
 void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
                      tn_update_result* res, std::vector<double>& eigs,
-                     const double* time_step = nullptr) {
+                     const double* time_step = nullptr, double time_im = 0.0) {
     check_params(prm);
     tn_mps* psi = env->psi.get();
+    TN_REQUIRE(!psi->cplx || time_step,
+               "complex states are evolved by tdvpsweep; the eigensolver takes real states");
+    TN_REQUIRE(time_im == 0.0 || psi->cplx, "internal: a complex time step needs a complex state");
     TN_REQUIRE(p >= 0 && p < psi->N - 1, "bond position out of range");
     TN_REQUIRE((ortho == TN_ORTHO_LEFT && psi->center == p) ||
                    (ortho == TN_ORTHO_RIGHT && psi->center == p + 1),
@@ -1853,7 +2186,8 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     cudaStream_t st = ctx->stream;
     position(env, p, 2);
     Heff2Plan& P = heff_plan(env);
-    const int64_t n = P.ph.size;
+    const int64_t nph = P.ph.size;                 // complex dimension
+    const int64_t n = nph * psi->planes();         // reals of one (planar) vector
     env->vecA.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     env->vecB.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
     form_phi(env, p, P.ph, env->vecA.d());
@@ -1874,7 +2208,8 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         res->converged = eo.converged;
     } else {
         const int64_t mv0 = env->matvecs;
-        krylov_exp(env, apply2, n, *time_step, env->vecA.d(), env->vecB.d(), prm);
+        krylov_exp(env, apply2, n, *time_step, env->vecA.d(), env->vecB.d(), prm, time_im,
+                   psi->cplx ? nph : 0);
         res->energy = normalize_and_energy(env, apply2, n, env->vecB.d(), env->vecA.d(),
                                            prm->normalize != 0);
         res->matvecs = int32_t(env->matvecs - mv0);
@@ -1884,6 +2219,8 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
                "`updatePosition()` :: `noise` cannot be greater than zero for `reverse_step=true` !!");
     if (std::fabs(prm->noise) > 1e-15)  // Float64_threshold(), src/mps/update_site.jl:60
         replace_bond_noise(env, p, P, env->vecB.d(), prm, ortho, res, eigs);
+    else if (psi->cplx)
+        replace_bond_complex(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
     else
         replace_bond(env, p, P.ph, env->vecB.d(), prm, ortho, res, eigs);
     res->neigs = (int)eigs.size();
@@ -1892,7 +2229,8 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         const int p1 = (ortho == TN_ORTHO_LEFT) ? p + 1 : p;
         position(env, p1, 1);
         Heff1Plan& P1 = heff1_plan(env);
-        const int64_t n1 = P1.lay.size;
+        const int np = psi->planes();
+        const int64_t n1c = P1.lay.size, n1 = n1c * np;
         env->vecC.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
         env->vecD.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
         tn_site& site = psi->sites[p1];
@@ -1902,11 +2240,12 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
             TN_CUDA(cudaMemcpyAsync(env->vecC.p, site.buf.p, size_t(n1) * 8,
                                     cudaMemcpyDeviceToDevice, st));
         else
-            regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk);
+            regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk, np);
         auto apply1 = [&](const double* x, double* y) { heff1_apply(env, P1, x, y); };
         const double back = -*time_step;
         const int64_t mv0 = env->matvecs;
-        krylov_exp(env, apply1, n1, back, env->vecC.d(), env->vecD.d(), prm);
+        krylov_exp(env, apply1, n1, back, env->vecC.d(), env->vecD.d(), prm, -time_im,
+                   psi->cplx ? n1c : 0);
         res->energy = normalize_and_energy(env, apply1, n1, env->vecD.d(), env->vecC.d(),
                                            prm->normalize != 0);
         res->matvecs += int32_t(env->matvecs - mv0);
@@ -1914,7 +2253,7 @@ void update_two_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
             TN_CUDA(cudaMemcpyAsync(site.buf.p, env->vecD.p, size_t(n1) * 8,
                                     cudaMemcpyDeviceToDevice, st));
         else
-            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk);
+            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk, np);
         env->lpos = std::min(env->lpos, p1);
         env->rpos = std::max(env->rpos, p1);
         env->hp_pos = -1;
@@ -1937,6 +2276,7 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     check_params(prm);
     tn_mps* psi = env->psi.get();
     const int N = psi->N;
+    TN_REQUIRE(!psi->cplx, "one-site updates of complex states are not built");
     TN_REQUIRE(p >= 0 && p < N, "site position out of range");
     TN_REQUIRE(psi->center == p, "one-site update: the orthogonality center must be at pos");
     tn_ctx* ctx = env->ctx;
@@ -2151,15 +2491,53 @@ std::unique_ptr<tn_mps> copy_mps(const tn_mps* src) {
     m->pq = src->pq;
     m->links = src->links;
     m->center = src->center;
+    m->cplx = src->cplx;
     m->sites.resize(src->N);
     for (int i = 0; i < src->N; ++i) {
         m->sites[i].lay = src->sites[i].lay;
-        const size_t nb = size_t(std::max<int64_t>(src->sites[i].lay.size, 1)) * 8;
+        const size_t nb = size_t(std::max<int64_t>(src->sites[i].lay.size, 1)) * 8 * src->planes();
         m->sites[i].buf.alloc(nb, src->ctx->stream);
         TN_CUDA(cudaMemcpyAsync(m->sites[i].buf.p, src->sites[i].buf.p, nb,
                                 cudaMemcpyDeviceToDevice, src->ctx->stream));
     }
     return m;
+}
+
+// a complex copy of every site tensor in place (imaginary planes zero)
+void mps_to_complex(tn_mps* m) {
+    if (m->cplx) return;
+    cudaStream_t st = m->ctx->stream;
+    for (auto& S : m->sites) {
+        const int64_t n = S.lay.size;
+        DevBuf b;
+        b.alloc(size_t(std::max<int64_t>(n, 1)) * 16, st);
+        if (n) TN_CUDA(cudaMemcpyAsync(b.p, S.buf.p, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
+        TN_CUDA(cudaMemsetAsync(b.d() + n, 0, size_t(std::max<int64_t>(n, 1)) * 8, st));
+        S.buf = std::move(b);
+    }
+    m->cplx = true;
+}
+
+// a real environment made complex: the state and every environment tensor it holds
+void env_to_complex(tn_env* e) {
+    if (e->psi->cplx) return;
+    TN_REQUIRE(e->proj.empty(), "complex states with excited-state projectors are not built");
+    cudaStream_t st = e->ctx->stream;
+    mps_to_complex(e->psi.get());
+    for (auto* side : {&e->L, &e->R})
+        for (auto& E : *side) {
+            if (!E.buf.p) continue;
+            const int64_t n = E.lay.size;
+            DevBuf b;
+            b.alloc(size_t(std::max<int64_t>(n, 1)) * 16, st);
+            if (n) TN_CUDA(cudaMemcpyAsync(b.p, E.buf.p, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
+            TN_CUDA(cudaMemsetAsync(b.d() + n, 0, size_t(std::max<int64_t>(n, 1)) * 8, st));
+            E.buf = std::move(b);
+        }
+    e->hp.reset();
+    e->h1p.reset();
+    e->hp_pos = e->h1p_pos = -1;
+    TN_CUDA(cudaStreamSynchronize(st));
 }
 
 // dense (Dl, d, Dr) column-major <-> site blocks
@@ -2506,6 +2884,47 @@ int tn_mps_create(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q, const i
     });
 }
 
+int tn_mps_create_complex(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
+                          const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
+                          const double* site_data, int center, tn_mps** out) {
+    return guarded([&] {
+        TN_REQUIRE(ctx && out && nsec && sec_dim && site_data, "null argument");
+        // total dense length from the link dimensions
+        std::vector<int64_t> tot(size_t(nsites) + 1, 0);
+        size_t so = 0;
+        for (int i = 0; i <= nsites; ++i) {
+            for (int k = 0; k < nsec[i]; ++k) tot[size_t(i)] += sec_dim[so + k];
+            so += nsec[i];
+        }
+        int64_t len = 0;
+        for (int i = 0; i < nsites; ++i) len += tot[size_t(i)] * d * tot[size_t(i) + 1];
+        std::vector<double> re(static_cast<size_t>(len)), im(static_cast<size_t>(len));
+        for (int64_t e = 0; e < len; ++e) {
+            re[size_t(e)] = site_data[2 * e];
+            im[size_t(e)] = site_data[2 * e + 1];
+        }
+        tn_mps* m = nullptr;
+        const int rc = tn_mps_create(ctx, nsites, d, phys_q, nsec, sec_q, sec_dim, re.data(),
+                                     center, &m);
+        if (rc != TN_OK) throw Error(rc, g_err);
+        std::unique_ptr<tn_mps> hold(m);
+        mps_to_complex(m);
+        size_t off = 0;
+        std::vector<double> blocks;
+        for (int i = 0; i < nsites; ++i) {
+            const Link& lk = m->links[i];
+            const Link& rk = m->links[i + 1];
+            site_from_dense(m->sites[i].lay, lk, rk, d, im.data() + off, blocks);
+            off += size_t(lk.total()) * d * rk.total();
+            if (!blocks.empty())
+                TN_CUDA(cudaMemcpyAsync(m->sites[i].buf.d() + m->sites[i].lay.size, blocks.data(),
+                                        blocks.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+            sync(ctx);
+        }
+        *out = hold.release();
+    });
+}
+
 int tn_mps_create_blocks(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
                          const int32_t* nsec, const int32_t* sec_q, const int32_t* sec_dim,
                          const double* block_data, const int64_t* site_len, int center,
@@ -2569,6 +2988,7 @@ int tn_mps_create_blocks(tn_ctx* ctx, int nsites, int d, const int32_t* phys_q,
 int tn_mps_site_blocks(const tn_mps* mps, int site, double* out, int64_t cap, int64_t* len) {
     return guarded([&] {
         TN_REQUIRE(mps && len, "null argument");
+        TN_REQUIRE(!mps->cplx, "block download of complex states is not built");
         TN_REQUIRE(site >= 0 && site < mps->N, "site out of range");
         const tn_site& S = mps->sites[site];
         *len = S.lay.size;
@@ -2616,6 +3036,7 @@ int tn_mps_link(const tn_mps* mps, int link, int32_t* nsec, int32_t* q, int32_t*
 int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap) {
     return guarded([&] {
         TN_REQUIRE(mps && out, "null argument");
+        TN_REQUIRE(!mps->cplx, "complex state: read its sites with tn_mps_site_complex");
         TN_REQUIRE(site >= 0 && site < mps->N, "site out of range");
         const Link& lk = mps->links[site];
         const Link& rk = mps->links[site + 1];
@@ -2627,6 +3048,45 @@ int tn_mps_site(const tn_mps* mps, int site, double* out, int64_t cap) {
                                     cudaMemcpyDeviceToHost, mps->ctx->stream));
         TN_CUDA(cudaStreamSynchronize(mps->ctx->stream));
         site_to_dense(S.lay, lk, rk, mps->d, blocks, out);
+    });
+}
+
+int tn_mps_is_complex(const tn_mps* mps) { return mps ? (mps->cplx ? 1 : 0) : TN_E_INVALID; }
+
+int tn_mps_make_complex(tn_mps* mps) {
+    return guarded([&] {
+        TN_REQUIRE(mps, "null argument");
+        mps_to_complex(mps);
+        sync(mps->ctx);
+    });
+}
+
+int tn_mps_site_complex(const tn_mps* mps, int site, double* out, int64_t cap) {
+    return guarded([&] {
+        TN_REQUIRE(mps && out, "null argument");
+        TN_REQUIRE(site >= 0 && site < mps->N, "site out of range");
+        const Link& lk = mps->links[site];
+        const Link& rk = mps->links[site + 1];
+        const int64_t nd = int64_t(lk.total()) * mps->d * rk.total();
+        TN_REQUIRE(cap >= 2 * nd, "capacity too small");
+        const tn_site& S = mps->sites[site];
+        const int64_t n = S.lay.size;
+        std::vector<double> blocks(size_t(n) * mps->planes());
+        if (!blocks.empty())
+            TN_CUDA(cudaMemcpyAsync(blocks.data(), S.buf.p, blocks.size() * 8,
+                                    cudaMemcpyDeviceToHost, mps->ctx->stream));
+        TN_CUDA(cudaStreamSynchronize(mps->ctx->stream));
+        std::vector<double> re(static_cast<size_t>(nd)), im(static_cast<size_t>(nd), 0.0);
+        std::vector<double> part(blocks.begin(), blocks.begin() + n);
+        site_to_dense(S.lay, lk, rk, mps->d, part, re.data());
+        if (mps->cplx) {
+            part.assign(blocks.begin() + n, blocks.end());
+            site_to_dense(S.lay, lk, rk, mps->d, part, im.data());
+        }
+        for (int64_t e = 0; e < nd; ++e) {
+            out[2 * e] = re[size_t(e)];
+            out[2 * e + 1] = im[size_t(e)];
+        }
     });
 }
 
@@ -2644,8 +3104,8 @@ int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out) {
         const int N = psi->N;
         e->L.resize(N);
         e->R.resize(N);
-        make_trivial_env(e->ctx, e->L[0], psi->links[0], H->delta[0]);
-        make_trivial_env(e->ctx, e->R[N - 1], psi->links[N], H->delta[N]);
+        make_trivial_env(e->ctx, e->L[0], psi->links[0], H->delta[0], psi->planes());
+        make_trivial_env(e->ctx, e->R[N - 1], psi->links[N], H->delta[N], psi->planes());
         e->lpos = 0;
         e->rpos = N - 1;
         e->pos = 0;
@@ -2659,6 +3119,7 @@ int tn_env_set_projectors(tn_env* env, const tn_mps* const* Ms, int count, doubl
         TN_REQUIRE(env, "null argument");
         TN_REQUIRE(count >= 0 && count <= 32, "between 0 and 32 projector states");
         const tn_mps* psi = env->psi.get();
+        TN_REQUIRE(!psi->cplx || count == 0, "projectors on complex states are not built");
         if (count > 0) {
             TN_REQUIRE(Ms, "null argument");
             if (!(weight > 0.0)) {
@@ -2719,6 +3180,7 @@ int tn_env_environment(tn_env* env, int side, int i, double* out, int64_t cap,
         TN_REQUIRE(env && dims, "null argument");
         const tn_mps* psi = env->psi.get();
         const int N = psi->N;
+        TN_REQUIRE(!psi->cplx, "environment download of complex states is not built");
         TN_REQUIRE(i >= 0 && i < N, "environment index out of range");
         TN_REQUIRE(side == 0 ? i <= env->lpos : i >= env->rpos,
                    "environment is not built; call tn_env_position first");
@@ -2759,9 +3221,50 @@ int tn_env_product_flops(tn_env* env, double* flops) {
     });
 }
 
+int tn_env_product_complex(tn_env* env, const double* v, double* out, int64_t n) {
+    return guarded([&] {
+        TN_REQUIRE(env && v && out, "null argument");
+        TN_REQUIRE(env->psi->cplx, "a real state: use tn_env_product");
+        TN_REQUIRE(env->nsite == 2, "only nsite = 2 products are built");
+        const int p = env->pos;
+        position(env, p, 2);
+        Heff2Plan& P = heff_plan(env);
+        const tn_mps* psi = env->psi.get();
+        const Link& lk = psi->links[p];
+        const Link& rk = psi->links[p + 2];
+        const int64_t nd = int64_t(lk.total()) * psi->d * psi->d * rk.total();
+        TN_REQUIRE(n == nd, "dense two-site tensor has the wrong size");
+        std::vector<int64_t> map;
+        phi_dense_map(P.ph, lk, rk, psi->d, map);
+        const int64_t nb = P.ph.size;
+        std::vector<double> hb(size_t(2 * nb));
+        for (int64_t i = 0; i < nb; ++i) {
+            hb[size_t(i)] = v[2 * map[size_t(i)]];
+            hb[size_t(nb + i)] = v[2 * map[size_t(i)] + 1];
+        }
+        cudaStream_t st = env->ctx->stream;
+        env->vecA.alloc(std::max<size_t>(hb.size(), 1) * 8, st);
+        env->vecB.alloc(std::max<size_t>(hb.size(), 1) * 8, st);
+        if (!hb.empty())
+            TN_CUDA(cudaMemcpyAsync(env->vecA.p, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
+        heff_apply(env, P, env->vecA.d(), env->vecB.d());
+        if (!hb.empty())
+            TN_CUDA(cudaMemcpyAsync(hb.data(), env->vecB.p, hb.size() * 8, cudaMemcpyDeviceToHost, st));
+        sync(env->ctx);
+        check_device_error(env->ctx);
+        env->ctx->timer.collect(env->acc_ms);
+        std::fill(out, out + 2 * nd, 0.0);
+        for (int64_t i = 0; i < nb; ++i) {
+            out[2 * map[size_t(i)]] = hb[size_t(i)];
+            out[2 * map[size_t(i)] + 1] = hb[size_t(nb + i)];
+        }
+    });
+}
+
 int tn_env_product(tn_env* env, const double* v, double* out, int64_t n) {
     return guarded([&] {
         TN_REQUIRE(env && v && out, "null argument");
+        TN_REQUIRE(!env->psi->cplx, "complex state: use tn_env_product_complex");
         TN_REQUIRE(env->nsite == 2, "only nsite = 2 products are built");
         const int p = env->pos;
         position(env, p, 2);
@@ -2829,7 +3332,8 @@ namespace {
 // fullsweep! (TenNetLib src/mps/sweep.jl:94-196) with the eigensolver (time_step null) or
 // the exponential solver at time_step with reverse steps (tdvpsweep!, src/mps/tdvp.jl:268)
 void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
-                int mid_cap, int32_t* n_mid_eigs, const double* time_step, int nsite = 2) {
+                int mid_cap, int32_t* n_mid_eigs, const double* time_step, int nsite = 2,
+                double time_im = 0.0) {
     TN_REQUIRE(env && res, "null argument");
     check_params(p);
     tn_mps* psi = env->psi.get();
@@ -2853,13 +3357,13 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     if (nsite == 2) {
         for (int b = 0; b < N - 1; ++b) {
             tn_update_result r{};
-            update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step);
+            update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
         }
         for (int b = N - 2; b >= 0; --b) {
             tn_update_result r{};
-            update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step);
+            update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
             if (b == N / 2 - 1) mid = ev;
@@ -2938,6 +3442,25 @@ int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_swee
         TN_REQUIRE(std::isfinite(tau), "time step must be finite");
         const double half = 0.5 * tau;
         full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half);
+    });
+}
+
+int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn_update_params* p,
+                             tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                             int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(env, "null argument");
+        TN_REQUIRE(std::isfinite(tau_re) && std::isfinite(tau_im), "time step must be finite");
+        if (tau_im != 0.0) env_to_complex(env);
+        const double half = 0.5 * tau_re;
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half, 2, 0.5 * tau_im);
+    });
+}
+
+int tn_env_make_complex(tn_env* env) {
+    return guarded([&] {
+        TN_REQUIRE(env, "null argument");
+        env_to_complex(env);
     });
 }
 

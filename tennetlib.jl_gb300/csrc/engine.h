@@ -124,6 +124,8 @@ struct tn_site {
     tn::DevBuf buf;
 };
 
+// A complex MPS (cplx) keeps each site's blocks as two planes in one buffer: the real parts
+// (lay.size values), then the imaginary parts.
 struct tn_mps {
     tn_ctx* ctx = nullptr;
     int N = 0, d = 0;
@@ -131,6 +133,8 @@ struct tn_mps {
     std::vector<tn::Link> links;   // N+1
     std::vector<tn_site> sites;    // N
     int center = 0;
+    bool cplx = false;
+    int planes() const { return cplx ? 2 : 1; }
 };
 
 struct tn_envt {
@@ -142,6 +146,8 @@ struct tn_envt {
 struct Heff2Plan {
     tn::PhiLayout ph;
     tn::GemmPlan g1, g3;
+    tn::GemmPlan g1c, g3c;  // complex forms (complex states)
+    tn::CombPlan cbc;
     std::unique_ptr<tn::SplitPlan> s1, s3;  // split-precision plans (built on first use)
     tn::CombPlan cb;
     int64_t ysize = 0, zsize = 0;
@@ -157,6 +163,8 @@ struct Heff1Plan {
     tn::SiteLayout lay;
     tn::GemmPlan g1, g3;
     tn::CombPlan cb;
+    tn::GemmPlan g1c, g3c;  // complex forms (complex states)
+    tn::CombPlan cbc;
     std::unique_ptr<tn::SplitPlan> s1, s3;
     int64_t ysize = 0, zsize = 0;
     double flops = 0;
@@ -184,12 +192,12 @@ struct tn_env {
     tn_ctx* ctx = nullptr;
     std::unique_ptr<tn_mps> psi;
     const tn_mpo* H = nullptr;
-    std::vector<tn_envt> L, R;
+    std::vector<tn_envt> L, R;  // planar complex (two planes) when psi is complex
     int lpos = 0, rpos = 0;
     int pos = 0, nsite = 2;
     // work buffers
     tn::DevBuf t1, t2, kry, part, dots, ticket, svdX, svdW, svdV, svdP, svdS, svdPerm, desc, desc2,
-        vecA, vecB;
+        vecA, vecB, cx;  // cx: realified complex blocks
     std::unique_ptr<Heff2Plan> hp;
     int hp_pos = -1;
     std::unique_ptr<Heff1Plan> h1p;

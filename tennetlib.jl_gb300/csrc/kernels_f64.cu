@@ -44,7 +44,7 @@ gemm_f64_kernel(const Seg* __restrict__ segs, const Task* __restrict__ tasks,
                 double v = 0.0;
                 if (gi < tk.m && gk < sg.k)
                     v = sg.ta ? A[gk + int64_t(gi) * sg.lda] : A[gi + int64_t(gk) * sg.lda];
-                As[kk][i] = v;
+                As[kk][i] = sg.sgn < 0 ? -v : v;
             }
             for (int e = tid; e < GEMM_BN * BK; e += 256) {
                 int j, kk;

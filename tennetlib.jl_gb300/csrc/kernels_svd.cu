@@ -573,7 +573,88 @@ __global__ void svd_extract_kernel(const ExtractDesc* __restrict__ desc,
     }
 }
 
+// rows, cols: the complex block; QV / PY hold the realified block's factors (m = 2 rows or
+// 2 cols after orientation, n = the realified n)
+__global__ void svd_extract_complex_kernel(const ExtractDesc* __restrict__ desc,
+                                           const double* __restrict__ QV,
+                                           const double* __restrict__ PY,
+                                           const double* __restrict__ S,
+                                           const int* __restrict__ perm, double* __restrict__ left,
+                                           int64_t lplane, double* __restrict__ right,
+                                           int64_t rplane, int ortho, double inv_norm) {
+    const ExtractDesc d = desc[blockIdx.x];
+    const int rows = d.rows, cols = d.cols, n = d.n, k = d.k;
+    const double* qv = QV + d.x_off;
+    const double* py = PY + d.v_off;
+    const int m = d.trans ? 2 * cols : 2 * rows;
+    const double* s = S + d.s_off;
+    const int* pm = perm + d.s_off;
+    double* Lr = left + d.left_off;
+    double* Li = Lr + lplane;
+    double* Rr = right + d.right_off;
+    double* Ri = Rr + rplane;
+    const int64_t nl = int64_t(rows) * k;
+    for (int64_t e = threadIdx.x; e < nl; e += blockDim.x) {
+        const int i = int(e % rows), c = int(e / rows);
+        const int pc = pm[2 * c];
+        const double sg = s[2 * c];
+        double ur, ui;
+        if (!d.trans) {  // U column
+            const double a = qv[i + int64_t(pc) * m], b = qv[rows + i + int64_t(pc) * m];
+            const double f = (ortho == 0) ? 1.0 : sg * inv_norm;
+            ur = a * f;
+            ui = b * f;
+        } else {         // U S column
+            const double a = py[i + int64_t(pc) * n], b = py[rows + i + int64_t(pc) * n];
+            if (ortho == 0) {
+                ur = a / sg;
+                ui = b / sg;
+            } else {
+                ur = a * inv_norm;
+                ui = b * inv_norm;
+            }
+        }
+        Lr[e] = ur;
+        Li[e] = ui;
+    }
+    const int64_t nr = int64_t(k) * cols;
+    for (int64_t e = threadIdx.x; e < nr; e += blockDim.x) {
+        const int c = int(e % k), j = int(e / k);
+        const int pc = pm[2 * c];
+        const double sg = s[2 * c];
+        double vr, vi;  // the entry of S V^H (ortho 0) or V^H (ortho 1)
+        if (!d.trans) {  // V S column
+            const double a = py[j + int64_t(pc) * n], b = py[cols + j + int64_t(pc) * n];
+            if (ortho == 0) {
+                vr = a * inv_norm;
+                vi = -b * inv_norm;
+            } else {
+                vr = a / sg;
+                vi = -b / sg;
+            }
+        } else {         // V column
+            const double a = qv[j + int64_t(pc) * m], b = qv[cols + j + int64_t(pc) * m];
+            const double f = (ortho == 0) ? sg * inv_norm : 1.0;
+            vr = a * f;
+            vi = -b * f;
+        }
+        Rr[e] = vr;
+        Ri[e] = vi;
+    }
+}
+
 }  // namespace
+
+void launch_svd_extract_complex(const ExtractDesc* d, int nb, const double* QV, const double* PY,
+                                const double* S, const int* perm, double* left, int64_t lplane,
+                                double* right, int64_t rplane, int ortho, double inv_norm,
+                                cudaStream_t s) {
+    if (nb <= 0) return;
+    svd_extract_complex_kernel<<<nb, 256, 0, s>>>(d, QV, PY, S, perm, left, lplane, right, rplane,
+                                                  ortho, inv_norm);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+}
 
 void launch_svd_jacobi(const SvdBlockDesc* d, int nb, int max_n, const double* src, double* X,
                        double* W, double* V, double* P, double* S, int* perm, int* sweeps_out,

@@ -189,9 +189,10 @@ void GemmPlan::add_task(int cbuf, int64_t coff, int m, int n, int ldc, int accum
 }
 
 void GemmPlan::add_seg(int abuf, int64_t aoff, int lda, int ta, int bbuf, int64_t boff,
-                       int ldb, int tb, int k) {
+                       int ldb, int tb, int k, int sgn) {
     if (k <= 0) return;
     Seg s;
+    s.sgn = sgn;
     s.aoff = aoff;
     s.boff = boff;
     s.abuf = abuf;
@@ -236,6 +237,50 @@ void GemmPlan::finalize(cudaStream_t s) {
     upload(dsegs, segs, s);
     upload(dtasks, tasks, s);
     upload(dtiles, tiles, s);
+}
+
+// (A_re + i a A_im)(B_re + i b B_im) = A_re B_re - a b A_im B_im + i (b A_re B_im + a A_im B_re)
+// with a, b = -1 for a conjugated operand
+GemmPlan complex_plan(const GemmPlan& g, unsigned conj_mask) {
+    GemmPlan c;
+    for (const Task& t : g.tasks) {
+        for (int part = 0; part < 2; ++part) {
+            c.add_task(t.cbuf + part * S_IM, t.coff, t.m, t.n, t.ldc, t.accum);
+            for (int j = 0; j < t.nseg; ++j) {
+                const Seg& s = g.segs[size_t(t.seg0 + j)];
+                const int sa = (conj_mask >> s.abuf) & 1 ? -1 : 1;
+                const int sb = (conj_mask >> s.bbuf) & 1 ? -1 : 1;
+                const int ai = s.abuf + S_IM, bi = s.bbuf + S_IM;
+                if (part == 0) {
+                    c.add_seg(s.abuf, s.aoff, s.lda, s.ta, s.bbuf, s.boff, s.ldb, s.tb, s.k, s.sgn);
+                    c.add_seg(ai, s.aoff, s.lda, s.ta, bi, s.boff, s.ldb, s.tb, s.k,
+                              -sa * sb * s.sgn);
+                } else {
+                    c.add_seg(s.abuf, s.aoff, s.lda, s.ta, bi, s.boff, s.ldb, s.tb, s.k, sb * s.sgn);
+                    c.add_seg(ai, s.aoff, s.lda, s.ta, s.bbuf, s.boff, s.ldb, s.tb, s.k, sa * s.sgn);
+                }
+            }
+        }
+    }
+    return c;
+}
+
+CombPlan complex_comb(const CombPlan& c) {
+    CombPlan z;
+    z.outs = c.outs;
+    z.terms = c.terms;
+    z.flops = 2 * c.flops;
+    const int nt = int(c.terms.size());
+    for (CombTerm t : c.terms) {
+        t.sbuf += S_IM;
+        z.terms.push_back(t);
+    }
+    for (CombOut o : c.outs) {
+        o.dbuf += S_IM;
+        o.t0 += nt;
+        z.outs.push_back(o);
+    }
+    return z;
 }
 
 void CombPlan::finalize(cudaStream_t s) {

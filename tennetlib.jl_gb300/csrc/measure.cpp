@@ -45,15 +45,19 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
         tn_ctx* ctx = mps->ctx;
         cudaStream_t st = ctx->stream;
         const int N = mps->N, d = mps->d;
+        const int np = mps->planes();  // complex: every buffer below holds two planes
         // concatenated site blocks and their sub-matrices A_s[l, r]
         std::vector<int64_t> soff(N + 1, 0);
         for (int i = 0; i < N; ++i) soff[i + 1] = soff[i] + mps->sites[i].lay.size;
         DevBuf S;
-        S.alloc(size_t(std::max<int64_t>(soff[N], 1)) * 8, st);
+        S.alloc(size_t(std::max<int64_t>(soff[N], 1)) * 8 * np, st);
         for (int i = 0; i < N; ++i)
-            if (mps->sites[i].lay.size)
-                TN_CUDA(cudaMemcpyAsync(S.d() + soff[i], mps->sites[i].buf.p,
-                                        size_t(mps->sites[i].lay.size) * 8, cudaMemcpyDeviceToDevice, st));
+            for (int pl = 0; pl < np; ++pl)
+                if (mps->sites[i].lay.size)
+                    TN_CUDA(cudaMemcpyAsync(S.d() + pl * soff[N] + soff[i],
+                                            mps->sites[i].buf.d() + pl * mps->sites[i].lay.size,
+                                            size_t(mps->sites[i].lay.size) * 8,
+                                            cudaMemcpyDeviceToDevice, st));
         std::vector<std::vector<SubBlock>> subs(N);
         for (int i = 0; i < N; ++i) {
             const SiteLayout& L = mps->sites[i].lay;
@@ -88,10 +92,10 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
                 etot += int64_t(mps->links[i].dim[x]) * mps->links[i].dim[x];
             }
         DevBuf E, F, T, X;
-        E.alloc(size_t(etot) * 8, st);
-        F.alloc(size_t(etot) * 8, st);
-        TN_CUDA(cudaMemsetAsync(E.p, 0, size_t(etot) * 8, st));
-        TN_CUDA(cudaMemsetAsync(F.p, 0, size_t(etot) * 8, st));
+        E.alloc(size_t(etot) * 8 * np, st);
+        F.alloc(size_t(etot) * 8 * np, st);
+        TN_CUDA(cudaMemsetAsync(E.p, 0, size_t(etot) * 8 * np, st));
+        TN_CUDA(cudaMemsetAsync(F.p, 0, size_t(etot) * 8 * np, st));
         const double one = 1.0;
         TN_CUDA(cudaMemcpyAsync(E.d() + eoff[0][0], &one, 8, cudaMemcpyHostToDevice, st));
         TN_CUDA(cudaMemcpyAsync(F.d() + eoff[N][0], &one, 8, cudaMemcpyHostToDevice, st));
@@ -107,14 +111,34 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
             ttot += t;
             tmax = std::max(tmax, t);
         }
-        T.alloc(size_t(std::max<int64_t>(ttot, 1)) * 8, st);
-        X.alloc(size_t(std::max<int64_t>(ttot, 1)) * 8, st);
+        T.alloc(size_t(std::max<int64_t>(ttot, 1)) * 8 * np, st);
+        X.alloc(size_t(std::max<int64_t>(ttot, 1)) * 8 * np, st);
         Bases bs{};
         bs.p[S_L] = E.d();
         bs.p[S_R] = F.d();
         bs.p[S_X] = S.d();
         bs.p[S_T1] = T.d();
         bs.p[S_T2] = X.d();
+        if (np == 2) {
+            bs.p[S_L + S_IM] = E.d() + etot;
+            bs.p[S_R + S_IM] = F.d() + etot;
+            bs.p[S_X + S_IM] = S.d() + soff[N];
+            bs.p[S_T1 + S_IM] = T.d() + ttot;
+            bs.p[S_T2 + S_IM] = X.d() + ttot;
+        }
+        // complex states: the bra factors (the conjugated site tensors) enter through
+        // complex_plan's conjugation; F is Hermitian, so the local stage's F^T becomes F^H = F
+        auto run = [&](GemmPlan& g, unsigned conj) {
+            if (np == 2) {
+                GemmPlan c = complex_plan(g, conj);
+                c.finalize(st);
+                launch_gemm_f64(c, bs, st);
+                TN_CUDA(cudaStreamSynchronize(st));  // the plan goes out of scope
+            } else {
+                g.finalize(st);
+                launch_gemm_f64(g, bs, st);
+            }
+        };
         const int e0 = ctx->timer.mark();
         // left pass: T = E_i[l] A_s ; E_{i+1}[r] = sum_s A_s^T T
         for (int i = 0; i < N; ++i) {
@@ -137,10 +161,8 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
                     g2.add_seg(S_X, x.off, x.ld, 1, S_T1, toff[i][k], lk.dim[x.l], 0, lk.dim[x.l]);
                 }
             }
-            g1.finalize(st);
-            g2.finalize(st);
-            launch_gemm_f64(g1, bs, st);
-            launch_gemm_f64(g2, bs, st);
+            run(g1, 0);
+            run(g2, 1u << S_X);
             TN_CUDA(cudaStreamSynchronize(st));  // plans go out of scope
         }
         // right pass: U = A_s F_{i+1}[r] ; F_i[l] = sum_s U A_s^T
@@ -164,10 +186,8 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
                     g2.add_seg(S_T1, toff[i][k], Dl, 0, S_X, x.off, x.ld, 1, rk.dim[x.r]);
                 }
             }
-            g1.finalize(st);
-            g2.finalize(st);
-            launch_gemm_f64(g1, bs, st);
-            launch_gemm_f64(g2, bs, st);
+            run(g1, 0);
+            run(g2, 1u << S_X);
             TN_CUDA(cudaStreamSynchronize(st));
         }
         // local stage, all sites at once: W = E_i[l] A_s ; X = W F_{i+1}[r]^T ; dots with A_{s'}
@@ -196,13 +216,17 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
                     bd.cols = Dr;
                     dots.push_back(bd);
                     keys.push_back(Key{i, y.s, x.s});
+                    if (np == 2) {  // Re sum conj(a) x = a_re . x_re + a_im . x_im
+                        bd.x = X.d() + ttot + toff[i][k];
+                        bd.y = S.d() + soff[N] + y.off;
+                        dots.push_back(bd);
+                        keys.push_back(Key{i, y.s, x.s});
+                    }
                 }
             }
         }
-        ga.finalize(st);
-        gb.finalize(st);
-        launch_gemm_f64(ga, bs, st);
-        launch_gemm_f64(gb, bs, st);
+        run(ga, 0);
+        run(gb, 1u << S_R);
         DevBuf dd, dout;
         dd.alloc(std::max<size_t>(dots.size(), 1) * sizeof(BlockDot), st);
         dout.alloc(std::max<size_t>(dots.size(), 1) * 8, st);
@@ -231,8 +255,9 @@ extern "C" int tn_mps_expect_local(tn_mps* mps, const double* op, double* out) {
 // <a|b> of two MPS on the same sites (ITensorMPS inner(psi, phi) on the sweep's states):
 // mixed transfer matrices E_{i+1}[q] (Da_q x Db_q) = sum_s A_s[l, q]^T E_i[l] B_s[l, q] over
 // the charge sectors present in both states, FP64 grouped GEMMs; the result is E_N.
-extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
-    return guarded_m([&] {
+namespace {
+void overlap_impl(const tn_mps* a, const tn_mps* b, double* out, bool cx) {
+    {
         TN_REQUIRE(a && b && out, "null argument");
         TN_REQUIRE(a->ctx == b->ctx && a->N == b->N && a->d == b->d && a->pq == b->pq,
                    "overlap needs two states of one context on the same sites");
@@ -278,8 +303,9 @@ extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
             }
         }
         TN_REQUIRE(!eoff[0].empty() && !eoff[N].empty(), "the states have different total charges");
-        DevBuf E, T;
-        E.alloc(size_t(std::max<int64_t>(etot, 1)) * 8, st);
+        const int np = cx ? 2 : 1;
+        DevBuf E, T, Za, Zb;  // Za / Zb: zero imaginary planes of a real state in a complex overlap
+        E.alloc(size_t(std::max<int64_t>(etot, 1)) * 8 * np, st);
         TN_CUDA(cudaMemsetAsync(E.p, 0, E.bytes, st));
         const double one = 1.0;
         TN_CUDA(cudaMemcpyAsync(E.d() + eoff[0].begin()->second, &one, 8, cudaMemcpyHostToDevice, st));
@@ -309,12 +335,25 @@ extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
                 t += int64_t(j.Dla) * j.Drb;
                 jobs.push_back(j);
             }
-            T.alloc(size_t(std::max<int64_t>(t, 1)) * 8, st);
+            T.alloc(size_t(std::max<int64_t>(t, 1)) * 8 * np, st);
             Bases bs{};
             bs.p[S_L] = E.d();
             bs.p[S_X] = a->sites[i].buf.d();
             bs.p[S_A] = b->sites[i].buf.d();
             bs.p[S_T1] = T.d();
+            if (cx) {
+                auto im_of = [&](const tn_mps* m, DevBuf& Z) {
+                    const int64_t n = m->sites[i].lay.size;
+                    if (m->cplx) return m->sites[i].buf.d() + n;
+                    Z.alloc(size_t(std::max<int64_t>(n, 1)) * 8, st);
+                    TN_CUDA(cudaMemsetAsync(Z.p, 0, Z.bytes, st));
+                    return Z.d();
+                };
+                bs.p[S_L + S_IM] = E.d() + etot;
+                bs.p[S_X + S_IM] = im_of(a, Za);
+                bs.p[S_A + S_IM] = im_of(b, Zb);
+                bs.p[S_T1 + S_IM] = T.d() + t;
+            }
             GemmPlan g1, g2;
             std::map<int, std::vector<size_t>> byr;
             for (size_t k = 0; k < jobs.size(); ++k) {
@@ -332,15 +371,36 @@ extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
                     g2.add_seg(S_X, j.xa.off, j.xa.ld, 1, S_T1, j.toff, j.Dla, 0, j.Dla);
                 }
             }
-            g1.finalize(st);
-            g2.finalize(st);
-            launch_gemm_f64(g1, bs, st);
-            launch_gemm_f64(g2, bs, st);
+            if (cx) {  // <a|b>: a conjugated
+                GemmPlan c1 = complex_plan(g1, 0), c2 = complex_plan(g2, 1u << S_X);
+                c1.finalize(st);
+                c2.finalize(st);
+                launch_gemm_f64(c1, bs, st);
+                launch_gemm_f64(c2, bs, st);
+            } else {
+                g1.finalize(st);
+                g2.finalize(st);
+                launch_gemm_f64(g1, bs, st);
+                launch_gemm_f64(g2, bs, st);
+            }
             TN_CUDA(cudaStreamSynchronize(st));
         }
-        double v = 0.0;
-        TN_CUDA(cudaMemcpyAsync(&v, E.d() + eoff[N].begin()->second, 8, cudaMemcpyDeviceToHost, st));
+        const int64_t eN = eoff[N].begin()->second;
+        TN_CUDA(cudaMemcpyAsync(&out[0], E.d() + eN, 8, cudaMemcpyDeviceToHost, st));
+        if (cx) TN_CUDA(cudaMemcpyAsync(&out[1], E.d() + etot + eN, 8, cudaMemcpyDeviceToHost, st));
         TN_CUDA(cudaStreamSynchronize(st));
-        *out = v;
+    }
+}
+}  // namespace
+
+extern "C" int tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* out) {
+    return guarded_m([&] {
+        TN_REQUIRE(a && b, "null argument");
+        TN_REQUIRE(!a->cplx && !b->cplx, "complex states: use tn_mps_overlap_complex");
+        overlap_impl(a, b, out, false);
     });
+}
+
+extern "C" int tn_mps_overlap_complex(const tn_mps* a, const tn_mps* b, double* out) {
+    return guarded_m([&] { overlap_impl(a, b, out, true); });
 }

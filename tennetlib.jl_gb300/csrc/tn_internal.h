@@ -130,16 +130,17 @@ enum BufSlot {
     S_T2 = 5,
     S_A = 6,   // second site tensor
     S_B = 7,
-    NSLOT = 8
+    S_IM = 8,  // slot s + S_IM: the imaginary plane of slot s's complex buffer
+    NSLOT = 16
 };
 struct Bases {
     double* p[NSLOT];
 };
 
-// C[task] = sum over its segments of op(A) * op(B); op = transpose when t* = 1.
+// C[task] = sum over its segments of sgn * op(A) * op(B); op = transpose when t* = 1.
 struct Seg {
     int64_t aoff, boff;
-    int32_t abuf, bbuf, lda, ldb, k, ta, tb;
+    int32_t abuf, bbuf, lda, ldb, k, ta, tb, sgn;
 };
 struct Task {
     int64_t coff;
@@ -171,7 +172,7 @@ struct GemmPlan {
     DevBuf dsegs, dtasks, dtiles;
     void add_task(int cbuf, int64_t coff, int m, int n, int ldc, int accum = 0);
     void add_seg(int abuf, int64_t aoff, int lda, int ta, int bbuf, int64_t boff, int ldb,
-                 int tb, int k);
+                 int tb, int k, int sgn = 1);
     void finalize(cudaStream_t s);  // builds tiles, uploads
 };
 struct CombPlan {
@@ -182,6 +183,13 @@ struct CombPlan {
     DevBuf douts, dterms, dtiles;
     void finalize(cudaStream_t s);
 };
+
+// Complex forms of real plans over planar complex buffers (real plane in slot s, imaginary
+// plane in slot s + S_IM).  Every task C = sum op(A) op(B) becomes two, C_re and C_im, of
+// two segments per original one; operands read from a slot in conj_mask (bit s) enter
+// conjugated.  A combine plan (real coefficients) is applied to both planes.  Unfinalized.
+GemmPlan complex_plan(const GemmPlan& g, unsigned conj_mask);
+CombPlan complex_comb(const CombPlan& c);
 
 // split-precision (bf16 slice) GEMM descriptors.  A packed operand is a list of tiles
 // (row tile, k tile, slice) of the canonical K-major SWIZZLE_128B layout.
@@ -349,5 +357,13 @@ struct ExtractDesc {
 void launch_svd_extract(const ExtractDesc* d, int nb, const double* QV, const double* PY,
                         const double* S, const int* perm, double* left, double* right, int ortho,
                         double inv_norm, cudaStream_t s);
+// The same for complex blocks A (rows x cols) whose SVD was taken of the realified
+// [[Re A, -Im A], [Im A, Re A]]: kept complex value c is the realified pair (2c, 2c + 1), its
+// vectors the realified column of the first of them read as [re; im]; left and right are
+// planar (imaginary planes at left + lplane, right + rplane), the right tensor gets V^H.
+void launch_svd_extract_complex(const ExtractDesc* d, int nb, const double* QV, const double* PY,
+                                const double* S, const int* perm, double* left, int64_t lplane,
+                                double* right, int64_t rplane, int ortho, double inv_norm,
+                                cudaStream_t s);
 
 }  // namespace tn
