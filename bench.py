@@ -372,6 +372,10 @@ def run_ours(args, world, rank, local, pg):
         if rank == 0:
             print(json.dumps({"svd_bond": run_svd_bond(tn, local, args)}), flush=True)
         return
+    if args.quench_only:
+        if rank == 0:
+            print(json.dumps({"quench": run_quench(tn, local, args)}), flush=True)
+        return
     ctx = tn.Context(local)
     if args.precision == "split":
         ctx.set_precision("split", args.slices)
@@ -529,6 +533,11 @@ def run_ours(args, world, rank, local, pg):
                          "gpu_maxlinkdim": int(e2e_chi), "cpu_maxlinkdim": cb["maxlinkdim"]}
     if not args.no_ttn:
         res["ttn"] = run_ttn(tn, local, args, world)
+    if not args.no_quench:
+        try:
+            res["quench"] = run_quench(tn, local, args)
+        except Exception as e:  # an extra leg: report it, keep the headline line
+            res["quench"] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_j1j2:
         try:
             res["j1j2_chi2048"] = run_j1j2(tn, local, args)
@@ -608,6 +617,88 @@ def run_j1j2(tn, local, args):
     return out
 
 
+# Real-time two-site TDVP quench (ComplexF64): the N = 64 Heisenberg chain from the Neel
+# state, tau = -0.05i, maxdim 512, cutoff 1e-9, Krylov dimension 30.  The state is first
+# evolved (untimed) to t = 5 in steps of 0.25, where the bond dimension has grown to ~100;
+# then --steps sweeps of the workload's step are timed.
+QUENCH_N, QUENCH_DT, QUENCH_CHI, QUENCH_CUTOFF, QUENCH_KRYLOV = 64, 0.05, 512, 1e-9, 30
+QUENCH_PREP_DT, QUENCH_PREP_SWEEPS = 0.25, 20
+QUENCH_CPU_BONDS = 6
+
+
+def run_quench(tn, local, args):
+    """Complex TDVP sweeps on the GPU (FP64 complex contractions, realified block SVD) and the
+    oracle's complex restatement timed on a bounded sample of the same sweep."""
+    import numpy as np
+    N = QUENCH_N
+    ctx = tn.Context(local)
+    W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
+    H = tn.MPO(W, delta, pq, ctx)
+    eng = tn.TDVPEngine(tn.MPS.product(tn.models.neel_states(N), pq, ctx), H)
+    kw = dict(maxdim=QUENCH_CHI, cutoff=QUENCH_CUTOFF, solver_krylovdim=QUENCH_KRYLOV)
+    t0 = time.perf_counter()
+    for _ in range(QUENCH_PREP_SWEEPS):
+        tn.tdvpsweep_(eng, -1j * QUENCH_PREP_DT, **kw)
+    prep = time.perf_counter() - t0
+    psi0 = eng.getpsi()
+    chi0 = int(psi0.maxlinkdim())
+    sweeps = []
+    for _ in range(max(args.steps, 1)):
+        tn.tdvpsweep_(eng, -1j * QUENCH_DT, **kw)
+        st = eng.swdata.stats[-1]
+        sweeps.append({"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
+                       "svd_s": st["svd_ms"] / 1e3, "env_s": st["env_ms"] / 1e3,
+                       "krylov_s": st["lanczos_ms"] / 1e3, "matvecs": st["matvecs"],
+                       "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
+                       "maxlinkdim": eng.maxchi(), "energy": eng.getenergy()})
+    psi = eng.getpsi()
+    sz = np.array(tn.measure(psi, "Sz"))
+    e_neel = -0.25 * (N - 1)  # <Neel| sum S_i . S_i+1 |Neel>, conserved by the evolution
+    out = {"workload": f"heisenberg_chain_N{N}_neel_quench_tau-{QUENCH_DT}i_maxdim{QUENCH_CHI}"
+                       f"_cutoff{QUENCH_CUTOFF:g}_krylov{QUENCH_KRYLOV}",
+           "dtype": "c128 (planar complex FP64)",
+           "prepare": f"{QUENCH_PREP_SWEEPS} untimed sweeps of tau = -{QUENCH_PREP_DT}i (t = "
+                      f"{QUENCH_PREP_SWEEPS * QUENCH_PREP_DT:g})",
+           "prepare_s": prep, "chi_start": chi0, "timed_sweeps": sweeps,
+           "sweep_s_mean": sum(x["sweep_s"] for x in sweeps) / len(sweeps),
+           "energy_drift_rel": abs(sweeps[-1]["energy"] - e_neel) / abs(e_neel),
+           "total_sz": float(sz.sum()), "norm": abs(psi.inner(psi))}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = quench_cpu_sample(psi0)
+        out["speedup_vs_cpu_port"] = out["cpu_baseline"]["value"] / out["sweep_s_mean"]
+    return out
+
+
+def quench_cpu_sample(psi, budget_s=20.0):
+    """The oracle's complex TDVP updates of the left-moving half sweep from the same state
+    (right environments built untimed), bond after bond until budget_s is spent; the sweep
+    time is estimated as twice (the measured bonds + the remaining bonds of the half sweep at
+    the mean time of the last four measured), the right-moving half being the mirror image."""
+    import numpy as np
+    from oracle import tn_oracle as O
+    N = psi.N
+    tensors, links = download_state(psi)
+    st = O.MPS([np.asarray(t) for t in tensors], [np.asarray(q, dtype=np.int64) for q in links],
+               O.SPIN_HALF_Q.copy(), center=0)
+    env = O.StateEnvs(st, O.heisenberg_mpo(N))
+    env.position(0, 2)
+    times = []
+    for b in range(N - 1):
+        t0 = time.perf_counter()
+        O.update_two_site_tdvp(env, b, "left", -0.5j * QUENCH_DT, QUENCH_CHI, 1, QUENCH_CUTOFF,
+                               QUENCH_KRYLOV, 100, 1e-12, True)
+        times.append(time.perf_counter() - t0)
+        if sum(times) > budget_s:
+            break
+    last = sum(times[-4:]) / len(times[-4:])
+    est = 2 * (sum(times) + (N - 1 - len(times)) * last)
+    return {"value": est, "unit": "s/sweep", "cores": cores(), "kind": "port", "dense": True,
+            "sample": f"the first {len(times)} of the {N - 1} updates of the left-moving half "
+                      f"sweep ({sum(times):.1f} s, numpy FP64 complex oracle, dense tensors with "
+                      "charge labels) from the same state; the rest of the half sweep at the "
+                      "mean time of the last four, times two for the right-moving half"}
+
+
 # one bond's charge blocks at chi ~ 2048 (the sizes of the largest bond of the 6 x 16 J1-J2
 # cylinder): rows x cols of the seven largest blocks
 SVD_BOND_SHAPES = [(1200, 1100), (1150, 1050), (1100, 1000), (900, 850), (600, 450), (300, 250),
@@ -681,6 +772,10 @@ def main():
                     help="only the J1-J2 cylinder comparison at chi = 2048 (split vs FP64)")
     ap.add_argument("--svd-bond", action="store_true",
                     help="only the block SVD of one chi ~ 2048 bond (--steps calls)")
+    ap.add_argument("--no-quench", action="store_true",
+                    help="skip the real-time TDVP quench (complex) leg of the default run")
+    ap.add_argument("--quench-only", action="store_true",
+                    help="only the real-time TDVP quench (complex) leg")
     ap.add_argument("--no-j1j2", action="store_true",
                     help="skip the chi = 2048 J1-J2 comparison leg of the default run")
     ap.add_argument("--j1j2-lx", type=int, default=J1J2_LX,
