@@ -261,6 +261,14 @@ int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_swee
 int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn_update_params* p,
                              tn_sweep_result* res, double* mid_eigs, int mid_cap,
                              int32_t* n_mid_eigs);
+/* tdvpsweep!(engine, tau; nsite) with nsite 1 or 2 and tau = tau_re + i tau_im.  nsite = 1
+ * is the one-site sweep of fullsweep! (src/mps/sweep.jl:118-152) with _update_one_site!'s
+ * exponential solver and reverse step (src/mps/update_site.jl:94-190): each site evolves by
+ * tau/2, is split by the block SVD (ITensors truncation), and the bond matrix evolves back
+ * by -tau/2 under the zero-site effective Hamiltonian before it enters the next site. */
+int tn_env_tdvpsweep_nsite(tn_env* env, int nsite, double tau_re, double tau_im,
+                           const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
+                           int mid_cap, int32_t* n_mid_eigs);
 
 /* ---- block SVD + truncation -------------------------------------------------------
  * The SVD/truncation of replacebond! (called at TenNetLib src/mps/update_site.jl:64-76)

@@ -277,6 +277,14 @@ def heff1_apply(L, W, R, phi):
     return t
 
 
+def heff0_apply(L, R, C):
+    """Zero-site H_eff * C for the bond matrix C[x, y] between the environments L (sites left
+    of the bond) and R (sites right of it): y[x', y'] = sum L[x', a, x] C[x, y] R[y', a, y]
+    (ProjMPO with nsite = 0, the reverse step of one-site TDVP)."""
+    t = np.tensordot(L, C, axes=([2], [0]))               # [x', a, y]
+    return np.tensordot(t, R, axes=([1, 2], [1, 2]))      # [x', y']
+
+
 def heff2_flops(L_shape, W1, W2, R_shape, phi_shape):
     """Dense multiply-add count of the four-step contraction above (x2 = flops)."""
     Dl, w0, _ = L_shape
@@ -851,11 +859,34 @@ def update_two_site_tdvp(env: StateEnvs, pos, ortho, time_step, maxdim, mindim, 
 
 
 def tdvp_sweep(env: StateEnvs, swdata: SweepData, tau, maxdim, cutoff, mindim=1, krylovdim=30,
-               maxiter=100, tol=1e-12, normalize=True):
-    """``tdvpsweep!`` with nsite = 2 (``src/mps/tdvp.jl:247-277``): a full sweep with
-    ``exp_solver`` at time step tau/2 and reverse steps."""
+               maxiter=100, tol=1e-12, normalize=True, nsite=2):
+    """``tdvpsweep!`` (``src/mps/tdvp.jl:247-277``): a full sweep with ``exp_solver`` at time
+    step tau/2 and reverse steps, two-site (nsite = 2) or one-site (nsite = 1: the sweep
+    order of ``fullsweep1``, the one-site update with its zero-site reverse step)."""
     N = env.N
     assert env.psi.center == 0
+    if nsite == 1:
+        swdata.sweepcount += 1
+        energy = float("nan")
+        maxtruncerr = 0.0
+        lasteigs = [None] * (N - 1)
+        for q in range(N):
+            energy, spec, _ = update_one_site(env, q, "left", maxdim, mindim, cutoff, krylovdim,
+                                              maxiter, tol, normalize, 0.0, 0.5 * tau)
+            maxtruncerr = max(spec.truncerr, maxtruncerr)
+        for q in range(N - 1, -1, -1):
+            energy, spec, _ = update_one_site(env, q, "right", maxdim, mindim, cutoff, krylovdim,
+                                              maxiter, tol, normalize, 0.0, 0.5 * tau)
+            if q >= 1:
+                lasteigs[q - 1] = spec.eigs
+            maxtruncerr = max(spec.truncerr, maxtruncerr)
+        swdata.maxchi.append(env.psi.maxlinkdim())
+        swdata.energy.append(energy)
+        mid = lasteigs[N // 2 - 1]
+        swdata.entropy.append(entropy(mid / np.sum(mid)))
+        swdata.maxtruncerr.append(maxtruncerr)
+        swdata.lasteigs = lasteigs
+        return energy
     swdata.sweepcount += 1
     energy = float("nan")
     maxtruncerr = 0.0
@@ -944,13 +975,16 @@ def fullsweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, krylo
 
 
 def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdim, maxiter,
-                    tol, normalize=True, noise=0.0):
-    """``_update_one_site!`` (``src/mps/update_site.jl:94-190``) for the eigensolver: solve
-    the one-site problem at the orthogonality center; unless the half sweep is done, SVD the
-    tensor with the link toward the next site on the V side (ITensors truncation), keep U at
-    pos and multiply S V into the next site.  With noise > 0 (``:135-152``) the solved tensor
-    times the next site is split as a two-site tensor at pos0 (pos for "left", pos - 1 for
-    "right") with the density-matrix perturbation of that bond."""
+                    tol, normalize=True, noise=0.0, time_step=None):
+    """``_update_one_site!`` (``src/mps/update_site.jl:94-190``): solve the one-site problem
+    at the orthogonality center (time_step None: the eigensolver; else ``exp_solver``,
+    exp(time_step H_eff) phi); unless the half sweep is done, SVD the tensor with the link
+    toward the next site on the V side (ITensors truncation), keep U at pos and multiply S V
+    into the next site -- with a time step after evolving that bond matrix by -time_step
+    under the zero-site H_eff (``reverse_step``, ``:175-182``).  With noise > 0
+    (``:135-152``) the solved tensor times the next site is split as a two-site tensor at
+    pos0 (pos for "left", pos - 1 for "right") with the density-matrix perturbation of that
+    bond."""
     psi = env.psi
     N = psi.N
     assert psi.center == pos
@@ -961,10 +995,18 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
     def apply(v):
         return env.product1(pos, v.reshape(shape)).reshape(-1)
 
-    energy, vec, info = eigsolve_lowest(apply, phi.reshape(-1), krylovdim, maxiter, tol)
+    if time_step is None:
+        energy, vec, info = eigsolve_lowest(apply, phi.reshape(-1), krylovdim, maxiter, tol)
+    else:
+        if abs(noise) > FLOAT64_THRESHOLD:
+            raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
+                             "`reverse_step=true` !!")
+        vec, info = exponentiate(apply, time_step, phi.reshape(-1), krylovdim, maxiter, tol)
     phi = vec.reshape(shape)
     if normalize:
         phi = phi / np.linalg.norm(phi)
+    if time_step is not None:
+        energy = float(np.real(np.vdot(phi.reshape(-1), apply(phi.reshape(-1)))))
     if halfsweep_done(N, pos, 1, ortho):
         psi.A[pos] = phi
         env.lpos = min(env.lpos, pos)
@@ -1009,8 +1051,8 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
     res, spec, kept = svd_blocks_truncate(blocks, maxdim, mindim, cutoff)
     chi = sum(kept)
     norm = math.sqrt(sum(float(np.sum(S ** 2)) for _, S, _ in res)) if normalize else 1.0
-    Lm = np.zeros((M.shape[0], chi))
-    Rm = np.zeros((chi, M.shape[1]))
+    Lm = np.zeros((M.shape[0], chi), dtype=M.dtype)
+    Rm = np.zeros((chi, M.shape[1]), dtype=M.dtype)
     qnew = []
     off = 0
     for m, ri, ci, (U, S, Vh), k in zip(charges, rows, cols, res, kept):
@@ -1026,6 +1068,31 @@ def update_one_site(env: StateEnvs, pos, ortho, maxdim, mindim, cutoff, krylovdi
         qnew.extend([m] * k)
         off += k
     qnew = np.array(qnew, dtype=np.int64)
+    if time_step is not None:
+        # reverse step: the bond matrix C evolves by -time_step under the zero-site H_eff;
+        # the environment on the side of the new site includes it
+        W = env.H.W[pos]
+        if ortho == "left":
+            Lx = left_env_update(env.L[pos], Lm.reshape(Dl, d, chi), W)
+            Rx = env.R[pos]
+            C = Rm
+        else:
+            Lx = env.L[pos]
+            Rx = right_env_update(env.R[pos], Rm.reshape(chi, d, Dr), W)
+            C = Lm
+
+        def apply0(v):
+            return heff0_apply(Lx, Rx, v.reshape(C.shape)).reshape(-1)
+
+        c, nmv = exponentiate(apply0, -time_step, C.reshape(-1), krylovdim, maxiter, tol)
+        info += nmv
+        if normalize:
+            c = c / np.linalg.norm(c)
+        energy = float(np.real(np.vdot(c, apply0(c))))
+        if ortho == "left":
+            Rm = c.reshape(C.shape)
+        else:
+            Lm = c.reshape(C.shape)
     if ortho == "left":
         psi.A[pos] = Lm.reshape(Dl, d, chi)
         psi.A[pos + 1] = np.tensordot(Rm, psi.A[pos + 1], axes=([1], [0]))

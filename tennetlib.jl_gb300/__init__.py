@@ -692,12 +692,13 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
 
     A real time step is imaginary-time evolution exp(time_step H); a complex one (real-time
     evolution exp(-i dt H) is ``time_step = -1j * dt``) makes the state complex first, as
-    ITensors promotes the MPS to ComplexF64.  ``nsite = "dynamic"`` is not built.
+    ITensors promotes the MPS to ComplexF64.  nsite = 1 is the one-site sweep with the
+    zero-site reverse step; ``nsite = "dynamic"`` is not built.
     """
     if solver is not exp_solver:
         raise ValueError("`tdvpsweep!()`: `solver` must be `exp_solver` !!")
-    if nsite != 2:
-        raise ValueError("only nsite = 2 TDVP sweeps are built")
+    if nsite not in (1, 2):
+        raise ValueError("nsite = 1 and 2 TDVP sweeps are built (\"dynamic\" is not)")
     if kwargs.get("noise", 0.0):
         raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
                          "`reverse_step=true` !!")
@@ -709,7 +710,11 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     sysenv = engine.sysenv
     t0 = time.perf_counter()
     tau = complex(time_step)
-    if tau.imag != 0.0:
+    if nsite == 1:
+        L.check(sysenv.ctx.lib.tn_env_tdvpsweep_nsite(
+            sysenv.h, 1, tau.real, tau.imag, C.byref(p), C.byref(res),
+            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    elif tau.imag != 0.0:
         L.check(sysenv.ctx.lib.tn_env_tdvpsweep_complex(
             sysenv.h, tau.real, tau.imag, C.byref(p), C.byref(res), mid.ctypes.data_as(L.f64p),
             cap, C.byref(nmid)))

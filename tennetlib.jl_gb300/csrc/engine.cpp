@@ -1661,20 +1661,21 @@ void replace_bond(tn_env* env, int p, const PhiLayout& ph, const double* phi,
     eigs = D.eigs;
 }
 
-// replacebond! of a complex two-site tensor (planar phi, ITensors' complex svd +
-// truncate!): each complex block A = Ar + i Ai is factorised through the real SVD of
-// [[Ar, -Ai], [Ai, Ar]] (2 rows x 2 cols), whose singular values are those of A, each twice;
-// the columns of one pair span a complex singular vector [re; im] and i times it, so the
-// first column of each pair is taken.  Within a cluster of (nearly) equal complex values the
-// taken columns are made complex-orthonormal on the host (the same combinations applied to
-// the partner factor), which keeps A v = s u.
-void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double* phi,
-                          const tn_update_params* prm, int ortho, tn_update_result* res,
-                          std::vector<double>& eigs) {
+// Block SVD of complex blocks (planar source, imaginary plane at src + plane) with
+// ITensors' truncation (complex svd + truncate!): each block A = Ar + i Ai (r x c) is
+// factorised through the real SVD of [[Ar, -Ai], [Ai, Ar]] (2r x 2c), whose singular values
+// are those of A, each twice; the columns of one pair span a complex singular vector
+// [re; im] and i times it, so the first column of each pair is taken (by
+// launch_svd_extract_complex).  Within a cluster of (nearly) equal complex values the taken
+// columns are made complex-orthonormal on the host (the same combinations applied to the
+// partner factor), which keeps A v = s u.  R holds the realified blocks' results, D the
+// truncation of the complex values.
+void complex_block_svd(tn_env* env, const std::vector<int>& rows, const std::vector<int>& cols,
+                       const std::vector<int64_t>& offs, const double* src, int64_t plane,
+                       const tn_update_params* prm, SvdResult& R, TruncDecision& D) {
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
-    tn_mps* psi = env->psi.get();
-    const int nb = ph.nblk();
+    const int nb = int(rows.size());
     std::vector<int> rows2(nb), cols2(nb);
     std::vector<int64_t> off2(nb);
     int64_t tot = 0;
@@ -1692,26 +1693,25 @@ void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double*
         rb.outs.push_back(o);
     };
     for (int b = 0; b < nb; ++b) {
-        const int r = ph.rows[b], c = ph.cols[b];
+        const int r = rows[b], c = cols[b];
         rows2[b] = 2 * r;
         cols2[b] = 2 * c;
         off2[b] = tot;
-        quad(tot, 2 * r, r, c, S_X, ph.off[b], 1.0);
-        quad(tot + r, 2 * r, r, c, S_X + S_IM, ph.off[b], 1.0);
-        quad(tot + int64_t(c) * 2 * r, 2 * r, r, c, S_X + S_IM, ph.off[b], -1.0);
-        quad(tot + r + int64_t(c) * 2 * r, 2 * r, r, c, S_X, ph.off[b], 1.0);
+        quad(tot, 2 * r, r, c, S_X, offs[b], 1.0);
+        quad(tot + r, 2 * r, r, c, S_X + S_IM, offs[b], 1.0);
+        quad(tot + int64_t(c) * 2 * r, 2 * r, r, c, S_X + S_IM, offs[b], -1.0);
+        quad(tot + r + int64_t(c) * 2 * r, 2 * r, r, c, S_X, offs[b], 1.0);
         tot += int64_t(4) * r * c;
     }
     env->cx.alloc(size_t(std::max<int64_t>(tot, 1)) * 8, st);
     rb.finalize(st);
     {
         Bases bs{};
-        bs.p[S_X] = const_cast<double*>(phi);
-        set_im(bs, S_X, ph.size);
+        bs.p[S_X] = const_cast<double*>(src);
+        set_im(bs, S_X, plane);
         bs.p[S_Y] = env->cx.d();
         launch_combine(rb, bs, st);
     }
-    SvdResult R;
     block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm,
               env->desc, rows2, cols2, off2, env->cx.d(), R);
     // the complex values: the first of each realified pair
@@ -1723,7 +1723,7 @@ void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double*
         for (int j = 0; j < C.desc[b].n; ++j) C.S.push_back(R.S[size_t(R.desc[b].s_off + 2 * j)]);
     }
     C.total_n = int64_t(C.S.size());
-    TruncDecision D = decide(C, prm->maxdim, prm->mindim, prm->cutoff);
+    D = decide(C, prm->maxdim, prm->mindim, prm->cutoff);
     // clusters of kept values closer than 1e-8 of the block's largest: complex Gram-Schmidt
     std::vector<int> perm;
     for (int b = 0; b < nb; ++b) {
@@ -1800,6 +1800,20 @@ void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double*
             j0 = j1 + 1;
         }
     }
+}
+
+// replacebond! of a complex two-site tensor (planar phi): complex_block_svd of the phi
+// blocks, U to the left tensor and S V^H to the right one (or U S and V^H), planar.
+void replace_bond_complex(tn_env* env, int p, const PhiLayout& ph, const double* phi,
+                          const tn_update_params* prm, int ortho, tn_update_result* res,
+                          std::vector<double>& eigs) {
+    tn_ctx* ctx = env->ctx;
+    cudaStream_t st = ctx->stream;
+    tn_mps* psi = env->psi.get();
+    const int nb = ph.nblk();
+    SvdResult R;
+    TruncDecision D;
+    complex_block_svd(env, ph.rows, ph.cols, ph.off, phi, ph.size, prm, R, D);
     Link nl;
     for (int b = 0; b < nb; ++b)
         if (D.kept[b] > 0) {
@@ -2266,24 +2280,84 @@ bool halfsweep_done1(int N, int pos, int ortho) {
     return (pos == 0 && ortho == TN_ORTHO_RIGHT) || (pos == N - 1 && ortho == TN_ORTHO_LEFT);
 }
 
-// _update_one_site! (TenNetLib src/mps/update_site.jl:94-190) with the eigensolver: solve
-// the one-site problem at pos; unless the half sweep is done, split the new tensor by the
+// zero-site effective Hamiltonian (ProjMPO with nsite = 0, the reverse step of one-site
+// TDVP) on a bond matrix C between the links Ll and Lr, one block C_j (Ll.dim[xs[j]] x
+// Lr.dim[ys[j]], column-major at moff[j]) per charge: y = sum_a L(a) C R(a)^T with L the
+// environment of the sites left of the bond and R that of the sites right of it.
+struct Heff0Plan {
+    GemmPlan g1, g2;
+    int64_t tsize = 0;
+};
+void build_heff0(const tn_envt& EL, const tn_envt& ER, const Link& Ll, const Link& Lr,
+                 const std::vector<int>& xs, const std::vector<int>& ys,
+                 const std::vector<int64_t>& moff, Heff0Plan& P) {
+    std::map<int, int> jof;  // charge -> block
+    for (size_t j = 0; j < xs.size(); ++j) jof[Ll.q[xs[j]]] = int(j);
+    const int w = EL.lay.w;
+    TN_REQUIRE(w == ER.lay.w, "internal: zero-site environments on different MPO links");
+    struct Pend {
+        int64_t toff, roff;
+        int Dy;
+    };
+    std::vector<std::vector<Pend>> per_out(xs.size());
+    int64_t t = 0;
+    for (size_t j = 0; j < xs.size(); ++j) {
+        const int x = xs[j], y = ys[j];
+        for (int a = 0; a < w; ++a) {
+            const int64_t lo = EL.lay.off[size_t(a) * EL.lay.nsec + x];
+            const int64_t ro = ER.lay.off[size_t(a) * ER.lay.nsec + y];
+            if (lo < 0 || ro < 0) continue;
+            const int xp = EL.lay.bra[size_t(a) * EL.lay.nsec + x];
+            const int yp = ER.lay.bra[size_t(a) * ER.lay.nsec + y];
+            auto it = jof.find(Ll.q[xp]);
+            if (it == jof.end()) continue;
+            const int jp = it->second;
+            TN_REQUIRE(ys[size_t(jp)] == yp, "internal: zero-site charge mismatch");
+            const int Dxp = Ll.dim[xp], Dx = Ll.dim[x], Dy = Lr.dim[y];
+            // T = L(a, x) C_j  (Dxp x Dy)
+            P.g1.add_task(S_T1, t, Dxp, Dy, Dxp);
+            P.g1.add_seg(S_L, lo, Dxp, 0, S_X, moff[j], Dx, 0, Dx);
+            per_out[size_t(jp)].push_back(Pend{t, ro, Dy});
+            t += int64_t(Dxp) * Dy;
+        }
+    }
+    for (size_t jp = 0; jp < xs.size(); ++jp) {
+        const int Dxp = Ll.dim[xs[jp]], Dyp = Lr.dim[ys[jp]];
+        // y_j' = sum T R(a, y)^T
+        P.g2.add_task(S_Y, moff[jp], Dxp, Dyp, Dxp);
+        for (const auto& e : per_out[jp]) P.g2.add_seg(S_T1, e.toff, Dxp, 0, S_R, e.roff, Dyp, 1, e.Dy);
+    }
+    P.tsize = t;
+}
+
+// _update_one_site! (TenNetLib src/mps/update_site.jl:94-190): solve the one-site problem
+// at pos (time_step null: the eigensolver; else the exponential solver, exp(time_step H_eff),
+// complex when time_im != 0); unless the half sweep is done, split the new tensor by the
 // block SVD with ITensors truncation, keep U at pos (a left isometry for ortho "left", a
-// right one for "right") and multiply S V (resp. U S) into the next site.  With noise > 0
-// the new tensor times the next site goes through the two-site noise split instead.
+// right one for "right") and multiply S V (resp. U S) into the next site, after evolving
+// that bond matrix back by -time_step with the zero-site H_eff (reverse_step).  With
+// noise > 0 the new tensor times the next site goes through the two-site noise split.
 void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
-                     tn_update_result* res, std::vector<double>& eigs) {
+                     tn_update_result* res, std::vector<double>& eigs,
+                     const double* time_step = nullptr, double time_im = 0.0) {
     check_params(prm);
     tn_mps* psi = env->psi.get();
     const int N = psi->N;
-    TN_REQUIRE(!psi->cplx, "one-site updates of complex states are not built");
+    TN_REQUIRE(!psi->cplx || time_step,
+               "complex states are evolved by tdvpsweep; the eigensolver takes real states");
+    TN_REQUIRE(time_im == 0.0 || psi->cplx, "internal: a complex time step needs a complex state");
+    TN_REQUIRE(!(time_step && prm->noise > 1e-15),
+               "`updatePosition()` :: `noise` cannot be greater than zero for `reverse_step=true` !!");
+    TN_REQUIRE(!time_step || env->proj.empty(),
+               "excited-state projectors are built for the eigensolver only");
     TN_REQUIRE(p >= 0 && p < N, "site position out of range");
     TN_REQUIRE(psi->center == p, "one-site update: the orthogonality center must be at pos");
     tn_ctx* ctx = env->ctx;
     cudaStream_t st = ctx->stream;
+    const int np = psi->planes();
     position(env, p, 1);
     Heff1Plan& P1 = heff1_plan(env);
-    const int64_t n1 = P1.lay.size;
+    const int64_t n1c = P1.lay.size, n1 = n1c * np;
     env->vecC.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
     env->vecD.alloc(size_t(std::max<int64_t>(n1, 1)) * 8, st);
     tn_site& site = psi->sites[p];
@@ -2292,18 +2366,28 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     if (site.lay.layout == RG)
         TN_CUDA(cudaMemcpyAsync(env->vecC.p, site.buf.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
     else
-        regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk);
+        regroup(ctx, site.lay, site.buf.d(), P1.lay, env->vecC.d(), lk, rk, np);
     if (!env->proj.empty()) proj_vectors1(env, p, P1.lay);
     auto apply1 = [&](const double* x, double* y) {
         heff1_apply(env, P1, x, y);
         proj_apply(env, x, y, n1);
     };
-    EigOut eo = lanczos_lowest(env, apply1, n1, env->vecC.d(), env->vecD.d(), prm);
-    if (prm->check_convergence && eo.converged < 1)
-        throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
-    res->energy = eo.energy;
-    res->matvecs = eo.matvecs;
-    res->converged = eo.converged;
+    if (!time_step) {
+        EigOut eo = lanczos_lowest(env, apply1, n1, env->vecC.d(), env->vecD.d(), prm);
+        if (prm->check_convergence && eo.converged < 1)
+            throw Error(TN_E_NOTCONV, "`eig_solver()` not converged !!");
+        res->energy = eo.energy;
+        res->matvecs = eo.matvecs;
+        res->converged = eo.converged;
+    } else {
+        const int64_t mv0 = env->matvecs;
+        krylov_exp(env, apply1, n1, *time_step, env->vecC.d(), env->vecD.d(), prm, time_im,
+                   psi->cplx ? n1c : 0);
+        res->energy = normalize_and_energy(env, apply1, n1, env->vecD.d(), env->vecC.d(),
+                                           prm->normalize != 0);
+        res->matvecs = int32_t(env->matvecs - mv0);
+        res->converged = 1;
+    }
     res->truncerr = 0.0;
     eigs.clear();
     // the solver's vector is normalised (normalize!(phi) is then the identity)
@@ -2311,7 +2395,7 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         if (site.lay.layout == RG)
             TN_CUDA(cudaMemcpyAsync(site.buf.p, env->vecD.p, size_t(n1) * 8, cudaMemcpyDeviceToDevice, st));
         else
-            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk);
+            regroup(ctx, P1.lay, env->vecD.d(), site.lay, site.buf.d(), lk, rk, np);
         env->lpos = std::min(env->lpos, p);
         env->rpos = std::max(env->rpos, p);
         env->h1p_pos = -1;
@@ -2354,13 +2438,18 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     SiteLayout sv_lay = left ? make_site_layout(LG, lk, rk, psi->pq) : P1.lay;
     const double* phi = env->vecD.d();
     if (left) {
-        regroup(ctx, P1.lay, env->vecD.d(), sv_lay, env->vecC.d(), lk, rk);
+        regroup(ctx, P1.lay, env->vecD.d(), sv_lay, env->vecC.d(), lk, rk, np);
         phi = env->vecC.d();
     }
     SvdResult R;
-    block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm, env->desc,
-              sv_lay.rows, sv_lay.cols, sv_lay.off, phi, R);
-    TruncDecision D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
+    TruncDecision D;
+    if (psi->cplx) {
+        complex_block_svd(env, sv_lay.rows, sv_lay.cols, sv_lay.off, phi, sv_lay.size, prm, R, D);
+    } else {
+        block_svd(ctx, env->svdX, env->svdW, env->svdV, env->svdP, env->svdS, env->svdPerm,
+                  env->desc, sv_lay.rows, sv_lay.cols, sv_lay.off, phi, R);
+        D = decide(R, prm->maxdim, prm->mindim, prm->cutoff);
+    }
     const Link& olink = left ? rk : lk;  // the link that is truncated
     Link nl;
     std::vector<int> osec;  // sector of the old link of each kept block
@@ -2373,7 +2462,7 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         }
     tn_site here;
     here.lay = left ? make_site_layout(LG, lk, nl, psi->pq) : make_site_layout(RG, nl, rk, psi->pq);
-    here.buf.alloc(size_t(std::max<int64_t>(here.lay.size, 1)) * 8, st);
+    here.buf.alloc(size_t(std::max<int64_t>(here.lay.size, 1)) * 8 * np, st);
     // bond matrix per kept sector: S V^T (k x D) for "left", U S (D x k) for "right"
     std::vector<int64_t> moff;
     int64_t msize = 0;
@@ -2381,7 +2470,7 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
         moff.push_back(msize);
         msize += int64_t(nl.dim[j]) * olink.dim[osec[j]];
     }
-    env->t1.alloc(size_t(std::max<int64_t>(msize, 1)) * 8, st);
+    env->t1.alloc(size_t(std::max<int64_t>(msize, 1)) * 8 * np, st);
     std::vector<ExtractDesc> ed;
     for (int b = 0, j = 0; b < sv_lay.nblk(); ++b) {
         if (D.kept[b] == 0) continue;
@@ -2412,7 +2501,17 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     const double inv = (prm->normalize && D.norm > 0) ? 1.0 / D.norm : 1.0;
     const int e0 = ctx->timer.mark();
     // "left": U stays (ortho 0), S V^T to the bond matrix; "right": V^T stays (ortho 1)
-    if (left)
+    if (psi->cplx && left)
+        launch_svd_extract_complex(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(),
+                                   env->svdV.d(), env->svdS.d(), env->svdPerm.as<int>(),
+                                   here.buf.d(), here.lay.size, env->t1.d(), msize, TN_ORTHO_LEFT,
+                                   inv, st);
+    else if (psi->cplx)
+        launch_svd_extract_complex(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(),
+                                   env->svdV.d(), env->svdS.d(), env->svdPerm.as<int>(),
+                                   env->t1.d(), msize, here.buf.d(), here.lay.size,
+                                   TN_ORTHO_RIGHT, inv, st);
+    else if (left)
         launch_svd_extract(env->desc2.as<ExtractDesc>(), (int)ed.size(), env->svdW.d(), env->svdV.d(),
                            env->svdS.d(), env->svdPerm.as<int>(), here.buf.d(), env->t1.d(),
                            TN_ORTHO_LEFT, inv, st);
@@ -2421,6 +2520,77 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
                            env->svdS.d(), env->svdPerm.as<int>(), env->t1.d(), here.buf.d(),
                            TN_ORTHO_RIGHT, inv, st);
     ctx->timer.add(T_SVD, e0, ctx->timer.mark());
+    if (time_step) {
+        // reverse step (update_site.jl:175-182): the bond matrix C between the new link and
+        // the old one evolves by -time_step under the zero-site H_eff, whose left (right)
+        // environment contains the new site for ortho "left" ("right")
+        const int64_t n0 = msize * np;
+        env->vecA.alloc(size_t(std::max<int64_t>(n0, 1)) * 8, st);
+        env->vecB.alloc(size_t(std::max<int64_t>(n0, 1)) * 8, st);
+        if (n0) TN_CUDA(cudaMemcpyAsync(env->vecA.p, env->t1.p, size_t(n0) * 8,
+                                        cudaMemcpyDeviceToDevice, st));
+        const int li = left ? p + 1 : p;
+        std::swap(psi->sites[p], here);
+        const Link saved = psi->links[li];
+        psi->links[li] = nl;
+        if (left) env_left_step(env, p);
+        else env_right_step(env, p);
+        const tn_envt& EL = left ? env->L[p + 1] : env->L[p];
+        const tn_envt& ER = left ? env->R[p] : env->R[p - 1];
+        std::vector<int> xs, ys;
+        for (size_t j = 0; j < osec.size(); ++j) {
+            xs.push_back(left ? int(j) : osec[j]);
+            ys.push_back(left ? osec[j] : int(j));
+        }
+        Heff0Plan H0;
+        build_heff0(EL, ER, left ? nl : olink, left ? olink : nl, xs, ys, moff, H0);
+        GemmPlan c1, c2;
+        if (psi->cplx) {
+            c1 = complex_plan(H0.g1, 0);
+            c2 = complex_plan(H0.g2, 0);
+            c1.finalize(st);
+            c2.finalize(st);
+        } else {
+            H0.g1.finalize(st);
+            H0.g2.finalize(st);
+        }
+        env->cx.alloc(size_t(std::max<int64_t>(H0.tsize, 1)) * 8 * np, st);
+        auto apply0 = [&](const double* x, double* y) {
+            Bases bs{};
+            bs.p[S_L] = EL.buf.d();
+            bs.p[S_R] = ER.buf.d();
+            bs.p[S_X] = const_cast<double*>(x);
+            bs.p[S_Y] = y;
+            bs.p[S_T1] = env->cx.d();
+            const int h0 = ctx->timer.mark();
+            if (psi->cplx) {
+                set_im(bs, S_L, EL.lay.size);
+                set_im(bs, S_R, ER.lay.size);
+                set_im(bs, S_X, msize);
+                set_im(bs, S_Y, msize);
+                set_im(bs, S_T1, H0.tsize);
+                launch_gemm_f64(c1, bs, st);
+                launch_gemm_f64(c2, bs, st);
+            } else {
+                launch_gemm_f64(H0.g1, bs, st);
+                launch_gemm_f64(H0.g2, bs, st);
+            }
+            ctx->timer.add(T_HEFF, h0, ctx->timer.mark());
+            env->matvecs++;
+        };
+        const int64_t mv0 = env->matvecs;
+        krylov_exp(env, apply0, n0, -*time_step, env->vecA.d(), env->vecB.d(), prm, -time_im,
+                   psi->cplx ? msize : 0);
+        res->energy = normalize_and_energy(env, apply0, n0, env->vecB.d(), env->vecA.d(),
+                                           prm->normalize != 0);
+        res->matvecs += int32_t(env->matvecs - mv0);
+        env->t1.alloc(size_t(std::max<int64_t>(msize, 1)) * 8 * np, st);
+        if (n0) TN_CUDA(cudaMemcpyAsync(env->t1.p, env->vecB.p, size_t(n0) * 8,
+                                        cudaMemcpyDeviceToDevice, st));
+        std::swap(psi->sites[p], here);
+        psi->links[li] = saved;
+        sync(ctx);  // the zero-site plans go out of scope
+    }
     // next site: RG (blocks per left sector) for "left", LG (per right sector) for "right"
     const int q = left ? p + 1 : p - 1;
     tn_site& nxt = psi->sites[q];
@@ -2430,13 +2600,13 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
     DevBuf oldbuf;
     const double* oldp = nxt.buf.d();
     if (nxt.lay.layout != nlay_old.layout) {
-        oldbuf.alloc(size_t(std::max<int64_t>(nlay_old.size, 1)) * 8, st);
-        regroup(ctx, nxt.lay, nxt.buf.d(), nlay_old, oldbuf.d(), qa, qb);
+        oldbuf.alloc(size_t(std::max<int64_t>(nlay_old.size, 1)) * 8 * np, st);
+        regroup(ctx, nxt.lay, nxt.buf.d(), nlay_old, oldbuf.d(), qa, qb, np);
         oldp = oldbuf.d();
     }
     tn_site nnew;
     nnew.lay = left ? make_site_layout(RG, nl, qb, psi->pq) : make_site_layout(LG, qa, nl, psi->pq);
-    nnew.buf.alloc(size_t(std::max<int64_t>(nnew.lay.size, 1)) * 8, st);
+    nnew.buf.alloc(size_t(std::max<int64_t>(nnew.lay.size, 1)) * 8 * np, st);
     GemmPlan g;
     for (size_t j = 0; j < osec.size(); ++j) {
         const int sec = osec[j], k = nl.dim[j], D0 = olink.dim[sec];
@@ -2454,14 +2624,24 @@ void update_one_site(tn_env* env, int p, int ortho, const tn_update_params* prm,
             g.add_seg(S_A, nlay_old.off[sec], rows, 0, S_X, moff[j], D0, 0, D0);
         }
     }
+    GemmPlan gc;
     if (!g.tasks.empty()) {
-        g.finalize(st);
         Bases bs{};
         bs.p[S_X] = env->t1.d();
         bs.p[S_A] = const_cast<double*>(oldp);
         bs.p[S_Y] = nnew.buf.d();
         const int e1 = ctx->timer.mark();
-        launch_gemm_f64(g, bs, st);  // the small bond matrix is multiplied in FP64
+        if (psi->cplx) {
+            set_im(bs, S_X, msize);
+            set_im(bs, S_A, nlay_old.size);
+            set_im(bs, S_Y, nnew.lay.size);
+            gc = complex_plan(g, 0);
+            gc.finalize(st);
+            launch_gemm_f64(gc, bs, st);
+        } else {
+            g.finalize(st);
+            launch_gemm_f64(g, bs, st);  // the small bond matrix is multiplied in FP64
+        }
         ctx->timer.add(T_SVD, e1, ctx->timer.mark());
     }
     psi->sites[p] = std::move(here);
@@ -3371,16 +3551,15 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     } else {
         // one-site sweep (src/mps/sweep.jl:118-152 with nsite = 1): sites 1..N left, then
         // N..1 right; lasteigs[bond] comes from the right-moving update at site bond + 1
-        TN_REQUIRE(!time_step, "one-site TDVP is not built");
         for (int q = 0; q < N; ++q) {
             tn_update_result r{};
-            update_one_site(env, q, TN_ORTHO_LEFT, p, &r, ev);
+            update_one_site(env, q, TN_ORTHO_LEFT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
         }
         for (int q = N - 1; q >= 0; --q) {
             tn_update_result r{};
-            update_one_site(env, q, TN_ORTHO_RIGHT, p, &r, ev);
+            update_one_site(env, q, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
             if (q == N / 2) mid = ev;
@@ -3454,6 +3633,19 @@ int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn
         if (tau_im != 0.0) env_to_complex(env);
         const double half = 0.5 * tau_re;
         full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half, 2, 0.5 * tau_im);
+    });
+}
+
+int tn_env_tdvpsweep_nsite(tn_env* env, int nsite, double tau_re, double tau_im,
+                           const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
+                           int mid_cap, int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(env, "null argument");
+        TN_REQUIRE(nsite == 1 || nsite == 2, "nsite must be 1 or 2");
+        TN_REQUIRE(std::isfinite(tau_re) && std::isfinite(tau_im), "time step must be finite");
+        if (tau_im != 0.0) env_to_complex(env);
+        const double half = 0.5 * tau_re;
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half, nsite, 0.5 * tau_im);
     });
 }
 

@@ -6,7 +6,9 @@ restatement and the exact quench (tests/golden/quench_sz.json).
 Tolerances: the complex H_eff product 1e-12 relative; complex overlaps and local expectation
 values 1e-12; per sweep <S^z_i(t)> within 1e-8 of the oracle (the TDVP observable bound),
 energies 1e-10 relative, bond dimensions and link charges bit-exact; against the exact
-evolution 1e-6 (the TDVP projection error of the small bond dimensions, as for the oracle)."""
+evolution 1e-6 (the TDVP projection error of the small bond dimensions, as for the oracle).
+One-site TDVP (nsite = 1, zero-site reverse step), real and complex steps: per sweep energies
+1e-10, entropy 1e-9, <S^z_i> 1e-8, bond dimensions and link charges exact."""
 import json
 import os
 
@@ -101,3 +103,31 @@ def test_real_time_quench_matches_oracle_and_exact(tn, precision):
         assert np.array_equal(psi.link_charges(i), eo.psi.links[i]), i
     assert abs(psi.inner(psi) - 1.0) < 1e-12
     assert eng.abstime == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("tau", [-0.1, -0.05j])
+def test_one_site_tdvp_matches_oracle(tn, ctx, tau):
+    """tdvpsweep! with nsite = 1 (one-site updates with the zero-site reverse step) after
+    three two-site sweeps that grow the bonds, real and complex steps, against the oracle."""
+    N = 10
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+    po = O.product_mps(start, O.SPIN_HALF_Q)
+    if isinstance(tau, complex):
+        po.A = [a.astype(np.complex128) for a in po.A]
+    eo = O.StateEnvs(po, H)
+    so = O.SweepData()
+    eng = tn.TDVPEngine(tn.MPS.product(start, np.array([1, -1], dtype=np.int32), ctx),
+                        upload_mpo(tn, ctx, H))
+    for nsite in (2, 2, 2, 1, 1, 1, 1):
+        O.tdvp_sweep(eo, so, tau, 16, 1e-12, krylovdim=30, nsite=nsite)
+        tn.tdvpsweep_(eng, tau, nsite=nsite, maxdim=16, cutoff=1e-12, solver_krylovdim=30)
+        assert abs(eng.getenergy() - so.energy[-1]) <= 1e-10 * abs(so.energy[-1]), nsite
+        assert eng.maxchi() == so.maxchi[-1]
+        assert abs(eng.getentropy() - so.entropy[-1]) < 1e-9
+        psi = eng.getpsi()
+        sz = np.array(tn.measure(psi, "Sz"))
+        assert np.abs(sz - O.expect_local(eo.psi, SZ)).max() < 1e-8
+    for i in range(N + 1):
+        assert np.array_equal(psi.link_charges(i), eo.psi.links[i]), i
+    assert abs(psi.inner(psi) - 1.0) < 1e-12

@@ -339,3 +339,40 @@ def test_oracle_excited_state_projector(nsite):
             O.fullsweep1(ex, sx, 32, 1e-14, 1, 5, 2, 1e-14)
     assert abs(sx.energy[-1] - ev[1]) < 1e-8
     assert abs(O.inner(ex.psi, gr)) < 1e-6
+
+
+def test_oracle_one_site_tdvp_is_exact_at_full_rank():
+    """One-site TDVP (tdvpsweep! with nsite = 1: _update_one_site! with exp_solver and the
+    zero-site reverse step, src/mps/update_site.jl:94-190) has no projection error when every
+    bond has full rank: from a full-rank N = 6 state (two-site real-time sweeps) five sweeps of
+    tau = -0.1i and of tau = -0.1 reproduce exp(-i H t) psi and exp(-H t) psi / |.| of the
+    dense Hamiltonian (t = 0.5) to 1e-11, and the real-time sweeps conserve the energy."""
+    import scipy.linalg as sl
+    from tests.helpers import dense_mpo
+    N = 6
+    H = O.heisenberg_mpo(N)
+    D = dense_mpo(H)
+    psi = O.product_mps([0 if i % 2 == 0 else 1 for i in range(N)], O.SPIN_HALF_Q)
+    psi.A = [a.astype(np.complex128) for a in psi.A]
+    env = O.StateEnvs(psi, H)
+    sw = O.SweepData()
+    for _ in range(6):
+        O.tdvp_sweep(env, sw, -0.3j, 8, 1e-14)
+    assert [len(q) for q in env.psi.links] == [1, 2, 4, 8, 4, 2, 1]
+
+    def dense(m):
+        v = m.A[0]
+        for a in m.A[1:]:
+            v = np.tensordot(v, a, axes=([-1], [0]))
+        return v.reshape(-1)
+
+    psi0 = dense(env.psi)
+    for tau, ref in ((-0.1j, sl.expm(-0.5j * D) @ psi0), (-0.1, sl.expm(-0.5 * D) @ psi0)):
+        e = O.StateEnvs(env.psi, H)
+        s = O.SweepData()
+        for _ in range(5):
+            O.tdvp_sweep(e, s, tau, 64, 1e-14, nsite=1)
+        ref = ref / np.linalg.norm(ref)
+        assert np.abs(dense(e.psi) - ref).max() < 1e-11
+        if isinstance(tau, complex):
+            assert np.ptp(s.energy) < 1e-12
