@@ -627,11 +627,14 @@ QUENCH_CPU_BONDS = 6
 
 
 def run_quench(tn, local, args):
-    """Complex TDVP sweeps on the GPU (FP64 complex contractions, realified block SVD) and the
-    oracle's complex restatement timed on a bounded sample of the same sweep."""
+    """Complex TDVP sweeps on the GPU from one prepared state, in split precision (complex
+    H_eff products through the bf16-slice tensor-core GEMM, unsigned complex form) and in
+    FP64 (DFMA), and the oracle's complex restatement timed on a bounded sample of the same
+    sweep.  Environment updates, the realified block SVD and the Krylov exponential are FP64
+    on both paths."""
     import numpy as np
     N = QUENCH_N
-    ctx = tn.Context(local)
+    ctx = tn.Context(local, precision="split", slices=args.slices)
     W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
     H = tn.MPO(W, delta, pq, ctx)
     eng = tn.TDVPEngine(tn.MPS.product(tn.models.neel_states(N), pq, ctx), H)
@@ -641,31 +644,51 @@ def run_quench(tn, local, args):
         tn.tdvpsweep_(eng, -1j * QUENCH_PREP_DT, **kw)
     prep = time.perf_counter() - t0
     psi0 = eng.getpsi()
-    chi0 = int(psi0.maxlinkdim())
-    sweeps = []
-    for _ in range(max(args.steps, 1)):
-        tn.tdvpsweep_(eng, -1j * QUENCH_DT, **kw)
-        st = eng.swdata.stats[-1]
-        sweeps.append({"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
-                       "svd_s": st["svd_ms"] / 1e3, "env_s": st["env_ms"] / 1e3,
-                       "krylov_s": st["lanczos_ms"] / 1e3, "matvecs": st["matvecs"],
-                       "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
-                       "maxlinkdim": eng.maxchi(), "energy": eng.getenergy()})
-    psi = eng.getpsi()
-    sz = np.array(tn.measure(psi, "Sz"))
+    del eng
     e_neel = -0.25 * (N - 1)  # <Neel| sum S_i . S_i+1 |Neel>, conserved by the evolution
     out = {"workload": f"heisenberg_chain_N{N}_neel_quench_tau-{QUENCH_DT}i_maxdim{QUENCH_CHI}"
                        f"_cutoff{QUENCH_CUTOFF:g}_krylov{QUENCH_KRYLOV}",
            "dtype": "c128 (planar complex FP64)",
            "prepare": f"{QUENCH_PREP_SWEEPS} untimed sweeps of tau = -{QUENCH_PREP_DT}i (t = "
                       f"{QUENCH_PREP_SWEEPS * QUENCH_PREP_DT:g})",
-           "prepare_s": prep, "chi_start": chi0, "timed_sweeps": sweeps,
-           "sweep_s_mean": sum(x["sweep_s"] for x in sweeps) / len(sweeps),
-           "energy_drift_rel": abs(sweeps[-1]["energy"] - e_neel) / abs(e_neel),
-           "total_sz": float(sz.sum()), "norm": abs(psi.inner(psi))}
+           "prepare_s": prep, "chi_start": int(psi0.maxlinkdim())}
+    final = {}
+    for prec in ("split", "fp64"):
+        ctx.set_precision(prec, args.slices)
+        e = tn.TDVPEngine(psi0, H)
+        sweeps = []
+        for _ in range(max(args.steps, 1)):
+            tn.tdvpsweep_(e, -1j * QUENCH_DT, **kw)
+            st = e.swdata.stats[-1]
+            sweeps.append({"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
+                           "gemm_s": st["gemm_ms"] / 1e3, "svd_s": st["svd_ms"] / 1e3,
+                           "env_s": st["env_ms"] / 1e3, "krylov_s": st["lanczos_ms"] / 1e3,
+                           "matvecs": st["matvecs"],
+                           "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
+                           "maxlinkdim": e.maxchi(), "energy": e.getenergy()})
+        psi = e.getpsi()
+        final[prec] = psi
+        out[prec] = {"timed_sweeps": sweeps,
+                     "sweep_s_mean": sum(x["sweep_s"] for x in sweeps) / len(sweeps),
+                     "heff_s_mean": sum(x["heff_s"] for x in sweeps) / len(sweeps),
+                     "energy_drift_rel": abs(sweeps[-1]["energy"] - e_neel) / abs(e_neel),
+                     "sz": [float(v) for v in tn.measure(psi, "Sz")],
+                     "norm": abs(psi.inner(psi))}
+        del e
+    ctx.set_precision("split", args.slices)
+    ps, pd = final["split"], final["fp64"]
+    out["max_sz_diff_split_fp64"] = float(np.abs(np.array(out["split"]["sz"]) -
+                                                 np.array(out["fp64"]["sz"])).max())
+    out["total_sz"] = float(sum(out["split"]["sz"]))
+    out["overlap_split_fp64"] = abs(ps.inner(pd))
+    out["same_bond_dims"] = ps.linkdims() == pd.linkdims()
+    out["speedup_sweep_split_vs_fp64"] = out["fp64"]["sweep_s_mean"] / out["split"]["sweep_s_mean"]
+    out["speedup_heff_split_vs_fp64"] = out["fp64"]["heff_s_mean"] / out["split"]["heff_s_mean"]
+    for prec in ("split", "fp64"):
+        del out[prec]["sz"]
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = quench_cpu_sample(psi0)
-        out["speedup_vs_cpu_port"] = out["cpu_baseline"]["value"] / out["sweep_s_mean"]
+        out["speedup_vs_cpu_port"] = out["cpu_baseline"]["value"] / out["split"]["sweep_s_mean"]
     return out
 
 

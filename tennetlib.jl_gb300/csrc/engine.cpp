@@ -145,7 +145,7 @@ void make_trivial_env(tn_ctx* ctx, tn_envt& E, const Link& link, const std::vect
     E.lay = make_env_layout(link, delta);
     TN_REQUIRE(E.lay.size == 1, "boundary link and boundary MPO link must have dimension 1");
     E.buf.alloc(sizeof(double) * planes, ctx->stream);
-    const double one[2] = {1.0, 0.0};
+    const double one[3] = {1.0, 0.0, 0.0};
     TN_CUDA(cudaMemcpyAsync(E.buf.p, one, sizeof(double) * planes, cudaMemcpyHostToDevice,
                             ctx->stream));
     TN_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -153,6 +153,31 @@ void make_trivial_env(tn_ctx* ctx, tn_envt& E, const Link& link, const std::vect
 
 // the imaginary plane of a complex buffer of `plane` values per plane into slot s + S_IM
 void set_im(Bases& bs, int slot, int64_t plane) { bs.p[slot + S_IM] = bs.p[slot] + plane; }
+
+// planes of an environment buffer: 1 (real), 3 (complex: re, im, -im)
+int env_planes(const tn_mps* psi) { return psi->cplx ? 3 : 1; }
+
+// a complex plan with every segment positive: a negative segment reads the negated
+// imaginary plane of one of its operands from slot negslot[s] (s its real slot) instead
+std::unique_ptr<GemmPlan> unsigned_plan(const GemmPlan& c, const int (&negslot)[S_IM]) {
+    auto u = std::make_unique<GemmPlan>();
+    for (const Task& t : c.tasks) {
+        u->add_task(t.cbuf, t.coff, t.m, t.n, t.ldc, t.accum);
+        for (int j = 0; j < t.nseg; ++j) {
+            Seg sg = c.segs[size_t(t.seg0 + j)];
+            if (sg.sgn < 0) {
+                if (sg.abuf >= S_IM && negslot[sg.abuf - S_IM] >= 0)
+                    sg.abuf = negslot[sg.abuf - S_IM];
+                else if (sg.bbuf >= S_IM && negslot[sg.bbuf - S_IM] >= 0)
+                    sg.bbuf = negslot[sg.bbuf - S_IM];
+                else
+                    TN_REQUIRE(false, "internal: no negated plane for a negative segment");
+            }
+            u->add_seg(sg.abuf, sg.aoff, sg.lda, sg.ta, sg.bbuf, sg.boff, sg.ldb, sg.tb, sg.k, 1);
+        }
+    }
+    return u;
+}
 
 bool need_left(const tn_mpo* H, int site, int a, int s) {
     for (int b = 0; b < H->wd[site + 1]; ++b)
@@ -435,7 +460,8 @@ void env_left_step(tn_env* env, int i) {
     const int np = env->psi->planes();
     env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8 * np, st);
     env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8 * np, st);
-    Lout.buf.alloc(size_t(std::max<int64_t>(Lout.lay.size, 1)) * 8 * np, st);
+    Lout.buf.alloc(size_t(std::max<int64_t>(Lout.lay.size, 1)) * 8 * env_planes(env->psi.get()),
+                     st);
     Bases bs{};
     bs.p[S_L] = env->L[i].buf.d();
     bs.p[S_X] = A.buf.d();
@@ -457,6 +483,8 @@ void env_left_step(tn_env* env, int i) {
         launch_gemm_f64(c1, bs, st);
         launch_combine(cc, bs, st);
         launch_gemm_f64(c3, bs, st);
+        launch_scale_into(Lout.buf.d() + 2 * Lout.lay.size, Lout.buf.d() + Lout.lay.size,
+                          nullptr, -1.0, Lout.lay.size, st);
     } else {
         g1.finalize(st);
         g3.finalize(st);
@@ -547,7 +575,8 @@ void env_right_step(tn_env* env, int i) {
     const int np = env->psi->planes();
     env->t1.alloc(size_t(std::max<int64_t>(t1, 1)) * 8 * np, st);
     env->t2.alloc(size_t(std::max<int64_t>(t2, 1)) * 8 * np, st);
-    Rout.buf.alloc(size_t(std::max<int64_t>(Rout.lay.size, 1)) * 8 * np, st);
+    Rout.buf.alloc(size_t(std::max<int64_t>(Rout.lay.size, 1)) * 8 * env_planes(env->psi.get()),
+                     st);
     Bases bs{};
     bs.p[S_R] = env->R[i].buf.d();
     bs.p[S_X] = B.buf.d();
@@ -569,6 +598,8 @@ void env_right_step(tn_env* env, int i) {
         launch_gemm_f64(c1, bs, st);
         launch_combine(cc, bs, st);
         launch_gemm_f64(c3, bs, st);
+        launch_scale_into(Rout.buf.d() + 2 * Rout.lay.size, Rout.buf.d() + Rout.lay.size,
+                          nullptr, -1.0, Rout.lay.size, st);
     } else {
         g1.finalize(st);
         g3.finalize(st);
@@ -757,15 +788,36 @@ void heff_apply(tn_env* env, Heff2Plan& P, const double* x, double* y) {
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
     if (env->psi->cplx) {
-        set_im(bs, S_L, env->L[env->pos].lay.size);
-        set_im(bs, S_R, env->R[env->pos + 1].lay.size);
+        const int64_t ls = env->L[env->pos].lay.size, rs = env->R[env->pos + 1].lay.size;
+        set_im(bs, S_L, ls);
+        set_im(bs, S_R, rs);
         set_im(bs, S_X, P.ph.size);
         set_im(bs, S_Y, P.ph.size);
         set_im(bs, S_T1, P.ysize);
         set_im(bs, S_T2, P.zsize);
-        launch_gemm_f64(P.g1c, bs, ctx->stream);
-        launch_combine(P.cbc, bs, ctx->stream);
-        launch_gemm_f64(P.g3c, bs, ctx->stream);
+        if (ctx->prec == TN_PREC_SPLIT) {
+            // unsigned forms: -Im L and -Im R (third environment planes) in slots S_A, S_B
+            bs.p[S_A] = bs.p[S_L] + 2 * ls;
+            bs.p[S_B] = bs.p[S_R] + 2 * rs;
+            if (!P.s1c) {
+                const int nl[S_IM] = {S_A, -1, -1, -1, -1, -1, -1, -1};
+                const int nr[S_IM] = {-1, S_B, -1, -1, -1, -1, -1, -1};
+                auto u1 = unsigned_plan(P.g1c, nl);
+                auto u3 = unsigned_plan(P.g3c, nr);
+                P.s1c = make_split(*u1, ctx->slices, true, false, ctx->stream);   // A = L
+                P.s3c = make_split(*u3, ctx->slices, false, true, ctx->stream);   // B = R
+            }
+            int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+            run_split(ctx, *P.s1c, bs, &a0, &a1);
+            launch_combine(P.cbc, bs, ctx->stream);
+            run_split(ctx, *P.s3c, bs, &b0, &b1);
+            ctx->timer.add(T_GEMM, a0, a1);
+            ctx->timer.add(T_GEMM, b0, b1);
+        } else {
+            launch_gemm_f64(P.g1c, bs, ctx->stream);
+            launch_combine(P.cbc, bs, ctx->stream);
+            launch_gemm_f64(P.g3c, bs, ctx->stream);
+        }
         ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
         env->matvecs++;
         env->heff_flops += P.flops;
@@ -926,15 +978,36 @@ void heff1_apply(tn_env* env, Heff1Plan& P, const double* x, double* y) {
     bs.p[S_T2] = env->t2.d();
     const int e0 = ctx->timer.mark();
     if (env->psi->cplx) {
-        set_im(bs, S_L, env->L[env->pos].lay.size);
-        set_im(bs, S_R, env->R[env->pos].lay.size);
+        const int64_t ls = env->L[env->pos].lay.size, rs = env->R[env->pos].lay.size;
+        set_im(bs, S_L, ls);
+        set_im(bs, S_R, rs);
         set_im(bs, S_X, P.lay.size);
         set_im(bs, S_Y, P.lay.size);
         set_im(bs, S_T1, P.ysize);
         set_im(bs, S_T2, P.zsize);
-        launch_gemm_f64(P.g1c, bs, ctx->stream);
-        launch_combine(P.cbc, bs, ctx->stream);
-        launch_gemm_f64(P.g3c, bs, ctx->stream);
+        if (ctx->prec == TN_PREC_SPLIT) {
+            // unsigned forms: -Im L and -Im R (third environment planes) in slots S_A, S_B
+            bs.p[S_A] = bs.p[S_L] + 2 * ls;
+            bs.p[S_B] = bs.p[S_R] + 2 * rs;
+            if (!P.s1c) {
+                const int nl[S_IM] = {S_A, -1, -1, -1, -1, -1, -1, -1};
+                const int nr[S_IM] = {-1, S_B, -1, -1, -1, -1, -1, -1};
+                auto u1 = unsigned_plan(P.g1c, nl);
+                auto u3 = unsigned_plan(P.g3c, nr);
+                P.s1c = make_split(*u1, ctx->slices, true, false, ctx->stream);   // A = L
+                P.s3c = make_split(*u3, ctx->slices, false, true, ctx->stream);   // B = R
+            }
+            int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+            run_split(ctx, *P.s1c, bs, &a0, &a1);
+            launch_combine(P.cbc, bs, ctx->stream);
+            run_split(ctx, *P.s3c, bs, &b0, &b1);
+            ctx->timer.add(T_GEMM, a0, a1);
+            ctx->timer.add(T_GEMM, b0, b1);
+        } else {
+            launch_gemm_f64(P.g1c, bs, ctx->stream);
+            launch_combine(P.cbc, bs, ctx->stream);
+            launch_gemm_f64(P.g3c, bs, ctx->stream);
+        }
         ctx->timer.add(T_HEFF, e0, ctx->timer.mark());
         env->matvecs++;
         env->heff_flops += P.flops;
@@ -2709,9 +2782,9 @@ void env_to_complex(tn_env* e) {
             if (!E.buf.p) continue;
             const int64_t n = E.lay.size;
             DevBuf b;
-            b.alloc(size_t(std::max<int64_t>(n, 1)) * 16, st);
+            b.alloc(size_t(std::max<int64_t>(n, 1)) * 24, st);  // re, im = 0, -im = 0
             if (n) TN_CUDA(cudaMemcpyAsync(b.p, E.buf.p, size_t(n) * 8, cudaMemcpyDeviceToDevice, st));
-            TN_CUDA(cudaMemsetAsync(b.d() + n, 0, size_t(std::max<int64_t>(n, 1)) * 8, st));
+            TN_CUDA(cudaMemsetAsync(b.d() + n, 0, size_t(std::max<int64_t>(n, 1)) * 16, st));
             E.buf = std::move(b);
         }
     e->hp.reset();
@@ -3284,8 +3357,8 @@ int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out) {
         const int N = psi->N;
         e->L.resize(N);
         e->R.resize(N);
-        make_trivial_env(e->ctx, e->L[0], psi->links[0], H->delta[0], psi->planes());
-        make_trivial_env(e->ctx, e->R[N - 1], psi->links[N], H->delta[N], psi->planes());
+        make_trivial_env(e->ctx, e->L[0], psi->links[0], H->delta[0], env_planes(psi));
+        make_trivial_env(e->ctx, e->R[N - 1], psi->links[N], H->delta[N], env_planes(psi));
         e->lpos = 0;
         e->rpos = N - 1;
         e->pos = 0;

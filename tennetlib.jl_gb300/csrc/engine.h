@@ -149,6 +149,7 @@ struct Heff2Plan {
     tn::GemmPlan g1c, g3c;  // complex forms (complex states)
     tn::CombPlan cbc;
     std::unique_ptr<tn::SplitPlan> s1, s3;  // split-precision plans (built on first use)
+    std::unique_ptr<tn::SplitPlan> s1c, s3c;  // the same of the complex forms (unsigned)
     tn::CombPlan cb;
     int64_t ysize = 0, zsize = 0;
     double flops = 0;
@@ -166,6 +167,7 @@ struct Heff1Plan {
     tn::GemmPlan g1c, g3c;  // complex forms (complex states)
     tn::CombPlan cbc;
     std::unique_ptr<tn::SplitPlan> s1, s3;
+    std::unique_ptr<tn::SplitPlan> s1c, s3c;  // the same of the complex forms (unsigned)
     int64_t ysize = 0, zsize = 0;
     double flops = 0;
 };
@@ -192,7 +194,9 @@ struct tn_env {
     tn_ctx* ctx = nullptr;
     std::unique_ptr<tn_mps> psi;
     const tn_mpo* H = nullptr;
-    std::vector<tn_envt> L, R;  // planar complex (two planes) when psi is complex
+    // planar complex when psi is complex: real, imaginary and negated imaginary planes (the
+    // third lets every segment of the complex H_eff be a positive product)
+    std::vector<tn_envt> L, R;
     int lpos = 0, rpos = 0;
     int pos = 0, nsite = 2;
     // work buffers

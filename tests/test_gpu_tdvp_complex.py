@@ -3,7 +3,8 @@
 of src/mps/update_site.jl:78-87) on ComplexF64 states, against the oracle's complex
 restatement and the exact quench (tests/golden/quench_sz.json).
 
-Tolerances: the complex H_eff product 1e-12 relative; complex overlaps and local expectation
+Tolerances: the complex H_eff product 1e-12 relative (5e-11 in split precision, as for real
+states); complex overlaps and local expectation
 values 1e-12; per sweep <S^z_i(t)> within 1e-8 of the oracle (the TDVP observable bound),
 energies 1e-10 relative, bond dimensions and link charges bit-exact; against the exact
 evolution 1e-6 (the TDVP projection error of the small bond dimensions, as for the oracle).
@@ -50,6 +51,12 @@ def test_complex_product_overlap_and_expectation(tn, ctx):
         ref = eo.product2(p, v)
         got = eg.product(v)
         assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref), p
+        # the split-precision complex product (bf16-slice tensor-core GEMMs, unsigned form)
+        cs = tn.Context(0, precision="split", slices=5)
+        es = tn.StateEnvs(upload_mps(tn, cs, m, p), upload_mpo(tn, cs, H))
+        es.position_(p, 2)
+        got = es.product(v)
+        assert np.linalg.norm(got - ref) <= 5e-11 * np.linalg.norm(ref), p
     # overlap of two complex states on the same links (a conjugated)
     rng = np.random.default_rng(7)
     a = _complex_mps(N, 1)
@@ -105,10 +112,12 @@ def test_real_time_quench_matches_oracle_and_exact(tn, precision):
     assert eng.abstime == pytest.approx(1.0)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split"])
 @pytest.mark.parametrize("tau", [-0.1, -0.05j])
-def test_one_site_tdvp_matches_oracle(tn, ctx, tau):
+def test_one_site_tdvp_matches_oracle(tn, tau, precision):
     """tdvpsweep! with nsite = 1 (one-site updates with the zero-site reverse step) after
     three two-site sweeps that grow the bonds, real and complex steps, against the oracle."""
+    ctx = tn.Context(0, precision=precision, slices=5)
     N = 10
     H = O.heisenberg_mpo(N)
     start = [0 if i % 2 == 0 else 1 for i in range(N)]
