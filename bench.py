@@ -657,13 +657,16 @@ def run_quench(tn, local, args):
         ctx.set_precision(prec, args.slices)
         e = tn.TDVPEngine(psi0, H)
         sweeps = []
+        # kernel launches of this library before the path's first timed sweep (the offset of
+        # an ncu launch-list capture of that sweep)
+        out[f"launches_before_{prec}"] = int(ctx.lib.tn_kernel_launches())
         for _ in range(max(args.steps, 1)):
             tn.tdvpsweep_(e, -1j * QUENCH_DT, **kw)
             st = e.swdata.stats[-1]
             sweeps.append({"sweep_s": st["sweep_ms"] / 1e3, "heff_s": st["heff_ms"] / 1e3,
                            "gemm_s": st["gemm_ms"] / 1e3, "svd_s": st["svd_ms"] / 1e3,
                            "env_s": st["env_ms"] / 1e3, "krylov_s": st["lanczos_ms"] / 1e3,
-                           "matvecs": st["matvecs"],
+                           "matvecs": st["matvecs"], "kernel_launches": st["kernel_launches"],
                            "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
                            "maxlinkdim": e.maxchi(), "energy": e.getenergy()})
         psi = e.getpsi()
