@@ -669,9 +669,11 @@ def run_quench(tn, local, args):
                            "matvecs": st["matvecs"], "kernel_launches": st["kernel_launches"],
                            "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
                            "maxlinkdim": e.maxchi(), "energy": e.getenergy()})
+            if len(sweeps) == 1:
+                first_sz = [float(v) for v in tn.measure(e.getpsi(), "Sz")]
         psi = e.getpsi()
         final[prec] = psi
-        out[prec] = {"timed_sweeps": sweeps,
+        out[prec] = {"timed_sweeps": sweeps, "first_sz": first_sz,
                      "sweep_s_mean": sum(x["sweep_s"] for x in sweeps) / len(sweeps),
                      "heff_s_mean": sum(x["heff_s"] for x in sweeps) / len(sweeps),
                      "energy_drift_rel": abs(sweeps[-1]["energy"] - e_neel) / abs(e_neel),
@@ -687,19 +689,27 @@ def run_quench(tn, local, args):
     out["same_bond_dims"] = ps.linkdims() == pd.linkdims()
     out["speedup_sweep_split_vs_fp64"] = out["fp64"]["sweep_s_mean"] / out["split"]["sweep_s_mean"]
     out["speedup_heff_split_vs_fp64"] = out["fp64"]["heff_s_mean"] / out["split"]["heff_s_mean"]
+    if not args.no_cpu_baseline:
+        cb = quench_cpu_sample(psi0)
+        # the GPU's first sweep from psi0 (split path) against the oracle's sweep from psi0
+        sp = out["split"]
+        out["vs_cpu"] = {"max_sz_diff": float(np.abs(np.array(sp["first_sz"]) -
+                                                     np.array(cb.pop("sz"))).max()),
+                         "dE_rel": abs(sp["timed_sweeps"][0]["energy"] - cb["energy"]) /
+                                   abs(cb["energy"]),
+                         "same_bond_dims": sp["timed_sweeps"][0]["maxlinkdim"] == cb["maxlinkdim"]}
+        out["cpu_baseline"] = cb
+        out["speedup_vs_cpu_port"] = cb["value"] / out["split"]["sweep_s_mean"]
     for prec in ("split", "fp64"):
         del out[prec]["sz"]
-    if not args.no_cpu_baseline:
-        out["cpu_baseline"] = quench_cpu_sample(psi0)
-        out["speedup_vs_cpu_port"] = out["cpu_baseline"]["value"] / out["split"]["sweep_s_mean"]
+        del out[prec]["first_sz"]
     return out
 
 
-def quench_cpu_sample(psi, budget_s=20.0):
-    """The oracle's complex TDVP updates of the left-moving half sweep from the same state
-    (right environments built untimed), bond after bond until budget_s is spent; the sweep
-    time is estimated as twice (the measured bonds + the remaining bonds of the half sweep at
-    the mean time of the last four measured), the right-moving half being the mirror image."""
+def quench_cpu_sample(psi):
+    """One full complex TDVP sweep of the oracle (numpy FP64) from the same state on the host
+    cores (right environments built untimed): its time, and its <S^z_i>, energy and bond
+    dimension for the comparison with the GPU's first sweep from that state."""
     import numpy as np
     from oracle import tn_oracle as O
     N = psi.N
@@ -708,21 +718,16 @@ def quench_cpu_sample(psi, budget_s=20.0):
                O.SPIN_HALF_Q.copy(), center=0)
     env = O.StateEnvs(st, O.heisenberg_mpo(N))
     env.position(0, 2)
-    times = []
-    for b in range(N - 1):
-        t0 = time.perf_counter()
-        O.update_two_site_tdvp(env, b, "left", -0.5j * QUENCH_DT, QUENCH_CHI, 1, QUENCH_CUTOFF,
-                               QUENCH_KRYLOV, 100, 1e-12, True)
-        times.append(time.perf_counter() - t0)
-        if sum(times) > budget_s:
-            break
-    last = sum(times[-4:]) / len(times[-4:])
-    est = 2 * (sum(times) + (N - 1 - len(times)) * last)
-    return {"value": est, "unit": "s/sweep", "cores": cores(), "kind": "port", "dense": True,
-            "sample": f"the first {len(times)} of the {N - 1} updates of the left-moving half "
-                      f"sweep ({sum(times):.1f} s, numpy FP64 complex oracle, dense tensors with "
-                      "charge labels) from the same state; the rest of the half sweep at the "
-                      "mean time of the last four, times two for the right-moving half"}
+    sw = O.SweepData()
+    t0 = time.perf_counter()
+    O.tdvp_sweep(env, sw, -1j * QUENCH_DT, QUENCH_CHI, QUENCH_CUTOFF, 1, QUENCH_KRYLOV, 100, 1e-12)
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s/sweep", "cores": cores(), "kind": "port", "dense": True,
+            "energy": sw.energy[-1], "maxlinkdim": int(env.psi.maxlinkdim()),
+            "sz": [float(v) for v in O.expect_local(env.psi, np.diag([0.5, -0.5]))],
+            "sample": f"one full complex two-site TDVP sweep ({2 * (N - 1)} bond updates) of the "
+                      "numpy FP64 oracle (dense tensors with charge labels; OpenBLAS threads = "
+                      "all host cores) from the same state"}
 
 
 # one bond's charge blocks at chi ~ 2048 (the sizes of the largest bond of the 6 x 16 J1-J2

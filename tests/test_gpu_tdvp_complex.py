@@ -9,7 +9,9 @@ values 1e-12; per sweep <S^z_i(t)> within 1e-8 of the oracle (the TDVP observabl
 energies 1e-10 relative, bond dimensions and link charges bit-exact; against the exact
 evolution 1e-6 (the TDVP projection error of the small bond dimensions, as for the oracle).
 One-site TDVP (nsite = 1, zero-site reverse step), real and complex steps: per sweep energies
-1e-10, entropy 1e-9, <S^z_i> 1e-8, bond dimensions and link charges exact."""
+1e-10, entropy 1e-9, <S^z_i> 1e-8, bond dimensions and link charges exact.  At the scale of
+the real-time workload (N = 64, chi ~ 60, one sweep from a GPU-evolved state): energy
+1e-10, <S^z_i> 1e-8, link charges exact."""
 import json
 import os
 
@@ -140,3 +142,33 @@ def test_one_site_tdvp_matches_oracle(tn, tau, precision):
     for i in range(N + 1):
         assert np.array_equal(psi.link_charges(i), eo.psi.links[i]), i
     assert abs(psi.inner(psi) - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_quench_at_scale_matches_oracle(tn, precision):
+    """The config-4 chain (N = 64, maxdim 512, cutoff 1e-9, krylovdim 30): a state evolved on
+    the GPU to t = 2.5 (10 sweeps of tau = -0.25i), copied to the oracle, then the same sweep
+    of tau = -0.05i on both."""
+    ctx = tn.Context(0, precision=precision, slices=5)
+    N = 64
+    W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
+    H = tn.MPO(W, delta, pq, ctx)
+    eng = tn.TDVPEngine(tn.MPS.product(tn.models.neel_states(N), pq, ctx), H)
+    kw = dict(maxdim=512, cutoff=1e-9, solver_krylovdim=30)
+    for _ in range(10):
+        tn.tdvpsweep_(eng, -0.25j, **kw)
+    psi0 = eng.getpsi()
+    assert psi0.maxlinkdim() >= 16
+    po = O.MPS([psi0.site(i) for i in range(N)],
+               [psi0.link_charges(i).astype(np.int64) for i in range(N + 1)],
+               O.SPIN_HALF_Q.copy(), center=0)
+    eo = O.StateEnvs(po, O.heisenberg_mpo(N))
+    so = O.SweepData()
+    O.tdvp_sweep(eo, so, -0.05j, 512, 1e-9, 1, 30, 100, 1e-12)
+    e2 = tn.TDVPEngine(psi0, H)
+    tn.tdvpsweep_(e2, -0.05j, **kw)
+    psi = e2.getpsi()
+    assert abs(e2.getenergy() - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
+    assert np.abs(np.array(tn.measure(psi, "Sz")) - O.expect_local(eo.psi, SZ)).max() < 1e-8
+    for i in range(N + 1):
+        assert np.array_equal(psi.link_charges(i), eo.psi.links[i]), i
