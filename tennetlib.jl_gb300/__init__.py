@@ -832,7 +832,7 @@ def checkpoint_arrays(tensors, links, phys_q, center, swdata: SweepData | None =
     out = {"phys_q": np.asarray(phys_q, dtype=np.int32), "center": np.int64(center),
            "nsites": np.int64(len(tensors))}
     for i, t in enumerate(tensors):
-        t = np.asarray(t, dtype=np.float64)
+        t = np.asarray(t, dtype=np.complex128 if np.iscomplexobj(t) else np.float64)
         out[f"shape_{i}"] = np.array(t.shape, dtype=np.int64)
         out[f"blocks_{i}"] = t[_charge_mask(links[i], phys_q, links[i + 1])]
     for i, q in enumerate(links):
@@ -856,8 +856,9 @@ def arrays_from_checkpoint(z) -> tuple:
     links = [np.asarray(z[f"link_{i}"], dtype=np.int32) for i in range(n + 1)]
     tensors = []
     for i in range(n):
-        t = np.zeros(tuple(int(x) for x in z[f"shape_{i}"]))
-        t[_charge_mask(links[i], pq, links[i + 1])] = z[f"blocks_{i}"]
+        b = z[f"blocks_{i}"]
+        t = np.zeros(tuple(int(x) for x in z[f"shape_{i}"]), dtype=b.dtype)
+        t[_charge_mask(links[i], pq, links[i + 1])] = b
         tensors.append(t)
     sw = None
     if "sw_sweepcount" in z:

@@ -283,6 +283,11 @@ def test_checkpoint_arrays_round_trip():
     assert sw2.stats == [{"sweep_ms": 1.0}]
     # only the allowed entries are stored
     assert sum(v.size for k, v in z.items() if k.startswith("blocks_")) < sum(t.size for t in tensors)
+    # a complex state (real-time evolution) keeps its imaginary parts
+    ct = [t + 1j * rng.standard_normal(t.shape) * (t != 0) for t in tensors]
+    t3 = tn.arrays_from_checkpoint(tn.checkpoint_arrays(ct, links, pq, 0, None))[0]
+    for a, b in zip(ct, t3):
+        assert b.dtype == np.complex128 and np.array_equal(a, b)
 
 
 def test_oracle_noise_term():
