@@ -18,9 +18,16 @@ Plain numpy FP64 restatement of TenNetLib's TTN ground-state path (no charge con
   ``src/ttn/state_envs_ttn.jl:120-141``
 * ``update_position!`` with ``eig_solver`` -- ``src/ttn/update_site_ttn.jl:42-63``,
   ``src/base/solver.jl:23-43``
-* ``fullsweep!`` (noise = 0 branch: path then reversed path, cutoff = -1) and
-  ``default_sweeppath`` -- ``src/ttn/sweep_ttn.jl:49-65``, ``:117-274``
-* ``optimize!`` stage loop -- ``src/ttn/optimize_ttn.jl:148-226``
+* ``fullsweep!`` (noise = 0 branch: path then reversed path, cutoff = -1; noise > 0
+  branch: position with ``node_to_skip``, ``subspace_expand!`` toward the central node and
+  ``expand_numiter`` updates with the widened maxdims) and ``default_sweeppath`` --
+  ``src/ttn/sweep_ttn.jl:49-65``, ``:117-274``, ``src/ttn/update_site_ttn.jl:75-109``
+* ``optimize!`` stage loop with the noise schedule -- ``src/ttn/optimize_ttn.jl:148-226``
+
+Subspace-expansion padding: the reference draws it with ``random_itensor`` (Julia's RNG,
+normal entries); here it is a counter-based stream shared bit for bit with the engine
+(splitmix64, uniform entries in [-1, 1), ``padding_values``), then scaled to
+noise * |tensor| as in the reference, so that GPU and oracle expand identically.
 
 Conventions shared with the engine (``include/tennet.h``):
 
@@ -47,7 +54,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from oracle.tn_oracle import eigsolve_lowest, svd_blocks_truncate
+from oracle.tn_oracle import FLOAT64_THRESHOLD, eigsolve_lowest, svd_blocks_truncate
 
 PAULI_X = np.array([[0.0, 1.0], [1.0, 0.0]])
 PAULI_Z = np.array([[1.0, 0.0], [0.0, -1.0]])
@@ -522,6 +529,50 @@ class SweepDataTTN:
     energy: list = field(default_factory=list)
 
 
+# --------------------------------------------------------------------------------------
+# subspace expansion (noise > 0)
+# --------------------------------------------------------------------------------------
+
+def _splitmix64(x):
+    """splitmix64 of a uint64 array (wrapping arithmetic)."""
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    z = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def padding_values(seed, event, instance, which, n):
+    """n values in [-1, 1): value j is the top 53 bits of splitmix64(key + j) scaled, with
+    key = splitmix64(seed + 2 (4096 event + instance) + which) (which: 0 for the node's
+    padding, 1 for the next node's) -- the engine's stream, bit for bit."""
+    with np.errstate(over="ignore"):
+        base = np.array([seed], dtype=np.uint64) + np.array(
+            [2 * (4096 * event + instance) + which], dtype=np.uint64)
+        key = _splitmix64(base)
+        x = _splitmix64(key + np.arange(n, dtype=np.uint64))
+    return (x >> np.uint64(11)).astype(np.float64) * 2.0 ** -52 - 1.0
+
+
+def subspace_expand(psi: TTN, node, nextnode, max_expand_dim, noise, seed, event, instance=0):
+    """``subspace_expand!`` (src/ttn/update_site_ttn.jl:75-109): the link (node, nextnode)
+    grows by pad = min(sum of the other leg dims of each tensor, max_expand_dim)
+    (``indexintersection``, src/base/helper_internal_funcs.jl:182-188); each tensor gets a
+    random block along it scaled to noise * its norm (direct sum, old components first)."""
+    A, B = psi.tensors[node], psi.tensors[nextnode]
+    la, lb = psi.leg_index(node, nextnode), psi.leg_index(nextnode, node)
+    pad = min(sum(A.shape) - A.shape[la], sum(B.shape) - B.shape[lb], max_expand_dim)
+    if pad <= 0:
+        return 0
+    for which, (v, T, leg) in enumerate(((node, A, la), (nextnode, B, lb))):
+        shp = list(T.shape)
+        shp[leg] = pad
+        P = padding_values(seed, event, instance, which, int(np.prod(shp))).reshape(shp,
+                                                                                    order="F")
+        P *= noise * np.linalg.norm(T) / np.linalg.norm(P)
+        psi.tensors[v] = np.concatenate([T, P], axis=leg)
+    return pad
+
+
 class StateEnvsTTN:
     """``StateEnvsTTN(psi, M)`` (state_envs_ttn.jl:27-31); with ``Ms`` and ``weight`` the
     projected environment ``EnvCouplingModelProjTTN`` (src/ttn/environment.jl:44-110):
@@ -538,14 +589,19 @@ class StateEnvsTTN:
                                  f"`weight={weight}`)")
             self.proj = [LinkProj(self.psi, M) for M in Ms]
             self.weight = float(weight)
+        self.expand_events = 0  # subspace expansions so far (the padding stream's counter)
 
-    def position(self, node, normalize=True, maxdim=2**62, mindim=1, cutoff=1e-15):
-        """``position!`` (state_envs_ttn.jl:120-141)."""
+    def position(self, node, normalize=True, maxdim=2**62, mindim=1, cutoff=1e-15,
+                 node_to_skip=None):
+        """``position!`` (state_envs_ttn.jl:120-141); the link moves out of
+        ``node_to_skip`` are left out (``move_linktensors!``, linktensors.jl:130-154)."""
         oc = self.psi.center
         isometrize(self.psi, node, normalize=normalize, maxdim=maxdim, mindim=mindim,
                    cutoff=cutoff)
         path = shortest_path(self.psi.adj, oc, node)
         for a, b in zip(path[:-1], path[1:]):
+            if a == node_to_skip:
+                continue
             self.env.move_to_next(self.psi, a, b)
             for P in self.proj:
                 P.move_to_next(self.psi, a, b)
@@ -571,24 +627,75 @@ def update_position(se: StateEnvsTTN, node, maxdim=2**62, mindim=1, cutoff=-1.0,
 
 
 def fullsweep(se: StateEnvsTTN, path, sw: SweepDataTTN, maxdim=2**62, mindim=1,
-              krylovdim=5, maxiter=2, tol=1e-14):
-    """``fullsweep!`` (sweep_ttn.jl:117-274), noise = 0 branch."""
+              krylovdim=5, maxiter=2, tol=1e-14, noise=0.0, cutoff=FLOAT64_THRESHOLD,
+              expand_dim=None, max_expand_dim=None, expand_numiter=4, seed=0):
+    """``fullsweep!`` (sweep_ttn.jl:117-274).  noise below 100 Float64_threshold: every node
+    of path and of the reversed path is updated with cutoff = -1 (QR moves).  Otherwise each
+    node but the eccentric central one is expanded toward the central node: position there
+    (QR moves, the link move out of the next node left out), ``subspace_expand!`` of the
+    link, the centre set to the next node, then expand_numiter updates alternating node and
+    next node with maxdims maxdim + max_expand_dim, maxdim + expand_dim, ..., maxdim and the
+    given cutoff (SVD moves)."""
     sw.sweepcount += 1
     e = float("nan")
-    for node in list(path) + list(reversed(path)):
-        e, _ = update_position(se, node, maxdim=maxdim, mindim=mindim, cutoff=-1.0,
-                               krylovdim=krylovdim, maxiter=maxiter, tol=tol)
+    kw = dict(krylovdim=krylovdim, maxiter=maxiter, tol=tol)
+    if abs(noise) < 100 * FLOAT64_THRESHOLD:
+        for node in list(path) + list(reversed(path)):
+            e, _ = update_position(se, node, maxdim=maxdim, mindim=mindim, cutoff=-1.0, **kw)
+    else:
+        if expand_dim is None:
+            expand_dim = 20
+        if max_expand_dim is None:
+            max_expand_dim = 2 * expand_dim
+        if expand_dim != 0 and expand_numiter < 2:
+            raise ValueError(f"`fullsweep!()`: `expand_numiter={expand_numiter}` cannot be "
+                             f"less than 2 for `expand_dim={expand_dim}` !!")
+        adj = se.psi.adj
+        central = eccentric_center(adj)
+        for node in list(path) + list(reversed(path)):
+            if node == central:
+                e, _ = update_position(se, node, maxdim=maxdim, mindim=mindim, cutoff=-1.0,
+                                       **kw)
+                continue
+            nxt = shortest_path(adj, node, central)[1]
+            se.position(node, normalize=True, maxdim=maxdim, mindim=mindim, cutoff=-1.0,
+                        node_to_skip=nxt)
+            subspace_expand(se.psi, node, nxt, max_expand_dim, noise, seed, se.expand_events)
+            se.expand_events += 1
+            se.psi.center = nxt
+            for it in range(1, expand_numiter + 1):
+                md = (maxdim if it == expand_numiter else
+                      maxdim + max_expand_dim if it == 1 else maxdim + expand_dim)
+                e, _ = update_position(se, node if it % 2 == 1 else nxt, maxdim=md,
+                                       mindim=mindim, cutoff=cutoff, **kw)
     sw.maxchi.append(se.psi.maxlinkdim())
     sw.energy.append(e)
     return (sw.energy[-1] - sw.energy[-2]) if sw.sweepcount > 1 else float("nan")
 
 
-def optimize(se: StateEnvsTTN, maxdims, nsweeps, path, energy_err_goal=None, **kw):
-    """``optimize!`` (optimize_ttn.jl:148-226) with noise 0."""
+def optimize(se: StateEnvsTTN, maxdims, nsweeps, path, energy_err_goal=None, cutoff=None,
+             noise=0.0, noisedecay=1.0, disable_noise_after=2**62, **kw):
+    """``optimize!`` (optimize_ttn.jl:148-226): stages of (maxdim, nsweeps) with the noise
+    schedule (noise divided by noisedecay after each sweep, zero after disable_noise_after
+    sweeps of a stage or below 100 Float64_threshold)."""
     sw = SweepDataTTN()
-    for md, ns in zip(maxdims, nsweeps):
-        for _ in range(ns):
-            de = fullsweep(se, path, sw, maxdim=md, **kw)
-            if energy_err_goal is not None and abs(de) < abs(energy_err_goal):
+    n = len(nsweeps)
+
+    def vec(x):
+        return list(x) if isinstance(x, (list, tuple)) else [x] * n
+
+    cutoffs = vec(FLOAT64_THRESHOLD if cutoff is None else cutoff)
+    noises, decays, offs = vec(noise), vec(noisedecay), vec(disable_noise_after)
+    for ii, (md, ns) in enumerate(zip(maxdims, nsweeps)):
+        nz = noises[ii]
+        for jj in range(1, ns + 1):
+            de = fullsweep(se, path, sw, maxdim=md, noise=nz, cutoff=cutoffs[ii], **kw)
+            if (energy_err_goal is not None and abs(de) < abs(energy_err_goal)
+                    and abs(nz) < FLOAT64_THRESHOLD):
                 break
+            if jj == offs[ii]:
+                nz = 0.0
+            nz /= decays[ii]
+            if nz < 100 * FLOAT64_THRESHOLD:
+                nz = 0.0
     return sw

@@ -112,3 +112,31 @@ def test_ttn_oracle_excited_state_projector():
     assert abs(sx.energy[-1] - ev[1]) < 1e-8
     ov = float(np.vdot(T.ttn_to_dense(ex.psi), T.ttn_to_dense(gs)))
     assert abs(ov) < 1e-6
+
+
+def test_ttn_oracle_subspace_expansion_grows_bonds_to_exact():
+    """fullsweep! with noise > 0 (subspace_expand!, src/ttn/update_site_ttn.jl:75-109, and the
+    noisy branch of src/ttn/sweep_ttn.jl:180-243), as in the reference's own TTN test
+    (test/test_TTN.jl:26-48: a chi = 12 random TTN, maxdim 128, cutoff 1e-14, noise 1e-2,
+    noisedecay 5, noise off after 2 sweeps): the bonds grow beyond the initial 12 and the
+    Heisenberg N = 12 ground energy and, with the ground state projected out (weight 10),
+    the second eigenvalue of the dense Hamiltonian are reached.  The padding stream is
+    deterministic: the same seed gives the same sweep."""
+    N = 12
+    terms = T.heisenberg_terms(N)
+    ev = np.linalg.eigvalsh(T.dense_hamiltonian(N, terms))
+    path = T.default_sweeppath(N, T.default_graph_sitenodes(N)[0].keys())
+    kw = dict(cutoff=1e-14, noise=1e-2, noisedecay=5, disable_noise_after=2, seed=7)
+    se = T.StateEnvsTTN(T.random_ttn(N, 12, 1), terms)
+    sw = T.optimize(se, [128], [5], path, **kw)
+    assert sw.maxchi[0] > 12
+    assert abs(sw.energy[-1] - ev[0]) < 1e-10
+    se2 = T.StateEnvsTTN(T.random_ttn(N, 12, 1), terms)
+    sw2 = T.optimize(se2, [128], [5], path, **kw)
+    assert sw2.energy == sw.energy and sw2.maxchi == sw.maxchi
+    ex = T.StateEnvsTTN(T.random_ttn(N, 12, 2), terms, [se.psi], weight=10.0)
+    sx = T.optimize(ex, [128], [10], path, cutoff=1e-14, noise=1e-2, noisedecay=5,
+                    disable_noise_after=6, seed=8)
+    assert abs(sx.energy[-1] - ev[1]) < 1e-8
+    vals = T.padding_values(7, 3, 1, 0, 5)
+    assert vals.min() >= -1.0 and vals.max() < 1.0 and len(set(vals.tolist())) == 5
