@@ -357,6 +357,19 @@ int tn_ttn_env_update_position(tn_ttn_env* env, int node, const tn_update_params
  * receives each environment's energy and maxlinkdim; the timings are of the whole group. */
 int tn_ttn_envs_fullsweep(int count, tn_ttn_env* const* envs, int npath, const int32_t* path,
                           const tn_update_params* p, tn_sweep_result* res);
+/* fullsweep! with noise = p->noise > 0 (src/ttn/sweep_ttn.jl:180-243): every node of path and
+ * of the reversed path but `central` (find_eccentric_central_node) is first made the centre
+ * (QR moves, the link move out of its next node toward `central` left out), the link to
+ * that next node is widened by subspace_expand! (src/ttn/update_site_ttn.jl:75-109; at most
+ * max_expand_dim, padding scaled to noise * |tensor|), and expand_numiter updates alternate
+ * between the two nodes with maxdims maxdim + max_expand_dim, maxdim + expand_dim, ...,
+ * maxdim and cutoff p->cutoff (truncating SVD moves).  The padding is a counter-based stream
+ * keyed by `seed`, the instance and the expansion count (the reference draws it from Julia's
+ * RNG).  The group's arena grows when the widened tensors need room. */
+int tn_ttn_envs_fullsweep_expand(int count, tn_ttn_env* const* envs, int npath,
+                                 const int32_t* path, int central, const tn_update_params* p,
+                                 int expand_dim, int max_expand_dim, int expand_numiter,
+                                 uint64_t seed, tn_sweep_result* res);
 
 /* ---- allocation-free block singular values ----------------------------------------
  * No counterpart in the reference.  For callers that cannot let the library allocate

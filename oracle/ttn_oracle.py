@@ -628,7 +628,7 @@ def update_position(se: StateEnvsTTN, node, maxdim=2**62, mindim=1, cutoff=-1.0,
 
 def fullsweep(se: StateEnvsTTN, path, sw: SweepDataTTN, maxdim=2**62, mindim=1,
               krylovdim=5, maxiter=2, tol=1e-14, noise=0.0, cutoff=FLOAT64_THRESHOLD,
-              expand_dim=None, max_expand_dim=None, expand_numiter=4, seed=0):
+              expand_dim=None, max_expand_dim=None, expand_numiter=4, seed=0, instance=0):
     """``fullsweep!`` (sweep_ttn.jl:117-274).  noise below 100 Float64_threshold: every node
     of path and of the reversed path is updated with cutoff = -1 (QR moves).  Otherwise each
     node but the eccentric central one is expanded toward the central node: position there
@@ -660,7 +660,8 @@ def fullsweep(se: StateEnvsTTN, path, sw: SweepDataTTN, maxdim=2**62, mindim=1,
             nxt = shortest_path(adj, node, central)[1]
             se.position(node, normalize=True, maxdim=maxdim, mindim=mindim, cutoff=-1.0,
                         node_to_skip=nxt)
-            subspace_expand(se.psi, node, nxt, max_expand_dim, noise, seed, se.expand_events)
+            subspace_expand(se.psi, node, nxt, max_expand_dim, noise, seed, se.expand_events,
+                            instance)
             se.expand_events += 1
             se.psi.center = nxt
             for it in range(1, expand_numiter + 1):

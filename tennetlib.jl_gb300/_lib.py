@@ -165,6 +165,9 @@ PROTOS = {
                                              C.POINTER(UpdateResult)]),
     "tn_ttn_envs_fullsweep": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, i32p,
                                         C.POINTER(UpdateParams), C.POINTER(SweepResult)]),
+    "tn_ttn_envs_fullsweep_expand": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, i32p, C.c_int,
+                                               C.POINTER(UpdateParams), C.c_int, C.c_int,
+                                               C.c_int, C.c_uint64, C.POINTER(SweepResult)]),
 }
 
 _lib = None

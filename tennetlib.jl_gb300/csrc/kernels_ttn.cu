@@ -142,6 +142,21 @@ __global__ void __launch_bounds__(BT) permute_kernel(const PermDesc* __restrict_
     }
 }
 
+__global__ void __launch_bounds__(BT) concat_kernel(const ConcatDesc* __restrict__ descs) {
+    const ConcatDesc& D = descs[blockIdx.y];
+    const int64_t Dt = D.D1 + D.D2;
+    const int64_t total = D.P * Dt * D.Q;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
+        const int64_t p = e % D.P;
+        const int64_t r = e / D.P;
+        const int64_t k = r % Dt;
+        const int64_t q = r / Dt;
+        D.dst[e] = k < D.D1 ? D.a[p + D.P * (k + D.D1 * q)]
+                            : D.b[p + D.P * ((k - D.D1) + D.D2 * q)];
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // Householder reflector of x = (alpha, tail), LAPACK dlarfg convention:
 //   H = I - tau v v^T, v = (1, tail * scale), H x = (beta, 0).
@@ -752,6 +767,13 @@ void launch_blincomb(const BLinDesc* d, int ninst, int64_t nmax, cudaStream_t s)
 void launch_permute(const PermDesc* d, int ninst, int64_t nmax, cudaStream_t s) {
     if (ninst <= 0) return;
     permute_kernel<<<dim3(grid_x(nmax, 4 * TTN_PARTS), ninst), BT, 0, s>>>(d);
+    TN_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+void launch_concat(const ConcatDesc* d, int ninst, int64_t nmax, cudaStream_t s) {
+    if (ninst <= 0) return;
+    concat_kernel<<<dim3(grid_x(nmax, 4 * TTN_PARTS), ninst), BT, 0, s>>>(d);
     TN_CUDA(cudaGetLastError());
     count_launch();
 }

@@ -295,6 +295,11 @@ struct tn_ttn_env {
     int kry_vecs = 0;
     int nchunk_t = 1;                 // k chunks of the link-tensor contractions
     int nchunk_q = 1;                 // k chunks of the QR panel products
+    // slot capacities (elements per node slot, link dimension per edge slot); grow_group
+    // raises them when subspace expansion needs room, empty: the creation sizes
+    std::vector<int64_t> node_cap;
+    std::vector<int> link_cap;
+    int64_t expand_events = 0;        // subspace expansions so far (the padding stream's counter)
     // excited-state projectors (none when empty): H_eff x + proj_weight sum_k m_k (m_k . x)
     std::vector<TtnProj> proj;
     double proj_weight = 0;
@@ -310,6 +315,7 @@ struct TtnGroup {
     std::vector<tn_ttn_env*> envs;  // members in creation order (null once destroyed)
     int alive = 0;
     DevBuf arena, work, packs, tickets, scal, bpart, bars;
+    DevBuf pads, d_cat;  // subspace-expansion padding and its direct-sum descriptors
     DevBuf d_gs, d_sc, d_lin, d_perm, d_qr, d_hh;  // descriptor tables of the batched kernels
     int work_kd = 0;
     std::map<int, std::unique_ptr<ProductPlan>> pcache;
@@ -509,7 +515,8 @@ void build_arena_layout(tn_ttn_env* e, int64_t& cursor) {
     e->dmax = 1;
     for (int v = 0; v < t.nn; ++v) {
         e->node_off[v] = cursor;
-        const int64_t n = vol(e->dims[v]);
+        int64_t n = vol(e->dims[v]);
+        if (size_t(v) < e->node_cap.size()) n = std::max(n, e->node_cap[size_t(v)]);
         cursor += (n + 31) / 32 * 32;
         e->S = std::max(e->S, n);
         for (int x : e->dims[v]) e->dmax = std::max(e->dmax, x);
@@ -538,6 +545,8 @@ void build_arena_layout(tn_ttn_env* e, int64_t& cursor) {
         const int a = t.edges[ei].first, b = t.edges[ei].second;
         const auto sa = t.side(a, b);  // sites on a's side
         es.cap_dim = e->dims[a][t.leg_nbr(a, b)];
+        if (ei < e->link_cap.size()) es.cap_dim = std::max(es.cap_dim, e->link_cap[ei]);
+        e->dmax = std::max(e->dmax, es.cap_dim);
         for (size_t ti = 0; ti < e->model.terms.size(); ++ti) {
             int ina = 0;
             for (int s : e->model.terms[ti].sites) ina += sa[s];
@@ -1138,8 +1147,9 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
             to.push_back(PermDesc{aptr(G, e->node_off[v]), A, P, n, Qd, 1, 0});
         }
         nmax = std::max(nmax, vol(dv));
-        // a link larger than maxdim: truncating SVD move (moveisometry_to_next!, ttn.jl:292-300)
-        truncate[i] = n > maxdim;
+        // cutoff > 0 or a link larger than maxdim: truncating SVD move (moveisometry_to_next!,
+        // ttn.jl:292-300)
+        truncate[i] = n > maxdim || cutoff > 0.0;
         if (truncate[i]) continue;
         const bool blk = m * n > SMALL_QR && m >= n;
         blocked[i] = blk;
@@ -1290,13 +1300,18 @@ void run_qr_move(TtnGroup& G, int v, int u, int maxdim, int mindim = 1, double c
 }
 
 // ---- position!, update_position!, fullsweep! ---------------------------------------------
-void position_group(TtnGroup& G, int node, bool normalize, int maxdim) {
+// position! (state_envs_ttn.jl:120-141): isometry moves from the centre to node (QR, or the
+// truncating SVD when cutoff > 0 or a link exceeds maxdim), then the link tensors moved along
+// the same path but out of `skip` (move_linktensors!'s node_to_skip, linktensors.jl:130-154)
+void position_group(TtnGroup& G, int node, bool normalize, int maxdim, int mindim = 1,
+                    double cutoff = -1.0, int skip = -1) {
     auto E = members(G);
     const int oc = E[0]->center;
     for (auto* e : E) TN_REQUIRE(e->center == oc, "TTN: environments of a group have different centres");
     TN_REQUIRE(oc >= 0, "TTN: the state has no orthogonality centre");
     const auto path = E[0]->tree.path(oc, node);
-    for (size_t k = 0; k + 1 < path.size(); ++k) run_qr_move(G, path[k], path[k + 1], maxdim);
+    for (size_t k = 0; k + 1 < path.size(); ++k)
+        run_qr_move(G, path[k], path[k + 1], maxdim, mindim, cutoff);
     if (normalize) {
         std::vector<double*> x;
         std::vector<int64_t> n;
@@ -1307,6 +1322,7 @@ void position_group(TtnGroup& G, int node, bool normalize, int maxdim) {
         normalize_batch(G, E, x, n);
     }
     for (size_t k = 0; k + 1 < path.size(); ++k) {
+        if (path[k] == skip) continue;
         run_link_move(G, path[k], path[k + 1]);
         proj_move_all(G, path[k], path[k + 1]);
     }
@@ -1548,17 +1564,17 @@ void lanczos_group(TtnGroup& G, int node, const tn_update_params* prm) {
     }
 }
 
-void check_ttn_params(const tn_update_params* p) {
+void check_ttn_params(const tn_update_params* p, bool allow_noise = false) {
     TN_REQUIRE(p != nullptr, "null parameters");
-    TN_REQUIRE(p->noise == 0.0,
-               "TTN: noise > 0 (subspace expansion, src/ttn/sweep_ttn.jl:211-262) is not built");
+    TN_REQUIRE(allow_noise || p->noise == 0.0,
+               "TTN: noise > 0 takes the subspace-expansion sweep (tn_ttn_envs_fullsweep_expand)");
     TN_REQUIRE(p->maxiter >= 1 && p->krylovdim >= 1, "bad solver parameters");
 }
 
-void update_group(TtnGroup& G, int node, const tn_update_params* p) {
-    check_ttn_params(p);
+void update_group(TtnGroup& G, int node, const tn_update_params* p, double cutoff = -1.0) {
+    check_ttn_params(p, true);
     ensure_work(G, p->krylovdim);
-    position_group(G, node, p->normalize != 0, p->maxdim);
+    position_group(G, node, p->normalize != 0, p->maxdim, std::max(1, p->mindim), cutoff);
     lanczos_group(G, node, p);
     if (p->check_convergence)
         for (auto* e : members(G))
@@ -1620,6 +1636,8 @@ std::unique_ptr<tn_ttn> copy_out(TtnGroup& G, tn_ttn_env* e) {
 // -------------------------------------------------------------------------------------
 namespace {
 
+void upload_site_ops(TtnGroup& G, tn_ttn_env* e);
+
 std::shared_ptr<TtnGroup> make_group(tn_ctx* ctx, const std::vector<const tn_ttn*>& psis,
                                      const std::vector<const tn_ttn_model*>& models,
                                      std::vector<tn_ttn_env*>& out) {
@@ -1660,27 +1678,7 @@ std::shared_ptr<TtnGroup> make_group(tn_ctx* ctx, const std::vector<const tn_ttn
         for (int v = 0; v < e->tree.nn; ++v)
             TN_CUDA(cudaMemcpyAsync(aptr(*G, e->node_off[v]), p->node[v].p,
                                     size_t(vol(e->dims[v])) * 8, cudaMemcpyDeviceToDevice, st));
-        // site operators: local sums and per-term operators
-        const int dd = e->tree.d * e->tree.d;
-        std::vector<std::vector<double>> loc(e->tree.N);
-        for (size_t ti = 0; ti < e->model.terms.size(); ++ti) {
-            const auto& tm = e->model.terms[ti];
-            for (size_t j = 0; j < tm.sites.size(); ++j) {
-                const int s = tm.sites[j];
-                if (tm.sites.size() == 1) {
-                    if (loc[s].empty()) loc[s].assign(dd, 0.0);
-                    for (int k = 0; k < dd; ++k) loc[s][k] += tm.ops[j][k];
-                } else {
-                    TN_CUDA(cudaMemcpyAsync(aptr(*G, e->sstore[s].open.at(int(ti))), tm.ops[j].data(),
-                                            dd * 8, cudaMemcpyHostToDevice, st));
-                }
-            }
-        }
-        for (int s = 0; s < e->tree.N; ++s)
-            if (!loc[s].empty())
-                TN_CUDA(cudaMemcpyAsync(aptr(*G, e->sstore[s].local), loc[s].data(), dd * 8,
-                                        cudaMemcpyHostToDevice, st));
-        TN_CUDA(cudaStreamSynchronize(st));  // host operator copies go out of scope
+        upload_site_ops(*G, e);  // local sums and per-term operators
     }
     G->alive = int(envs.size());
     ensure_work(*G, 5);
@@ -1721,50 +1719,42 @@ void fill_sweep_result(TtnGroup& G, tn_ttn_env* e, tn_sweep_result* r, int64_t l
     r->krylov_bytes = G.krylov_bytes;
 }
 
-// StateEnvsTTN(psi, H, Ms; weight) (src/ttn/state_envs_ttn.jl:36-52): copies of the Ms and
-// their overlaps built from the leaves toward the centre (LinkProjTTN, linkproj.jl:188-224)
-void proj_setup(TtnGroup& G, tn_ttn_env* e, const tn_ttn* const* Ms, int count, double weight) {
+// Overlap slots, temporaries and projected-vector buffers of every projector of e, sized
+// by the slot capacities of psi (link dimensions only grow through grow_group, which calls
+// this again), and the overlaps rebuilt from the leaves toward the centre (LinkProjTTN,
+// linkproj.jl:188-224).
+void proj_layout_and_build(TtnGroup& G, tn_ttn_env* e) {
+    if (e->proj.empty()) return;
     cudaStream_t st = e->ctx->stream;
     const TtnTree& t = e->tree;
-    TN_CUDA(cudaStreamSynchronize(st));
-    e->proj.clear();
-    e->proj_weight = count > 0 ? weight : 0.0;
-    if (count == 0) return;
     auto r32 = [](int64_t n) { return (n + 31) / 32 * 32; };
+    auto cap_of_leg = [&](int v, int l) {
+        const int ns = int(t.sites[v].size());
+        if (l < ns) return e->dims[v][size_t(l)];
+        return std::max(e->dims[v][size_t(l)], e->estore[t.edge(v, t.nbr[v][l - ns])].cap_dim);
+    };
     int64_t tn = 32;
-    for (int k = 0; k < count; ++k) {
-        const tn_ttn* M = Ms[k];
-        TtnProj P;
-        P.mdims = M->dims;
-        P.moff.assign(t.nn, 0);
-        int64_t c = 0;
+    for (auto& P : e->proj) {
         for (int v = 0; v < t.nn; ++v) {
-            P.moff[v] = c;
-            c += r32(vol(M->dims[v]));
             // a temporary holds M[v] with any subset of its links mapped to psi's dimensions
             int64_t big = 1;
-            for (size_t l = 0; l < M->dims[v].size(); ++l)
-                big *= std::max(M->dims[v][l], e->dims[v][l]);
+            for (size_t l = 0; l < P.mdims[v].size(); ++l)
+                big *= std::max(P.mdims[v][l], cap_of_leg(v, int(l)));
             tn = std::max(tn, big);
         }
-        P.mbuf.alloc(size_t(std::max<int64_t>(c, 32)) * 8, st);
-        for (int v = 0; v < t.nn; ++v)
-            TN_CUDA(cudaMemcpyAsync(P.mbuf.d() + P.moff[v], M->node[v].p,
-                                    size_t(vol(M->dims[v])) * 8, cudaMemcpyDeviceToDevice, st));
-        // psi's link dimensions only shrink while the environment lives: slots sized now fit
-        c = 0;
+        int64_t c = 0;
         P.eoff.assign(t.edges.size(), 0);
         for (size_t ei = 0; ei < t.edges.size(); ++ei) {
             const int a = t.edges[ei].first, b = t.edges[ei].second;
             const int la = t.leg_nbr(a, b);
             P.eoff[ei] = c;
-            c += r32(int64_t(e->dims[a][la]) * M->dims[a][la]);
+            c += r32(int64_t(cap_of_leg(a, la)) * P.mdims[a][la]);
         }
         P.ebuf.alloc(size_t(std::max<int64_t>(c, 32)) * 8, st);
         TN_CUDA(cudaMemsetAsync(P.ebuf.p, 0, P.ebuf.bytes, st));
         P.efrom.assign(t.edges.size(), -1);
-        e->proj.push_back(std::move(P));
     }
+    const int count = int(e->proj.size());
     e->proj_tn = tn;
     e->proj_t1.alloc(size_t(tn) * 8, st);
     e->proj_t2.alloc(size_t(tn) * 8, st);
@@ -1778,6 +1768,285 @@ void proj_setup(TtnGroup& G, tn_ttn_env* e, const tn_ttn* const* Ms, int count, 
         for (auto& P : e->proj) proj_move(G, e, P, v, next);
     }
     TN_CUDA(cudaStreamSynchronize(st));
+}
+
+// StateEnvsTTN(psi, H, Ms; weight) (src/ttn/state_envs_ttn.jl:36-52): copies of the Ms and
+// their overlaps built from the leaves toward the centre (LinkProjTTN, linkproj.jl:188-224)
+void proj_setup(TtnGroup& G, tn_ttn_env* e, const tn_ttn* const* Ms, int count, double weight) {
+    cudaStream_t st = e->ctx->stream;
+    const TtnTree& t = e->tree;
+    TN_CUDA(cudaStreamSynchronize(st));
+    e->proj.clear();
+    e->proj_weight = count > 0 ? weight : 0.0;
+    if (count == 0) return;
+    auto r32 = [](int64_t n) { return (n + 31) / 32 * 32; };
+    for (int k = 0; k < count; ++k) {
+        const tn_ttn* M = Ms[k];
+        TtnProj P;
+        P.mdims = M->dims;
+        P.moff.assign(t.nn, 0);
+        int64_t c = 0;
+        for (int v = 0; v < t.nn; ++v) {
+            P.moff[v] = c;
+            c += r32(vol(M->dims[v]));
+        }
+        P.mbuf.alloc(size_t(std::max<int64_t>(c, 32)) * 8, st);
+        for (int v = 0; v < t.nn; ++v)
+            TN_CUDA(cudaMemcpyAsync(P.mbuf.d() + P.moff[v], M->node[v].p,
+                                    size_t(vol(M->dims[v])) * 8, cudaMemcpyDeviceToDevice, st));
+        e->proj.push_back(std::move(P));
+    }
+    proj_layout_and_build(G, e);
+}
+
+// site operators of an instance into its arena slots: per site the sum of its one-site terms
+// (local) and the operator of every longer term (open)
+void upload_site_ops(TtnGroup& G, tn_ttn_env* e) {
+    cudaStream_t st = G.ctx->stream;
+    const int dd = e->tree.d * e->tree.d;
+    std::vector<std::vector<double>> loc(e->tree.N);
+    for (size_t ti = 0; ti < e->model.terms.size(); ++ti) {
+        const auto& tm = e->model.terms[ti];
+        for (size_t j = 0; j < tm.sites.size(); ++j) {
+            const int s = tm.sites[j];
+            if (tm.sites.size() == 1) {
+                if (loc[s].empty()) loc[s].assign(dd, 0.0);
+                for (int k = 0; k < dd; ++k) loc[s][k] += tm.ops[j][k];
+            } else {
+                TN_CUDA(cudaMemcpyAsync(aptr(G, e->sstore[s].open.at(int(ti))), tm.ops[j].data(),
+                                        dd * 8, cudaMemcpyHostToDevice, st));
+            }
+        }
+    }
+    for (int s = 0; s < e->tree.N; ++s)
+        if (!loc[s].empty())
+            TN_CUDA(cudaMemcpyAsync(aptr(G, e->sstore[s].local), loc[s].data(), dd * 8,
+                                    cudaMemcpyHostToDevice, st));
+    TN_CUDA(cudaStreamSynchronize(st));  // host operator copies go out of scope
+}
+
+// ---- subspace expansion (noise > 0) -------------------------------------------------------
+// The arena re-laid with room for larger tensors: node slots of node_cap[i][v] elements and
+// link slots of link dimension link_cap[i][e] (at least the current sizes); node tensors are
+// copied over, site operators re-uploaded, link tensors and projector overlaps rebuilt from
+// the leaves toward the centre, plans and work buffers dropped.
+void grow_group(TtnGroup& G, const std::vector<std::vector<int64_t>>& node_cap,
+                const std::vector<std::vector<int>>& link_cap) {
+    auto E = members(G);
+    cudaStream_t st = G.ctx->stream;
+    TN_CUDA(cudaStreamSynchronize(st));
+    std::vector<std::vector<int64_t>> old_off(E.size());
+    int64_t cursor = 0;
+    for (size_t i = 0; i < E.size(); ++i) {
+        tn_ttn_env* e = E[i];
+        old_off[i] = e->node_off;
+        e->node_cap = node_cap[i];
+        e->link_cap = link_cap[i];
+        build_arena_layout(e, cursor);  // link slots re-laid: their tensors are rebuilt below
+    }
+    DevBuf na;
+    na.alloc(size_t(std::max<int64_t>(cursor, 32)) * 8, st);
+    TN_CUDA(cudaMemsetAsync(na.p, 0, na.bytes, st));
+    for (size_t i = 0; i < E.size(); ++i) {
+        tn_ttn_env* e = E[i];
+        for (int v = 0; v < e->tree.nn; ++v)
+            TN_CUDA(cudaMemcpyAsync(na.d() + e->node_off[v], G.arena.d() + old_off[i][v],
+                                    size_t(vol(e->dims[v])) * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    TN_CUDA(cudaStreamSynchronize(st));
+    G.arena = std::move(na);
+    for (auto* e : E) upload_site_ops(G, e);
+    G.work_kd = 0;  // work layouts depend on the slot sizes
+    ensure_work(G, 5);
+    ensure_scal(G);
+    G.dims_version++;
+    check_cache(G);
+    build_links(G);
+    for (auto* e : E) proj_layout_and_build(G, e);
+}
+
+// dimension of the largest meaningful state space on one side of edge ei: d^(sites), capped
+int full_link_dim(const TtnTree& t, int ei) {
+    const auto side = t.side(t.edges[ei].first, t.edges[ei].second);
+    int na = 0;
+    for (char c : side) na += c ? 1 : 0;
+    const int nmin = std::min(na, t.N - na);
+    int64_t f = 1;
+    for (int k = 0; k < nmin && f < (int64_t(1) << 30); ++k) f *= t.d;
+    return int(std::min<int64_t>(f, int64_t(1) << 30));
+}
+
+// Capacity for a noisy sweep at maxdim with expansions of up to mx: every link up to
+// max(current, min(maxdim, full)) and one link of a node more by mx (after each expansion
+// the truncating moves bring that link back to maxdim before the next one grows).
+void ensure_expand_capacity(TtnGroup& G, int maxdim, int mx) {
+    auto E = members(G);
+    bool grow = false;
+    std::vector<std::vector<int64_t>> ncap(E.size());
+    std::vector<std::vector<int>> lcap(E.size());
+    for (size_t i = 0; i < E.size(); ++i) {
+        tn_ttn_env* e = E[i];
+        const TtnTree& t = e->tree;
+        std::vector<int> c(t.edges.size());
+        lcap[i].resize(t.edges.size());
+        for (size_t ei = 0; ei < t.edges.size(); ++ei) {
+            const int a = t.edges[ei].first, b = t.edges[ei].second;
+            const int cur = e->dims[a][t.leg_nbr(a, b)];
+            c[ei] = std::max(cur, std::min(maxdim, full_link_dim(t, int(ei))));
+            lcap[i][ei] = std::max(e->estore[ei].cap_dim, int(std::min<int64_t>(
+                                                              int64_t(c[ei]) + mx, INT_MAX)));
+            grow = grow || lcap[i][ei] > e->estore[ei].cap_dim;
+        }
+        ncap[i].resize(t.nn);
+        for (int v = 0; v < t.nn; ++v) {
+            const int ns = int(t.sites[v].size());
+            std::vector<int64_t> leg(size_t(t.nlegs(v)));
+            for (int l = 0; l < t.nlegs(v); ++l)
+                leg[l] = l < ns ? t.d : c[t.edge(v, t.nbr[v][l - ns])];
+            int64_t need = vol(e->dims[v]);
+            for (int l = ns; l < t.nlegs(v); ++l) {
+                double prodv = 1.0;
+                for (int l2 = 0; l2 < t.nlegs(v); ++l2) prodv *= double(l2 == l ? leg[l2] + mx : leg[l2]);
+                TN_REQUIRE(prodv < 4e9, "TTN: subspace expansion needs a node tensor too large "
+                                        "for this engine (lower maxdim or max_expand_dim)");
+                need = std::max(need, int64_t(prodv));
+            }
+            const int64_t have = std::max(vol(e->dims[v]),
+                                          size_t(v) < e->node_cap.size() ? e->node_cap[v] : 0);
+            ncap[i][v] = std::max(need, have);
+            grow = grow || need > have;
+        }
+    }
+    if (grow) grow_group(G, ncap, lcap);
+}
+
+uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// subspace_expand! (src/ttn/update_site_ttn.jl:75-109) of the link (node, nxt) in every
+// member: the link grows by pad = min(sum of the other leg dims of each tensor,
+// max_expand_dim) (indexintersection, src/base/helper_internal_funcs.jl:182-188); each tensor
+// gets a random block along it scaled to noise * its norm (direct sum, old components
+// first).  The padding is the counter-based stream value j = top 53 bits of
+// splitmix64(key + j) mapped to [-1, 1), key = splitmix64(seed + 2 (4096 event + instance) +
+// which), drawn on the host (which: 0 for node, 1 for nxt).
+void expand_group(TtnGroup& G, int node, int nxt, int mx, double noise, uint64_t seed) {
+    auto E = members(G);
+    const TtnTree& t = E[0]->tree;
+    const int la = t.leg_nbr(node, nxt), lb = t.leg_nbr(nxt, node);
+    cudaStream_t st = G.ctx->stream;
+    ensure_scal(G);
+    std::vector<BGsDesc> ga(E.size()), gb(E.size());
+    for (size_t i = 0; i < E.size(); ++i) {
+        tn_ttn_env* e = E[i];
+        ga[i] = BGsDesc{};
+        ga[i].w = aptr(G, e->node_off[node]);
+        ga[i].out = scal_of(G, e->idx) + 66;
+        ga[i].n = vol(e->dims[node]);
+        gb[i] = BGsDesc{};
+        gb[i].w = aptr(G, e->node_off[nxt]);
+        gb[i].out = scal_of(G, e->idx) + 67;
+        gb[i].n = vol(e->dims[nxt]);
+    }
+    gs_launch(G, ga, 1, 0.0, false, true);
+    gs_launch(G, gb, 1, 0.0, false, true);
+    std::vector<double> hs(G.envs.size() * SCAL_PER);
+    TN_CUDA(cudaMemcpyAsync(hs.data(), G.scal.p, hs.size() * 8, cudaMemcpyDeviceToHost, st));
+    TN_CUDA(cudaStreamSynchronize(st));
+    std::vector<double> host;
+    struct Pend {
+        ConcatDesc d;
+        int64_t off;
+    };
+    std::vector<Pend> pend;
+    std::vector<std::pair<tn_ttn_env*, int>> grown;
+    int64_t nmax = 1;
+    for (tn_ttn_env* e : E) {
+        const auto& dA = e->dims[node];
+        const auto& dB = e->dims[nxt];
+        int64_t sa = 0, sb = 0;
+        for (size_t l = 0; l < dA.size(); ++l) sa += int(l) == la ? 0 : dA[l];
+        for (size_t l = 0; l < dB.size(); ++l) sb += int(l) == lb ? 0 : dB[l];
+        const int pad = int(std::min<int64_t>(std::min(sa, sb), mx));
+        if (pad <= 0) continue;
+        for (int which = 0; which < 2; ++which) {
+            const int v = which ? nxt : node, leg = which ? lb : la;
+            const auto& dv = e->dims[v];
+            const int64_t P = prod(dv, 0, leg), D = dv[leg], Q = prod(dv, leg + 1, int(dv.size()));
+            const int64_t np = P * pad * Q;
+            TN_REQUIRE(P * (D + pad) * Q <= std::max(vol(dv), e->node_cap.empty() ? 0 : e->node_cap[v]),
+                       "TTN internal: no room for the subspace expansion");
+            const uint64_t key = splitmix64(seed + uint64_t(2) * (uint64_t(4096) * uint64_t(e->expand_events) +
+                                                                 uint64_t(e->idx)) + uint64_t(which));
+            const int64_t off = int64_t(host.size());
+            double n2 = 0.0;
+            for (int64_t j = 0; j < np; ++j) {
+                const double x = double(splitmix64(key + uint64_t(j)) >> 11) * 0x1p-52 - 1.0;
+                host.push_back(x);
+                n2 += x * x;
+            }
+            const double tn2 = hs[size_t(e->idx) * SCAL_PER + 66 + which];
+            const double scale = n2 > 0.0 ? noise * std::sqrt(std::max(tn2, 0.0)) / std::sqrt(n2) : 0.0;
+            for (int64_t j = 0; j < np; ++j) host[size_t(off + j)] *= scale;
+            // the old tensor to a work temporary, then the direct sum into the node slot
+            double* tmp = wptr(G, e, which ? e->w_rt : e->w_qa);
+            TN_CUDA(cudaMemcpyAsync(tmp, aptr(G, e->node_off[v]), size_t(vol(dv)) * 8,
+                                    cudaMemcpyDeviceToDevice, st));
+            pend.push_back(Pend{ConcatDesc{tmp, nullptr, aptr(G, e->node_off[v]), P, D, pad, Q}, off});
+            nmax = std::max(nmax, P * (D + pad) * Q);
+        }
+        grown.push_back({e, pad});
+    }
+    for (tn_ttn_env* e : E) e->expand_events++;
+    if (pend.empty()) return;
+    G.pads.alloc(std::max<size_t>(host.size(), 1) * 8, st);
+    TN_CUDA(cudaMemcpyAsync(G.pads.p, host.data(), host.size() * 8, cudaMemcpyHostToDevice, st));
+    std::vector<ConcatDesc> cd;
+    for (auto& pd : pend) {
+        pd.d.b = G.pads.d() + pd.off;
+        cd.push_back(pd.d);
+    }
+    upload_descs(G, G.d_cat, cd);
+    launch_concat(G.d_cat.as<ConcatDesc>(), int(cd.size()), nmax, st);
+    for (auto& gp : grown) {
+        gp.first->dims[node][la] += gp.second;
+        gp.first->dims[nxt][lb] += gp.second;
+    }
+    G.dims_version++;
+    TN_CUDA(cudaStreamSynchronize(st));  // the host padding goes out of scope
+}
+
+// fullsweep!'s noise > 0 branch (src/ttn/sweep_ttn.jl:180-243): every node of path and of the
+// reversed path but the central one is expanded toward the central node, then updated
+// expand_numiter times alternately with its next node
+void fullsweep_expand(TtnGroup& G, const std::vector<int>& path, const tn_update_params* p,
+                      int central, int expand_dim, int mx, int numiter, uint64_t seed) {
+    const TtnTree& t = members(G)[0]->tree;
+    ensure_expand_capacity(G, p->maxdim, mx);
+    std::vector<int> order(path);
+    order.insert(order.end(), path.rbegin(), path.rend());
+    for (int node : order) {
+        if (node == central) {
+            update_group(G, node, p);
+            continue;
+        }
+        const int nxt = t.path(node, central)[1];
+        ensure_work(G, p->krylovdim);
+        position_group(G, node, p->normalize != 0, p->maxdim, std::max(1, p->mindim), -1.0, nxt);
+        expand_group(G, node, nxt, mx, p->noise, seed);
+        for (auto* e : members(G)) e->center = nxt;
+        for (int it = 1; it <= numiter; ++it) {
+            tn_update_params q = *p;
+            const int64_t md = it == numiter ? p->maxdim
+                               : int64_t(p->maxdim) + (it == 1 ? mx : expand_dim);
+            q.maxdim = int(std::min<int64_t>(md, INT_MAX));
+            update_group(G, it % 2 == 1 ? node : nxt, &q, p->cutoff);
+        }
+    }
 }
 
 }  // namespace
@@ -2067,6 +2336,52 @@ int tn_ttn_env_update_position(tn_ttn_env* env, int node, const tn_update_params
             res->matvecs = env->matvecs;
             res->converged = env->converged;
         }
+    });
+}
+
+int tn_ttn_envs_fullsweep_expand(int count, tn_ttn_env* const* envs, int npath,
+                                 const int32_t* path, int central, const tn_update_params* p,
+                                 int expand_dim, int max_expand_dim, int expand_numiter,
+                                 uint64_t seed, tn_sweep_result* res) {
+    return guarded([&] {
+        TN_REQUIRE(count >= 1 && envs && envs[0] && path && res, "bad arguments");
+        TtnGroup& G = *envs[0]->grp;
+        TN_REQUIRE(count == G.alive && count == int(G.envs.size()),
+                   "TTN: pass every environment of the group");
+        for (int i = 0; i < count; ++i)
+            TN_REQUIRE(envs[i] == G.envs[i], "TTN: environments must be given in creation order");
+        const TtnTree& t = envs[0]->tree;
+        std::vector<char> seen(t.nn, 0);
+        for (int k = 0; k < npath; ++k) {
+            TN_REQUIRE(path[k] >= 0 && path[k] < t.nn, "sweep path node out of range");
+            seen[path[k]] = 1;
+        }
+        for (int v = 0; v < t.nn; ++v)
+            TN_REQUIRE(seen[v], "the sweep path must contain every node (sweep_ttn.jl:120)");
+        TN_REQUIRE(central >= 0 && central < t.nn, "central node out of range");
+        check_ttn_params(p, true);
+        TN_REQUIRE(p->noise > 0.0 && std::isfinite(p->noise), "noise must be > 0");
+        TN_REQUIRE(expand_dim >= 0 && max_expand_dim >= 0, "expansion dimensions must be >= 0");
+        if (expand_dim != 0 && expand_numiter < 2) {
+            char msg[160];
+            std::snprintf(msg, sizeof msg,
+                          "`fullsweep!()`: `expand_numiter=%d` cannot be less than 2 for "
+                          "`expand_dim=%d` !!", expand_numiter, expand_dim);
+            throw Error(TN_E_INVALID, msg);
+        }
+        TN_REQUIRE(expand_numiter >= 1, "expand_numiter must be >= 1");
+        reset_stats(G);
+        const int64_t l0 = launch_count();
+        const int64_t kb0 = krylov_bytes();
+        const int s0 = G.ctx->timer.mark();
+        fullsweep_expand(G, std::vector<int>(path, path + npath), p, central, expand_dim,
+                         max_expand_dim, expand_numiter, seed);
+        G.ctx->timer.add(T_SWEEP, s0, G.ctx->timer.mark());
+        collect_stats(G);
+        check_device_error_public(G.ctx);
+        const int64_t launches = launch_count() - l0;
+        G.krylov_bytes = double(krylov_bytes() - kb0);
+        for (int i = 0; i < count; ++i) fill_sweep_result(G, envs[i], &res[i], launches);
     });
 }
 

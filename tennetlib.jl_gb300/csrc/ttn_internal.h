@@ -61,6 +61,12 @@ struct PermDesc {                // (P, D, Q) <-> (P, Q, D)
     int64_t P, D, Q;
     int32_t to_end, pad;
 };
+struct ConcatDesc {              // dst (P, D1 + D2, Q) = [a (P, D1, Q) | b (P, D2, Q)]
+    const double* a;
+    const double* b;
+    double* dst;
+    int64_t P, D1, D2, Q;
+};
 struct QrDesc {                  // small QR: A (m x n, ld m) -> Q in place, R out
     double* A;
     double* R;
@@ -100,6 +106,8 @@ void launch_bgs_pass(const BGsDesc* d, int ninst, int kmax, int64_t nmax, double
 void launch_bscale(const BScaleDesc* d, int ninst, int64_t nmax, cudaStream_t s);
 void launch_blincomb(const BLinDesc* d, int ninst, int64_t nmax, cudaStream_t s);
 void launch_permute(const PermDesc* d, int ninst, int64_t nmax, cudaStream_t s);
+// the direct sum of subspace expansion along one leg; nmax >= every P (D1 + D2) Q
+void launch_concat(const ConcatDesc* d, int ninst, int64_t nmax, cudaStream_t s);
 void launch_qr_small(const QrDesc* d, int ninst, cudaStream_t s);
 void launch_hh_column(const HhDesc* d, int ninst, int64_t mmax, int j, int p0, int pend,
                       cudaStream_t s);

@@ -472,18 +472,34 @@ def _stats(r: L.SweepResult):
 
 
 def fullsweep_batch_(envs, sweeppath, solver, swdatas, **kwargs):
-    """``fullsweep!`` (noise = 0) on environments made by ``StateEnvsTTN.batch`` (or one
-    environment), in lockstep; returns the energy changes."""
+    """``fullsweep!`` (src/ttn/sweep_ttn.jl:117-274) on environments made by
+    ``StateEnvsTTN.batch`` (or one environment), in lockstep; returns the energy changes.
+    noise >= 100 Float64_threshold takes the subspace-expansion branch (``expand_dim``
+    default 20, ``max_expand_dim`` 2 expand_dim, ``expand_numiter`` 4, ``cutoff`` the SVD
+    cutoff of its updates, ``seed`` of the padding stream)."""
+    from . import Float64_threshold
     _eig_solver_token(solver)
-    if kwargs.get("noise", 0.0) != 0.0:
-        raise NotImplementedError("subspace expansion (noise > 0) is not built")
     t = envs[0].template
     path = np.array([t.index[v] for v in sweeppath], dtype=np.int32)
     p = _params(kwargs)
     n = len(envs)
     res = (L.SweepResult * n)()
-    L.check(envs[0].ctx.lib.tn_ttn_envs_fullsweep(n, (L.vp * n)(*[e.h for e in envs]), len(path),
-                                                  path.ctypes.data_as(L.i32p), C.byref(p), res))
+    hs = (L.vp * n)(*[e.h for e in envs])
+    noise = float(kwargs.get("noise", 0.0))
+    if abs(noise) < 100 * Float64_threshold():
+        p.noise = 0.0
+        L.check(envs[0].ctx.lib.tn_ttn_envs_fullsweep(n, hs, len(path),
+                                                      path.ctypes.data_as(L.i32p), C.byref(p),
+                                                      res))
+    else:
+        expand_dim = int(kwargs.get("expand_dim", 20))
+        max_expand_dim = int(kwargs.get("max_expand_dim", 2 * expand_dim))
+        numiter = int(kwargs.get("expand_numiter", 4))
+        p.cutoff = float(kwargs.get("cutoff", Float64_threshold()))
+        central = t.index[eccentric_central_node(t.graph)]
+        L.check(envs[0].ctx.lib.tn_ttn_envs_fullsweep_expand(
+            n, hs, len(path), path.ctypes.data_as(L.i32p), central, C.byref(p), expand_dim,
+            max_expand_dim, numiter, int(kwargs.get("seed", 0)) & (2 ** 64 - 1), res))
     out = []
     for sw, r in zip(swdatas, res):
         sw.sweepcount += 1
@@ -497,7 +513,7 @@ def fullsweep_batch_(envs, sweeppath, solver, swdatas, **kwargs):
 
 
 def fullsweep_(sysenv: StateEnvsTTN, sweeppath, solver, swdata: SweepDataTTN, **kwargs):
-    """``fullsweep!`` (src/ttn/sweep_ttn.jl:117-274), noise = 0."""
+    """``fullsweep!`` (src/ttn/sweep_ttn.jl:117-274)."""
     return fullsweep_batch_([sysenv], sweeppath, solver, [swdata], **kwargs)[0]
 
 
@@ -522,17 +538,24 @@ class OptimizeParamsTTN:
 
 
 def optimize_(sysenv, params: OptimizeParamsTTN, sweeppath, **kwargs) -> SweepDataTTN:
-    """``optimize!`` (src/ttn/optimize_ttn.jl:148-226) with noise 0."""
-    from . import eig_solver
+    """``optimize!`` (src/ttn/optimize_ttn.jl:148-226): the stages of params with the noise
+    schedule (noise divided by noisedecay after every sweep, zero after disable_noise_after
+    sweeps of a stage or below 100 Float64_threshold)."""
+    from . import Float64_threshold, eig_solver
     goal = kwargs.pop("energyErrGoal", None)
     sw = SweepDataTTN()
     for ii in range(len(params.nsweeps)):
-        if params.noise[ii] != 0.0:
-            raise NotImplementedError("subspace expansion (noise > 0) is not built")
-        for _ in range(params.nsweeps[ii]):
-            de = fullsweep_(sysenv, sweeppath, eig_solver, sw, maxdim=params.maxdim[ii], **kwargs)
-            if goal is not None and abs(de) < abs(goal):
+        noise = float(params.noise[ii])
+        for jj in range(1, params.nsweeps[ii] + 1):
+            de = fullsweep_(sysenv, sweeppath, eig_solver, sw, maxdim=params.maxdim[ii],
+                            cutoff=params.cutoff[ii], noise=noise, **kwargs)
+            if goal is not None and abs(de) < abs(goal) and abs(noise) < Float64_threshold():
                 break
+            if jj == params.disable_noise_after[ii]:
+                noise = 0.0
+            noise /= params.noisedecay[ii]
+            if noise < 100 * Float64_threshold():
+                noise = 0.0
     return sw
 
 

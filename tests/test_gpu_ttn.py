@@ -159,7 +159,7 @@ def test_batched_sweeps_equal_single_sweeps_and_reach_exact(tn, ctx):
         tn.ttn.fullsweep_(batch[0], path, tn.eig_solver, tn.ttn.SweepDataTTN(), outputlevel=0)
 
 
-def test_optimize_api_and_unbuilt_modes(tn, ctx):
+def test_optimize_api_and_argument_errors(tn, ctx):
     N = 8
     terms, exact = tfim(N, 6)
     psi = tn.ttn.default_randomTTN(N, 16, 2, ctx=ctx)
@@ -169,9 +169,10 @@ def test_optimize_api_and_unbuilt_modes(tn, ctx):
     assert abs(e - exact) < 1e-10 * abs(exact)
     assert psi2.maxlinkdim() == 16
     se = tn.ttn.StateEnvsTTN(psi, H)
-    with pytest.raises(NotImplementedError):
+    # the reference's check of the expansion settings (sweep_ttn.jl:146-149)
+    with pytest.raises(tn.TenNetError, match="expand_numiter"):
         tn.ttn.fullsweep_(se, tn.ttn.default_sweeppath(N), tn.eig_solver, tn.ttn.SweepDataTTN(),
-                          noise=1e-3)
+                          noise=1e-3, expand_numiter=1, outputlevel=0)
     with pytest.raises(tn.TenNetError):
         tn.ttn.fullsweep_(se, tn.ttn.default_sweeppath(N)[:-1], tn.eig_solver,
                           tn.ttn.SweepDataTTN(), outputlevel=0)
