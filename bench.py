@@ -156,7 +156,7 @@ def download_blocks(psi):
 
 
 # ------------------------------------------------------------------------------------
-# CPU oracle legs (the checker, timed as the CPU baseline / reference arm)
+# CPU oracle legs (timed as the CPU baseline / reference arm)
 # ------------------------------------------------------------------------------------
 
 def oracle_env_from(tensors, links):

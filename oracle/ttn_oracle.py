@@ -1,7 +1,8 @@
 """CPU oracle for the tree tensor network (TTN) sweep (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()``
-and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.  The
+This module is the oracle, never the product: only ``tests/``,
+``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` legs of
+``bench.py`` may import it.  The
 product path (``libtennet_cuda.so``) never calls into it.
 
 Plain numpy FP64 restatement of TenNetLib's TTN ground-state path (no charge conservation):
