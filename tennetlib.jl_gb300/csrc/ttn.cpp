@@ -295,8 +295,9 @@ struct tn_ttn_env {
     int kry_vecs = 0;
     int nchunk_t = 1;                 // k chunks of the link-tensor contractions
     int nchunk_q = 1;                 // k chunks of the QR panel products
-    // slot capacities (elements per node slot, link dimension per edge slot); grow_group
-    // raises them when subspace expansion needs room, empty: the creation sizes
+    // slot capacities (elements per node slot, set by the arena layout; link dimensions per
+    // edge slot: link_cap, or the creation sizes when empty); grow_group raises them when
+    // subspace expansion needs room
     std::vector<int64_t> node_cap;
     std::vector<int> link_cap;
     int64_t expand_events = 0;        // subspace expansions so far (the padding stream's counter)
@@ -513,10 +514,11 @@ void build_arena_layout(tn_ttn_env* e, int64_t& cursor) {
     e->node_off.assign(t.nn, 0);
     e->S = 0;
     e->dmax = 1;
+    e->node_cap.resize(size_t(t.nn), 0);
     for (int v = 0; v < t.nn; ++v) {
         e->node_off[v] = cursor;
-        int64_t n = vol(e->dims[v]);
-        if (size_t(v) < e->node_cap.size()) n = std::max(n, e->node_cap[size_t(v)]);
+        const int64_t n = std::max(vol(e->dims[v]), e->node_cap[size_t(v)]);
+        e->node_cap[size_t(v)] = n;  // the slot's size: what the node tensor may grow to
         cursor += (n + 31) / 32 * 32;
         e->S = std::max(e->S, n);
         for (int x : e->dims[v]) e->dmax = std::max(e->dmax, x);
@@ -1911,8 +1913,7 @@ void ensure_expand_capacity(TtnGroup& G, int maxdim, int mx) {
                                         "for this engine (lower maxdim or max_expand_dim)");
                 need = std::max(need, int64_t(prodv));
             }
-            const int64_t have = std::max(vol(e->dims[v]),
-                                          size_t(v) < e->node_cap.size() ? e->node_cap[v] : 0);
+            const int64_t have = e->node_cap[size_t(v)];
             ncap[i][v] = std::max(need, have);
             grow = grow || need > have;
         }
@@ -1978,7 +1979,7 @@ void expand_group(TtnGroup& G, int node, int nxt, int mx, double noise, uint64_t
             const auto& dv = e->dims[v];
             const int64_t P = prod(dv, 0, leg), D = dv[leg], Q = prod(dv, leg + 1, int(dv.size()));
             const int64_t np = P * pad * Q;
-            TN_REQUIRE(P * (D + pad) * Q <= std::max(vol(dv), e->node_cap.empty() ? 0 : e->node_cap[v]),
+            TN_REQUIRE(P * (D + pad) * Q <= e->node_cap[size_t(v)],
                        "TTN internal: no room for the subspace expansion");
             const uint64_t key = splitmix64(seed + uint64_t(2) * (uint64_t(4096) * uint64_t(e->expand_events) +
                                                                  uint64_t(e->idx)) + uint64_t(which));

@@ -80,3 +80,23 @@ def test_noisy_batched_sweeps_match_oracle(tn, ctx):
         assert all(abs(a - b) <= 1 for a, b in zip(sws[i].maxchi, refs[i].maxchi))
         for a, b in zip(sws[i].energy, refs[i].energy):
             assert abs(a - b) <= 1e-10 * abs(b), i
+
+
+def test_noisy_sweeps_within_the_creation_slots(tn, ctx):
+    """A chi = 32 TTN truncated to maxdim 12 by a noise-free sweep, then noisy sweeps at the
+    same maxdim (expand_dim 4): the widened tensors fit the slots laid out at creation, so
+    the arena is not re-laid."""
+    terms, ev = _setup()
+    path = tn.ttn.default_sweeppath(N)
+    psi = T.random_ttn(N, 32, 4)
+    se = T.StateEnvsTTN(psi, terms)
+    so = T.SweepDataTTN()
+    eg = tn.ttn.StateEnvsTTN(upload(tn, ctx, psi), tn.ttn.CouplingModel(terms, N))
+    sg = tn.ttn.SweepDataTTN()
+    kw = dict(maxdim=12, cutoff=1e-12, expand_dim=4)
+    for noise in (0.0, 1e-3, 1e-4):
+        T.fullsweep(se, path, so, noise=noise, seed=3, **kw)
+        tn.ttn.fullsweep_(eg, path, tn.eig_solver, sg, noise=noise, seed=3, outputlevel=0, **kw)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1]), noise
+        assert abs(sg.maxchi[-1] - so.maxchi[-1]) <= 1
+    assert sg.maxchi[-1] <= 12
