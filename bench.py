@@ -668,7 +668,8 @@ def run_quench(tn, local, args):
                            "env_s": st["env_ms"] / 1e3, "krylov_s": st["lanczos_ms"] / 1e3,
                            "matvecs": st["matvecs"], "kernel_launches": st["kernel_launches"],
                            "heff_tflops": st["heff_flops"] / max(st["heff_ms"], 1e-9) / 1e9,
-                           "maxlinkdim": e.maxchi(), "energy": e.getenergy()})
+                           "maxlinkdim": e.maxchi(), "energy": e.getenergy(),
+                           "maxtruncerr": e.sweeperror()})
             if len(sweeps) == 1:
                 first_sz = [float(v) for v in tn.measure(e.getpsi(), "Sz")]
         psi = e.getpsi()
