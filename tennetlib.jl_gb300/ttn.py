@@ -17,6 +17,7 @@ Python                              TenNetLib (file:line)
 ``default_sweeppath(psi)``          ``default_sweeppath``         src/ttn/sweep_ttn.jl:49-65
 ``OptimizeParamsTTN``               ``OptimizeParamsTTN``         src/ttn/optimize_ttn.jl:25-110
 ``optimize_`` / ``optimize``        ``optimize!`` / ``optimize``  src/ttn/optimize_ttn.jl:148-281
+``measure(psi, op[, pos])``         ``measure``                   src/ttn/measure_ttn.jl:12-170
 =================================  ===========================================================
 
 Beyond the reference: ``StateEnvsTTN.batch(psis, models)`` creates environments that share
@@ -25,7 +26,8 @@ contraction stage for all of them) -- the reference runs independent instances o
 the other.
 
 Sites are 0-based; nodes keep the reference's (layer, index) labels.  The tree logic here
-is integer bookkeeping; every floating-point operation runs in libtennet_cuda.so.
+is integer bookkeeping; the floating-point work runs in libtennet_cuda.so (``measure``'s
+last contraction of one node tensor with a d x d operator is done on the host).
 """
 from __future__ import annotations
 
@@ -314,6 +316,65 @@ class CouplingModel:
                 self.lib.tn_ttn_model_destroy(self.h)
         except Exception:
             pass
+
+
+def _op_matrix(op, d):
+    from . import SPIN_HALF_OPS
+    if isinstance(op, str):
+        if d != 2 or op not in SPIN_HALF_OPS:
+            raise ValueError(f"unknown operator name {op!r} (S=1/2 names: {sorted(SPIN_HALF_OPS)})")
+        return SPIN_HALF_OPS[op]
+    m = np.asarray(op, dtype=np.float64)
+    if m.shape != (d, d):
+        raise ValueError("an operator must be a d x d matrix [s', s]")
+    return m
+
+
+def measure(psi: TTN, op, pos=None, sites=None):
+    """``measure(T, psi, opstr[, pos]; sites)`` (src/ttn/measure_ttn.jl:12-86): <O_i> at every
+    site (or ``pos``, or ``sites``; 0-based) -- for each node holding such sites the centre is
+    moved there (``isometrize!`` with QR moves on the GPU, normalised; psi is changed as in the
+    reference) and O contracted with its tensor.  With a list of (operator, site) pairs,
+    ``measure(T, psi, ["Sz" => i, "Sz" => j, ...])`` (:96-170): the centre is moved to the
+    eccentric central node of the sites' nodes and <psi| O_i O_j ... |psi> is the product of
+    the link tensors of that one product term (``LinkTensorsTTN(psi, optens)``, GPU) with the
+    centre tensor.  Operators are S=1/2 names or d x d matrices; fermionic Jordan-Wigner
+    strings (``isfermions``) are not applied.  The engine's term groups act with at most two
+    factors at a node, so the multi-site form takes products whose sites lie in at most two
+    subtrees of every node (every two-point function); others raise TenNetError."""
+    if isinstance(op, (list, tuple)) and op and isinstance(op[0], (list, tuple)):
+        return _measure_product(psi, op)
+    mat = _op_matrix(op, psi.d)
+    targets = [int(pos)] if pos is not None else (
+        [int(x) for x in sites] if sites is not None else list(range(psi.N)))
+    bynode = {}
+    for site in targets:
+        bynode.setdefault(psi.sitenodes[site], []).append(site)
+    out = {}
+    for node, ss in bynode.items():
+        psi.isometrize_(node)
+        T = psi[node]
+        legs = psi.legs(node)
+        for site in ss:
+            li = legs.index(("s", site))
+            y = np.moveaxis(np.tensordot(mat, T, axes=([1], [li])), 0, li)
+            out[site] = float(np.vdot(T, y))
+    vals = [out[site] for site in targets]
+    return vals[0] if pos is not None else vals
+
+
+def _measure_product(psi: TTN, oppairs):
+    ops = {}
+    for name, site in oppairs:
+        m = _op_matrix(name, psi.d)
+        site = int(site)
+        ops[site] = ops[site] @ m if site in ops else m  # O_a(i) O_b(i) -> the product A B
+    model = CouplingModel([(1.0, [(site, ops[site]) for site in sorted(ops)])], psi.N, psi.d)
+    oc = eccentric_central_node(psi.graph, {psi.sitenodes[site] for site in ops})
+    psi.isometrize_(oc)
+    env = StateEnvsTTN(psi, model)
+    x = psi[oc]
+    return float(np.vdot(x, env.product(x)))
 
 
 def tfim_terms(J, h):
