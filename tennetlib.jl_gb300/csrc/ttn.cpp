@@ -15,7 +15,8 @@
 // results are the local matrix and whose order-3 results are the per-term ones.
 //
 // H_eff at node v is the sum over term groups of mode products: a local matrix acts on one
-// leg, a term crossing two of v's links acts with one matrix on each of the two legs.
+// leg, a term with factors on k of v's legs acts with one matrix on each of them (k - 1
+// chained stages into temporaries, the last factor in the final round of its leg).
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -220,12 +221,12 @@ struct TPlan {
 };
 
 struct ProductPlan {    // H_eff x at one node
-    TPlan stageA;
+    std::vector<TPlan> stages;  // chained factors of groups with several (stage j: factor j)
     std::vector<TPlan> rounds;
     double flops = 0;
 };
 struct MovePlan {       // link tensors of edge (v -> u)
-    TPlan stageA;
+    std::vector<TPlan> stages;
     std::vector<TPlan> rounds;
     TPlan tg;
     CombPlan comb;
@@ -495,17 +496,14 @@ std::vector<TGroup> collect_groups(const tn_ttn_env* e, int v, int skip) {
             g.pcs.push_back(Piece{leg, es.off + int64_t(1 + c) * D * D});
         }
     }
-    for (auto& kv : byterm) {
-        TN_REQUIRE(kv.second.pcs.size() <= 2,
-                   "TTN: a term spans more than two subtrees of one node (not supported)");
-        out.push_back(std::move(kv.second));
-    }
+    for (auto& kv : byterm) out.push_back(std::move(kv.second));
     return out;
 }
 
-// order the pieces of a two-piece group so that the last one acts on the larger leg
+// order the factors of a group by leg, so that the last one acts on the largest leg
 void order_pieces(TGroup& g) {
-    if (g.pcs.size() == 2 && g.pcs[0].leg > g.pcs[1].leg) std::swap(g.pcs[0], g.pcs[1]);
+    std::stable_sort(g.pcs.begin(), g.pcs.end(),
+                     [](const Piece& a, const Piece& b) { return a.leg < b.leg; });
 }
 
 // ---- per-instance layout -----------------------------------------------------------------
@@ -562,11 +560,11 @@ void build_arena_layout(tn_ttn_env* e, int64_t& cursor) {
         cursor += int64_t(1 + es.cross.size()) * es.cap_dim * es.cap_dim;
         cursor = (cursor + 31) / 32 * 32;
     }
-    // temporaries of one product or link move: one per two-piece group, one per open
+    // temporaries of one product or link move: k - 1 per group of k factors, one per open
     // group, one for the local sum
     int ntmp = 1;
     for (int v = 0; v < t.nn; ++v) {
-        // product at v: every group with two pieces needs a stage-A temporary
+        // product at v: a group of k factors chains k - 1 temporaries
         int n2 = 0, nall = 0;
         std::map<int, int> cnt;
         for (int s : t.sites[v])
@@ -575,7 +573,7 @@ void build_arena_layout(tn_ttn_env* e, int64_t& cursor) {
             for (int term : e->estore[t.edge(v, u)].cross) cnt[term]++;
         for (auto& kv : cnt) {
             nall++;
-            if (kv.second >= 2) n2++;
+            if (kv.second >= 2) n2 += kv.second - 1;
         }
         ntmp = std::max(ntmp, n2 + nall + 2);
     }
@@ -658,8 +656,8 @@ struct EvalTarget {
     std::vector<TGroup> groups;
 };
 void add_eval(tn_ttn_env* e, const std::vector<int>& dims, int srcbuf, int64_t srcoff,
-              std::vector<EvalTarget>& targets, TPlan& stageA, std::vector<TPlan>& rounds,
-              int tmp_first, double& flops) {
+              std::vector<EvalTarget>& targets, std::vector<TPlan>& stages,
+              std::vector<TPlan>& rounds, int tmp_first, double& flops) {
     const int64_t tmpcur = e->w_tmp + int64_t(tmp_first) * ((e->S + 31) / 32 * 32);
     const int64_t n = vol(dims);
     const int64_t S = (e->S + 31) / 32 * 32;
@@ -668,16 +666,22 @@ void add_eval(tn_ttn_env* e, const std::vector<int>& dims, int srcbuf, int64_t s
         std::map<int, std::vector<ModeIn>> bucket;  // final leg -> inputs
         for (auto& g : tg.groups) {
             order_pieces(g);
-            if (g.pcs.size() == 1) {
-                bucket[g.pcs[0].leg].push_back(ModeIn{srcbuf, srcoff, S_L, g.pcs[0].moff});
-            } else {
+            const size_t k = g.pcs.size();
+            int zb = srcbuf;
+            int64_t zo = srcoff;
+            // factors 0 .. k-2 chained through temporaries (stage j applies factor j of every
+            // group), the last one in the final round of its leg
+            for (size_t j = 0; j + 1 < k; ++j) {
                 const int64_t toff = e->wbase + tmpcur + int64_t(tmp_used++) * S;
                 TN_REQUIRE(tmp_first + tmp_used <= e->ntmp, "TTN internal: temporaries exhausted");
-                add_mode_tasks(stageA.g, dims, g.pcs[0].leg, dims[g.pcs[0].leg], S_R, toff,
-                               {ModeIn{srcbuf, srcoff, S_L, g.pcs[0].moff}}, 0);
-                flops += 2.0 * n * dims[g.pcs[0].leg];
-                bucket[g.pcs[1].leg].push_back(ModeIn{S_R, toff, S_L, g.pcs[1].moff});
+                if (stages.size() <= j) stages.emplace_back();
+                add_mode_tasks(stages[j].g, dims, g.pcs[j].leg, dims[g.pcs[j].leg], S_R, toff,
+                               {ModeIn{zb, zo, S_L, g.pcs[j].moff}}, 0);
+                flops += 2.0 * n * dims[g.pcs[j].leg];
+                zb = S_R;
+                zo = toff;
             }
+            bucket[g.pcs[k - 1].leg].push_back(ModeIn{zb, zo, S_L, g.pcs[k - 1].moff});
         }
         int r = 0;
         for (auto& kv : bucket) {
@@ -705,7 +709,7 @@ ProductPlan& product_plan(TtnGroup& G, int v) {
         tg[0].off = e->w_y;
         tg[0].groups = collect_groups(e, v, -1);
         TN_REQUIRE(!tg[0].groups.empty(), "TTN: the Hamiltonian has no term at this node");
-        add_eval(e, e->dims[v], S_R, e->wbase + e->w_x, tg, P.stageA, P.rounds, 0, P.flops);
+        add_eval(e, e->dims[v], S_R, e->wbase + e->w_x, tg, P.stages, P.rounds, 0, P.flops);
     }
     return P;
 }
@@ -758,7 +762,7 @@ MovePlan& move_plan(TtnGroup& G, int v, int u) {
         if (has_loc) all.push_back(loc);
         for (auto& o : tg) all.push_back(o);
         TN_REQUIRE(e->ntmp >= next, "TTN internal: too few temporaries");
-        add_eval(e, dims, S_L, e->node_off[v], all, M.stageA, M.rounds, next, M.flops);
+        add_eval(e, dims, S_L, e->node_off[v], all, M.stages, M.rounds, next, M.flops);
         // contractions with the node tensor into the link slots
         int pi = 0;
         auto contract = [&](int64_t yoff, int64_t slot_off) {
@@ -849,7 +853,7 @@ void run_product(TtnGroup& G, int v) {
     ProductPlan& P = product_plan(G, v);
     const int sl = prod_slices(G);
     const int e0 = G.ctx->timer.mark();
-    tplan_run(G, P.stageA, sl, T_HEFF);
+    for (auto& stp : P.stages) tplan_run(G, stp, sl, T_HEFF);
     for (auto& r : P.rounds) tplan_run(G, r, sl, T_HEFF);
     G.ctx->timer.add(T_HEFF, e0, G.ctx->timer.mark());
     G.heff_flops += P.flops;
@@ -861,7 +865,7 @@ void run_link_move(TtnGroup& G, int v, int u) {
     MovePlan& M = move_plan(G, v, u);
     const int sl = prod_slices(G);
     const int e0 = G.ctx->timer.mark();
-    tplan_run(G, M.stageA, sl, T_ENV);
+    for (auto& stp : M.stages) tplan_run(G, stp, sl, T_ENV);
     for (auto& r : M.rounds) tplan_run(G, r, sl, T_ENV);
     tplan_run(G, M.tg, sl, T_ENV);
     comb_run(G, M.comb);

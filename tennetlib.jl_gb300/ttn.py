@@ -339,9 +339,7 @@ def measure(psi: TTN, op, pos=None, sites=None):
     eccentric central node of the sites' nodes and <psi| O_i O_j ... |psi> is the product of
     the link tensors of that one product term (``LinkTensorsTTN(psi, optens)``, GPU) with the
     centre tensor.  Operators are S=1/2 names or d x d matrices; fermionic Jordan-Wigner
-    strings (``isfermions``) are not applied.  The engine's term groups act with at most two
-    factors at a node, so the multi-site form takes products whose sites lie in at most two
-    subtrees of every node (every two-point function); others raise TenNetError."""
+    strings (``isfermions``) are not applied."""
     if isinstance(op, (list, tuple)) and op and isinstance(op[0], (list, tuple)):
         return _measure_product(psi, op)
     mat = _op_matrix(op, psi.d)

@@ -1,9 +1,9 @@
 """TTN measurements (measure(T, psi, opstr[, pos]; sites) and the multi-site product form,
 src/ttn/measure_ttn.jl:12-170) against the dense state of the oracle's TTN.
 
-Tolerance 1e-12 (single- and two-point expectation values of a normalised state).  Strings
-whose sites span more than two subtrees of a node are refused (TenNetError): the engine's
-term groups act with at most two factors at a node."""
+Tolerance 1e-12 (single- and multi-site expectation values of a normalised state).  A
+three-body Hamiltonian term (factors on three legs of a node) is swept against the oracle
+and the dense spectrum: per sweep energies 1e-10, ground energy 1e-10."""
 import numpy as np
 import pytest
 
@@ -41,6 +41,31 @@ def test_local_and_product_expectations_match_dense(tn, ctx):
         assert abs(tn.ttn.measure(pg, pairs) - _dense_expect(po, ops)) < 1e-12, pairs
     with pytest.raises(ValueError):
         tn.ttn.measure(pg, "Q")
-    # a string over more than two subtrees of a node is outside the engine's term groups
-    with pytest.raises(tn.TenNetError):
-        tn.ttn.measure(pg, [("Sx", 0), ("Sz", 5), ("Sx", 11)])
+    # strings over three and more subtrees of a node (chained factors)
+    for pairs in ([("Sx", 0), ("Sz", 5), ("Sx", 11)],
+                  [("Sz", 0), ("Sz", 3), ("Sz", 6), ("Sz", 9)]):
+        ops = {site: {"Sz": SZ, "Sx": SX}[name] for name, site in pairs}
+        assert abs(tn.ttn.measure(pg, pairs) - _dense_expect(po, ops)) < 1e-12, pairs
+
+
+def test_three_body_terms_sweep_to_exact(tn, ctx):
+    """Heisenberg chain plus three-body terms 0.3 Sz_i Sz_{i+1} Sz_{i+2} (and a four-body
+    one): products whose factors sit on three and more legs of a node."""
+    terms = T.heisenberg_terms(N)
+    terms += [(0.3, [(i, SZ), (i + 1, SZ), (i + 2, SZ)]) for i in range(N - 2)]
+    terms += [(0.2, [(0, SX), (4, SX), (8, SX), (11, SX)])]
+    ev = np.linalg.eigvalsh(T.dense_hamiltonian(N, terms))
+    path = tn.ttn.default_sweeppath(N)
+    po = T.random_ttn(N, 64, 5)
+    eo = T.StateEnvsTTN(po, terms)
+    eg = tn.ttn.StateEnvsTTN(tn.ttn.TTN(po.adj, po.site_nodes, 2, po.tensors, po.center, ctx),
+                             tn.ttn.CouplingModel(terms, N))
+    x = np.random.default_rng(1).standard_normal(po.tensors[po.center].shape)
+    ref = eo.product(x)
+    assert np.linalg.norm(eg.product(x) - ref) <= 1e-12 * np.linalg.norm(ref)
+    so, sg = T.SweepDataTTN(), tn.ttn.SweepDataTTN()
+    for _ in range(6):
+        T.fullsweep(eo, path, so, maxdim=64)
+        tn.ttn.fullsweep_(eg, path, tn.eig_solver, sg, maxdim=64, outputlevel=0)
+        assert abs(sg.energy[-1] - so.energy[-1]) <= 1e-10 * abs(so.energy[-1])
+    assert abs(sg.energy[-1] - ev[0]) < 1e-9
