@@ -500,7 +500,17 @@ def measure(psi: MPS, op, pos: int | None = None, sites=None):
     """``measure(Float64, psi, opstr[, pos]; sites)`` (``src/mps/measure.jl:150-219``):
     local expectation values of a single-site operator, given by S=1/2 name ("Sz", "Sx",
     "S+", "S-", "Id", "Nup", "Ndn") or as a d x d matrix [s', s].  pos (0-based) returns one
-    value; sites selects a subset; default all sites."""
+    value; sites selects a subset; default all sites.
+
+    With a list of (operator, site) pairs, ``measure(T, psi, ["Sz" => i, "Sz" => j, ...])``
+    (src/mps/measure.jl:222-330, bosonic): <psi| O_i O_j ... |psi> / <psi|psi> (operators on
+    one site multiplied in order).  Each operator is split into its parts of definite charge
+    change q(s') - q(s); every combination whose changes add to zero is an MPO of bond
+    dimension one (link charges the running sum of the changes), evaluated on the GPU as
+    <phi| H_eff |phi> of the two-site tensor phi at the orthogonality centre, between the
+    environments of that MPO; the other combinations vanish in a state of definite charge."""
+    if isinstance(op, (list, tuple)) and op and isinstance(op[0], (list, tuple)):
+        return _measure_product(psi, op)
     mat = SPIN_HALF_OPS[op] if isinstance(op, str) else np.asarray(op, dtype=np.float64)
     vals = psi.expect_local(mat)
     if pos is not None:
@@ -508,6 +518,48 @@ def measure(psi: MPS, op, pos: int | None = None, sites=None):
     if sites is not None:
         return [float(vals[i]) for i in sites]
     return [float(v) for v in vals]
+
+
+def _measure_product(psi: MPS, oppairs):
+    import itertools
+    d, pq = psi.d, np.asarray(psi.phys_q)
+    ops = {}
+    for name, site in oppairs:
+        m = SPIN_HALF_OPS[name] if isinstance(name, str) else np.asarray(name, dtype=np.float64)
+        if m.shape != (d, d):
+            raise ValueError("an operator must be a d x d matrix [s', s]")
+        site = int(site)
+        ops[site] = ops[site] @ m if site in ops else m
+    sites = sorted(ops)
+    parts = []
+    for site in sites:
+        comp = {}
+        for sp in range(d):
+            for s0 in range(d):
+                if ops[site][sp, s0] != 0.0:
+                    comp.setdefault(int(pq[sp] - pq[s0]), np.zeros((d, d)))[sp, s0] = ops[site][sp, s0]
+        parts.append(sorted(comp.items()) or [(0, np.zeros((d, d)))])
+    N, c = psi.N, psi.center
+    pos = min(c, N - 2)  # the two-site window [pos, pos + 1] holds the centre
+    phi = np.tensordot(psi.site(pos), psi.site(pos + 1), axes=([2], [0]))
+    eye = np.eye(d)
+    total = 0.0
+    for combo in itertools.product(*parts):
+        if sum(dq for dq, _ in combo) != 0:
+            continue
+        which = dict(zip(sites, combo))
+        W, delta, q = [], [np.zeros(1, dtype=np.int32)], 0
+        for i in range(N):
+            dq, m = which.get(i, (0, eye))
+            W.append(np.asarray(m, dtype=np.float64).reshape(1, 1, d, d))
+            q += dq
+            delta.append(np.array([q], dtype=np.int32))
+        env = StateEnvs(psi, MPO(W, delta, pq, psi.ctx))
+        env.position_(pos, 2)
+        total = total + np.vdot(phi, env.product(phi))
+    nrm = psi.inner(psi)
+    val = total / nrm
+    return complex(val) if np.iscomplexobj(val) and abs(np.imag(val)) > 1e-13 else float(np.real(val))
 
 
 def exp_solver(*_args, **_kwargs):

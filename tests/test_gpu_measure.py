@@ -123,3 +123,36 @@ def test_overlap_split_vs_fp64_ground_state(tn):
     finally:
         states.clear()
         c.close()
+
+
+def test_operator_strings_match_dense(tn, ctx):
+    """measure(psi, [("Sz", i), ("Sz", j), ...]) (src/mps/measure.jl:222-330): two- and
+    three-site strings, charge-changing factors (S+ S-, Sx Sx: split into parts of definite
+    charge change) and same-site products, on a DMRG ground state, against its dense state
+    (1e-12)."""
+    N = 10
+    W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
+    env = tn.StateEnvs(tn.MPS.product(tn.models.neel_states(N), pq, ctx), tn.MPO(W, delta, pq, ctx))
+    tn.dmrg_(env, tn.DMRGParams(nsweeps=[4, 4], maxdim=[16, 32], cutoff=1e-14), 2, outputlevel=0)
+    psi = env.getpsi()
+    v = psi.site(0)
+    for i in range(1, N):
+        v = np.tensordot(v, psi.site(i), axes=([-1], [0]))
+    v = v.reshape(-1)
+    v = v / np.linalg.norm(v)
+    mats = {"Sz": np.diag([0.5, -0.5]), "Sx": np.array([[0.0, 0.5], [0.5, 0.0]]),
+            "S+": np.array([[0.0, 1.0], [0.0, 0.0]]), "S-": np.array([[0.0, 0.0], [1.0, 0.0]])}
+
+    def dense(pairs):
+        ops = {}
+        for name, site in pairs:
+            ops[site] = ops[site] @ mats[name] if site in ops else mats[name]
+        full = np.ones((1, 1))
+        for i in range(N):
+            full = np.kron(full, ops.get(i, np.eye(2)))
+        return float(v @ full @ v)
+
+    for pairs in ([("Sz", 1), ("Sz", 8)], [("Sx", 0), ("Sx", 5)], [("S+", 2), ("S-", 7)],
+                  [("Sz", 3), ("Sz", 3)], [("Sz", 0), ("Sz", 4), ("Sz", 9)],
+                  [("S+", 1), ("S-", 1), ("Sx", 6), ("Sx", 8)]):
+        assert abs(tn.measure(psi, pairs) - dense(pairs)) < 1e-12, pairs
