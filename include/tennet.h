@@ -257,7 +257,8 @@ int tn_env_tdvpsweep(tn_env* env, double tau, const tn_update_params* p, tn_swee
 /* tdvpsweep! with a complex time step tau = tau_re + i tau_im (real-time evolution
  * exp(-i dt H) is tau = -i dt).  A real state is made complex first (ITensors promotes the
  * MPS to ComplexF64 the same way); the Krylov exponential, the contractions and the block
- * SVD then run on complex tensors (FP64 on the GPU whatever the context's precision). */
+ * SVD then run on complex tensors (H_eff products in the context's precision, environment
+ * updates, the realified block SVD and the Krylov exponential in FP64). */
 int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn_update_params* p,
                              tn_sweep_result* res, double* mid_eigs, int mid_cap,
                              int32_t* n_mid_eigs);
