@@ -270,6 +270,32 @@ int tn_env_tdvpsweep_complex(tn_env* env, double tau_re, double tau_im, const tn
 int tn_env_tdvpsweep_nsite(tn_env* env, int nsite, double tau_re, double tau_im,
                            const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
                            int mid_cap, int32_t* n_mid_eigs);
+/* The sweep of dynamic_fullsweep! after its first sweep (TenNetLib src/mps/sweep.jl:284-355):
+ * left to right, then right to left, bond b (between sites b and b + 1, 0-based) takes a
+ * one-site update when last_min[b] (the smallest kept eigenvalue of the bond's spectrum from
+ * the previous sweep, SweepData.lasteigs[b][end]) is below eigthreshold or its link dimension
+ * is at p->maxdim, else a two-site update; the right half decides on the spectra of the left
+ * half, and a one-site update at the end bond adds the update of the end site.  last_min
+ * holds N - 1 values; choices (optional, 2 (N - 1) entries) receives the nsite of bond b in
+ * the left half at [b] and in the right half at [N - 1 + b].  Global subspace expansion
+ * (krylov_extend!, the first sweep and every extendat-th sweep of the reference) is not
+ * part of this call. */
+int tn_env_fullsweep_dynamic(tn_env* env, double eigthreshold, const double* last_min,
+                             int32_t* choices, const tn_update_params* p, tn_sweep_result* res,
+                             double* mid_eigs, int mid_cap, int32_t* n_mid_eigs);
+/* The same sweep with the exponential solver and reverse steps (tdvpsweep! with
+ * nsite = "dynamic", src/mps/tdvp.jl:256-260): each update evolves by tau/2, tau = tau_re +
+ * i tau_im (a complex step makes the state complex first, as tn_env_tdvpsweep_complex). */
+int tn_env_tdvpsweep_dynamic(tn_env* env, double tau_re, double tau_im, double eigthreshold,
+                             const double* last_min, int32_t* choices, const tn_update_params* p,
+                             tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                             int32_t* n_mid_eigs);
+/* SweepData.lasteigs of the last full sweep of any kind: counts[b] (N - 1 entries) receives
+ * the length of bond b's kept spectrum (descending squared singular values, 0 before the
+ * first sweep), out (cap doubles) the spectra one after another; with out null only the
+ * lengths are written. */
+int tn_env_bond_spectra(const tn_env* env, double* out, int64_t cap, int32_t* counts,
+                        int ncounts);
 
 /* ---- block SVD + truncation -------------------------------------------------------
  * The SVD/truncation of replacebond! (called at TenNetLib src/mps/update_site.jl:64-76)

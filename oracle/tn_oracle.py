@@ -1142,6 +1142,72 @@ def fullsweep1(env: StateEnvs, swdata: SweepData, maxdim, cutoff, mindim=1, kryl
     return float("nan"), float("nan")
 
 
+def dynamic_sweep(env: StateEnvs, swdata: SweepData, maxdim, cutoff, eigthreshold=1e-12,
+                  tau=None, mindim=1, krylovdim=None, maxiter=None, tol=None, normalize=True):
+    """The sweep of ``dynamic_fullsweep!`` after its first one (``src/mps/sweep.jl:284-355``;
+    the first sweep and every extendat-th open with ``krylov_extend!``, not restated here):
+    bond b (0-based, between sites b and b + 1) takes a one-site update when the smallest
+    kept eigenvalue of swdata.lasteigs[b] is below eigthreshold or its link dimension is at
+    maxdim, else a two-site update, left to right and back; a one-site update at the end bond
+    adds the update of the end site (``:314-316``, ``:333-335``).  ``lasteigs`` is shared
+    between the halves, so the right half decides on the left half's spectra.  tau None: the
+    eigensolver; else ``exp_solver`` at tau/2 with reverse steps (``tdvpsweep!``,
+    ``src/mps/tdvp.jl:256-260``).  Returns the choices (left half, right half by bond)."""
+    N = env.N
+    assert env.psi.center == 0
+    if krylovdim is None:
+        krylovdim = 5 if tau is None else 30
+    if maxiter is None:
+        maxiter = 2 if tau is None else 100
+    if tol is None:
+        tol = 1e-14 if tau is None else 1e-12
+    step = None if tau is None else 0.5 * tau
+
+    def update(pos, nsite, ortho):
+        if nsite == 1:
+            e, spec, _ = update_one_site(env, pos, ortho, maxdim, mindim, cutoff, krylovdim,
+                                         maxiter, tol, normalize, 0.0, step)
+        elif tau is None:
+            e, spec, _ = update_two_site(env, pos, ortho, maxdim, mindim, cutoff, krylovdim,
+                                         maxiter, tol, normalize)
+        else:
+            e, spec = update_two_site_tdvp(env, pos, ortho, step, maxdim, mindim, cutoff,
+                                           krylovdim, maxiter, tol, normalize)
+        return e, spec
+
+    def pick(b):
+        return 1 if (swdata.lasteigs[b][-1] < eigthreshold
+                     or len(env.psi.links[b + 1]) >= maxdim) else 2
+
+    swdata.sweepcount += 1
+    energy = float("nan")
+    maxtruncerr = 0.0
+    lasteigs = [None] * (N - 1)
+    left, right = [0] * (N - 1), [0] * (N - 1)
+    for b in range(N - 1):
+        ns = left[b] = pick(b)
+        energy, spec = update(b, ns, "left")
+        lasteigs[b] = spec.eigs
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+        if ns == 1 and b == N - 2:
+            energy, _ = update(N - 1, 1, "left")
+    swdata.lasteigs = lasteigs
+    for b in range(N - 2, -1, -1):
+        ns = right[b] = pick(b)
+        energy, spec = update(b + 1 if ns == 1 else b, ns, "right")
+        lasteigs[b] = spec.eigs
+        maxtruncerr = max(spec.truncerr, maxtruncerr)
+        if ns == 1 and b == 0:
+            energy, _ = update(0, 1, "right")
+    swdata.maxchi.append(env.psi.maxlinkdim())
+    swdata.energy.append(energy)
+    mid = lasteigs[N // 2 - 1]
+    swdata.entropy.append(entropy(mid / np.sum(mid)))
+    swdata.maxtruncerr.append(maxtruncerr)
+    swdata.lasteigs = lasteigs
+    return left, right
+
+
 def dmrg(psi0: MPS, H: MPO, maxdim, nsweeps, cutoff, krylovdim=5, maxiter=2, tol=1e-14,
          mindim=1):
     """``dmrg!`` stage loop without noise (``src/mps/dmrg.jl:148-227``)."""

@@ -45,7 +45,8 @@ INT32_MAX = 2**31 - 1
 
 __all__ = [
     "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
-    "update_position_", "fullsweep_", "dmrg_", "dmrg", "dmrg2", "entropy", "svd_truncate",
+    "update_position_", "fullsweep_", "dynamic_fullsweep_", "dmrg_", "dmrg", "dmrg2",
+    "entropy", "svd_truncate",
     "Float64_threshold", "TenNetError", "models", "TDVPEngine", "tdvpsweep_", "exp_solver",
     "ttn", "measure",
 ]
@@ -366,6 +367,7 @@ class StateEnvs:
         h = L.vp()
         L.check(self.ctx.lib.tn_env_create(psi.h, H.h, C.byref(h)))
         _own(self, h)
+        self._nproj = 0
         if Ms is not None:
             self.set_projectors(Ms, weight)
 
@@ -375,7 +377,21 @@ class StateEnvs:
         arr = (L.vp * max(len(Ms), 1))(*[m.h for m in Ms])
         w = -1.0 if weight is None else float(weight)
         L.check(self.ctx.lib.tn_env_set_projectors(self.h, arr, len(Ms), w))
+        self._nproj = len(Ms)
         return self
+
+    def bond_spectra(self):
+        """The kept spectrum of every bond from the last full sweep (``SweepData.lasteigs``):
+        N - 1 arrays of descending squared singular values, empty before the first sweep."""
+        counts = np.zeros(max(self.N - 1, 1), dtype=np.int32)
+        lib = self.ctx.lib
+        L.check(lib.tn_env_bond_spectra(self.h, None, 0, counts.ctypes.data_as(L.i32p),
+                                        len(counts)))
+        out = np.zeros(max(int(counts.sum()), 1))
+        L.check(lib.tn_env_bond_spectra(self.h, out.ctypes.data_as(L.f64p), len(out),
+                                        counts.ctypes.data_as(L.i32p), len(counts)))
+        offs = np.concatenate([[0], np.cumsum(counts[: self.N - 1])])
+        return [out[offs[b]:offs[b + 1]].copy() for b in range(self.N - 1)]
 
     def __len__(self):
         return self.N
@@ -660,7 +676,7 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
     swdata.energy.append(float(res.energy))
     swdata.entropy.append(entropy(mid / mid.sum()) if mid.size else 0.0)
     swdata.maxtruncerr.append(float(res.maxtruncerr))
-    swdata.lasteigs = [mid]
+    swdata.lasteigs = sysenv.bond_spectra()
     swdata.stats.append({
         "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
@@ -685,14 +701,14 @@ def fullsweep_(sysenv: StateEnvs, solver, nsite: int, swdata: SweepData, **kwarg
     return enerr, enterr
 
 
-def _record_sweep(swdata, res, mid, wall, noise=0.0, outputlevel=0):
+def _record_sweep(swdata, res, mid, wall, spectra):
     mid = np.asarray(mid)
     swdata.sweepcount += 1
     swdata.maxchi.append(int(res.maxlinkdim))
     swdata.energy.append(float(res.energy))
     swdata.entropy.append(entropy(mid / mid.sum()) if mid.size else 0.0)
     swdata.maxtruncerr.append(float(res.maxtruncerr))
-    swdata.lasteigs = [mid]
+    swdata.lasteigs = spectra
     swdata.stats.append({
         "matvecs": res.matvecs, "heff_flops": res.heff_flops, "heff_ms": res.heff_ms,
         "env_ms": res.env_ms, "svd_ms": res.svd_ms, "lanczos_ms": res.lanczos_ms,
@@ -738,6 +754,103 @@ class TDVPEngine:
         return self.swdata
 
 
+def _sweep_printout(swdata, wall, noise, outputlevel):
+    if swdata.sweepcount > 1:
+        enerr = swdata.energy[-1] - swdata.energy[-2]
+        enterr = swdata.entropy[-1] - swdata.entropy[-2]
+    else:
+        enerr = enterr = float("nan")
+    if outputlevel > 0:
+        print("-" * 83)
+        print(f"At sweep {swdata.sweepcount} => E={swdata.energy[-1]}, S={swdata.entropy[-1]}, "
+              f"MaxLinkDim={swdata.maxchi[-1]}, Noise={noise:.2g}")
+        print(f"At sweep {swdata.sweepcount} => ΔE={enerr}, ΔS={enterr}, "
+              f"MaxErr={swdata.maxtruncerr[-1]:.2g}, Time={round(wall, 3)}")
+        print("-" * 83)
+    return enerr, enterr
+
+
+def _dynamic_sweep(sysenv, swdata, tau, eigthreshold, **kwargs):
+    """The mixed one-/two-site sweep of ``dynamic_fullsweep!`` (``src/mps/sweep.jl:284-355``)
+    with the eigensolver (tau None) or the exponential solver at tau/2 per update.  Returns the
+    per-bond choices (left half, right half)."""
+    N = sysenv.N
+    if len(swdata.lasteigs) != N - 1 or any(len(e) == 0 for e in swdata.lasteigs):
+        raise ValueError("dynamic_fullsweep!: swdata.lasteigs must hold the spectra of the "
+                         f"{N - 1} bonds from a previous full sweep of this state")
+    last_min = np.array([float(np.asarray(e)[-1]) for e in swdata.lasteigs], dtype=np.float64)
+    choices = np.zeros(2 * (N - 1), dtype=np.int32)
+    p = _params(kwargs, exp=tau is not None)
+    res = L.SweepResult()
+    cap = max(int(p.maxdim if p.maxdim < 1 << 20 else 1 << 16), 1)
+    mid = np.zeros(cap)
+    nmid = C.c_int32()
+    lib = sysenv.ctx.lib
+    t0 = time.perf_counter()
+    if tau is None:
+        L.check(lib.tn_env_fullsweep_dynamic(
+            sysenv.h, float(eigthreshold), last_min.ctypes.data_as(L.f64p),
+            choices.ctypes.data_as(L.i32p), C.byref(p), C.byref(res),
+            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    else:
+        tau = complex(tau)
+        L.check(lib.tn_env_tdvpsweep_dynamic(
+            sysenv.h, tau.real, tau.imag, float(eigthreshold), last_min.ctypes.data_as(L.f64p),
+            choices.ctypes.data_as(L.i32p), C.byref(p), C.byref(res),
+            mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
+    wall = time.perf_counter() - t0
+    _record_sweep(swdata, res, mid[: nmid.value], wall, sysenv.bond_spectra())
+    left, right = choices[: N - 1].copy(), choices[N - 1:].copy()
+    swdata.stats[-1]["nsite_left"], swdata.stats[-1]["nsite_right"] = left, right
+    _sweep_printout(swdata, wall, p.noise, kwargs.get("outputlevel", 1))
+    return left, right
+
+
+def _needs_extension(sysenv, swdata, extendat):
+    """``dynamic_fullsweep!``'s first sweep and every extendat-th sweep (``sweep.jl:
+    266-282``): global subspace expansion then a one-site sweep for a single MPO, a two-site
+    sweep when excited-state projectors are present."""
+    ext = swdata.sweepcount == 0 or (extendat is not None
+                                     and (swdata.sweepcount + 1) % int(extendat) == 0)
+    if ext and not sysenv._nproj:
+        raise NotImplementedError(
+            "dynamic_fullsweep!: this sweep of a single-MPO StateEnvs starts with krylov_extend! "
+            "(global subspace expansion), which is not built; run a sweep with a fixed nsite "
+            "first (and leave extendat = nothing)")
+    return ext
+
+
+def dynamic_fullsweep_(sysenv: StateEnvs, solver, swdata: SweepData, eigthreshold=1e-12,
+                       extendat=None, **kwargs):
+    """``dynamic_fullsweep!`` (``src/mps/sweep.jl:257-355``): per bond a one-site update when
+    the bond's last kept spectrum ends below ``eigthreshold`` or its link is at ``maxdim``,
+    else a two-site update.  With ``exp_solver`` the keyword ``time_step`` is the step of each
+    update (``tdvpsweep!`` passes half its step) and ``reverse_step`` must be true.  The
+    sweeps that the reference opens with ``krylov_extend!`` raise ``NotImplementedError``
+    (single MPO); with excited-state projectors they are two-site sweeps.  Returns
+    (Delta E, Delta S)."""
+    if solver is exp_solver:
+        if kwargs.get("time_step") is None or not kwargs.get("reverse_step", False):
+            raise ValueError("exp_solver sweeps need time_step and reverse_step = true")
+        tau = 2.0 * complex(kwargs.pop("time_step"))
+        kwargs.pop("reverse_step")
+        if tau.imag == 0.0:
+            tau = tau.real
+    elif solver is eig_solver:
+        tau = None
+    else:
+        raise ValueError("only eig_solver and exp_solver are built")
+    if _needs_extension(sysenv, swdata, extendat):
+        if tau is not None:
+            raise ValueError("excited-state projectors are built for the eigensolver only")
+        return fullsweep_(sysenv, solver, 2, swdata, **kwargs)
+    _dynamic_sweep(sysenv, swdata, tau, eigthreshold, **kwargs)
+    n = swdata.sweepcount
+    if n > 1:
+        return (swdata.energy[-1] - swdata.energy[-2], swdata.entropy[-1] - swdata.entropy[-2])
+    return float("nan"), float("nan")
+
+
 def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwargs):
     """``tdvpsweep!`` (``src/mps/tdvp.jl:247-277``) with nsite = 2: one full sweep with
     ``exp_solver`` at time_step/2 and reverse one-site steps; ``abstime += |time_step|``.
@@ -745,12 +858,30 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     A real time step is imaginary-time evolution exp(time_step H); a complex one (real-time
     evolution exp(-i dt H) is ``time_step = -1j * dt``) makes the state complex first, as
     ITensors promotes the MPS to ComplexF64.  nsite = 1 is the one-site sweep with the
-    zero-site reverse step; ``nsite = "dynamic"`` is not built.
+    zero-site reverse step.  ``nsite = "dynamic"`` is ``dynamic_fullsweep!``'s mixed sweep
+    (keywords ``eigthreshold``, default 1e-12, and ``extendat``); its sweeps that open with
+    global subspace expansion (the first one, every extendat-th) are not built and raise
+    ``NotImplementedError``, so a dynamic run starts after one sweep with a fixed nsite.  The
+    default nsite is 2 (the reference's default is "dynamic").
     """
     if solver is not exp_solver:
         raise ValueError("`tdvpsweep!()`: `solver` must be `exp_solver` !!")
+    if nsite == "dynamic":
+        if kwargs.get("noise", 0.0):
+            raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
+                             "`reverse_step=true` !!")
+        eigthreshold = kwargs.pop("eigthreshold", 1e-12)
+        extendat = kwargs.pop("extendat", None)
+        _needs_extension(engine.sysenv, engine.swdata, extendat)
+        _dynamic_sweep(engine.sysenv, engine.swdata, time_step, eigthreshold,
+                       **{"outputlevel": 0, **kwargs})
+        engine.abstime += abs(time_step)
+        return None
     if nsite not in (1, 2):
-        raise ValueError("nsite = 1 and 2 TDVP sweeps are built (\"dynamic\" is not)")
+        raise ValueError("`tdvpsweep!()`: `nsite` must be `\"dynamic\"`, `2`, or `1` !!")
+    if kwargs.get("extendat") is not None:
+        raise ValueError("`tdvpsweep!()`: `extendat` must be `nothing` for `nsite == 2` or "
+                         "`nsite == 1`.")
     if kwargs.get("noise", 0.0):
         raise ValueError("`updatePosition()` :: `noise` cannot be greater than zero for "
                          "`reverse_step=true` !!")
@@ -773,7 +904,8 @@ def tdvpsweep_(engine: TDVPEngine, time_step, nsite=2, solver=exp_solver, **kwar
     else:
         L.check(sysenv.ctx.lib.tn_env_tdvpsweep(sysenv.h, tau.real, C.byref(p), C.byref(res),
                                                 mid.ctypes.data_as(L.f64p), cap, C.byref(nmid)))
-    _record_sweep(engine.swdata, res, mid[: nmid.value], time.perf_counter() - t0)
+    _record_sweep(engine.swdata, res, mid[: nmid.value], time.perf_counter() - t0,
+                  sysenv.bond_spectra())
     engine.abstime += abs(time_step)
     return None
 

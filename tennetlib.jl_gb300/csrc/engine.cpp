@@ -3582,11 +3582,22 @@ int tn_env_update_position_nsite(tn_env* env, int pos, int nsite, int ortho,
 }  // extern "C"
 
 namespace {
+// per-bond choice of dynamic_fullsweep! (TenNetLib src/mps/sweep.jl:257-355): the smallest
+// kept eigenvalue of each bond's last spectrum (SweepData.lasteigs[bond][end]), the threshold
+// under which a bond takes a one-site update, and where the choices are reported (bond b of
+// the left half at [b], of the right half at [N - 1 + b]; may be null)
+struct DynamicSweep {
+    const double* last_min;
+    double eigthreshold;
+    int32_t* choices;
+};
+
 // fullsweep! (TenNetLib src/mps/sweep.jl:94-196) with the eigensolver (time_step null) or
-// the exponential solver at time_step with reverse steps (tdvpsweep!, src/mps/tdvp.jl:268)
+// the exponential solver at time_step with reverse steps (tdvpsweep!, src/mps/tdvp.jl:268);
+// with dyn, dynamic_fullsweep!'s mixed one-/two-site sweep (sweep.jl:284-355)
 void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, double* mid_eigs,
                 int mid_cap, int32_t* n_mid_eigs, const double* time_step, int nsite = 2,
-                double time_im = 0.0) {
+                double time_im = 0.0, const DynamicSweep* dyn = nullptr) {
     TN_REQUIRE(env && res, "null argument");
     check_params(p);
     tn_mps* psi = env->psi.get();
@@ -3607,7 +3618,51 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
     const int es = ctx->timer.mark();
     double maxerr = 0.0, energy = NAN;
     std::vector<double> ev, mid;
-    if (nsite == 2) {
+    std::vector<std::vector<double>> last(size_t(N - 1));
+    if (dyn) {
+        // per bond (sweep.jl:302-304, 322-324): one site when the bond's last spectrum ends
+        // below eigthreshold or its link is at maxdim, else two sites; the right half reads
+        // the spectra the left half left (lasteigs is shared between the halves)
+        auto pick = [&](int b, double lmin) {
+            return (lmin < dyn->eigthreshold || psi->links[b + 1].total() >= p->maxdim) ? 1 : 2;
+        };
+        for (int b = 0; b < N - 1; ++b) {
+            const int ns = pick(b, dyn->last_min[b]);
+            if (dyn->choices) dyn->choices[b] = ns;
+            tn_update_result r{};
+            if (ns == 1)
+                update_one_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step, time_im);
+            else
+                update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step, time_im);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+            last[size_t(b)] = ev;
+            if (ns == 1 && b == N - 2) {  // the last site (sweep.jl:314-316)
+                tn_update_result r2{};
+                update_one_site(env, N - 1, TN_ORTHO_LEFT, p, &r2, ev, time_step, time_im);
+                energy = r2.energy;
+            }
+        }
+        for (int b = N - 2; b >= 0; --b) {
+            const auto& e = last[size_t(b)];
+            const int ns = pick(b, e.empty() ? HUGE_VAL : e.back());
+            if (dyn->choices) dyn->choices[N - 1 + b] = ns;
+            tn_update_result r{};
+            if (ns == 1)
+                update_one_site(env, b + 1, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
+            else
+                update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
+            energy = r.energy;
+            maxerr = std::max(maxerr, r.truncerr);
+            last[size_t(b)] = ev;
+            if (ns == 1 && b == 0) {  // the first site (sweep.jl:333-335)
+                tn_update_result r2{};
+                update_one_site(env, 0, TN_ORTHO_RIGHT, p, &r2, ev, time_step, time_im);
+                energy = r2.energy;
+            }
+        }
+        mid = last[size_t(N / 2 - 1)];
+    } else if (nsite == 2) {
         for (int b = 0; b < N - 1; ++b) {
             tn_update_result r{};
             update_two_site(env, b, TN_ORTHO_LEFT, p, &r, ev, time_step, time_im);
@@ -3619,6 +3674,7 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
             update_two_site(env, b, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
+            last[size_t(b)] = ev;
             if (b == N / 2 - 1) mid = ev;
         }
     } else {
@@ -3635,9 +3691,11 @@ void full_sweep(tn_env* env, const tn_update_params* p, tn_sweep_result* res, do
             update_one_site(env, q, TN_ORTHO_RIGHT, p, &r, ev, time_step, time_im);
             energy = r.energy;
             maxerr = std::max(maxerr, r.truncerr);
+            if (q >= 1) last[size_t(q - 1)] = ev;
             if (q == N / 2) mid = ev;
         }
     }
+    env->bond_eigs = std::move(last);
     ctx->timer.add(T_SWEEP, es, ctx->timer.mark());
     sync(ctx);
     ctx->timer.collect(env->acc_ms);
@@ -3719,6 +3777,52 @@ int tn_env_tdvpsweep_nsite(tn_env* env, int nsite, double tau_re, double tau_im,
         if (tau_im != 0.0) env_to_complex(env);
         const double half = 0.5 * tau_re;
         full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half, nsite, 0.5 * tau_im);
+    });
+}
+
+int tn_env_fullsweep_dynamic(tn_env* env, double eigthreshold, const double* last_min,
+                             int32_t* choices, const tn_update_params* p, tn_sweep_result* res,
+                             double* mid_eigs, int mid_cap, int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(env && last_min, "null argument");
+        TN_REQUIRE(!std::isnan(eigthreshold), "eigthreshold must be a number");
+        const DynamicSweep dyn{last_min, eigthreshold, choices};
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, nullptr, 2, 0.0, &dyn);
+    });
+}
+
+int tn_env_tdvpsweep_dynamic(tn_env* env, double tau_re, double tau_im, double eigthreshold,
+                             const double* last_min, int32_t* choices, const tn_update_params* p,
+                             tn_sweep_result* res, double* mid_eigs, int mid_cap,
+                             int32_t* n_mid_eigs) {
+    return guarded([&] {
+        TN_REQUIRE(env && last_min, "null argument");
+        TN_REQUIRE(std::isfinite(tau_re) && std::isfinite(tau_im), "time step must be finite");
+        TN_REQUIRE(!std::isnan(eigthreshold), "eigthreshold must be a number");
+        if (tau_im != 0.0) env_to_complex(env);
+        const double half = 0.5 * tau_re;
+        const DynamicSweep dyn{last_min, eigthreshold, choices};
+        full_sweep(env, p, res, mid_eigs, mid_cap, n_mid_eigs, &half, 2, 0.5 * tau_im, &dyn);
+    });
+}
+
+int tn_env_bond_spectra(const tn_env* env, double* out, int64_t cap, int32_t* counts,
+                        int ncounts) {
+    return guarded([&] {
+        TN_REQUIRE(env && counts, "null argument");
+        const int nb = env->psi->N - 1;
+        TN_REQUIRE(ncounts >= nb, "counts must hold one entry per bond (N - 1)");
+        int64_t total = 0;
+        for (int b = 0; b < nb; ++b) {
+            const bool have = b < int(env->bond_eigs.size());
+            counts[b] = have ? int32_t(env->bond_eigs[size_t(b)].size()) : 0;
+            total += counts[b];
+        }
+        if (!out) return;  // lengths only
+        TN_REQUIRE(total <= cap, "output buffer too small for the spectra");
+        int64_t o = 0;
+        for (int b = 0; b < nb && b < int(env->bond_eigs.size()); ++b)
+            for (double v : env->bond_eigs[size_t(b)]) out[o++] = v;
     });
 }
 

@@ -217,4 +217,7 @@ struct tn_env {
     std::vector<ProjState> proj;
     double proj_weight = 0.0;
     tn::DevBuf projm, projc, projt1, projt2;
+    // kept spectrum (squared singular values, descending) of every bond from the last full
+    // sweep, bond b between sites b and b + 1 (SweepData.lasteigs)
+    std::vector<std::vector<double>> bond_eigs;
 };

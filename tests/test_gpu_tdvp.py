@@ -56,11 +56,24 @@ def test_tdvp_imaginary_time_reaches_ground_state(tn):
     assert eng.totalerror() >= 0.0
 
 
-def test_tdvp_rejects_unbuilt_modes(tn):
+def test_tdvp_mode_errors(tn):
+    """nsite outside {1, 2, "dynamic"} and extendat with a fixed nsite are errors, as in
+    tdvp.jl:262-274; a first dynamic sweep of a single MPO would open with global subspace
+    expansion, which is not built, and raises NotImplementedError without touching the state."""
     ctx = tn.Context(0)
     N = 6
     W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
     eng = tn.TDVPEngine(tn.MPS.product(tn.models.neel_states(N), pq, ctx),
                         tn.MPO(W, delta, pq, ctx))
-    with pytest.raises(ValueError):
+    with pytest.raises(NotImplementedError, match="krylov_extend"):
         tn.tdvpsweep_(eng, -0.05, nsite="dynamic", maxdim=8)
+    with pytest.raises(ValueError, match="nsite"):
+        tn.tdvpsweep_(eng, -0.05, nsite=3, maxdim=8)
+    with pytest.raises(ValueError, match="extendat"):
+        tn.tdvpsweep_(eng, -0.05, nsite=2, maxdim=8, extendat=2)
+    assert eng.sweepcount() == 0
+    tn.tdvpsweep_(eng, -0.05, maxdim=8)
+    with pytest.raises(NotImplementedError, match="krylov_extend"):  # (1 + 1) % 2 == 0
+        tn.tdvpsweep_(eng, -0.05, nsite="dynamic", maxdim=8, extendat=2)
+    tn.tdvpsweep_(eng, -0.05, nsite="dynamic", maxdim=8)
+    assert eng.sweepcount() == 2

@@ -381,3 +381,49 @@ def test_oracle_one_site_tdvp_is_exact_at_full_rank():
         assert np.abs(dense(e.psi) - ref).max() < 1e-11
         if isinstance(tau, complex):
             assert np.ptp(s.energy) < 1e-12
+
+
+@pytest.mark.parametrize("tau", [None, -0.1, -0.1j])
+def test_oracle_dynamic_sweep_limits_are_the_fixed_sweeps(tau):
+    """dynamic_fullsweep!'s mixed sweep (src/mps/sweep.jl:284-355) with every bond choosing
+    two sites (threshold 0, no link at maxdim) is the two-site sweep, and with every bond
+    choosing one site (threshold inf) the one-site sweep (sweep.jl:94-196), bit for bit, with
+    the eigensolver and with real and complex TDVP steps; at maxdim every bond takes one site
+    whatever the threshold."""
+    N = 8
+    H = O.heisenberg_mpo(N)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+
+    def prepared():
+        psi = O.product_mps(start, O.SPIN_HALF_Q)
+        if isinstance(tau, complex):
+            psi.A = [a.astype(np.complex128) for a in psi.A]
+        env, sw = O.StateEnvs(psi, H), O.SweepData()
+        for _ in range(2):
+            if tau is None:
+                O.fullsweep(env, sw, 64, 1e-12)
+            else:
+                O.tdvp_sweep(env, sw, tau, 64, 1e-12)
+        return env, sw
+
+    for thr, nsite in ((0.0, 2), (np.inf, 1)):
+        a, sa = prepared()
+        b, sb = prepared()
+        left, right = O.dynamic_sweep(a, sa, 64, 1e-12, thr, tau)
+        assert left == right == [nsite] * (N - 1)
+        if tau is None:
+            (O.fullsweep if nsite == 2 else O.fullsweep1)(b, sb, 64, 1e-12)
+        else:
+            O.tdvp_sweep(b, sb, tau, 64, 1e-12, nsite=nsite)
+        assert sa.energy[-1] == sb.energy[-1] and sa.entropy[-1] == sb.entropy[-1]
+        for x, y in zip(a.psi.A, b.psi.A):
+            assert np.array_equal(x, y)
+        for x, y in zip(sa.lasteigs, sb.lasteigs):
+            assert np.array_equal(x, y)
+    a, sa = prepared()
+    dims = [len(q) for q in a.psi.links]
+    md = max(dims)
+    left, _ = O.dynamic_sweep(a, sa, md, 1e-12, 0.0, tau)
+    # the left half meets each link as the previous sweep left it
+    assert left == [1 if dims[b + 1] >= md else 2 for b in range(N - 1)]
+    assert 1 in left and 2 in left
