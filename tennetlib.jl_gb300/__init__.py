@@ -755,7 +755,7 @@ class TDVPEngine:
 
 
 def _sweep_printout(swdata, wall, noise, outputlevel):
-    if swdata.sweepcount > 1:
+    if swdata.sweepcount > 1 and len(swdata.energy) > 1:
         enerr = swdata.energy[-1] - swdata.energy[-2]
         enterr = swdata.entropy[-1] - swdata.entropy[-2]
     else:
@@ -845,8 +845,7 @@ def dynamic_fullsweep_(sysenv: StateEnvs, solver, swdata: SweepData, eigthreshol
             raise ValueError("excited-state projectors are built for the eigensolver only")
         return fullsweep_(sysenv, solver, 2, swdata, **kwargs)
     _dynamic_sweep(sysenv, swdata, tau, eigthreshold, **kwargs)
-    n = swdata.sweepcount
-    if n > 1:
+    if swdata.sweepcount > 1 and len(swdata.energy) > 1:
         return (swdata.energy[-1] - swdata.energy[-2], swdata.entropy[-1] - swdata.entropy[-2])
     return float("nan"), float("nan")
 
