@@ -198,6 +198,15 @@ int tn_mps_overlap_complex(const tn_mps* a, const tn_mps* b, double* out);
  * StateEnvs(psi, H) (TenNetLib src/mps/state_envs.jl:54-60): copies psi, builds ProjMPO
  * environments lazily. */
 int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out);
+/* updateH!(sysenv, H; recalcEnv) (TenNetLib src/mps/state_envs.jl:181-212, through
+ * updateH!(engine, H; recalcEnv) of src/mps/tdvp.jl:182-196): H replaces the MPO of env (same
+ * site indices; env keeps a pointer, H must outlive env or the next update).  recalc_env != 0
+ * drops every environment (rebuilt from H as positions are taken); recalc_env == 0 keeps the
+ * environments built so far -- allowed with no excited-state projectors, the left
+ * environments unset (after a full sweep) and the MPO link indices unchanged -- so the next
+ * half sweep reads right environments of the old MPO, as the reference does.  Projector
+ * environments do not depend on H and stay. */
+int tn_env_update_mpo(tn_env* env, tn_mpo* H, int recalc_env);
 /* StateEnvs(psi, H, Ms; weight) (src/mps/state_envs.jl:88-105): excited-state projectors.
  * The effective Hamiltonian of every later update and product becomes ProjMPO_MPS2's
  * (src/mps/projmpo_mps2.jl:94-101), H_eff + weight sum_k |m_k><m_k| with m_k the projection

@@ -645,6 +645,26 @@ class StateEnvs:
     def N(self):
         return self.psi.N
 
+    def update_h(self, H: MPO, recalc_env=True):
+        """``updateH!(sysenv, H; recalcEnv)`` (``src/mps/state_envs.jl:181-212``): with
+        recalc_env a new ProjMPO, every MPO environment dropped; without it (single MPO, left
+        environments unset, same MPO link indices) H takes the old MPO's place and the right
+        environments already built stay, so the next half sweep reads environments of the old
+        MPO."""
+        assert H.N == self.N
+        N = self.N
+        if recalc_env:
+            self.H = H
+            self.L = [None] * (N + 1)
+            self.R = [None] * (N + 1)
+            self.L[0] = np.ones((1, 1, 1))
+            self.R[N - 1] = np.ones((1, 1, 1))
+            self.lpos, self.rpos = 0, N - 1
+            return
+        assert not self.Ms and self.lpos == 0 and self.psi.center == 0
+        assert all(a.shape[:2] == b.shape[:2] for a, b in zip(H.W, self.H.W))
+        self.H = H
+
     def position(self, pos, nsite):
         """Make L[pos] and R[pos+nsite-1] valid (ProjMPO ``position!`` restated; the
         projector environments follow the same positions)."""

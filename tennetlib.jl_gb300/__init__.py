@@ -45,7 +45,7 @@ INT32_MAX = 2**31 - 1
 
 __all__ = [
     "Context", "MPO", "MPS", "StateEnvs", "DMRGParams", "SweepData", "eig_solver",
-    "update_position_", "fullsweep_", "dynamic_fullsweep_", "dmrg_", "dmrg", "dmrg2",
+    "update_position_", "fullsweep_", "dynamic_fullsweep_", "updateH_", "dmrg_", "dmrg", "dmrg2",
     "entropy", "svd_truncate",
     "Float64_threshold", "TenNetError", "models", "TDVPEngine", "tdvpsweep_", "exp_solver",
     "ttn", "measure",
@@ -752,6 +752,31 @@ class TDVPEngine:
 
     def sweepdata(self):
         return self.swdata
+
+
+def updateH_(target, H: MPO, Ms=None, *, weight=None, recalcEnv=True):
+    """``updateH!`` of a ``StateEnvs`` (``src/mps/state_envs.jl:181-212, 241-260``) or of a
+    ``TDVPEngine`` (``src/mps/tdvp.jl:182-196``): H replaces the Hamiltonian.  With
+    ``recalcEnv`` every environment is rebuilt from H as positions are taken; without it (a
+    single MPO only, after a full sweep, same MPO link indices) the environments built so far
+    stay, so the next half sweep reads right environments of the old H, as in the reference.
+    A StateEnvs with excited-state projectors takes the new states ``Ms`` and ``weight`` too
+    (``recalcEnv`` true only)."""
+    sysenv = target.sysenv if isinstance(target, TDVPEngine) else target
+    if Ms is not None and not sysenv._nproj:
+        raise ValueError("`updateH!()` with Ms needs a StateEnvs made with projector states")
+    if sysenv._nproj and Ms is None:
+        raise ValueError("`updateH!()` of a StateEnvs with projector states takes Ms and weight")
+    if sysenv._nproj and not recalcEnv:
+        raise ValueError(f"`updateH!()` :: Not implemented for `recalcEnv={recalcEnv}` with "
+                         "excited-state projectors !!")
+    if H.ctx is not sysenv.ctx:
+        raise ValueError("the MPO belongs to another context")
+    L.check(sysenv.ctx.lib.tn_env_update_mpo(sysenv.h, H.h, int(bool(recalcEnv))))
+    sysenv.H = H
+    if Ms is not None:
+        sysenv.set_projectors(Ms, weight)
+    return None
 
 
 def _sweep_printout(swdata, wall, noise, outputlevel):

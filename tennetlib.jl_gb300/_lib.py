@@ -145,6 +145,7 @@ PROTOS = {
                                            C.POINTER(UpdateParams), C.POINTER(SweepResult), f64p,
                                            C.c_int, i32p]),
     "tn_env_bond_spectra": (C.c_int, [vp, f64p, C.c_int64, i32p, C.c_int]),
+    "tn_env_update_mpo": (C.c_int, [vp, vp, C.c_int]),
     "tn_svd_truncate": (C.c_int, [vp, C.c_int, i32p, i32p, f64p, C.c_int32, C.c_int32,
                                   C.c_double, i32p, f64p, f64p]),
     "tn_block_svals_noalloc": (C.c_int, [C.c_int, vp, C.c_int, i32p, i32p, vp, vp]),

@@ -3367,6 +3367,40 @@ int tn_env_create(tn_mps* psi, tn_mpo* H, tn_env** out) {
     });
 }
 
+int tn_env_update_mpo(tn_env* env, tn_mpo* H, int recalc_env) {
+    return guarded([&] {
+        TN_REQUIRE(env && H, "null argument");
+        const tn_mps* psi = env->psi.get();
+        TN_REQUIRE(H->ctx == env->ctx, "the MPO belongs to another context");
+        TN_REQUIRE(psi->N == H->N && psi->d == H->d && psi->pq == H->pq,
+                   "MPS and MPO site indices differ");
+        const int N = psi->N;
+        if (recalc_env) {
+            // a new ProjMPO (src/mps/state_envs.jl:183-188): every environment is dropped and
+            // rebuilt from the new MPO as positions are taken
+            env->H = H;
+            make_trivial_env(env->ctx, env->L[0], psi->links[0], H->delta[0], env_planes(psi));
+            make_trivial_env(env->ctx, env->R[N - 1], psi->links[N], H->delta[N], env_planes(psi));
+            env->lpos = 0;
+            env->rpos = N - 1;
+        } else {
+            // the new MPO takes the old one's place and the environments built so far stay
+            // (state_envs.jl:189-208): the next half sweep reads right environments of the
+            // old MPO
+            TN_REQUIRE(env->proj.empty(),
+                       "`updateH!()` :: recalcEnv = false is defined for a single MPO only");
+            TN_REQUIRE(env->lpos == 0, "`updateH!()` :: recalcEnv = false needs lpos == 0");
+            TN_REQUIRE(psi->center == 0,
+                       "`updateH!()` :: recalcEnv = false needs the orthogonality center at site 1");
+            TN_REQUIRE(H->wd == env->H->wd && H->delta == env->H->delta,
+                       "`updateH!()` :: recalcEnv = false needs the link indices of the old MPO");
+            env->H = H;
+        }
+        env->hp_pos = -1;  // the H_eff plans carry the old MPO's tensors
+        env->h1p_pos = -1;
+    });
+}
+
 int tn_env_set_projectors(tn_env* env, const tn_mps* const* Ms, int count, double weight) {
     return guarded([&] {
         TN_REQUIRE(env, "null argument");

@@ -427,3 +427,26 @@ def test_oracle_dynamic_sweep_limits_are_the_fixed_sweeps(tau):
     # the left half meets each link as the previous sweep left it
     assert left == [1 if dims[b + 1] >= md else 2 for b in range(N - 1)]
     assert 1 in left and 2 in left
+
+
+def test_oracle_update_h_reuse_and_recalc():
+    """updateH! (src/mps/state_envs.jl:181-212): with recalcEnv = false the first half sweep
+    after the change reads right environments of the old MPO, so after a quench of the
+    couplings the two choices differ (here by ~1.7e-7 in the energy); with the MPO unchanged
+    the reused environments are exact and both choices agree to rounding."""
+    N = 10
+    H1, H2 = O.heisenberg_mpo(N), O.heisenberg_mpo(N, 0.5, Jz=2.0)
+    start = [0 if i % 2 == 0 else 1 for i in range(N)]
+
+    def run(Hnew, recalc):
+        psi = O.product_mps(start, O.SPIN_HALF_Q)
+        psi.A = [a.astype(np.complex128) for a in psi.A]
+        env, sw = O.StateEnvs(psi, H1), O.SweepData()
+        for _ in range(4):
+            O.tdvp_sweep(env, sw, -0.2j, 16, 1e-12)
+        env.update_h(Hnew, recalc)
+        O.tdvp_sweep(env, sw, -0.2j, 16, 1e-12)
+        return sw.energy[-1]
+
+    assert abs(run(H2, True) - run(H2, False)) > 1e-8
+    assert abs(run(H1, True) - run(H1, False)) < 1e-12
