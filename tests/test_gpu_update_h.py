@@ -64,8 +64,10 @@ def test_update_h_argument_errors(tn, ctx):
     tn.updateH_(eng, upload_mpo(tn, ctx, wide), recalcEnv=True)
     tn.tdvpsweep_(eng, -0.1, maxdim=8)
     assert np.isfinite(eng.getenergy())
-    # left environments built: reuse is refused, as the reference asserts lpos == 0
-    eng.sysenv.position_(3, 2)
+    # left environments built (two left-moving updates): reuse is refused, as the reference
+    # asserts lpos == 0
+    for b in range(2):
+        tn.update_position_(eng.sysenv, tn.eig_solver, b, 2, "left", maxdim=8)
     with pytest.raises(tn.TenNetError, match="lpos"):
         tn.updateH_(eng, upload_mpo(tn, ctx, H1), recalcEnv=False)
     # site indices must match
