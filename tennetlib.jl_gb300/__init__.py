@@ -181,6 +181,8 @@ class MPO:
         self.N = len(W)
         self.d = len(phys_q)
         self.phys_q = np.asarray(phys_q, dtype=np.int32)
+        self.W = [np.asarray(w, dtype=np.float64) for w in W]   # host copies (MPO sums)
+        self.delta = [np.asarray(x, dtype=np.int32) for x in delta]
         wd = [W[0].shape[0]] + [w.shape[1] for w in W]
         flat = np.concatenate([np.asarray(w, dtype=np.float64).ravel(order="F") for w in W])
         q = np.concatenate([np.asarray(x, dtype=np.int32) for x in delta])
@@ -196,6 +198,21 @@ class MPO:
     def from_terms(cls, N, terms, conserve_qns=True, ctx=None):
         W, delta, pq = models.mpo_from_terms(N, terms, conserve_qns)
         return cls(W, delta, pq, ctx)
+
+    @classmethod
+    def sum(cls, mpos):
+        """The Hamiltonian H_1 + H_2 + ... of ``StateEnvs(psi, Vector{MPO})`` (ProjMPOSum2,
+        ``src/mps/projmposum2.jl``) as one MPO with block-diagonal bonds, whose H_eff products
+        are the sums of the summands' products."""
+        mpos = list(mpos)
+        if not mpos:
+            raise ValueError("no MPO to sum")
+        ctx = mpos[0].ctx
+        for m in mpos:
+            if m.ctx is not ctx or not np.array_equal(m.phys_q, mpos[0].phys_q):
+                raise ValueError("the MPOs of a sum need one context and the same sites")
+        W, delta = models.mpo_direct_sum([(m.W, m.delta) for m in mpos])
+        return cls(W, delta, mpos[0].phys_q, ctx)
 
     def __del__(self):
         try:
@@ -356,10 +373,14 @@ class StateEnvs:
 
     ``StateEnvs(psi, H, Ms, weight=w)`` (``src/mps/state_envs.jl:88-105``) adds the
     excited-state projectors of the states Ms: the effective Hamiltonian becomes
-    ProjMPO_MPS2's, H_eff + w sum_k |m_k><m_k| (``src/mps/projmpo_mps2.jl:94-101``)."""
+    ProjMPO_MPS2's, H_eff + w sum_k |m_k><m_k| (``src/mps/projmpo_mps2.jl:94-101``).
+    ``StateEnvs(psi, [H1, H2, ...])`` (``state_envs.jl:70-78``, ProjMPOSum2) takes the sum of
+    the MPOs through ``MPO.sum``."""
 
     def __init__(self, psi: MPS, H: MPO, Ms=None, *, weight=None):
         self.ctx = psi.ctx
+        if isinstance(H, (list, tuple)):  # StateEnvs(psi, Vector{MPO}): ProjMPOSum2
+            H = MPO.sum(H)
         self.H = H
         self.phys_q = psi.phys_q
         self.N = psi.N
@@ -763,6 +784,11 @@ def updateH_(target, H: MPO, Ms=None, *, weight=None, recalcEnv=True):
     A StateEnvs with excited-state projectors takes the new states ``Ms`` and ``weight`` too
     (``recalcEnv`` true only)."""
     sysenv = target.sysenv if isinstance(target, TDVPEngine) else target
+    if isinstance(H, (list, tuple)):
+        if not recalcEnv:
+            raise ValueError(f"`updateH!()` :: Not implemented for `recalcEnv={recalcEnv}` "
+                             "with `ProjMPOSum2` !!")
+        H = MPO.sum(H)
     if Ms is not None and not sysenv._nproj:
         raise ValueError("`updateH!()` with Ms needs a StateEnvs made with projector states")
     if sysenv._nproj and Ms is None:

@@ -101,6 +101,46 @@ def mpo_from_terms(N: int, terms, conserve_qns: bool = True):
     return W, delta, pq
 
 
+def mpo_direct_sum(mpos):
+    """One MPO equal to the sum of several: ``[(W, delta), ...]`` with equal site counts,
+    physical dimensions and edge charges, edge MPO bonds of dimension one.  The site tensors
+    are block diagonal in the MPO bonds (the first concatenated along its right bond, the last
+    along its left one), the bond charges concatenated, so its environments are those of the
+    summands side by side and every H_eff product is the sum of theirs -- the product of
+    ProjMPOSum2 (TenNetLib src/mps/projmposum2.jl:86-101).  Returns (W, delta)."""
+    Ws = [[np.asarray(w, dtype=np.float64) for w in W] for W, _ in mpos]
+    ds = [[np.asarray(x, dtype=np.int64) for x in delta] for _, delta in mpos]
+    if not Ws:
+        raise ValueError("no MPO to sum")
+    N = len(Ws[0])
+    d = Ws[0][0].shape[2]
+    for W, delta in zip(Ws, ds):
+        if len(W) != N or len(delta) != N + 1 or any(w.shape[2:] != (d, d) for w in W):
+            raise ValueError("the MPOs of a sum need the same sites")
+        if W[0].shape[0] != 1 or W[-1].shape[1] != 1:
+            raise ValueError("the MPOs of a sum need edge bonds of dimension one")
+        if not (np.array_equal(delta[0], ds[0][0]) and np.array_equal(delta[N], ds[0][N])):
+            raise ValueError("the MPOs of a sum need the same edge charges")
+    if N == 1:
+        return [sum(W[0] for W in Ws)], [ds[0][0], ds[0][1]]
+    out = []
+    for i in range(N):
+        rows = [1] if i == 0 else [W[i].shape[0] for W in Ws]
+        cols = [1] if i == N - 1 else [W[i].shape[1] for W in Ws]
+        T = np.zeros((sum(rows), sum(cols), d, d))
+        r0 = c0 = 0
+        for k, W in enumerate(Ws):
+            a, b = W[i].shape[:2]
+            T[r0:r0 + a, c0:c0 + b] = W[i]
+            if i > 0:
+                r0 += a
+            if i < N - 1:
+                c0 += b
+        out.append(T)
+    delta = [ds[0][0]] + [np.concatenate([x[i] for x in ds]) for i in range(1, N)] + [ds[0][N]]
+    return out, delta
+
+
 def neel_states(N: int):
     """Up on odd (1-based) sites, Dn on even ones (test/test_MPS_DMRG.jl:35)."""
     return [0 if i % 2 == 0 else 1 for i in range(N)]
