@@ -146,9 +146,9 @@ def test_one_site_tdvp_matches_oracle(tn, tau, precision):
 
 @pytest.mark.parametrize("precision", ["fp64", "split"])
 def test_quench_at_scale_matches_oracle(tn, precision):
-    """The config-4 chain (N = 64, maxdim 512, cutoff 1e-9, krylovdim 30): a state evolved on
-    the GPU to t = 2.5 (10 sweeps of tau = -0.25i), copied to the oracle, then the same sweep
-    of tau = -0.05i on both."""
+    """The real-time quench workload (N = 64 chain, maxdim 512, cutoff 1e-9, krylovdim 30):
+    a state evolved on the GPU to t = 2.5 (10 sweeps of tau = -0.25i), copied to the oracle,
+    then the same sweep of tau = -0.05i on both."""
     ctx = tn.Context(0, precision=precision, slices=5)
     N = 64
     W, delta, pq = tn.models.mpo_from_terms(N, tn.models.heisenberg_chain_terms(N))
