@@ -42,3 +42,21 @@ def test_mpo_direct_sum_is_the_sum_of_the_mpos(tn):
     with pytest.raises(ValueError, match="same sites"):
         tn.models.mpo_direct_sum([(parts[0].W, parts[0].delta),
                                   (O.heisenberg_mpo(N + 1).W, O.heisenberg_mpo(N + 1).delta)])
+
+
+def test_mpo_direct_sum_edge_cases(tn):
+    """One site: the summands' 1 x 1 site matrices add up; a summand whose edge bond is
+    wider than one, or whose edge charges differ, is refused."""
+    s = tn.models.mpo_direct_sum
+    q = np.zeros(2, dtype=np.int64)
+    a = np.arange(4.0).reshape(1, 1, 2, 2)
+    b = np.ones((1, 1, 2, 2))
+    W, delta = s([([a], [q[:1], q[:1]]), ([b], [q[:1], q[:1]])])
+    assert len(W) == 1 and np.array_equal(W[0], a + b)
+    wide = [np.ones((2, 1, 2, 2)), np.ones((1, 1, 2, 2))]
+    with pytest.raises(ValueError, match="dimension one"):
+        s([(wide, [np.zeros(2), np.zeros(1), np.zeros(1)])])
+    ok = [np.ones((1, 1, 2, 2)), np.ones((1, 1, 2, 2))]
+    with pytest.raises(ValueError, match="edge charges"):
+        s([(ok, [np.zeros(1), np.zeros(1), np.zeros(1)]),
+           (ok, [np.ones(1), np.zeros(1), np.ones(1)])])
